@@ -1,0 +1,298 @@
+"""Benchmark of the SaclayMocks hot path on GB300: one production chunk per step.
+
+Step = 2560 x 2560 x 1536 GRF delta + eta_par boxes (white noise -> sqrt(P/Vcell) -> c2r, five
+HBM passes) + 2e5 skewer transmissions (start uniform in the box, direction within 10 deg of +z,
+400-1200 pixels of 0.2 Mpc/h, trilinear read, P1D_miss = 0.05 exp(-(k/2)^2) on a 2048-point
+grid, FGPA a(z) = 0.1((1+z)/3.2)^4.5, b = 1.58, c = 0.6, z = 1.8 -> 3.6 along x).  Noise is drawn
+on the GPU (Philox).  Every step reads and writes ~560 GB (boxes of 40 GB >> 129 MB L2), so no
+L2 flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--small]
+
+Prints one JSON line.  --impl reference times the CPU restatement of the reference's path on the
+host cores (the reference itself does not run there).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GRF cells/s, flux pixels/s, (a,b,c) fit time: adjoint vs finite-diff, 1 GB300"
+
+PRODUCTION = dict(nx=2560, ny=2560, nz=1536, dcell=2.19, n_skewers=200_000, npix=(400, 1200),
+                  ss_nz=2048, seed=1)
+SMALL = dict(nx=256, ny=256, nz=256, dcell=2.19, n_skewers=2_000, npix=(400, 1200), ss_nz=2048, seed=1)
+
+
+def hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        return dist, rank, world
+    return None, 0, 1
+
+
+def cpu_baseline(cfg, sample_div, workers):
+    """CPU restatement on a bounded sample: a box with 1/sample_div of the cells per axis
+    product (same cell size) and the same number of skewers per cell."""
+    import numpy as np
+    from oracle import cpu_pipeline, skewers as osk
+    from saclaymocks_gb300 import spectra
+    f = round(sample_div ** (1 / 3))
+    nx, ny, nz = cfg["nx"] // f, cfg["ny"] // f, cfg["nz"] // f
+    nz -= nz % 2
+    cells = nx * ny * nz
+    nsk = max(1, int(cfg["n_skewers"] * cells / (cfg["nx"] * cfg["ny"] * cfg["nz"])))
+    t0 = time.perf_counter()
+    d, e, tg = cpu_pipeline.grf_cpu(nx, ny, nz, cfg["dcell"], cfg["seed"], workers=workers)
+    t_grf = time.perf_counter() - t0
+    tb = spectra.skewers_cone(nsk, np.array([nx, ny, nz]) * cfg["dcell"], seed=cfg["seed"],
+                              npix_range=cfg["npix"])
+    t0 = time.perf_counter()
+    F, ts = cpu_pipeline.skewers_cpu(d, e, cfg["dcell"], tb.start, tb.direction, tb.npix, 0.2,
+                                     cfg["ss_nz"], osk.pmiss_analytic, cfg["seed"], workers=workers)
+    t_sk = time.perf_counter() - t0
+    return dict(cells=cells, pixels=tb.total_pixels, t_grf=t_grf, t_sk=t_sk, stages={**tg, **ts},
+                sample=f"{nx}x{ny}x{nz} box (1/{f ** 3} of the cells) + {nsk} skewers")
+
+
+def run_reference(args, cfg):
+    dist, rank, world = dist_setup()
+    if rank != 0:
+        return
+    workers = os.cpu_count() or 1
+    cpu_baseline(cfg, 512, workers)            # warm-up: imports, FFT plans, C oracle build
+    vals = []
+    for _ in range(args.steps):
+        r = cpu_baseline(cfg, 64 if not args.small else 8, workers)
+        vals.append(r)
+    cells = sum(r["cells"] for r in vals)
+    t = sum(r["t_grf"] + r["t_sk"] for r in vals)
+    v = cells / t
+    out = {"metric": METRIC, "value": v, "unit": "cells/s", "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic",
+           "config": {"workload": "production chunk 2560x2560x1536 + 2e5 skewers (bounded CPU sample)",
+                      "sample": vals[0]["sample"]},
+           "flux_pixels_per_s": sum(r["pixels"] for r in vals) / sum(r["t_sk"] for r in vals),
+           "cpu_baseline": {"value": v, "unit": "cells/s", "cores": workers, "kind": "port",
+                            "sample": vals[0]["sample"]},
+           "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "stages_s": vals[0]["stages"]}
+    print(json.dumps(out))
+
+
+def run_ours(args, cfg):
+    import numpy as np
+    import torch
+
+    from saclaymocks_gb300 import _lib, grf, pipeline, spectra
+
+    dist, rank, world = dist_setup()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    L = np.array([cfg["nx"], cfg["ny"], cfg["nz"]]) * cfg["dcell"]
+    table = spectra.skewers_cone(cfg["n_skewers"], L, seed=cfg["seed"] + rank, npix_range=cfg["npix"])
+    scfg = spectra.SpectraConfig(ss_mode=_lib.SMK_SS_PHILOX, ss_nz=cfg["ss_nz"],
+                                 pmiss=spectra.pmiss_gauss(0.05, 2.0), seed=cfg["seed"] + rank,
+                                 abc_mode=_lib.SMK_ABC_POWERLAW, a=0.1, a_zref1=3.2, a_power=4.5,
+                                 b=1.58, c=0.6, z_lo=1.8, z_hi=3.6)
+    chunk = pipeline.MockChunk(cfg["nx"], cfg["ny"], cfg["nz"], cfg["dcell"], seed=cfg["seed"] + rank,
+                               cfg=scfg)
+    runner = chunk._prepare(table.start, table.direction, table.npix)
+    boxes, ws = chunk.boxes, chunk.ws
+    nx, ny, nz = cfg["nx"], cfg["ny"], cfg["nz"]
+    cells = nx * ny * nz
+    pixels = table.total_pixels
+
+    def device_step(ev=None, sk_ev=None):
+        out = grf.make_boxes(nx, ny, nz, cfg["dcell"], seed=cfg["seed"] + rank, amp=chunk.amp,
+                             out=boxes, workspace=ws, pass_events=ev)
+        if sk_ev:
+            sk_ev[0].record()
+        runner.run(out.delta_pad[0], out.eta_pad[0], nx=nx, ny=ny, nz=nz, pitch=out.pitch,
+                   dcell=cfg["dcell"], flux=chunk._flux)
+        if sk_ev:
+            sk_ev[1].record()
+        return out
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        device_step()
+    barrier()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(args.steps)]
+    skevs = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(args.steps)]
+    for e in [x for row in evs for x in row]:
+        e.record()                              # materialise the raw event handles
+    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        barrier()
+        t_start.record()
+        for k in range(args.steps):
+            out = device_step(evs[k], skevs[k])
+        t_end.record()
+        barrier()
+    ms = t_start.elapsed_time(t_end)
+    out.check()
+    pass_ms = np.mean([[evs[k][i].elapsed_time(evs[k][i + 1]) for i in range(5)]
+                       for k in range(args.steps)], axis=0)
+    sk_ms = float(np.mean([skevs[k][0].elapsed_time(skevs[k][1]) for k in range(args.steps)]))
+    ms_t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+    if dist:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms = float(ms_t.item())
+
+    # e2e: through MockChunk.run with host skewer arrays, H2D + D2H inside the timed region
+    chunk.run(table.start, table.direction, table.npix)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        chunk.run(table.start, table.direction, table.npix)
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+    if dist:
+        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+    e2e_s = float(e2e_t.item())
+
+    if rank != 0:
+        return
+    peak, peak_kind = hbm_peak()
+    nzh = nz // 2 + 1
+    cbytes = 8.0 * nx * ny * nzh           # one half-complex box
+    rbytes = 4.0 * cells                   # one real box
+    pass_names = ["zfwd_r2c(philox)", "y_fwd", "x_fused", "y_inv(x2)", "zinv_c2r(x2)"]
+    pass_bytes = [cbytes, 2 * cbytes, 3 * cbytes, 4 * cbytes, 2 * cbytes + 2 * rbytes]
+    dom = int(np.argmax(pass_ms))
+    achieved = pass_bytes[dom] / (pass_ms[dom] * 1e-3) / 1e9
+    grf_ms = float(np.sum(pass_ms))
+    step_ms = ms / args.steps
+    value = world * cells / (step_ms * 1e-3)
+    res = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (Philox noise, synthetic skewers)",
+           "config": {"workload": f"production chunk {nx}x{ny}x{nz} delta+eta_par boxes + "
+                                  f"{cfg['n_skewers']} skewers ({pixels} pixels)",
+                      "parallelism": "replicas" if world > 1 else "1 GPU",
+                      "l2": "inputs larger than L2 (40 GB boxes), no flush needed"},
+           "grf_cells_per_s": world * cells / (grf_ms * 1e-3),
+           "flux_pixels_per_s": world * pixels / (sk_ms * 1e-3),
+           "pass_ms": dict(zip(pass_names, [round(float(x), 3) for x in pass_ms])),
+           "skewer_ms": round(sk_ms, 3),
+           "roofline": {"bound": "hbm", "kernel": pass_names[dom], "achieved": achieved, "peak": peak,
+                        "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                        "traffic": None,
+                        "per_pass_frac": {n: round(b / (m * 1e-3) / 1e9 / peak, 3)
+                                          for n, b, m in zip(pass_names, pass_bytes, pass_ms)}},
+           "e2e": {"value": world * cells / e2e_s, "unit": "cells/s",
+                   "h2d_bytes_per_step": chunk.h2d_bytes(), "d2h_bytes_per_step": chunk.d2h_bytes(),
+                   "ms_per_step": e2e_s * 1e3},
+           "gpu_launches": args.steps * 6,
+           "clocks": clk.summary()}
+    if not args.no_cpu:
+        workers = os.cpu_count() or 1
+        r = cpu_baseline(cfg, 64 if not args.small else 8, workers)
+        v = r["cells"] / (r["t_grf"] + r["t_sk"])
+        res["cpu_baseline"] = {"value": v, "unit": "cells/s", "cores": workers, "kind": "port",
+                               "sample": r["sample"]}
+    print(json.dumps(res))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true", help="256^3 box + 2000 skewers (quick check)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    cfg = SMALL if args.small else PRODUCTION
+    if args.impl == "reference":
+        run_reference(args, cfg)
+    else:
+        run_ours(args, cfg)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,203 @@
+/*
+ * smk.h -- C ABI of the GB300 (sm_103a) SaclayMocks hot-path library (libsmk.so).
+ *
+ * The reference (igmhub/SaclayMocks) is pure Python; its "operator API" for this path is
+ * a set of functions, scripts and file formats, not an FFI.  Each entry point below states
+ * which reference interface it replaces (file:line inside igmhub/SaclayMocks).
+ *
+ * Conventions
+ *  - Every buffer argument is a DEVICE pointer owned by the caller (e.g. a torch tensor's
+ *    data_ptr()); the library never allocates device memory.  Scratch memory is the
+ *    caller's ``workspace`` sized by the matching *_workspace_size() query.
+ *  - Work is enqueued on ``stream`` (a cudaStream_t, NULL = legacy default stream) and is
+ *    stream-ordered: results are ready when the stream is synchronised.  One host thread
+ *    per stream; calls on different streams may run concurrently unless they share
+ *    buffers or a workspace.
+ *  - Every function returns SMK_OK (0) or a negative SMK_E* code; it never calls exit,
+ *    abort or __trap.  smk_strerror() names a code, smk_last_error() gives the message of
+ *    the last failure on the calling host thread.
+ *  - Boxes are C-ordered [batch][nx][ny][pitch] float32 arrays, with the z row padded to
+ *    ``pitch = smk_grf_pitch(nz)`` floats (>= 2*(nz/2+1), a multiple of 8): the layout of
+ *    an in-place real<->half-complex transform.  Cell (x,y,z) of box b is element
+ *    ((b*nx + x)*ny + y)*pitch + z, z < nz.
+ */
+#ifndef SMK_H
+#define SMK_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+#define SMK_OK 0
+#define SMK_EINVAL (-1)     /* invalid argument (null pointer, size, mode)          */
+#define SMK_ENOTSUPP (-2)   /* size not handled by the kernels (see smk_fft_supported) */
+#define SMK_ECUDA (-3)      /* a CUDA runtime call or kernel launch failed            */
+#define SMK_EWORKSPACE (-4) /* workspace missing or smaller than the size query       */
+#define SMK_ENULLBOX (-5)   /* produced box is all zero or holds non-finite values    */
+
+/* Name of a status code (static string). */
+const char* smk_strerror(int status);
+/* Message of the last failure on this host thread ("" if none). */
+const char* smk_last_error(void);
+/* Library version as 10000*major + 100*minor + patch. */
+int smk_version(void);
+/* 1 if a line FFT of length n runs on the kernels (2 <= n <= 4096, n = 2^a 3^b 5^c). */
+int smk_fft_supported(int32_t n);
+
+/* ---------------------------------------------------------------- GRF boxes (make_boxes) */
+#define SMK_NOISE_HOST 0   /* white noise given by the caller (dense [batch][nx][ny][nz])  */
+#define SMK_NOISE_PHILOX 1 /* white noise drawn on the GPU: Philox4x32-10 + Box-Muller     */
+
+#define SMK_PK_ANALYTIC 0  /* P(k) = amp * k / (1 + (k/k0)^2)^2, evaluated in the kernel   */
+#define SMK_PK_GRID 1      /* sqrt(P/Vcell) read from a float32 [nx][ny][nz/2+1] grid       */
+
+typedef struct {
+    int32_t nx, ny, nz;   /* cells; nz even; every axis passes smk_fft_supported            */
+    int32_t batch;        /* independent boxes in one launch (>= 1)                          */
+    double dcell;         /* cell size, Mpc/h                                                */
+    int32_t pk_mode;      /* SMK_PK_ANALYTIC or SMK_PK_GRID                                  */
+    double k0;            /* break scale of the analytic spectrum, h/Mpc                     */
+    double amp;           /* amplitude A of the analytic spectrum; <= 0: A such that         */
+                          /* E[var delta] = 1, computed on the device in FP64                */
+    const float* pk_grid; /* SMK_PK_GRID: device sqrt(P/Vcell) grid (shared by the batch)    */
+    int32_t noise_mode;   /* SMK_NOISE_HOST or SMK_NOISE_PHILOX                              */
+    const float* noise;   /* SMK_NOISE_HOST: device dense noise [batch][nx][ny][nz]          */
+    uint64_t seed;        /* SMK_NOISE_PHILOX: box b uses seed + b                           */
+    int32_t want_eta;     /* 1: also produce eta_zz = irfftn(kz^2/k^2 delta_k)               */
+    void* const* pass_events; /* optional cudaEvent_t[6]: recorded on the stream before the    */
+    int32_t n_pass_events;    /* first HBM pass and after each of the five (0: none)          */
+} SmkGrfParams;
+
+/* Row pitch (floats) of the padded box layout for a z extent nz. */
+int64_t smk_grf_pitch(int32_t nz);
+/* Floats of one padded output box array (all batch members). */
+int64_t smk_grf_box_floats(const SmkGrfParams* p);
+/* Workspace bytes smk_grf_boxes needs (the FP64 normalisation accumulator). */
+size_t smk_grf_workspace_size(const SmkGrfParams* p);
+
+/*
+ * Replaces bin/make_boxes.py DrawGRF_boxk (:40-72), the P0 multiply (:288-292),
+ * FFTandStore's c2r + normalisation + sigma + null check (:77-105) and the eta_zz box
+ * (:299-306, :341-352).  delta (and eta when want_eta) are padded output boxes; the
+ * forward r2c runs in place in delta.  stats (device, may be NULL; 8*batch doubles,
+ * zeroed by the call) receives for box b and field f (0 = delta, 1 = eta_zz):
+ * stats[8b+4f+0] = sum, [8b+4f+1] = sum of squares, [8b+4f+2] = count of non-finite
+ * cells, [8b+4f+3] = 0 (FP64); the caller derives sigma and the null check
+ * (smk_grf_check does it on the host from one 4-double record).
+ */
+int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats,
+                  void* workspace, size_t workspace_bytes, void* stream);
+
+/* Host-side check of a stats record (copied to host): SMK_ENULLBOX if the box is all
+ * zero or holds non-finite cells (bin/make_boxes.py:100-105), else SMK_OK; sigma_out
+ * (may be NULL) gets the standard deviation of the box (bin/make_boxes.py:92). */
+int smk_grf_check(const double* stats_host, int64_t ncells, double* sigma_out);
+
+/* Normalisation A with E[var delta] = 1 for the analytic spectrum (FP64 sum over the
+ * half spectrum); enqueues on stream and writes *amp_dev (a device double). */
+int smk_pk_normalisation(int32_t nx, int32_t ny, int32_t nz, double dcell, double k0,
+                         double* amp_dev, void* stream);
+
+/* ---------------------------------------------------------------- skewers (make_spectra +
+ *                                                                   merge_spectra) */
+#define SMK_INTERP_TRILINEAR 0 /* 8-corner read, periodic, cell centres at (i+0.5)dcell */
+#define SMK_INTERP_PIXELS 1    /* no box read: delta_l, eta_par, z given per pixel      */
+                               /* (the merge_spectra input, bin/merge_spectra.py:282-300) */
+
+#define SMK_SS_NONE 0     /* no small-scale field                                      */
+#define SMK_SS_HOST 1     /* white noise given per skewer (length nz_s)                 */
+#define SMK_SS_PHILOX 2   /* Gaussian modes drawn on the GPU in Fourier space            */
+
+#define SMK_ABC_CONST 0    /* a, b, c constants                                        */
+#define SMK_ABC_POWERLAW 1 /* a(z) = a * ((1+z)/a_zref1)^a_power, b, c constants        */
+#define SMK_ABC_TABLE 2    /* a, b, c linear in z on a uniform table [z_tab0, +dz_tab)  */
+
+#define SMK_G_ONE 0        /* growth G = 1                                             */
+#define SMK_G_MERGE 1      /* G(z) = growth24 * (1+2.4) / (1+z)                        */
+
+typedef struct {
+    int64_t n;             /* number of skewers                                         */
+    const float* start;    /* [n][3] first pixel, box-corner frame, Mpc/h                */
+    const float* dir;      /* [n][3] unit direction                                      */
+    const int32_t* npix;   /* [n] pixels                                                 */
+    const int64_t* offset; /* [n] index of the skewer's first pixel in the packed outputs */
+    double dpix;           /* pixel spacing along the skewer, Mpc/h                      */
+    const int32_t* order;  /* [n_slots] schedule from smk_skewer_schedule (device)       */
+    int64_t n_slots;       /* 2 * work items                                             */
+    const float* pix_delta;/* SMK_INTERP_PIXELS: packed delta_l per pixel                */
+    const float* pix_eta;  /* SMK_INTERP_PIXELS: packed eta_par per pixel (NULL: no RSD)  */
+    const float* pix_z;    /* SMK_INTERP_PIXELS: packed redshift per pixel               */
+} SmkSkewers;
+
+typedef struct {
+    /* boxes */
+    int32_t nx, ny, nz;
+    int64_t pitch;         /* floats between consecutive (x,y) rows of the boxes          */
+    double dcell;
+    int32_t interp;        /* SMK_INTERP_TRILINEAR                                        */
+    /* small scales (bin/merge_spectra.py:303-331) */
+    int32_t ss_mode;       /* SMK_SS_NONE / SMK_SS_HOST / SMK_SS_PHILOX                   */
+    int32_t ss_nz;         /* FFT length (power of two 256..4096) or 0: 256*2^n >= npix+50 */
+    const float* ss_scale; /* sqrt(P1Dmiss(k)/pixsize) for nz = 256<<j, j = 0..4, table j  */
+                           /* (nz/2+1 floats) at offset sum_{i<j} ((256<<i)/2+1)           */
+    const float* ss_noise; /* SMK_SS_HOST: noise of skewer s at ss_noise_offset[s]          */
+    const int64_t* ss_noise_offset;
+    uint64_t seed;         /* SMK_SS_PHILOX                                               */
+    /* FGPA (util.fgpa, py/SaclayMocks/util.py:421-433) */
+    int32_t abc_mode;
+    float a, b, c;
+    float a_zref1, a_power;
+    const float* abc_tab;  /* SMK_ABC_TABLE: [n_tab][3] (a,b,c)                            */
+    int32_t n_tab;
+    float z_tab0, dz_tab;
+    float z_lo, z_hi;      /* redshift mapped linearly along x: z = z_lo + (z_hi-z_lo) x/Lx */
+    int32_t growth_mode;   /* SMK_G_ONE / SMK_G_MERGE                                     */
+    float growth24;        /* fgrowth(2.4) for SMK_G_MERGE                                */
+} SmkSpectraParams;
+
+/* Host: build the work schedule of smk_skewers_flux from the host copy of npix.  Skewers
+ * are grouped by small-scale FFT length, longest first, in pairs of equal length (one
+ * complex FFT carries two skewers); order_out must hold 2*n + 16 ints, n_slots_out gets
+ * the used length (even; empty slots are -1).  ss_nz is SmkSpectraParams.ss_nz: 0 applies
+ * the rule nz = 256*2^k >= npix + 50 (SMK_ENOTSUPP beyond 4096), a fixed nz must be
+ * >= every npix (SMK_EINVAL otherwise); a negative ss_nz (small-scale field off) pairs
+ * skewers by length only. */
+int smk_skewer_schedule(int64_t n, const int32_t* npix_host, int32_t ss_nz, int32_t* order_out,
+                        int64_t* n_slots_out);
+
+/* Workspace bytes smk_skewers_flux needs (the persistent launch's work counter). */
+size_t smk_skewers_workspace_size(const SmkSkewers* sk, const SmkSpectraParams* p);
+
+/*
+ * Replaces bin/make_spectra.py ReadSpec (:90-139, trilinear read instead of the Gaussian
+ * 7^3 read) + the small-scale loop and FGPA of bin/merge_spectra.py (:303-339).  For every
+ * pixel: delta_l, eta_par by trilinear read of the boxes (eta may be NULL: no RSD) or, with
+ * SMK_INTERP_PIXELS, from the per-pixel arrays of the skewer table (boxes unused, may be
+ * NULL; the redshift is then pix_z instead of the z_lo..z_hi map along x);
+ * delta = delta_l + delta_s, F = exp(-a exp(b G (delta + c eta_par))).  flux receives F
+ * in the packed layout; delta_out / eta_out / z_out (may be NULL) receive delta_l+delta_s,
+ * eta_par and the redshift of each pixel.
+ */
+int smk_skewers_flux(const SmkSkewers* sk, const SmkSpectraParams* p, const float* delta_box,
+                     const float* eta_box, float* flux, float* delta_out, float* eta_out,
+                     float* z_out, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---------------------------------------------------------------- FGPA (util.fgpa) */
+/*
+ * Replaces util.fgpa (py/SaclayMocks/util.py:421-433) as called from
+ * bin/merge_spectra.py:337 and fit_az.py:251: flux[i] = exp(-a exp(b G (delta + c eta))).
+ * eta may be NULL (no RSD: bin/merge_spectra.py:339).  Each of G, a, b, c is a per-element
+ * device array, or NULL to use the scalar that follows it.
+ */
+int smk_fgpa(int64_t n, const float* delta, const float* eta, const float* G, float G0,
+             const float* a, float a0, const float* b, float b0, const float* c, float c0,
+             float* flux, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SMK_H */

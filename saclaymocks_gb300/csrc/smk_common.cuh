@@ -1,0 +1,120 @@
+// Shared device/host helpers of libsmk: status reporting, complex arithmetic,
+// Philox4x32-10 counter-based random numbers, twiddle factors.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/smk.h"
+
+namespace smk {
+
+// ------------------------------------------------------------------ status (host)
+// Records a message for smk_last_error() and returns the code.
+int fail(int code, const char* fmt, ...);
+// Checks cudaGetLastError() after launches: SMK_ECUDA with the CUDA message on failure.
+int check_launch(const char* what);
+
+inline int64_t div_up(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// ------------------------------------------------------------------ complex helpers
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {  // a * conj(b)
+    return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+// exp(-2 pi i m / n) for 0 <= m < n <= 2^24.  The angle is reduced to a quadrant with
+// integer arithmetic so the float argument of sincospif stays in [0, 0.5) and is the
+// correctly rounded value of rem/(2n): the twiddle is accurate to about 1 ulp.
+__device__ __forceinline__ float2 twiddle(int m, int n) {
+    const int m4 = 4 * m;
+    const int q = m4 / n;
+    const int rem = m4 - q * n;
+    float s, c;
+    sincospif(0.5f * ((float)rem / (float)n), &s, &c);
+    // angle = q*pi/2 + phi, phi = (pi/2)*rem/n; result = (cos(angle), -sin(angle))
+    switch (q & 3) {
+        case 0: return make_float2(c, -s);
+        case 1: return make_float2(-s, -c);
+        case 2: return make_float2(-c, s);
+        default: return make_float2(s, c);
+    }
+}
+
+// ------------------------------------------------------------------ asynchronous copies
+// cp.async global -> shared of `bytes` (4, 8 or 16) with zero fill of the rest of the
+// `size`-byte slot: no register staging, so a thread keeps many copies in flight.  A
+// source that is not read (src_bytes == 0) is still given a valid address by the caller.
+template <int SIZE>
+__device__ __forceinline__ void cp_async(void* smem_dst, const void* gmem_src, int src_bytes) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    if (SIZE == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gmem_src), "r"(src_bytes));
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(d), "l"(gmem_src), "n"(SIZE),
+                     "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// ------------------------------------------------------------------ Philox4x32-10
+// Counter-based generator of Salmon, Moraes, Dror & Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3" (SC'11): 10 rounds of the 4x32 Philox bijection keyed by the seed.
+struct u32x4 { uint32_t v[4]; };
+
+__host__ __device__ __forceinline__ u32x4 philox4x32_10(u32x4 ctr, uint32_t k0, uint32_t k1) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+    const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = (uint64_t)M0 * ctr.v[0];
+        const uint64_t p1 = (uint64_t)M1 * ctr.v[2];
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        u32x4 o;
+        o.v[0] = hi1 ^ ctr.v[1] ^ k0;
+        o.v[1] = lo1;
+        o.v[2] = hi0 ^ ctr.v[3] ^ k1;
+        o.v[3] = lo0;
+        ctr = o;
+        k0 += W0;
+        k1 += W1;
+    }
+    return ctr;
+}
+
+// Stream tags keep the GRF box noise and the skewer noise in disjoint counter spaces.
+enum : uint32_t { STREAM_BOX = 0x42u, STREAM_SKEWER = 0x53u };
+
+// Four N(0,1) deviates from one Philox block: Box-Muller on (u0,u1) and (u2,u3) with
+// u = ((x >> 8) + 1) * 2^-24 in (0, 1] for the radius and (x >> 8) * 2^-23 in [0, 2)
+// as the angle in units of pi (both exact in float32).
+__device__ __forceinline__ void gauss4(u32x4 r, float g[4]) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const float u1 = (float)((r.v[2 * h] >> 8) + 1u) * 5.9604644775390625e-08f;  // 2^-24
+        const float t = (float)(r.v[2 * h + 1] >> 8) * 1.1920928955078125e-07f;       // 2^-23
+        const float rad = sqrtf(-2.0f * logf(u1));
+        float s, c;
+        sincospif(t, &s, &c);
+        g[2 * h] = rad * c;
+        g[2 * h + 1] = rad * s;
+    }
+}
+
+// Gaussians of group q (cells 4q..4q+3) of row `row` for seed `seed`, stream `tag`.
+__device__ __forceinline__ void philox_gauss4(uint64_t seed, uint64_t row, uint32_t q, uint32_t tag,
+                                              float g[4]) {
+    u32x4 c;
+    c.v[0] = q;
+    c.v[1] = (uint32_t)row;
+    c.v[2] = (uint32_t)(row >> 32);
+    c.v[3] = tag;
+    gauss4(philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32)), g);
+}
+
+}  // namespace smk

@@ -1,0 +1,123 @@
+// Host-side pieces of libsmk: status strings, thread-local error message, FFT radix plans,
+// and the skewer work schedule.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "smk_fft.cuh"
+
+namespace smk {
+
+static thread_local char g_last_error[512] = "";
+
+int fail(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int check_launch(const char* what) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(SMK_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+    return SMK_OK;
+}
+
+bool make_plan(int n, FftPlan* p) {
+    if (n < 2 || n > FFT_MAX_N) return false;
+    int m = n, p2 = 0, p3 = 0, p5 = 0;
+    while (m % 2 == 0) { m /= 2; ++p2; }
+    while (m % 3 == 0) { m /= 3; ++p3; }
+    while (m % 5 == 0) { m /= 5; ++p5; }
+    if (m != 1) return false;
+    int rad[32], nr = 0;
+    while (p2 >= 3 && p2 - 3 != 1) { rad[nr++] = 8; p2 -= 3; }
+    while (p2 >= 2) { rad[nr++] = 4; p2 -= 2; }
+    if (p2 == 1) rad[nr++] = 2;
+    for (int i = 0; i < p3; ++i) rad[nr++] = 3;
+    for (int i = 0; i < p5; ++i) rad[nr++] = 5;
+    if (nr > FFT_MAX_STAGES) return false;
+    p->n = n;
+    p->nst = nr;
+    int L = n;
+    for (int s = 0; s < nr; ++s) {
+        p->r[s] = rad[s];
+        p->m[s] = L / rad[s];
+        p->tstep[s] = n / L;
+        p->magic[s] = p->m[s] == 1 ? 0u : (uint32_t)((1ull << 32) / (uint64_t)p->m[s] + 1ull);
+        L = p->m[s];
+    }
+    return true;
+}
+
+}  // namespace smk
+
+extern "C" {
+
+const char* smk_strerror(int status) {
+    switch (status) {
+        case SMK_OK: return "SMK_OK";
+        case SMK_EINVAL: return "SMK_EINVAL: invalid argument";
+        case SMK_ENOTSUPP: return "SMK_ENOTSUPP: size not supported by the kernels";
+        case SMK_ECUDA: return "SMK_ECUDA: CUDA error";
+        case SMK_EWORKSPACE: return "SMK_EWORKSPACE: workspace missing or too small";
+        case SMK_ENULLBOX: return "SMK_ENULLBOX: box is null or holds non-finite values";
+        default: return "SMK_E?: unknown status";
+    }
+}
+
+const char* smk_last_error(void) { return smk::g_last_error; }
+
+int smk_version(void) { return 100; }
+
+int smk_fft_supported(int32_t n) {
+    smk::FftPlan p;
+    return smk::make_plan(n, &p) ? 1 : 0;
+}
+
+int smk_skewer_schedule(int64_t n, const int32_t* npix_host, int32_t ss_nz, int32_t* order_out,
+                        int64_t* n_slots_out) {
+    if (n < 0 || (n > 0 && (!npix_host || !order_out)) || !n_slots_out)
+        return smk::fail(SMK_EINVAL, "smk_skewer_schedule: null argument");
+    if (n > INT32_MAX) return smk::fail(SMK_EINVAL, "smk_skewer_schedule: too many skewers");
+    // order: small-scale FFT length (the pairing constraint), then length, both descending
+    struct Key { int32_t nz, np, s; };
+    std::vector<Key> key((size_t)n);
+    for (int64_t s = 0; s < n; ++s) {
+        const int32_t np = npix_host[s];
+        if (np < 0) return smk::fail(SMK_EINVAL, "smk_skewer_schedule: negative npix");
+        int32_t nz = ss_nz;
+        if (nz < 0) {
+            nz = 0;  // no small-scale field: one class, pairs by length only
+        } else if (nz == 0) {
+            nz = 256;
+            while (nz < np + 50 && nz <= smk::FFT_MAX_N) nz *= 2;
+            if (nz > smk::FFT_MAX_N)
+                return smk::fail(SMK_ENOTSUPP, "smk_skewer_schedule: skewer %lld needs a "
+                                 "small-scale FFT longer than %d", (long long)s, smk::FFT_MAX_N);
+        } else if (np > nz) {
+            return smk::fail(SMK_EINVAL, "smk_skewer_schedule: skewer %lld has %d pixels, more "
+                             "than the small-scale FFT length %d", (long long)s, np, nz);
+        }
+        key[(size_t)s] = {nz, np, (int32_t)s};
+    }
+    std::stable_sort(key.begin(), key.end(), [](const Key& a, const Key& b) {
+        return a.nz != b.nz ? a.nz > b.nz : a.np > b.np;
+    });
+    int64_t k = 0;
+    for (size_t i = 0; i < key.size();) {
+        size_t j = i;
+        while (j < key.size() && key[j].nz == key[i].nz) ++j;
+        for (size_t q = i; q < j; ++q) order_out[k++] = key[q].s;
+        if ((j - i) & 1) order_out[k++] = -1;
+        i = j;
+    }
+    *n_slots_out = k;
+    return SMK_OK;
+}
+
+}  // extern "C"

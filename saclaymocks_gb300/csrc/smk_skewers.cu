@@ -1,0 +1,358 @@
+// Fused skewer stage on GB300: trilinear read of the delta / eta_par boxes along each
+// skewer + missing small-scale 1D power (one complex FFT carries the Gaussian fields of two
+// skewers) + FGPA flux, in one persistent launch.
+//
+// Work items are pairs of skewers with the same small-scale FFT length (host schedule,
+// longest first); blocks take items from an atomic counter.  Per item:
+//   1. delta_s of both skewers in shared memory (SMK_SS_HOST: noise -> FFT -> x S_k -> IFFT;
+//      SMK_SS_PHILOX: Gaussian modes drawn directly in Fourier space -> IFFT),
+//   2. every pixel: position -> 8-corner trilinear read of delta (and eta), redshift,
+//      a(z), b, c, G(z), F = exp(-a exp(b G (delta_l + delta_s + c eta))).
+#include <algorithm>
+
+#include "smk_fft.cuh"
+
+namespace smk {
+
+constexpr int SK_T = 256;
+constexpr int SK_NCLASS = 5;  // small-scale FFT lengths 256 << j
+
+struct SkArgs {
+    const float* start;
+    const float* dir;
+    const int32_t* npix;
+    const int64_t* offset;
+    double dpix;
+    const int32_t* order;
+    int64_t n_items;
+    int interp;
+    const float* pix_delta;
+    const float* pix_eta;
+    const float* pix_z;
+    const float* delta;
+    const float* eta;
+    int nx, ny, nz;
+    int64_t pitch;
+    double dcell;
+    int ss_mode, ss_nz;
+    const float* ss_scale;
+    const float* ss_noise;
+    const int64_t* ss_noise_offset;
+    uint64_t seed;
+    FftPlan plans[SK_NCLASS];
+    int abc_mode;
+    float a, b, c, a_zref1, a_power;
+    const float* abc_tab;
+    int n_tab;
+    float z_tab0, dz_tab;
+    float z_lo, z_hi;
+    int growth_mode;
+    float growth24;
+    float* flux;
+    float* delta_out;
+    float* eta_out;
+    float* z_out;
+    unsigned long long* counter;
+};
+
+__device__ __forceinline__ int ss_class(int nzz) {
+    int j = 0;
+    while ((256 << j) < nzz) ++j;
+    return j;
+}
+
+__device__ __forceinline__ int ss_table_offset(int j) {
+    int off = 0;
+    for (int i = 0; i < j; ++i) off += (256 << i) / 2 + 1;
+    return off;
+}
+
+__device__ __forceinline__ int wrap(int64_t c, int n) {
+    int64_t r = c % n;
+    return (int)(r < 0 ? r + n : r);
+}
+
+struct SkewerGeo {
+    int i0[3];     // cell index of the first pixel's lower corner, wrapped
+    float f0[3];   // fractional coordinate (cells) of the first pixel above i0
+    float step[3]; // pixel step in cells
+};
+
+__global__ void __launch_bounds__(SK_T, 2) skewer_kernel(const SkArgs a) {
+    extern __shared__ float2 smem[];
+    float2* s = smem;                                          // FFT_MAX_N
+    float2* tw = smem + FFT_MAX_N;                             // FFT_MAX_N
+    int* sof = reinterpret_cast<int*>(smem + 2 * FFT_MAX_N);   // slot of each frequency
+    __shared__ long long item_sh;
+    __shared__ SkewerGeo geo[2];
+    __shared__ int sk_id[2], sk_np[2];
+    __shared__ int64_t sk_off[2];
+    int cur_nz = 0;
+    const int dims[3] = {a.nx, a.ny, a.nz};
+    for (;;) {
+        if (threadIdx.x == 0) item_sh = (long long)atomicAdd(a.counter, 1ULL);
+        __syncthreads();
+        const long long item = item_sh;
+        if (item >= a.n_items) break;
+        if (threadIdx.x < 2) {
+            const int t = threadIdx.x;
+            const int sid = a.order[2 * item + t];
+            sk_id[t] = sid;
+            sk_np[t] = sid >= 0 ? a.npix[sid] : 0;
+            sk_off[t] = sid >= 0 ? a.offset[sid] : 0;
+            if (sid >= 0 && a.interp == SMK_INTERP_TRILINEAR) {
+                for (int d = 0; d < 3; ++d) {
+                    const double u0 = (double)a.start[3 * sid + d] / a.dcell - 0.5;
+                    const double fl = floor(u0);
+                    geo[t].i0[d] = wrap((int64_t)fl, dims[d]);
+                    geo[t].f0[d] = (float)(u0 - fl);
+                    geo[t].step[d] = (float)(a.dpix * (double)a.dir[3 * sid + d] / a.dcell);
+                }
+            }
+        }
+        __syncthreads();
+        const int np0 = sk_np[0], np1 = sk_np[1];
+        float inv_nz = 0.f;
+        if (a.ss_mode != SMK_SS_NONE) {
+            int nzz = a.ss_nz;
+            if (nzz <= 0) {
+                nzz = 256;
+                while (nzz < np0 + 50) nzz *= 2;
+            }
+            const int cls = ss_class(nzz);
+            const FftPlan& pl = a.plans[cls];
+            if (nzz != cur_nz) {
+                fill_twiddles<SK_T>(tw, nzz);
+                for (int k = threadIdx.x; k < nzz; k += SK_T) sof[k] = slot_of_freq(pl, k);
+                cur_nz = nzz;
+                __syncthreads();
+            }
+            const float* S = a.ss_scale + ss_table_offset(cls);
+            const int half = nzz / 2;
+            if (a.ss_mode == SMK_SS_HOST) {
+                const float* n0 = a.ss_noise + a.ss_noise_offset[sk_id[0]];
+                const float* n1 = sk_id[1] >= 0 ? a.ss_noise + a.ss_noise_offset[sk_id[1]] : nullptr;
+                for (int e = threadIdx.x; e < nzz; e += SK_T)
+                    s[e] = make_float2(__ldg(n0 + e), n1 ? __ldg(n1 + e) : 0.f);
+                __syncthreads();
+                fft_tile<false, 1, 1, SK_T>(s, tw, pl);
+                for (int e = threadIdx.x; e < nzz; e += SK_T) {
+                    const int f = freq_of_slot(pl, e);
+                    s[e] = cscale(s[e], __ldg(S + (f <= half ? f : nzz - f)));
+                }
+                __syncthreads();
+            } else {
+                // Fourier modes of two white-noise fields: X_k = sqrt(nz/2)(g_re + i g_im), X_0 and
+                // X_{nz/2} real with variance nz; Z_k = S_k (X0_k + i X1_k), Z_{nz-k} = S_k (X0_k* + i X1_k*)
+                const float rh = sqrtf(0.5f * (float)nzz), r1 = sqrtf((float)nzz);
+                for (int j = threadIdx.x; 2 * j <= half; j += SK_T) {
+                    float g[2][4];
+#pragma unroll
+                    for (int t = 0; t < 2; ++t) {
+                        if (sk_id[t] >= 0)
+                            philox_gauss4(a.seed, (uint64_t)sk_id[t], (uint32_t)j, STREAM_SKEWER, g[t]);
+                        else
+                            g[t][0] = g[t][1] = g[t][2] = g[t][3] = 0.f;
+                    }
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int k = 2 * j + h;
+                        if (k > half) break;
+                        const float sk = __ldg(S + k);
+                        if (k == 0 || k == half) {
+                            s[sof[k]] = make_float2(sk * r1 * g[0][2 * h], sk * r1 * g[1][2 * h]);
+                        } else {
+                            const float ar = rh * g[0][2 * h], ai = rh * g[0][2 * h + 1];
+                            const float br = rh * g[1][2 * h], bi = rh * g[1][2 * h + 1];
+                            s[sof[k]] = make_float2(sk * (ar - bi), sk * (ai + br));
+                            s[sof[nzz - k]] = make_float2(sk * (ar + bi), sk * (br - ai));
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+            fft_tile<true, 1, 1, SK_T>(s, tw, pl);
+            inv_nz = 1.0f / (float)nzz;
+        }
+        // pixels of both skewers
+        const int64_t ntot = (int64_t)np0 + np1;
+        const float nxf = (float)a.nx;
+        for (int64_t idx = threadIdx.x; idx < ntot; idx += SK_T) {
+            const int t = idx < np0 ? 0 : 1;
+            const int i = (int)(idx - (t ? np0 : 0));
+            const int64_t o = sk_off[t] + i;
+            float dl, et, z;
+            if (a.interp == SMK_INTERP_PIXELS) {
+                dl = __ldg(a.pix_delta + o);
+                et = a.pix_eta ? __ldg(a.pix_eta + o) : 0.f;
+                z = __ldg(a.pix_z + o);
+            } else {
+                const SkewerGeo& g = geo[t];
+                int c0[3], c1[3];
+                float fr[3];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    const float v = fmaf((float)i, g.step[d], g.f0[d]);
+                    const float fl = floorf(v);
+                    fr[d] = v - fl;
+                    c0[d] = wrap((int64_t)g.i0[d] + (int64_t)fl, dims[d]);
+                    c1[d] = c0[d] + 1 == dims[d] ? 0 : c0[d] + 1;
+                }
+                const int64_t r00 = ((int64_t)c0[0] * a.ny + c0[1]) * a.pitch;
+                const int64_t r01 = ((int64_t)c0[0] * a.ny + c1[1]) * a.pitch;
+                const int64_t r10 = ((int64_t)c1[0] * a.ny + c0[1]) * a.pitch;
+                const int64_t r11 = ((int64_t)c1[0] * a.ny + c1[1]) * a.pitch;
+                const float wx1 = fr[0], wx0 = 1.f - fr[0], wy1 = fr[1], wy0 = 1.f - fr[1];
+                const float wz1 = fr[2], wz0 = 1.f - fr[2];
+                const int z0 = c0[2], z1 = c1[2];
+                auto tri = [&](const float* __restrict__ box) {
+                    const float v00 = wz0 * __ldg(box + r00 + z0) + wz1 * __ldg(box + r00 + z1);
+                    const float v01 = wz0 * __ldg(box + r01 + z0) + wz1 * __ldg(box + r01 + z1);
+                    const float v10 = wz0 * __ldg(box + r10 + z0) + wz1 * __ldg(box + r10 + z1);
+                    const float v11 = wz0 * __ldg(box + r11 + z0) + wz1 * __ldg(box + r11 + z1);
+                    return wx0 * (wy0 * v00 + wy1 * v01) + wx1 * (wy0 * v10 + wy1 * v11);
+                };
+                dl = tri(a.delta);
+                et = a.eta ? tri(a.eta) : 0.f;
+                // redshift from the wrapped x coordinate: x / dcell = c0x + frx + 0.5
+                float xc = (float)c0[0] + fr[0] + 0.5f;
+                if (xc >= nxf) xc -= nxf;
+                z = a.z_lo + (a.z_hi - a.z_lo) * (xc / nxf);
+            }
+            float ds = 0.f;
+            if (a.ss_mode != SMK_SS_NONE) ds = (t ? s[i].y : s[i].x) * inv_nz;
+            float pa = a.a, pb = a.b, pc = a.c;
+            if (a.abc_mode == SMK_ABC_POWERLAW) {
+                pa = a.a * powf((1.0f + z) / a.a_zref1, a.a_power);
+            } else if (a.abc_mode == SMK_ABC_TABLE) {
+                const float tt = (z - a.z_tab0) / a.dz_tab;
+                int it = (int)floorf(tt);
+                it = max(0, min(a.n_tab - 2, it));
+                const float ft = fminf(fmaxf(tt - (float)it, 0.f), 1.f);
+                const float* r0 = a.abc_tab + 3 * it;
+                pa = fmaf(ft, __ldg(r0 + 3) - __ldg(r0), __ldg(r0));
+                pb = fmaf(ft, __ldg(r0 + 4) - __ldg(r0 + 1), __ldg(r0 + 1));
+                pc = fmaf(ft, __ldg(r0 + 5) - __ldg(r0 + 2), __ldg(r0 + 2));
+            }
+            const float G = a.growth_mode == SMK_G_MERGE ? a.growth24 * 3.4f / (1.0f + z) : 1.0f;
+            const float dtot = dl + ds;
+            const float F = expf(-pa * expf(pb * G * (dtot + pc * et)));
+            a.flux[o] = F;
+            if (a.delta_out) a.delta_out[o] = dtot;
+            if (a.eta_out) a.eta_out[o] = et;
+            if (a.z_out) a.z_out[o] = z;
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace smk
+
+using namespace smk;
+
+extern "C" {
+
+size_t smk_skewers_workspace_size(const SmkSkewers* sk, const SmkSpectraParams* p) {
+    (void)sk;
+    (void)p;
+    return 256;  // work counter
+}
+
+int smk_skewers_flux(const SmkSkewers* sk, const SmkSpectraParams* p, const float* delta_box,
+                     const float* eta_box, float* flux, float* delta_out, float* eta_out, float* z_out,
+                     void* workspace, size_t workspace_bytes, void* stream) {
+    if (!sk || !p || !flux) return fail(SMK_EINVAL, "smk_skewers_flux: null argument");
+    if (p->interp == SMK_INTERP_TRILINEAR && !delta_box)
+        return fail(SMK_EINVAL, "smk_skewers_flux: trilinear read needs the delta box");
+    if (p->interp == SMK_INTERP_PIXELS && (!sk->pix_delta || !sk->pix_z))
+        return fail(SMK_EINVAL, "smk_skewers_flux: SMK_INTERP_PIXELS needs pix_delta and pix_z");
+    if (sk->n < 0 || sk->n_slots < 0 || (sk->n_slots & 1)) return fail(SMK_EINVAL, "smk_skewers_flux: bad counts");
+    if (sk->n_slots == 0) return SMK_OK;
+    if (!sk->npix || !sk->offset || !sk->order) return fail(SMK_EINVAL, "smk_skewers_flux: null skewer table array");
+    if (p->interp == SMK_INTERP_TRILINEAR) {
+        if (!sk->start || !sk->dir) return fail(SMK_EINVAL, "smk_skewers_flux: null start/dir");
+        if (p->nx < 1 || p->ny < 1 || p->nz < 1 || p->pitch < p->nz || !(p->dcell > 0) || !(sk->dpix > 0))
+            return fail(SMK_EINVAL, "smk_skewers_flux: bad box geometry");
+    } else if (p->interp != SMK_INTERP_PIXELS) {
+        return fail(SMK_EINVAL, "smk_skewers_flux: unknown interp");
+    }
+    if (p->ss_mode != SMK_SS_NONE && p->ss_mode != SMK_SS_HOST && p->ss_mode != SMK_SS_PHILOX)
+        return fail(SMK_EINVAL, "smk_skewers_flux: unknown ss_mode");
+    if (p->ss_mode != SMK_SS_NONE) {
+        if (!p->ss_scale) return fail(SMK_EINVAL, "smk_skewers_flux: null ss_scale");
+        if (p->ss_nz != 0 && (p->ss_nz < 256 || p->ss_nz > FFT_MAX_N || (p->ss_nz & (p->ss_nz - 1))))
+            return fail(SMK_EINVAL, "smk_skewers_flux: ss_nz must be 0 or a power of two in 256..4096");
+        if (p->ss_mode == SMK_SS_HOST && (!p->ss_noise || !p->ss_noise_offset))
+            return fail(SMK_EINVAL, "smk_skewers_flux: SMK_SS_HOST needs ss_noise and offsets");
+    }
+    if (p->abc_mode == SMK_ABC_TABLE && (!p->abc_tab || p->n_tab < 2 || !(p->dz_tab > 0)))
+        return fail(SMK_EINVAL, "smk_skewers_flux: bad a,b,c table");
+    if (p->abc_mode == SMK_ABC_POWERLAW && !(p->a_zref1 > 0))
+        return fail(SMK_EINVAL, "smk_skewers_flux: a_zref1 must be > 0");
+    if (p->abc_mode < SMK_ABC_CONST || p->abc_mode > SMK_ABC_TABLE)
+        return fail(SMK_EINVAL, "smk_skewers_flux: unknown abc_mode");
+    if (!workspace || workspace_bytes < smk_skewers_workspace_size(sk, p))
+        return fail(SMK_EWORKSPACE, "smk_skewers_flux: needs %zu workspace bytes",
+                    smk_skewers_workspace_size(sk, p));
+    SkArgs a;
+    a.start = sk->start;
+    a.dir = sk->dir;
+    a.npix = sk->npix;
+    a.offset = sk->offset;
+    a.dpix = sk->dpix;
+    a.order = sk->order;
+    a.n_items = sk->n_slots / 2;
+    a.interp = p->interp;
+    a.pix_delta = sk->pix_delta;
+    a.pix_eta = sk->pix_eta;
+    a.pix_z = sk->pix_z;
+    a.delta = delta_box;
+    a.eta = eta_box;
+    a.nx = p->nx;
+    a.ny = p->ny;
+    a.nz = p->nz;
+    a.pitch = p->pitch;
+    a.dcell = p->dcell;
+    a.ss_mode = p->ss_mode;
+    a.ss_nz = p->ss_nz;
+    a.ss_scale = p->ss_scale;
+    a.ss_noise = p->ss_noise;
+    a.ss_noise_offset = p->ss_noise_offset;
+    a.seed = p->seed;
+    for (int j = 0; j < SK_NCLASS; ++j) make_plan(256 << j, &a.plans[j]);
+    a.abc_mode = p->abc_mode;
+    a.a = p->a;
+    a.b = p->b;
+    a.c = p->c;
+    a.a_zref1 = p->a_zref1;
+    a.a_power = p->a_power;
+    a.abc_tab = p->abc_tab;
+    a.n_tab = p->n_tab;
+    a.z_tab0 = p->z_tab0;
+    a.dz_tab = p->dz_tab;
+    a.z_lo = p->z_lo;
+    a.z_hi = p->z_hi;
+    a.growth_mode = p->growth_mode;
+    a.growth24 = p->growth24;
+    a.flux = flux;
+    a.delta_out = delta_out;
+    a.eta_out = eta_out;
+    a.z_out = z_out;
+    a.counter = reinterpret_cast<unsigned long long*>(workspace);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), st) != cudaSuccess)
+        return check_launch("cudaMemsetAsync(counter)");
+    const size_t smem = 2 * FFT_MAX_N * sizeof(float2) + FFT_MAX_N * sizeof(int);
+    if (cudaFuncSetAttribute(skewer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return check_launch("cudaFuncSetAttribute(skewer_kernel)");
+    int per_sm = 0, dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, skewer_kernel, SK_T, smem) != cudaSuccess)
+        return check_launch("occupancy(skewer_kernel)");
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(a.n_items, (int64_t)std::max(per_sm, 1) * nsm));
+    skewer_kernel<<<grid, SK_T, smem, st>>>(a);
+    return check_launch("skewer_kernel");
+}
+
+}  // extern "C"

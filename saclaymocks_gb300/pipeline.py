@@ -1,0 +1,72 @@
+"""One mock chunk end to end: the public call a user makes with HOST arrays.
+
+``MockChunk(...).run(start, direction, npix)`` does what the make_boxes -> make_spectra ->
+merge_spectra chain of the reference does for one chunk (bin/make_boxes.py main :131-437,
+bin/make_spectra.py main :31-606, bin/merge_spectra.py main :16-420): GRF delta and eta_par
+boxes, skewer read, small scales, FGPA, and returns the flux of every pixel to the host.
+Boxes and all intermediates stay in HBM; only the skewer table goes in and the flux comes
+out (pinned host buffers, asynchronous copies on the chunk's stream).
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib, grf, spectra
+
+
+class MockChunk:
+    def __init__(self, nx, ny, nz, dcell=2.19, *, seed=1, k0=0.02, want_eta=True,
+                 cfg: spectra.SpectraConfig | None = None, dpix=0.2, device="cuda"):
+        self.nx, self.ny, self.nz, self.dcell = nx, ny, nz, dcell
+        self.seed, self.k0, self.dpix = seed, k0, dpix
+        self.cfg = cfg or spectra.SpectraConfig()
+        self.device = torch.device(device)
+        self.boxes = grf.alloc_boxes(nx, ny, nz, 1, want_eta, self.device)
+        self.ws = grf.GrfWorkspace(1, self.device)
+        self.amp = grf.pk_normalisation(nx, ny, nz, dcell, k0)
+        self.stream = torch.cuda.current_stream(self.device)
+        self._runner = None
+        self._key = None
+
+    def _prepare(self, start, direction, npix):
+        """Schedule on the host, pinned staging buffers, device table (H2D on the stream)."""
+        table = spectra.SkewerTable(start, direction, npix, dpix=self.dpix)
+        key = (table.n, table.total_pixels)
+        if self._runner is None or self._key != key:
+            self._runner = spectra.SkewerRunner(table, self.cfg, device=self.device)
+            self._pin_in = [torch.empty(x.shape, dtype=t, pin_memory=True) for x, t in
+                            ((table.start, torch.float32), (table.direction, torch.float32),
+                             (table.npix, torch.int32), (table.offset, torch.int64))]
+            self._pin_order = torch.empty(self._runner.n_slots, dtype=torch.int32, pin_memory=True)
+            self._pin_out = torch.empty(table.total_pixels, dtype=torch.float32, pin_memory=True)
+            self._flux = torch.empty(table.total_pixels, dtype=torch.float32, device=self.device)
+            self._key = key
+        r = self._runner
+        r.table = table
+        order = table.schedule(self.cfg.ss_nz if self.cfg.ss_mode != _lib.SMK_SS_NONE else -1)
+        for pin, arr in zip(self._pin_in, (table.start, table.direction, table.npix, table.offset)):
+            pin.numpy()[...] = arr
+        self._pin_order.numpy()[...] = order
+        for dev, pin in zip((r.d_start, r.d_dir, r.d_npix, r.d_off), self._pin_in):
+            dev.copy_(pin, non_blocking=True)
+        r.d_order.copy_(self._pin_order, non_blocking=True)
+        return r
+
+    def h2d_bytes(self) -> int:
+        return sum(p.numel() * p.element_size() for p in self._pin_in) + self._pin_order.numel() * 4
+
+    def d2h_bytes(self) -> int:
+        return self._pin_out.numel() * 4
+
+    def run(self, start, direction, npix, pass_events=None) -> np.ndarray:
+        """Flux of every pixel (packed, float32, host) for the host skewer table."""
+        r = self._prepare(start, direction, npix)
+        out = grf.make_boxes(self.nx, self.ny, self.nz, self.dcell, seed=self.seed, k0=self.k0,
+                             amp=self.amp, want_eta=self.boxes[1] is not None, out=self.boxes,
+                             workspace=self.ws, pass_events=pass_events)
+        r.run(out.delta_pad[0], out.eta_pad[0] if out.eta_pad is not None else None, nx=self.nx,
+              ny=self.ny, nz=self.nz, pitch=out.pitch, dcell=self.dcell, flux=self._flux)
+        self._pin_out.copy_(self._flux, non_blocking=True)
+        torch.cuda.current_stream(self.device).synchronize()
+        return self._pin_out.numpy()

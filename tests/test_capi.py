@@ -1,0 +1,101 @@
+"""The C-ABI library: it loads without a GPU, exports every function include/smk.h declares,
+and its host-only entry points (plans, pitch, schedule, status checks, argument validation)
+behave as documented."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from saclaymocks_gb300 import _lib, build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _lib.load()
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "smk.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(smk_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_functions()
+    assert len(names) >= 12
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared in smk.h but not exported"
+        assert n in _lib.EXPORTED, f"{n} has no ctypes prototype"
+
+
+def test_fft_support_and_pitch(lib):
+    assert all(lib.smk_fft_supported(n) for n in (2, 3, 5, 16, 18, 600, 1536, 2560, 4000, 4096))
+    assert not any(lib.smk_fft_supported(n) for n in (1, 7, 14, 4097, 8192, 2 * 4096))
+    for nz in (2, 16, 18, 256, 1536):
+        p = lib.smk_grf_pitch(nz)
+        assert p >= 2 * (nz // 2 + 1) and p % 8 == 0 and p - 2 * (nz // 2 + 1) < 8
+
+
+def test_schedule_pairs_equal_fft_lengths(lib):
+    rs = np.random.RandomState(0)
+    npix = rs.randint(1, 2000, 1001).astype(np.int32)
+    order = np.empty(2 * len(npix) + 16, np.int32)
+    n = C.c_int64()
+    assert lib.smk_skewer_schedule(len(npix), npix.ctypes.data, 0, order.ctypes.data, C.byref(n)) == 0
+    o = order[:n.value]
+    assert n.value % 2 == 0
+    assert sorted(o[o >= 0].tolist()) == list(range(len(npix)))   # every skewer exactly once
+    rule = lambda m: 256 * 2 ** int(np.ceil(max(0, np.log2((m + 50) / 256))))  # noqa: E731
+    for a, b in o.reshape(-1, 2):
+        if b >= 0:
+            assert rule(npix[a]) == rule(npix[b])
+            assert npix[a] >= npix[b]
+    # fixed length shorter than a skewer, and lengths past 4096, are rejected
+    assert lib.smk_skewer_schedule(len(npix), npix.ctypes.data, 1024, order.ctypes.data, C.byref(n)) \
+        == _lib.SMK_EINVAL
+    big = np.array([5000], np.int32)
+    assert lib.smk_skewer_schedule(1, big.ctypes.data, 0, order.ctypes.data, C.byref(n)) == _lib.SMK_ENOTSUPP
+    assert lib.smk_skewer_schedule(1, big.ctypes.data, -1, order.ctypes.data, C.byref(n)) == 0
+
+
+def test_grf_check_flags_null_and_nan_boxes(lib):
+    ok = np.array([1.0, 100.0, 0.0, 0.0])
+    sig = C.c_double()
+    assert lib.smk_grf_check(ok.ctypes.data_as(C.POINTER(C.c_double)), 100, C.byref(sig)) == 0
+    assert sig.value == pytest.approx(np.sqrt(1.0 - 1e-4))
+    zero = np.zeros(4)
+    assert lib.smk_grf_check(zero.ctypes.data_as(C.POINTER(C.c_double)), 100, None) == _lib.SMK_ENULLBOX
+    bad = np.array([1.0, 100.0, 3.0, 0.0])
+    assert lib.smk_grf_check(bad.ctypes.data_as(C.POINTER(C.c_double)), 100, None) == _lib.SMK_ENULLBOX
+    assert b"non-finite" in lib.smk_last_error()
+
+
+def test_argument_validation_needs_no_gpu(lib):
+    """Invalid calls are refused on the host before any CUDA call."""
+    p = _lib.SmkGrfParams(nx=16, ny=16, nz=15, batch=1, dcell=2.19, k0=0.02, amp=1.0,
+                          noise_mode=_lib.SMK_NOISE_PHILOX)
+    assert lib.smk_grf_boxes(C.byref(p), 0x1000, None, None, None, 0, None) == _lib.SMK_EINVAL
+    p.nz = 16
+    p.nx = 14
+    assert lib.smk_grf_boxes(C.byref(p), 0x1000, None, None, None, 0, None) == _lib.SMK_ENOTSUPP
+    p.nx = 16
+    p.amp = 0.0                           # normalisation on the device needs a workspace
+    assert lib.smk_grf_boxes(C.byref(p), 0x1000, None, None, None, 0, None) == _lib.SMK_EWORKSPACE
+    assert lib.smk_grf_boxes(None, 0x1000, None, None, None, 0, None) == _lib.SMK_EINVAL
+    assert lib.smk_fgpa(-1, None, None, None, 0, None, 0, None, 0, None, 0, None, None) == _lib.SMK_EINVAL
+    assert lib.smk_fgpa(0, None, None, None, 0, None, 0, None, 0, None, 0, None, None) == 0
+    sk = _lib.SmkSkewers(n=1, n_slots=3)
+    sp = _lib.SmkSpectraParams()
+    assert lib.smk_skewers_flux(C.byref(sk), C.byref(sp), None, None, 0x1000, None, None, None,
+                                None, 0, None) == _lib.SMK_EINVAL
+    assert lib.smk_strerror(_lib.SMK_ENULLBOX).startswith(b"SMK_ENULLBOX")
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    with pytest.raises(_lib.SmkError):
+        _lib.load(str(tmp_path / "libsmk.so"))

@@ -1,0 +1,147 @@
+"""GRF boxes (make_boxes) on the GPU through the C ABI, against the reference's own output
+(golden boxes from bin/make_boxes.py) and the FP64 oracle.
+
+Tolerance (FP32 FFT path vs the FP64 oracle of the same noise): relative RMS <= 1e-6 and
+max |error| <= 1e-5 * sigma_delta, per field.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from oracle import grf as ograf          # noqa: E402
+from oracle import philox as ophilox     # noqa: E402
+
+REL_RMS = 1e-6
+MAX_ABS_SIGMA = 1e-5
+
+
+@pytest.fixture(scope="module")
+def G():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from saclaymocks_gb300 import grf
+    return grf
+
+
+def _err(gpu, ref):
+    d = gpu.astype(np.float64) - ref.astype(np.float64)
+    sig = np.std(ref)
+    return np.sqrt((d ** 2).mean() / (ref.astype(np.float64) ** 2).mean()), np.abs(d).max() / sig
+
+
+def _check(gpu, ref, tag):
+    rr, ma = _err(gpu, ref)
+    assert rr <= REL_RMS, f"{tag}: relative RMS {rr:.3e}"
+    assert ma <= MAX_ABS_SIGMA, f"{tag}: max abs / sigma {ma:.3e}"
+
+
+@pytest.mark.parametrize("tag", ["cube16", "rect"])
+def test_grf_matches_reference_golden(G, golden, tag):
+    f = golden(f"grf_{tag}.npz")
+    NX, NY, NZ = int(f["NX"]), int(f["NY"]), int(f["NZ"])
+    noise = ograf.draw_noise(NX, NY, NZ, int(f["seed"]))
+    out = G.make_boxes(NX, NY, NZ, float(f["DX"]), noise=torch.from_numpy(noise).cuda(),
+                       k0=float(f["k0"]))
+    torch.cuda.synchronize()
+    d = out.delta[0].cpu().numpy()
+    e = out.eta[0].cpu().numpy()
+    _check(d, f["delta"], "delta vs make_boxes")
+    _check(e, f["eta_zz"], "eta_zz vs make_boxes")
+    o64 = ograf.grf_boxes(noise, float(f["DX"]), float(f["k0"]), eta=("zz",), precision="f64")
+    _check(d, o64["delta"], "delta vs FP64 oracle")
+    _check(e, o64["eta_zz"], "eta_zz vs FP64 oracle")
+    assert out.sigma()[0] == pytest.approx(float(f["sigma"]), rel=1e-5)
+    out.check()
+
+
+def test_grf_pk_grid_mode_is_the_reference_multiply(G, golden):
+    """SMK_PK_GRID multiplies by the reference's own P0 grid (bin/make_boxes.py:290)."""
+    f = golden("grf_cube16.npz")
+    noise = ograf.draw_noise(16, 16, 16, int(f["seed"]))
+    out = G.make_boxes(16, 16, 16, float(f["DX"]), noise=torch.from_numpy(noise).cuda(),
+                       pk_grid=torch.from_numpy(f["P0"]).cuda())
+    torch.cuda.synchronize()
+    _check(out.delta[0].cpu().numpy(), f["delta"], "delta (P-grid) vs make_boxes")
+    _check(out.eta[0].cpu().numpy(), f["eta_zz"], "eta_zz (P-grid) vs make_boxes")
+
+
+# every tile class (n <= 512, <= 1024, <= 2560, <= 4096) on each axis, radices 2, 3, 4, 5, 8
+SHAPES = [(32, 24, 40), (12, 600, 10), (2560, 4, 6), (4, 6, 2560), (6, 4000, 4), (4, 4, 4096),
+          (2, 2, 2), (30, 18, 50), (1024, 8, 12), (10, 1536, 8)]
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=[f"{a}x{b}x{c}" for a, b, c in SHAPES])
+def test_grf_shapes_vs_fp64_oracle(G, shape):
+    nx, ny, nz = shape
+    rs = np.random.RandomState(nx * 7 + ny * 3 + nz)
+    noise = rs.normal(size=shape).astype(np.float32)
+    out = G.make_boxes(nx, ny, nz, 2.19, noise=torch.from_numpy(noise).cuda())
+    torch.cuda.synchronize()
+    o64 = ograf.grf_boxes(noise, 2.19, 0.02, eta=("zz",), precision="f64")
+    _check(out.delta[0].cpu().numpy(), o64["delta"], f"delta {shape}")
+    _check(out.eta[0].cpu().numpy(), o64["eta_zz"], f"eta {shape}")
+    # padding past nz is untouched by nothing else: the view excludes it
+    assert out.delta.shape == (1, nx, ny, nz)
+
+
+def test_grf_batch_equals_single_boxes(G):
+    nx, ny, nz, B = 16, 12, 20, 3
+    rs = np.random.RandomState(5)
+    noise = rs.normal(size=(B, nx, ny, nz)).astype(np.float32)
+    out = G.make_boxes(nx, ny, nz, 2.19, noise=torch.from_numpy(noise).cuda(), batch=B)
+    torch.cuda.synchronize()
+    sig = out.sigma()
+    for b in range(B):
+        o64 = ograf.grf_boxes(noise[b], 2.19, 0.02, eta=("zz",), precision="f64")
+        _check(out.delta[b].cpu().numpy(), o64["delta"], f"batch member {b}")
+        _check(out.eta[b].cpu().numpy(), o64["eta_zz"], f"batch member {b} eta")
+        assert sig[b] == pytest.approx(np.std(o64["delta"]), rel=1e-5)
+
+
+def test_grf_philox_mode_matches_oracle_noise(G):
+    nx, ny, nz, seed = 24, 20, 18, 123
+    out = G.make_boxes(nx, ny, nz, 2.19, seed=seed, batch=2)
+    torch.cuda.synchronize()
+    for b in range(2):
+        noise = ophilox.box_noise(nx, ny, nz, seed + b)
+        o64 = ograf.grf_boxes(noise, 2.19, 0.02, eta=("zz",), precision="f64")
+        _check(out.delta[b].cpu().numpy(), o64["delta"], f"philox delta {b}")
+        _check(out.eta[b].cpu().numpy(), o64["eta_zz"], f"philox eta {b}")
+
+
+def test_grf_philox_recovers_input_pk(G):
+    """GPU noise mode, checked statistically: var(delta) ~ 1 and the measured P(k) matches
+    the input spectrum within cosmic variance in every k bin."""
+    n, dx = 128, 2.19
+    out = G.make_boxes(n, n, n, dx, seed=7, want_eta=False)
+    torch.cuda.synchronize()
+    d = out.delta[0].cpu().numpy()
+    A = ograf.pk_normalisation(n, n, n, dx, 0.02)
+    kb = np.linspace(2 * np.pi / (n * dx), np.pi / dx, 17)
+    km, pm, nm = ograf.measured_pk(d, dx, kb)
+    pin = A * ograf.pk_shape(km, 0.02)
+    ok = nm > 50
+    z = (pm[ok] - pin[ok]) / (pin[ok] * np.sqrt(2.0 / nm[ok]))
+    assert np.all(np.abs(z) < 5), z
+    assert abs(np.mean(z)) < 3.0
+
+
+def test_pk_normalisation_fp64(G):
+    for shape in [(16, 16, 16), (64, 48, 40), (256, 256, 256)]:
+        a = G.pk_normalisation(*shape, 2.19, 0.02)
+        assert a == pytest.approx(ograf.pk_normalisation(*shape, 2.19, 0.02), rel=1e-9)
+
+
+def test_grf_rejects_bad_sizes(G):
+    from saclaymocks_gb300._lib import SmkError, SMK_EINVAL, SMK_ENOTSUPP
+    with pytest.raises(SmkError) as e:
+        G.make_boxes(16, 16, 15)              # odd nz
+    assert e.value.status == SMK_EINVAL
+    with pytest.raises(SmkError) as e:
+        G.make_boxes(14, 16, 16)              # 14 = 2 * 7
+    assert e.value.status == SMK_ENOTSUPP
+    with pytest.raises(SmkError) as e:
+        G.make_boxes(16, 8192, 16)            # axis longer than 4096
+    assert e.value.status == SMK_ENOTSUPP

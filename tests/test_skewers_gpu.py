@@ -1,0 +1,187 @@
+"""Fused skewer kernel (trilinear read + small scales + FGPA) through the C ABI against the
+oracle on the same boxes, skewers and noise; and the merge_spectra golden vectors.
+
+Tolerances (FP32 kernel vs FP64 oracle): |dF| <= 2e-6 (F in [0,1]); delta_l + delta_s and
+eta_par within 1e-5 * sigma_delta.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from oracle import grf as ograf          # noqa: E402
+from oracle import philox as ophilox     # noqa: E402
+from oracle import skewers as osk        # noqa: E402
+
+F_ATOL = 2e-6
+FIELD_TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def env():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from saclaymocks_gb300 import _lib, grf, spectra
+    return _lib, grf, spectra
+
+
+@pytest.fixture(scope="module")
+def boxes(env):
+    _, grf, _ = env
+    nx, ny, nz, dx = 32, 24, 40, 2.19
+    noise = np.random.RandomState(3).normal(size=(nx, ny, nz)).astype(np.float32)
+    out = grf.make_boxes(nx, ny, nz, dx, noise=torch.from_numpy(noise).cuda())
+    torch.cuda.synchronize()
+    return dict(out=out, d=out.delta[0].cpu().numpy().astype(np.float64),
+                e=out.eta[0].cpu().numpy().astype(np.float64), nx=nx, ny=ny, nz=nz, dx=dx)
+
+
+def _run(env, boxes, table, cfg, noise=None):
+    _lib, _, spectra = env
+    r = spectra.SkewerRunner(table, cfg)
+    out = boxes["out"]
+    F, dtot, eta, z = r.run(out.delta_pad[0], out.eta_pad[0], nx=boxes["nx"], ny=boxes["ny"],
+                            nz=boxes["nz"], pitch=out.pitch, dcell=boxes["dx"], noise=noise,
+                            want_fields=True)
+    torch.cuda.synchronize()
+    sp = spectra.split
+    return sp(F, table), sp(dtot, table), sp(eta, table), sp(z, table)
+
+
+def _oracle(boxes, table, fg, small=None, noise1d=None):
+    sk = dict(start=table.start.astype(np.float64), dir=table.direction.astype(np.float64),
+              npix=table.npix)
+    return osk.skewer_flux(boxes["d"], boxes["e"], sk, boxes["dx"], dpix=table.dpix,
+                           fgpa_mode=fg, small=small, noise1d=noise1d)
+
+
+def _cmp(gpu, ref, sig):
+    for s in range(len(ref["F"])):
+        np.testing.assert_allclose(gpu[0][s], ref["F"][s], rtol=0, atol=F_ATOL)
+        np.testing.assert_allclose(gpu[1][s], ref["delta"][s] + ref["delta_s"][s], rtol=0,
+                                   atol=FIELD_TOL * sig)
+        np.testing.assert_allclose(gpu[2][s], ref["eta"][s], rtol=0, atol=FIELD_TOL * sig)
+        np.testing.assert_allclose(gpu[3][s], ref["z"][s], rtol=0, atol=2e-6)
+
+
+def test_parallel_z_trilinear_fgpa_const(env, boxes):
+    """The small plain configuration: z-parallel skewers, trilinear read, a,b,c constant."""
+    _lib, _, spectra = env
+    t = spectra.skewers_parallel_z(40, boxes["nx"], boxes["ny"], 60, boxes["dx"], seed=0)
+    cfg = spectra.SpectraConfig(a=0.1, b=1.6, c=0.5)
+    g = _run(env, boxes, t, cfg)
+    ref = _oracle(boxes, t, dict(kind="const", a=0.1, b=1.6, c=0.5))
+    _cmp(g, ref, np.std(boxes["d"]))
+
+
+def test_cone_skewers_host_noise_small_scales_powerlaw(env, boxes):
+    """Tilted skewers wrapping through the periodic box, host white noise (reference rule
+    nz = 256*2^n >= npix+50), a(z) power law with z along x, G = merge_spectra growth."""
+    _lib, _, spectra = env
+    L = np.array([boxes["nx"], boxes["ny"], boxes["nz"]]) * boxes["dx"]
+    t = spectra.skewers_cone(25, L, seed=4, npix_range=(150, 700))
+    pm = spectra.pmiss_gauss(0.05, 2.0)
+    cfg = spectra.SpectraConfig(ss_mode=_lib.SMK_SS_HOST, ss_nz=0, pmiss=pm,
+                                abc_mode=_lib.SMK_ABC_POWERLAW, a=0.1, a_zref1=3.2, a_power=4.5,
+                                b=1.58, c=0.6, growth=_lib.SMK_G_MERGE)
+    rs = np.random.RandomState(9)
+    noises = [rs.normal(size=osk.nz_rule(int(n))) for n in t.npix]
+    offs = np.concatenate([[0], np.cumsum([len(x) for x in noises])[:-1]]).astype(np.int64)
+    packed = torch.from_numpy(np.concatenate(noises).astype(np.float32)).cuda()
+    g = _run(env, boxes, t, cfg, noise=(packed, torch.from_numpy(offs).cuda()))
+    fg = dict(kind="powerlaw_x", a0=0.1, zref1=3.2, power=4.5, b=1.58, c=0.6, G="merge")
+    ref = _oracle(boxes, t, fg, small=dict(pixsize=0.2, nz="rule", pmiss=pm),
+                  noise1d=[x.astype(np.float32).astype(np.float64) for x in noises])
+    _cmp(g, ref, np.std(boxes["d"]))
+
+
+def test_fixed_nz_philox_small_scales(env, boxes):
+    """Fixed 2048-point small-scale grid with the GPU noise, against the numpy restatement of
+    the same Philox stream."""
+    _lib, _, spectra = env
+    L = np.array([boxes["nx"], boxes["ny"], boxes["nz"]]) * boxes["dx"]
+    t = spectra.skewers_cone(15, L, seed=8, npix_range=(400, 1200))
+    pm = spectra.pmiss_gauss(0.05, 2.0)
+    cfg = spectra.SpectraConfig(ss_mode=_lib.SMK_SS_PHILOX, ss_nz=2048, pmiss=pm, seed=77,
+                                a=0.1, b=1.58, c=0.6)
+    g = _run(env, boxes, t, cfg)
+    scale = osk.small_scale_scale(2048, 0.2, pm)
+    ref = _oracle(boxes, t, dict(kind="const", a=0.1, b=1.58, c=0.6))
+    for s in range(t.n):
+        ds = ophilox.skewer_small_scales(s, 2048, 77, scale, int(t.npix[s]))
+        ref["delta_s"][s] = ds
+        ref["F"][s] = osk.fgpa(ref["delta"][s] + ds, ref["eta"][s], 1.0, 0.1, 1.58, 0.6)
+    _cmp(g, ref, np.std(boxes["d"]))
+
+
+def test_philox_small_scale_variance_matches_sigma_p1d(env, boxes):
+    """Statistical check of the GPU noise mode: std of delta_s vs util.sigma_p1d."""
+    _lib, _, spectra = env
+    n = 4000
+    t = spectra.skewers_parallel_z(n, boxes["nx"], boxes["ny"], 1000, boxes["dx"], seed=1, dpix=0.2)
+    pm = spectra.pmiss_gauss(0.05, 2.0)
+    cfg = spectra.SpectraConfig(ss_mode=_lib.SMK_SS_PHILOX, ss_nz=2048, pmiss=pm, seed=5)
+    r = spectra.SkewerRunner(t, cfg)
+    out = boxes["out"]
+    F, dtot, _, _ = r.run(out.delta_pad[0], out.eta_pad[0], nx=boxes["nx"], ny=boxes["ny"],
+                          nz=boxes["nz"], pitch=out.pitch, dcell=boxes["dx"], want_fields=True)
+    # delta_s = (delta_l + delta_s) - delta_l: rerun without small scales
+    r0 = spectra.SkewerRunner(t, spectra.SpectraConfig())
+    _, dl, _, _ = r0.run(out.delta_pad[0], out.eta_pad[0], nx=boxes["nx"], ny=boxes["ny"],
+                         nz=boxes["nz"], pitch=out.pitch, dcell=boxes["dx"], want_fields=True)
+    ds = (dtot - dl).double().cpu().numpy()
+    expect = osk.sigma_p1d(pm, 0.2, 2048)
+    assert ds.std() == pytest.approx(expect, rel=0.01)
+    assert abs(ds.mean()) < 0.01 * expect
+
+
+def test_abc_table_mode(env, boxes):
+    _lib, _, spectra = env
+    t = spectra.skewers_parallel_z(20, boxes["nx"], boxes["ny"], 80, boxes["dx"], seed=2)
+    zt = np.linspace(1.8, 3.6, 101)
+    tab = np.stack([zt, 0.05 + 0.1 * (zt - 1.8), 1.6 - 0.1 * (zt - 1.8), 0.5 + 0.05 * (zt - 1.8)], 1)
+    cfg = spectra.SpectraConfig(abc_mode=_lib.SMK_ABC_TABLE, abc_table=tab)
+    g = _run(env, boxes, t, cfg)
+    ref = _oracle(boxes, t, dict(kind="const", a=0, b=0, c=0))
+    for s in range(t.n):
+        z = ref["z"][s]
+        a = np.interp(z, zt, tab[:, 1])
+        b = np.interp(z, zt, tab[:, 2])
+        c = np.interp(z, zt, tab[:, 3])
+        ref["F"][s] = osk.fgpa(ref["delta"][s], ref["eta"][s], 1.0, a, b, c)
+    _cmp(g, ref, np.std(boxes["d"]))
+
+
+@pytest.mark.parametrize("tag", ["fitp1d"])
+def test_pixel_mode_matches_merge_spectra_golden(env, golden, tag):
+    """SMK_INTERP_PIXELS is the merge_spectra step: per-pixel delta_l, eta_par, z in, the
+    reference's own white noise (RandomState(seed+islice), ID order), FLUX out."""
+    _lib, _, spectra = env
+    f = golden(f"merge_{tag}.npz")
+    order = f["order"]
+    n_sp, npx = f["delta_l_in"].shape
+    z = f["redshift"].astype(np.float32)
+    table = spectra.SkewerTable(np.zeros((n_sp, 3)), np.tile([0, 0, 1.0], (n_sp, 1)),
+                                np.full(n_sp, npx), dpix=0.2)
+    dl = torch.from_numpy(np.ascontiguousarray(f["delta_l_in"][order]).reshape(-1)).cuda()
+    et = torch.from_numpy(np.ascontiguousarray(f["eta_par_in"][order]).reshape(-1)).cuda()
+    zz = torch.from_numpy(np.tile(z, n_sp)).cuda()
+    from scipy.interpolate import InterpolatedUnivariateSpline
+    kt = np.linspace(0.0, float(f["pm_kmax"]), int(f["pm_n"]))
+    spl = InterpolatedUnivariateSpline(kt, float(f["pm_amp"]) * np.exp(-(kt / float(f["pm_kscale"])) ** 2)
+                                       + float(f["pm_floor"]))
+    cfg = spectra.SpectraConfig(ss_mode=_lib.SMK_SS_HOST, ss_nz=0, pmiss=spl, a=0.1, b=1.6, c=0.5,
+                                growth=_lib.SMK_G_MERGE)
+    rs = np.random.RandomState(int(f["seed"]))
+    nz = osk.nz_rule(npx)
+    noise = np.concatenate([rs.normal(size=nz) for _ in range(n_sp)]).astype(np.float32)
+    offs = np.arange(n_sp, dtype=np.int64) * nz
+    r = spectra.SkewerRunner(table, cfg, pixels=(dl, et, zz))
+    F, dtot, _, _ = r.run(noise=(torch.from_numpy(noise).cuda(), torch.from_numpy(offs).cuda()),
+                          want_fields=True)
+    torch.cuda.synchronize()
+    F = F.cpu().numpy().reshape(n_sp, npx)
+    ds = dtot.cpu().numpy().reshape(n_sp, npx) - f["delta_l_in"][order]
+    np.testing.assert_allclose(ds, f["delta_s"], rtol=0, atol=2e-6)
+    np.testing.assert_allclose(F, f["flux"], rtol=0, atol=F_ATOL)
