@@ -278,6 +278,32 @@ def run_ours(args, cfg):
     print(json.dumps(res))
 
 
+def run_grf_only(args, shape):
+    """GRF boxes of one shape, Philox noise, W + K calls (the ncu profiling case)."""
+    import numpy as np
+    import torch
+
+    from saclaymocks_gb300 import grf
+    nx, ny, nz = shape
+    boxes = grf.alloc_boxes(nx, ny, nz)
+    ws = grf.GrfWorkspace(1)
+    amp = grf.pk_normalisation(nx, ny, nz)
+    for _ in range(args.warmup):
+        grf.make_boxes(nx, ny, nz, seed=1, amp=amp, out=boxes, workspace=ws)
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(args.steps)]
+    for e in [x for row in evs for x in row]:
+        e.record()
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        out = grf.make_boxes(nx, ny, nz, seed=1, amp=amp, out=boxes, workspace=ws, pass_events=evs[k])
+    torch.cuda.synchronize()
+    out.check()
+    pass_ms = np.mean([[evs[k][i].elapsed_time(evs[k][i + 1]) for i in range(5)]
+                       for k in range(args.steps)], axis=0)
+    print(json.dumps({"grf_shape": shape, "pass_ms": [round(float(x), 4) for x in pass_ms],
+                      "grf_cells_per_s": nx * ny * nz / (pass_ms.sum() * 1e-3)}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -286,8 +312,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="256^3 box + 2000 skewers (quick check)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--grf-shape", default=None,
+                    help="NX,NY,NZ: time only the GRF boxes of this shape (profiling case)")
     args = ap.parse_args()
     cfg = SMALL if args.small else PRODUCTION
+    if args.grf_shape:
+        run_grf_only(args, [int(x) for x in args.grf_shape.split(",")])
+        return
     if args.impl == "reference":
         run_reference(args, cfg)
     else:

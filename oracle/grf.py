@@ -117,9 +117,10 @@ def grf_boxes(noise: np.ndarray, dcell: float, k0: float = 0.02, A: float | None
     return out
 
 
-def measured_pk(box: np.ndarray, dcell: float, kbins: np.ndarray):
+def measured_pk(box: np.ndarray, dcell: float, kbins: np.ndarray, pk=None):
     """Binned power of a box, P(k) = |FFT|^2 * Vcell / N (inverse of the generator's
-    normalisation), averaged over modes in each |k| bin; returns (k_mean, P_mean, n_modes)."""
+    normalisation), averaged over modes in each |k| bin; returns (k_mean, P_mean, n_modes),
+    plus the mode-averaged pk(k) of each bin when a spectrum function is given."""
     NX, NY, NZ = box.shape
     bk = np.fft.rfftn(box.astype(np.float64))
     kx, ky, kz = k_components(NX, NY, NZ, dcell)
@@ -130,7 +131,10 @@ def measured_pk(box: np.ndarray, dcell: float, kbins: np.ndarray):
     idx = np.digitize(k.ravel(), kbins) - 1
     ok = (idx >= 0) & (idx < len(kbins) - 1) & (k.ravel() > 0)
     wn = np.bincount(idx[ok], w.ravel()[ok], len(kbins) - 1)
-    pk = np.bincount(idx[ok], (w * p).ravel()[ok], len(kbins) - 1)
+    pk_ = np.bincount(idx[ok], (w * p).ravel()[ok], len(kbins) - 1)
     km = np.bincount(idx[ok], (w * k).ravel()[ok], len(kbins) - 1)
     with np.errstate(invalid="ignore", divide="ignore"):
-        return km / wn, pk / wn, wn
+        if pk is None:
+            return km / wn, pk_ / wn, wn
+        pe = np.bincount(idx[ok], (w * pk(k)).ravel()[ok], len(kbins) - 1)
+        return km / wn, pk_ / wn, wn, pe / wn
