@@ -50,7 +50,9 @@ int smk_fft_supported(int32_t n);
 
 /* ---------------------------------------------------------------- GRF boxes (make_boxes) */
 #define SMK_NOISE_HOST 0   /* white noise given by the caller (dense [batch][nx][ny][nz])  */
-#define SMK_NOISE_PHILOX 1 /* white noise drawn on the GPU: Philox4x32-10 + Box-Muller     */
+#define SMK_NOISE_PHILOX 1 /* Fourier modes of white noise drawn on the GPU (Philox4x32-10 */
+                           /* + Box-Muller, Hermitian planes kz = 0, nz/2): same statistics */
+                           /* as the r2c of N(0,1) noise, two HBM passes fewer              */
 
 #define SMK_PK_ANALYTIC 0  /* P(k) = amp * k / (1 + (k/k0)^2)^2, evaluated in the kernel   */
 #define SMK_PK_GRID 1      /* sqrt(P/Vcell) read from a float32 [nx][ny][nz/2+1] grid       */
@@ -66,7 +68,7 @@ typedef struct {
     const float* pk_grid; /* SMK_PK_GRID: device sqrt(P/Vcell) grid (shared by the batch)    */
     int32_t noise_mode;   /* SMK_NOISE_HOST or SMK_NOISE_PHILOX                              */
     const float* noise;   /* SMK_NOISE_HOST: device dense noise [batch][nx][ny][nz]          */
-    uint64_t seed;        /* SMK_NOISE_PHILOX: box b uses seed + b                           */
+    uint64_t seed;        /* SMK_NOISE_PHILOX: box b uses key seed + b                       */
     int32_t want_eta;     /* 1: also produce eta_zz = irfftn(kz^2/k^2 delta_k)               */
     void* const* pass_events; /* optional cudaEvent_t[6]: recorded on the stream before the    */
     int32_t n_pass_events;    /* first HBM pass and after each of the five (0: none)          */

@@ -91,10 +91,18 @@ def grf_boxes(noise: np.ndarray, dcell: float, k0: float = 0.02, A: float | None
     NX, NY, NZ = noise.shape
     if NZ % 2:
         raise ValueError("NZ must be even (the c2r output length is 2*(NZ/2))")
+    nk = np.fft.rfftn(noise.astype(np.float64))
+    return grf_from_modes(nk, NZ, dcell, k0, A, eta, precision)
+
+
+def grf_from_modes(nk: np.ndarray, NZ: int, dcell: float, k0: float = 0.02, A: float | None = None,
+                   eta=("zz",), precision: str = "f32") -> dict:
+    """The GRF step from the (unnormalised) Fourier transform nk [NX, NY, NZ//2+1] of the
+    white noise: everything of grf_boxes after the forward r2c."""
+    NX, NY = nk.shape[:2]
     N = NX * NY * NZ
     P0 = sqrt_pk_grid(NX, NY, NZ, dcell, k0, A)
     kx, ky, kz = k_components(NX, NY, NZ, dcell)
-    nk = np.fft.rfftn(noise.astype(np.float64))
     if precision == "f32":
         dk = nk.astype(np.complex64) * P0
     else:

@@ -15,7 +15,7 @@ import numpy as np
 M0, M1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57)
 W0, W1 = np.uint64(0x9E3779B9), np.uint64(0xBB67AE85)
 MASK = np.uint64(0xFFFFFFFF)
-STREAM_BOX, STREAM_SKEWER = 0x42, 0x53
+STREAM_KMODE, STREAM_SKEWER = 0x4B, 0x53
 
 
 def philox4x32_10(c0, c1, c2, c3, seed: int):
@@ -43,15 +43,35 @@ def gauss4(x):
     return out
 
 
-def box_noise(nx: int, ny: int, nz: int, seed: int) -> np.ndarray:
-    """White-noise box of the GPU Philox mode ([nx, ny, nz], float64)."""
-    rows = nx * ny
-    ng = (nz + 3) // 4
-    row = np.repeat(np.arange(rows, dtype=np.uint64), ng)
-    q = np.tile(np.arange(ng, dtype=np.uint64), rows)
-    x = philox4x32_10(q, row & MASK, row >> np.uint64(32), STREAM_BOX, seed)
-    g = np.stack(gauss4(x), 1).reshape(rows, ng * 4)[:, :nz]
-    return g.reshape(nx, ny, nz)
+def kspace_noise(nx: int, ny: int, nz: int, seed: int) -> np.ndarray:
+    """Fourier modes of white noise as the GPU noise mode draws them ([nx, ny, nz//2+1]
+    complex128): mode (ix, iy, kz) takes Gaussians (2h, 2h+1), h = kz % 2, of the Philox block
+    (kz // 2, ix, iy, STREAM_KMODE) keyed by seed; Re/Im scaled by sqrt(N/2).  On the kz = 0
+    and kz = nz/2 planes, (ix, iy) and (-ix, -iy) are conjugate: the pair's lower flat index
+    (ix*ny + iy) owns the draw, self-conjugate modes are real with scale sqrt(N)."""
+    nzh = nz // 2 + 1
+    N = nx * ny * nz
+    ix = np.arange(nx, dtype=np.uint64)[:, None, None]
+    iy = np.arange(ny, dtype=np.uint64)[None, :, None]
+    kz = np.arange(nzh, dtype=np.uint64)[None, None, :]
+    x = philox4x32_10(kz >> np.uint64(1), ix, iy, STREAM_KMODE, seed)
+    g = gauss4(x)
+    odd = (np.arange(nzh) % 2 == 1)[None, None, :]
+    re = np.where(odd, g[2], g[0])
+    im = np.where(odd, g[3], g[1])
+    X = np.sqrt(N / 2.0) * (re + 1j * im)
+    ixm = (-np.arange(nx)) % nx
+    iym = (-np.arange(ny)) % ny
+    I, J = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    IM, JM = ixm[I], iym[J]
+    selfc = (IM == I) & (JM == J)
+    canon = I * ny + J < IM * ny + JM
+    for p in sorted({0, nz // 2}):
+        plane = X[:, :, p]
+        mirrored = np.conj(plane[IM, JM])
+        X[:, :, p] = np.where(selfc, np.sqrt(float(N)) * re[:, :, p],
+                              np.where(canon, plane, mirrored))
+    return X
 
 
 def skewer_modes(skewer_id: int, nz: int, seed: int):

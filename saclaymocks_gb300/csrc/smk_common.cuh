@@ -87,8 +87,9 @@ __host__ __device__ __forceinline__ u32x4 philox4x32_10(u32x4 ctr, uint32_t k0, 
     return ctr;
 }
 
-// Stream tags keep the GRF box noise and the skewer noise in disjoint counter spaces.
-enum : uint32_t { STREAM_BOX = 0x42u, STREAM_SKEWER = 0x53u };
+// Stream tags keep the Fourier-mode noise of the boxes and the skewer noise in disjoint
+// counter spaces.
+enum : uint32_t { STREAM_KMODE = 0x4Bu, STREAM_SKEWER = 0x53u };
 
 // Four N(0,1) deviates from one Philox block: Box-Muller on (u0,u1) and (u2,u3) with
 // u = ((x >> 8) + 1) * 2^-24 in (0, 1] for the radius and (x >> 8) * 2^-23 in [0, 2)

@@ -65,13 +65,13 @@ struct ZFwdArgs {
     ZTiling zt;
     int batch;
     int64_t pitch;
-    const float* noise;  // dense [batch][rows_per_box][nz] or null (Philox)
+    const float* noise;  // dense [batch][rows_per_box][nz]
     float* out;
-    uint64_t seed;
 };
 
+// r2c along z of the caller's white noise (two rows per complex line).
 // smem: s[n*SN] | tw[n] | sof[n] (slot of each frequency)
-template <class C, bool PHILOX>
+template <class C>
 __global__ void __launch_bounds__(C::T, 1) zfwd_kernel(const ZFwdArgs a) {
     constexpr int W = C::W, SN = W + 1, T = C::T;
     extern __shared__ float2 smem[];
@@ -91,44 +91,25 @@ __global__ void __launch_bounds__(C::T, 1) zfwd_kernel(const ZFwdArgs a) {
         const int64_t lrow0 = (tile - b * a.zt.tiles_per_box) * (2 * W);  // row inside box b
         const int64_t grow0 = b * a.zt.rows_per_box + lrow0;               // global row
         const int rows_here = (int)min((int64_t)(2 * W), a.zt.rows_per_box - lrow0);
-        if (PHILOX) {
-            const int ng = (n + 3) / 4;
-            for (int idx = threadIdx.x; idx < 2 * W * ng; idx += T) {
-                const int rl = idx / ng, q = idx - rl * ng;
-                float g[4] = {0.f, 0.f, 0.f, 0.f};
-                if (rl < rows_here)
-                    philox_gauss4(a.seed + (uint64_t)b, (uint64_t)(lrow0 + rl), (uint32_t)q, STREAM_BOX, g);
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int e = 4 * q + u;
-                    if (e < n) sf[2 * (e * SN + (rl >> 1)) + (rl & 1)] = g[u];
-                }
-            }
-        } else {
-            const float* src = a.noise + grow0 * n;
-            for (int idx = threadIdx.x; idx < 2 * W * n; idx += T) {
-                const int rl = idx / n, e = idx - rl * n;
-                const bool ok = rl < rows_here;
-                cp_async<4>(sf + 2 * (e * SN + (rl >> 1)) + (rl & 1), ok ? src + idx : a.noise, ok ? 4 : 0);
-            }
-            cp_async_wait_all();
+        const float* src = a.noise + grow0 * n;
+        for (int rl = 0; rl < 2 * W; ++rl) {
+            const bool ok = rl < rows_here;
+            float* dst = sf + 2 * (rl >> 1) + (rl & 1);
+            for (int e = threadIdx.x; e < n; e += T)
+                cp_async<4>(dst + 2 * e * SN, ok ? src + (int64_t)rl * n + e : a.noise, ok ? 4 : 0);
         }
+        cp_async_wait_all();
         __syncthreads();
         fft_tile<false, W, SN, T>(s, tw, a.pl);
         // split the two real transforms packed as re/im and store the half spectra
-        for (int idx = threadIdx.x; idx < 2 * W * nh; idx += T) {
-            const int rl = idx / nh, k = idx - rl * nh;
-            if (rl < rows_here) {
-                const int w = rl >> 1;
-                const float2 zk = s[sof[k] * SN + w];
-                const float2 zm = s[sof[k == 0 ? 0 : n - k] * SN + w];
-                float2 x;
-                if ((rl & 1) == 0)
-                    x = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
-                else
-                    x = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
-                out2[(grow0 + rl) * cp + k] = x;
-            }
+        for (int idx = threadIdx.x; idx < W * nh; idx += T) {
+            const int k = idx / W, w = idx % W;
+            const float2 zk = s[sof[k] * SN + w];
+            const float2 zm = s[sof[k == 0 ? 0 : n - k] * SN + w];
+            if (2 * w < rows_here)
+                out2[(grow0 + 2 * w) * cp + k] = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+            if (2 * w + 1 < rows_here)
+                out2[(grow0 + 2 * w + 1) * cp + k] = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
         }
         __syncthreads();
     }
@@ -273,6 +254,141 @@ __global__ void __launch_bounds__(C::T, 1) xpass_kernel(const XArgs a) {
     }
 }
 
+// ------------------------------------------------------------------ Fourier-space noise pass
+// GPU noise mode: the x pass draws the Fourier modes of white noise directly (the forward
+// r2c of N(0,1) noise has independent Re/Im ~ N(0, N/2) per mode, real N(0, N) on
+// self-conjugate modes, and X(-kx,-ky,kz) = X(kx,ky,kz)* on the kz = 0 and kz = nz/2 planes),
+// multiplies by sqrt(P/Vcell), forms eta_k = kz^2/k^2 delta_k, and takes the inverse x
+// transform of both fields as 2*WC lines of one tile.  No forward z / y passes are needed.
+struct XGenArgs {
+    FftPlan pl;            // x axis
+    FftPlan ply;           // y axis (output stays in the y-digit-reversed order of the y inverse)
+    float2* A;             // delta out
+    float2* B;             // eta out, or null
+    int nx, ny, nz, nzh, batch;
+    int64_t cp;
+    int pk_mode;
+    const float* grid;
+    const double* amp_dev;
+    double amp_host;
+    double kfac;
+    float inv_k0, inv_vcell;
+    float sig_c, sig_r;    // sqrt(N/2), sqrt(N)
+    uint64_t seed;
+};
+
+template <int W_, int T_>
+struct XGenCfg {
+    static constexpr int W = W_, T = T_;   // W lines = W/2 delta columns + W/2 eta columns
+};
+using XGenA = XGenCfg<32, 256>;  // n <= 512
+using XGenB = XGenCfg<16, 512>;  // n <= 1024
+using XGenC = XGenCfg<8, 512>;   // n <= 2560
+using XGenD = XGenCfg<4, 512>;   // n <= 4096
+
+// smem: s[n*W] | tw[n] | kx[n] | ix[n]
+template <class C>
+__global__ void __launch_bounds__(C::T, 1) xgen_kernel(const XGenArgs a) {
+    constexpr int W = C::W, WC = W / 2, NP = WC / 2, T = C::T;
+    extern __shared__ float2 smem[];
+    const int n = a.pl.n;  // == nx
+    float2* s = smem;
+    float2* tw = s + n * W;
+    float* kx = reinterpret_cast<float*>(tw + n);
+    int* ix = reinterpret_cast<int*>(kx + n);
+    fill_twiddles<T>(tw, n);
+    for (int e = threadIdx.x; e < n; e += T) {
+        const int f = freq_of_slot(a.pl, e);
+        ix[e] = f;
+        kx[e] = kaxis(f, n, a.kfac, true);
+    }
+    __syncthreads();
+    float amp = 0.f;
+    if (a.pk_mode == SMK_PK_ANALYTIC) amp = (float)(a.amp_host > 0.0 ? a.amp_host : *a.amp_dev);
+    const int64_t ncolt = ceil_div(a.nzh, WC);
+    const int64_t ntiles = (int64_t)a.batch * a.ny * ncolt;
+    const int64_t estride = (int64_t)a.ny * a.cp;
+    const int half = a.nz / 2;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t o = tile / ncolt;  // b*ny + y slot
+        const int cb = (int)(tile - o * ncolt);
+        const int64_t b = o / a.ny;
+        const int yslot = (int)(o - b * a.ny);
+        const int iy = freq_of_slot(a.ply, yslot);
+        const int iym = iy == 0 ? 0 : a.ny - iy;
+        const float ky = kaxis(iy, a.ny, a.kfac, true);
+        const uint64_t seed = a.seed + (uint64_t)b;
+        for (int idx = threadIdx.x; idx < n * NP; idx += T) {
+            const int e = idx / NP, pr = idx % NP;
+            const int c0 = 2 * pr, kz0 = cb * WC + c0;
+            const int ixe = ix[e];
+            float g[4];
+            {
+                u32x4 ctr;
+                ctr.v[0] = (uint32_t)(kz0 >> 1);
+                ctr.v[1] = (uint32_t)ixe;
+                ctr.v[2] = (uint32_t)iy;
+                ctr.v[3] = STREAM_KMODE;
+                gauss4(philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32)), g);
+            }
+            const float kxv = kx[e];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int kz = kz0 + h;
+                float2 d = make_float2(0.f, 0.f), et = make_float2(0.f, 0.f);
+                if (kz < a.nzh) {
+                    float2 X = make_float2(a.sig_c * g[2 * h], a.sig_c * g[2 * h + 1]);
+                    if (kz == 0 || kz == half) {
+                        const int ixm = ixe == 0 ? 0 : a.nx - ixe;
+                        if (ixm == ixe && iym == iy) {
+                            X = make_float2(a.sig_r * g[2 * h], 0.f);
+                        } else if ((int64_t)ixe * a.ny + iy > (int64_t)ixm * a.ny + iym) {
+                            // the partner (-kx, -ky) owns the draw: take its conjugate
+                            u32x4 ctr;
+                            ctr.v[0] = (uint32_t)(kz0 >> 1);
+                            ctr.v[1] = (uint32_t)ixm;
+                            ctr.v[2] = (uint32_t)iym;
+                            ctr.v[3] = STREAM_KMODE;
+                            float gm[4];
+                            gauss4(philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32)), gm);
+                            X = make_float2(a.sig_c * gm[2 * h], -a.sig_c * gm[2 * h + 1]);
+                        }
+                    }
+                    const float kz_ = kaxis(kz, a.nz, a.kfac, false);
+                    const float kk = __fadd_rn(__fadd_rn(__fmul_rn(kxv, kxv), __fmul_rn(ky, ky)), __fmul_rn(kz_, kz_));
+                    float sc;
+                    if (a.pk_mode == SMK_PK_GRID) {
+                        sc = __ldg(a.grid + ((int64_t)ixe * a.ny + iy) * a.nzh + kz);
+                    } else {
+                        const float k = __fsqrt_rn(kk);
+                        const float kr = k * a.inv_k0;
+                        const float den = fmaf(kr, kr, 1.0f);
+                        sc = sqrtf(amp * k / (den * den) * a.inv_vcell);
+                    }
+                    d = cscale(X, sc);
+                    const float kk1 = (kk == 0.0f) ? 1.0f : kk;
+                    et = cscale(d, __fdiv_rn(__fmul_rn(kz_, kz_), kk1));
+                }
+                s[e * W + c0 + h] = d;
+                s[e * W + WC + c0 + h] = et;
+            }
+        }
+        __syncthreads();
+        fft_tile<true, W, W, T>(s, tw, a.pl);
+        const int cols = min(WC, a.nzh - cb * WC);
+        const int64_t off = b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)cb * WC;
+        for (int idx = threadIdx.x; idx < n * W; idx += T) {
+            const int e = idx / W, l = idx % W;
+            const int c = l % WC;
+            if (c < cols) {
+                float2* dst = l < WC ? a.A : a.B;
+                if (dst) dst[off + e * estride + c] = s[idx];
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------------------------ z inverse (c2r) + stats
 struct ZInvArgs {
     FftPlan pl;
@@ -353,9 +469,10 @@ __global__ void __launch_bounds__(C::T, 1) zinv_kernel(const ZInvArgs a) {
         }
         const float2* in2 = reinterpret_cast<const float2*>(a.buf[buf]) + grow0 * cp;
         // X1_k (even row) to the slot of frequency k, X2_k (odd row) to the slot of n-k;
-        // DC and Nyquist keep their real parts (re: X1, im: X2)
+        // DC and Nyquist keep their real parts (re: X1, im: X2).  Rows are the fast index of
+        // the thread mapping so the permuted shared-memory slots are written W-contiguous.
         for (int idx = threadIdx.x; idx < 2 * W * nh; idx += T) {
-            const int rl = idx / nh, k = idx - rl * nh;
+            const int k = idx / (2 * W), rl = idx % (2 * W);
             const int w = rl >> 1, odd = rl & 1;
             const bool ok = rl < rows_here;
             const float2* src = ok ? in2 + (int64_t)rl * cp + k : in2;
@@ -378,11 +495,12 @@ __global__ void __launch_bounds__(C::T, 1) zinv_kernel(const ZInvArgs a) {
         fft_tile<true, W, SN, T>(s, tw, a.pl);
         float p1 = 0.f, p2 = 0.f, pb = 0.f;
         float* out = a.buf[buf] + grow0 * a.pitch;
-        for (int idx = threadIdx.x; idx < 2 * W * n; idx += T) {
-            const int rl = idx / n, e = idx - rl * n;
-            if (rl < rows_here) {
-                const float v = sf[2 * (e * SN + (rl >> 1)) + (rl & 1)] * a.scale;
-                out[(int64_t)rl * a.pitch + e] = v;
+        for (int rl = 0; rl < rows_here; ++rl) {
+            const float* srow = sf + 2 * (rl >> 1) + (rl & 1);
+            float* orow = out + (int64_t)rl * a.pitch;
+            for (int e = threadIdx.x; e < n; e += T) {
+                const float v = srow[2 * e * SN] * a.scale;
+                orow[e] = v;
                 if (isfinite(v)) {
                     p1 += v;
                     p2 = fmaf(v, v, p2);
@@ -467,14 +585,19 @@ static int launch_zfwd(const ZFwdArgs& a, cudaStream_t st) {
     const size_t smem = zpass_smem<C>(a.pl.n);
     const int64_t ntiles = a.zt.tiles_per_box * a.batch;
     int grid = 0, rc;
-    if (a.noise) {
-        if ((rc = persistent_grid(zfwd_kernel<C, false>, C::T, smem, ntiles, &grid))) return rc;
-        zfwd_kernel<C, false><<<grid, C::T, smem, st>>>(a);
-    } else {
-        if ((rc = persistent_grid(zfwd_kernel<C, true>, C::T, smem, ntiles, &grid))) return rc;
-        zfwd_kernel<C, true><<<grid, C::T, smem, st>>>(a);
-    }
+    if ((rc = persistent_grid(zfwd_kernel<C>, C::T, smem, ntiles, &grid))) return rc;
+    zfwd_kernel<C><<<grid, C::T, smem, st>>>(a);
     return check_launch("zfwd_kernel");
+}
+
+template <class C>
+static int launch_xgen(const XGenArgs& a, cudaStream_t st) {
+    const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8;
+    const int64_t ntiles = (int64_t)a.batch * a.ny * ceil_div(a.nzh, C::W / 2);
+    int grid = 0, rc;
+    if ((rc = persistent_grid(xgen_kernel<C>, C::T, smem, ntiles, &grid))) return rc;
+    xgen_kernel<C><<<grid, C::T, smem, st>>>(a);
+    return check_launch("xgen_kernel");
 }
 
 template <class C>
@@ -513,6 +636,11 @@ static int launch_zinv(const ZInvArgs& a, cudaStream_t st) {
 }
 
 // n -> tile class; the dispatch macro instantiates every pass for the four classes
+#define SMK_DISPATCH_X(n, FN, ...)                                \
+    ((n) <= 512 ? FN<XGenA>(__VA_ARGS__)                          \
+                : (n) <= 1024 ? FN<XGenB>(__VA_ARGS__)            \
+                              : (n) <= 2560 ? FN<XGenC>(__VA_ARGS__) : FN<XGenD>(__VA_ARGS__))
+
 #define SMK_DISPATCH(n, FN, ...)                                  \
     ((n) <= 512 ? FN<CfgA>(__VA_ARGS__)                           \
                 : (n) <= 1024 ? FN<CfgB>(__VA_ARGS__)             \
@@ -615,19 +743,6 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         return SMK_OK;
     };
     if ((rc = mark(0))) return rc;
-    // 1. r2c along z
-    ZFwdArgs za;
-    za.pl = plz;
-    za.zt.init((int64_t)p->nx * p->ny, zfwd_w(p->nz));
-    za.batch = p->batch;
-    za.pitch = pitch;
-    za.noise = p->noise_mode == SMK_NOISE_HOST ? p->noise : nullptr;
-    za.out = delta;
-    za.seed = p->seed;
-    if ((rc = SMK_DISPATCH(p->nz, launch_zfwd, za, st))) return rc;
-    if ((rc = mark(1))) return rc;
-
-    // 2. c2c along y, forward
     float2* d2 = reinterpret_cast<float2*>(delta);
     float2* e2 = reinterpret_cast<float2*>(eta);
     LineArgs ya;
@@ -639,29 +754,71 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
     ya.ostride = (int64_t)p->ny * cp;
     ya.estride = cp;
     ya.ncol = nzh;
-    if ((rc = SMK_DISPATCH(p->ny, launch_line, ya, false, st))) return rc;
-    if ((rc = mark(2))) return rc;
-
-    // 3. x: forward, P(k) scaling + eta split, inverse
-    XArgs xa;
-    xa.pl = plx;
-    xa.ply = ply;
-    xa.A = d2;
-    xa.B = p->want_eta ? e2 : nullptr;
-    xa.nx = p->nx;
-    xa.ny = p->ny;
-    xa.nzh = nzh;
-    xa.batch = p->batch;
-    xa.cp = cp;
-    xa.pk_mode = p->pk_mode;
-    xa.grid = p->pk_grid;
-    xa.amp_dev = amp_dev;
-    xa.amp_host = amp_dev ? 0.0 : p->amp;
-    xa.kfac = kfac;
-    xa.inv_k0 = p->pk_mode == SMK_PK_ANALYTIC ? (float)(1.0 / p->k0) : 0.f;
-    xa.inv_vcell = 1.0f / (float)(p->dcell * p->dcell * p->dcell);
-    if ((rc = SMK_DISPATCH(p->nx, launch_xpass, xa, st))) return rc;
-    if ((rc = mark(3))) return rc;
+    ZTiling zt;
+    zt.init((int64_t)p->nx * p->ny, zfwd_w(p->nz));
+    const float inv_vcell = 1.0f / (float)(p->dcell * p->dcell * p->dcell);
+    if (p->noise_mode == SMK_NOISE_PHILOX) {
+        // Fourier modes drawn in the x pass: no forward z / y passes
+        if ((rc = mark(1)) || (rc = mark(2))) return rc;
+        XGenArgs ga;
+        ga.pl = plx;
+        ga.ply = ply;
+        ga.A = d2;
+        ga.B = p->want_eta ? e2 : nullptr;
+        ga.nx = p->nx;
+        ga.ny = p->ny;
+        ga.nz = p->nz;
+        ga.nzh = nzh;
+        ga.batch = p->batch;
+        ga.cp = cp;
+        ga.pk_mode = p->pk_mode;
+        ga.grid = p->pk_grid;
+        ga.amp_dev = amp_dev;
+        ga.amp_host = amp_dev ? 0.0 : p->amp;
+        ga.kfac = kfac;
+        ga.inv_k0 = p->pk_mode == SMK_PK_ANALYTIC ? (float)(1.0 / p->k0) : 0.f;
+        ga.inv_vcell = inv_vcell;
+        const double ncell = (double)p->nx * p->ny * p->nz;
+        ga.sig_c = (float)sqrt(0.5 * ncell);
+        ga.sig_r = (float)sqrt(ncell);
+        ga.seed = p->seed;
+        if ((rc = SMK_DISPATCH_X(p->nx, launch_xgen, ga, st))) return rc;
+        if ((rc = mark(3))) return rc;
+    } else {
+        // 1. r2c along z of the caller's noise
+        ZFwdArgs za;
+        za.pl = plz;
+        za.zt = zt;
+        za.batch = p->batch;
+        za.pitch = pitch;
+        za.noise = p->noise;
+        za.out = delta;
+        if ((rc = SMK_DISPATCH(p->nz, launch_zfwd, za, st))) return rc;
+        if ((rc = mark(1))) return rc;
+        // 2. c2c along y, forward (the y spectrum stays in digit-reversed order)
+        if ((rc = SMK_DISPATCH(p->ny, launch_line, ya, false, st))) return rc;
+        if ((rc = mark(2))) return rc;
+        // 3. x: forward, P(k) scaling + eta split, inverse
+        XArgs xa;
+        xa.pl = plx;
+        xa.ply = ply;
+        xa.A = d2;
+        xa.B = p->want_eta ? e2 : nullptr;
+        xa.nx = p->nx;
+        xa.ny = p->ny;
+        xa.nzh = nzh;
+        xa.batch = p->batch;
+        xa.cp = cp;
+        xa.pk_mode = p->pk_mode;
+        xa.grid = p->pk_grid;
+        xa.amp_dev = amp_dev;
+        xa.amp_host = amp_dev ? 0.0 : p->amp;
+        xa.kfac = kfac;
+        xa.inv_k0 = p->pk_mode == SMK_PK_ANALYTIC ? (float)(1.0 / p->k0) : 0.f;
+        xa.inv_vcell = inv_vcell;
+        if ((rc = SMK_DISPATCH(p->nx, launch_xpass, xa, st))) return rc;
+        if ((rc = mark(3))) return rc;
+    }
 
     // 4. c2c along y, inverse, on delta (and eta)
     ya.nbuf = p->want_eta ? 2 : 1;
@@ -671,7 +828,7 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
     // 5. c2r along z, / N, statistics
     ZInvArgs ia;
     ia.pl = plz;
-    ia.zt = za.zt;
+    ia.zt = zt;
     ia.batch = p->batch;
     ia.buf[0] = delta;
     ia.buf[1] = eta;

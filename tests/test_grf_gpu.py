@@ -100,15 +100,30 @@ def test_grf_batch_equals_single_boxes(G):
         assert sig[b] == pytest.approx(np.std(o64["delta"]), rel=1e-5)
 
 
-def test_grf_philox_mode_matches_oracle_noise(G):
-    nx, ny, nz, seed = 24, 20, 18, 123
+@pytest.mark.parametrize("shape", [(24, 20, 18), (15, 9, 10), (16, 16, 16), (600, 6, 4)])
+def test_grf_philox_mode_matches_oracle_modes(G, shape):
+    """GPU noise mode: the Fourier modes drawn in the x pass (Hermitian kz = 0, nz/2 planes,
+    odd and even axes) against the numpy restatement of the same Philox draws."""
+    nx, ny, nz = shape
+    seed = 123
     out = G.make_boxes(nx, ny, nz, 2.19, seed=seed, batch=2)
     torch.cuda.synchronize()
     for b in range(2):
-        noise = ophilox.box_noise(nx, ny, nz, seed + b)
-        o64 = ograf.grf_boxes(noise, 2.19, 0.02, eta=("zz",), precision="f64")
+        nk = ophilox.kspace_noise(nx, ny, nz, seed + b)
+        o64 = ograf.grf_from_modes(nk, nz, 2.19, 0.02, eta=("zz",), precision="f64")
         _check(out.delta[b].cpu().numpy(), o64["delta"], f"philox delta {b}")
         _check(out.eta[b].cpu().numpy(), o64["eta_zz"], f"philox eta {b}")
+
+
+def test_kspace_noise_is_hermitian_on_the_real_planes():
+    nk = ophilox.kspace_noise(6, 5, 8, 3)
+    for p in (0, 4):
+        pl = nk[:, :, p]
+        mir = np.conj(pl[(-np.arange(6)) % 6][:, (-np.arange(5)) % 5])
+        np.testing.assert_allclose(pl, mir, rtol=0, atol=0)
+    # unnormalised |X|^2 averages N = nx*ny*nz
+    big = ophilox.kspace_noise(32, 32, 32, 9)
+    assert np.mean(np.abs(big[:, :, 1:16]) ** 2) == pytest.approx(32 ** 3, rel=0.02)
 
 
 def test_grf_philox_recovers_input_pk(G):
