@@ -188,6 +188,26 @@ int smk_skewers_flux(const SmkSkewers* sk, const SmkSpectraParams* p, const floa
                      const float* eta_box, float* flux, float* delta_out, float* eta_out,
                      float* z_out, void* workspace, size_t workspace_bytes, void* stream);
 
+/*
+ * Allocation-free form of smk_skewers_flux, for callers that cannot allocate device memory
+ * (code that runs where cudaMalloc is not allowed, e.g. inside a host framework that owns all
+ * device memory, or a program that must not allocate after start-up).  No counterpart in the
+ * reference, which runs on the CPU.  Same inputs and outputs as smk_skewers_flux except that
+ * the work schedule is built here from the host copy of npix (sk->order and sk->n_slots are
+ * ignored) and all scratch (schedule + work counter) lives in a static device array of
+ * 4 MiB + 256 B that every process loading the library holds on each GPU it uses until exit:
+ * at most SMK_STATIC_MAX_SLOTS - 16 skewers (1,048,560; the schedule has at most n + 6 slots);
+ * larger tables are rejected with SMK_EINVAL.  The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.  Calls share the
+ * array: calls that overlap on the GPU (other streams, other host threads) race and must be
+ * serialised by the caller.  No device memory is allocated or freed.
+ */
+#define SMK_STATIC_MAX_SLOTS (1 << 20)
+#define SMK_STATIC_MAX_DEVICES 64
+int smk_skewers_flux_static(const SmkSkewers* sk, const int32_t* npix_host, const SmkSpectraParams* p,
+                            const float* delta_box, const float* eta_box, float* flux,
+                            float* delta_out, float* eta_out, float* z_out, void* stream);
+
 /* ---------------------------------------------------------------- FGPA (util.fgpa) */
 /*
  * Replaces util.fgpa (py/SaclayMocks/util.py:421-433) as called from

@@ -81,6 +81,9 @@ _SIGS = [
     ("smk_skewers_flux", C.c_int, [C.POINTER(SmkSkewers), C.POINTER(SmkSpectraParams), C.c_void_p,
                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_void_p, C.c_size_t, C.c_void_p]),
+    ("smk_skewers_flux_static", C.c_int, [C.POINTER(SmkSkewers), C.c_void_p, C.POINTER(SmkSpectraParams),
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_void_p]),
     ("smk_fgpa", C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p,
                            C.c_float, C.c_void_p, C.c_float, C.c_void_p, C.c_float, C.c_void_p,
                            C.c_void_p]),

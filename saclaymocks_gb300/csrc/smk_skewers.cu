@@ -9,6 +9,8 @@
 //   2. every pixel: position -> 8-corner trilinear read of delta (and eta), redshift,
 //      a(z), b, c, G(z), F = exp(-a exp(b G (delta_l + delta_s + c eta))).
 #include <algorithm>
+#include <mutex>
+#include <vector>
 
 #include "smk_fft.cuh"
 
@@ -358,3 +360,66 @@ int smk_skewers_flux(const SmkSkewers* sk, const SmkSpectraParams* p, const floa
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ allocation-free variant
+// Scratch of smk_skewers_flux_static, resident in every process that loads the library:
+// words [0, 64) hold the persistent launch's work counter (the 256-byte workspace of
+// smk_skewers_flux), words [64, 64 + SMK_STATIC_MAX_SLOTS) the work schedule.  Host code may
+// not use this name as a device address; it takes the address from cudaGetSymbolAddress.
+static __device__ __align__(256) int32_t g_skewer_scratch[64 + SMK_STATIC_MAX_SLOTS];
+
+namespace {
+std::mutex g_scratch_mutex;
+int32_t* g_scratch_ptr[SMK_STATIC_MAX_DEVICES] = {};
+
+// Device address of the scratch on the current device, looked up once per device.
+int scratch_address(int32_t** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return check_launch("cudaGetDevice");
+    if (dev < 0 || dev >= SMK_STATIC_MAX_DEVICES)
+        return fail(SMK_ENOTSUPP, "smk_skewers_flux_static: device %d beyond the %d supported", dev,
+                    SMK_STATIC_MAX_DEVICES);
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_ptr[dev]) {
+        void* ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_skewer_scratch);
+        if (e != cudaSuccess)
+            return fail(SMK_ECUDA, "smk_skewers_flux_static: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+        g_scratch_ptr[dev] = static_cast<int32_t*>(ptr);
+    }
+    *out = g_scratch_ptr[dev];
+    return SMK_OK;
+}
+}  // namespace
+
+extern "C" int smk_skewers_flux_static(const SmkSkewers* sk, const int32_t* npix_host,
+                                       const SmkSpectraParams* p, const float* delta_box,
+                                       const float* eta_box, float* flux, float* delta_out,
+                                       float* eta_out, float* z_out, void* stream) {
+    if (!sk || !p || !npix_host) return fail(SMK_EINVAL, "smk_skewers_flux_static: null argument");
+    if (sk->n < 0 || sk->n > SMK_STATIC_MAX_SLOTS - 16)
+        return fail(SMK_EINVAL, "smk_skewers_flux_static: %lld skewers; the static scratch holds the "
+                    "schedule of at most %d", (long long)sk->n, SMK_STATIC_MAX_SLOTS - 16);
+    int32_t* scratch = nullptr;
+    int rc = scratch_address(&scratch);
+    if (rc) return rc;
+    // host-side schedule (same as smk_skewer_schedule), then into the static scratch
+    std::vector<int32_t> order((size_t)(2 * sk->n + 16));
+    int64_t n_slots = 0;
+    const int32_t ss_nz = p->ss_mode != SMK_SS_NONE ? p->ss_nz : -1;
+    if ((rc = smk_skewer_schedule(sk->n, npix_host, ss_nz, order.data(), &n_slots))) return rc;
+    if (n_slots > SMK_STATIC_MAX_SLOTS)
+        return fail(SMK_EINVAL, "smk_skewers_flux_static: schedule of %lld slots exceeds %d",
+                    (long long)n_slots, SMK_STATIC_MAX_SLOTS);
+    cudaStream_t st = (cudaStream_t)stream;
+    // pageable source: the copy has read it when cudaMemcpyAsync returns
+    if (n_slots > 0 && cudaMemcpyAsync(scratch + 64, order.data(), (size_t)n_slots * sizeof(int32_t),
+                                       cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return check_launch("smk_skewers_flux_static: schedule copy");
+    SmkSkewers s2 = *sk;
+    s2.order = scratch + 64;
+    s2.n_slots = n_slots;
+    // the work counter is zeroed by smk_skewers_flux itself (cudaMemsetAsync on the stream)
+    return smk_skewers_flux(&s2, p, delta_box, eta_box, flux, delta_out, eta_out, z_out, scratch,
+                            64 * sizeof(int32_t), stream);
+}
