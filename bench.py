@@ -176,6 +176,10 @@ def run_ours(args, cfg):
                                cfg=scfg)
     runner = chunk._prepare(table.start, table.direction, table.npix)
     boxes, ws = chunk.boxes, chunk.ws
+    tuned = None
+    if not args.no_tune:
+        from saclaymocks_gb300 import tune
+        tuned = tune.tune_grf(cfg["nx"], cfg["ny"], cfg["nz"], cfg["dcell"], out=boxes, workspace=ws)
     nx, ny, nz = cfg["nx"], cfg["ny"], cfg["nz"]
     cells = nx * ny * nz
     pixels = table.total_pixels
@@ -267,7 +271,8 @@ def run_ours(args, cfg):
            "e2e": {"value": world * cells / e2e_s, "unit": "cells/s",
                    "h2d_bytes_per_step": chunk.h2d_bytes(), "d2h_bytes_per_step": chunk.d2h_bytes(),
                    "ms_per_step": e2e_s * 1e3},
-           "gpu_launches": args.steps * 6,
+           "gpu_launches": args.steps * 4,
+           "tile_variants": tuned,
            "clocks": clk.summary()}
     if not args.no_cpu:
         workers = os.cpu_count() or 1
@@ -288,6 +293,10 @@ def run_grf_only(args, shape):
     boxes = grf.alloc_boxes(nx, ny, nz)
     ws = grf.GrfWorkspace(1)
     amp = grf.pk_normalisation(nx, ny, nz)
+    tuned = None
+    if not args.no_tune:
+        from saclaymocks_gb300 import tune
+        tuned = tune.tune_grf(nx, ny, nz, out=boxes, workspace=ws, use_cache=False)
     for _ in range(args.warmup):
         grf.make_boxes(nx, ny, nz, seed=1, amp=amp, out=boxes, workspace=ws)
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(args.steps)]
@@ -300,7 +309,7 @@ def run_grf_only(args, shape):
     out.check()
     pass_ms = np.mean([[evs[k][i].elapsed_time(evs[k][i + 1]) for i in range(5)]
                        for k in range(args.steps)], axis=0)
-    print(json.dumps({"grf_shape": shape, "pass_ms": [round(float(x), 4) for x in pass_ms],
+    print(json.dumps({"grf_shape": shape, "pass_ms": [round(float(x), 4) for x in pass_ms], "tuned": tuned,
                       "grf_cells_per_s": nx * ny * nz / (pass_ms.sum() * 1e-3)}))
 
 
@@ -312,6 +321,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="256^3 box + 2000 skewers (quick check)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-tune", action="store_true", help="built-in tile variants, no autotuning")
     ap.add_argument("--grf-shape", default=None,
                     help="NX,NY,NZ: time only the GRF boxes of this shape (profiling case)")
     args = ap.parse_args()

@@ -104,6 +104,20 @@ int smk_grf_check(const double* stats_host, int64_t ncells, double* sigma_out);
 int smk_pk_normalisation(int32_t nx, int32_t ny, int32_t nz, double dcell, double k0,
                          double* amp_dev, void* stream);
 
+/* Tile variants of the HBM passes (autotuner hooks; no counterpart in the reference).  Each
+ * pass has a table of variants (tile width W and threads per block T, valid up to a line
+ * length); smk_tune_set picks the variant used for the lengths of n's class (<=512, <=1024,
+ * <=2560, <=4096; v = -1 restores the built-in choice).  Process-wide setting. */
+#define SMK_PASS_ZFWD 0  /* r2c along z (host noise)                              */
+#define SMK_PASS_LINE 1  /* c2c along y                                            */
+#define SMK_PASS_XPASS 2 /* x pass of host noise                                   */
+#define SMK_PASS_XGEN 3  /* x pass drawing the GPU noise                           */
+#define SMK_PASS_ZINV 4  /* c2r along z + statistics                               */
+int smk_tune_count(int32_t pass);
+int smk_tune_info(int32_t pass, int32_t variant, int32_t* w, int32_t* threads, int32_t* n_max);
+int smk_tune_set(int32_t pass, int32_t n, int32_t variant);
+int smk_tune_get(int32_t pass, int32_t n);
+
 /* ---------------------------------------------------------------- skewers (make_spectra +
  *                                                                   merge_spectra) */
 #define SMK_INTERP_TRILINEAR 0 /* 8-corner read, periodic, cell centres at (i+0.5)dcell */

@@ -24,6 +24,7 @@ SMK_INTERP_TRILINEAR, SMK_INTERP_PIXELS = 0, 1
 SMK_SS_NONE, SMK_SS_HOST, SMK_SS_PHILOX = 0, 1, 2
 SMK_ABC_CONST, SMK_ABC_POWERLAW, SMK_ABC_TABLE = 0, 1, 2
 SMK_G_ONE, SMK_G_MERGE = 0, 1
+SMK_PASS_ZFWD, SMK_PASS_LINE, SMK_PASS_XPASS, SMK_PASS_XGEN, SMK_PASS_ZINV = 0, 1, 2, 3, 4
 
 
 class SmkError(RuntimeError):
@@ -75,6 +76,11 @@ _SIGS = [
     ("smk_grf_check", C.c_int, [C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_double)]),
     ("smk_pk_normalisation", C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_double,
                                        C.c_void_p, C.c_void_p]),
+    ("smk_tune_count", C.c_int, [C.c_int32]),
+    ("smk_tune_info", C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                C.POINTER(C.c_int32)]),
+    ("smk_tune_set", C.c_int, [C.c_int32, C.c_int32, C.c_int32]),
+    ("smk_tune_get", C.c_int, [C.c_int32, C.c_int32]),
     ("smk_skewer_schedule", C.c_int, [C.c_int64, C.c_void_p, C.c_int32, C.c_void_p,
                                       C.POINTER(C.c_int64)]),
     ("smk_skewers_workspace_size", C.c_size_t, [C.POINTER(SmkSkewers), C.POINTER(SmkSpectraParams)]),

@@ -168,7 +168,7 @@ __device__ __forceinline__ void fft_stage(float2* __restrict__ s, const float2* 
     const int m = pl.m[st];
     const int tstep = pl.tstep[st];
     const int nb = (pl.n / R) * W;
-#pragma unroll 2
+#pragma unroll(T >= 1024 ? 1 : 2)
     for (int bf = threadIdx.x; bf < nb; bf += T) {
         const int j = bf / W, w = bf % W;
         const int blk = div_m(pl, st, j);

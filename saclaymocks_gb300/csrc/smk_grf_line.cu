@@ -1,0 +1,15 @@
+// Tile variants of the strided c2c pass along y.
+#include "smk_grf_kernels.cuh"
+
+namespace smk {
+
+int run_line(int v, const LineArgs& a, bool inv, cudaStream_t st) {
+    int i = 0;
+#define X(W, T, N) \
+    if (v == i++) return launch_line<TileCfg<W, T>>(a, inv, st);
+    SMK_LINE_VARIANTS(X)
+#undef X
+    return fail(SMK_EINVAL, "line: no tile variant %d", v);
+}
+
+}  // namespace smk

@@ -1,0 +1,24 @@
+// Tile variants of the x passes (host noise: xpass; GPU noise: xgen).
+#include "smk_grf_kernels.cuh"
+
+namespace smk {
+
+int run_xpass(int v, const XArgs& a, cudaStream_t st) {
+    int i = 0;
+#define X(W, T, N) \
+    if (v == i++) return launch_xpass<TileCfg<W, T>>(a, st);
+    SMK_X_VARIANTS(X)
+#undef X
+    return fail(SMK_EINVAL, "xpass: no tile variant %d", v);
+}
+
+int run_xgen(int v, const XGenArgs& a, cudaStream_t st) {
+    int i = 0;
+#define X(W, T, N) \
+    if (v == i++) return launch_xgen<TileCfg<W, T>>(a, st);
+    SMK_XGEN_VARIANTS(X)
+#undef X
+    return fail(SMK_EINVAL, "xgen: no tile variant %d", v);
+}
+
+}  // namespace smk

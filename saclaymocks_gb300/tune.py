@@ -1,0 +1,134 @@
+"""Autotuner of the GRF passes' tile variants (tile width W, threads per block).
+
+For a box shape, every valid variant of each pass is timed with the per-pass CUDA events of
+``smk_grf_boxes`` (all passes of one call use the i-th variant of their own table, so one
+sweep of ``max(variants)`` calls times every candidate), the fastest is kept per pass and line
+length class, applied through ``smk_tune_set``, and cached in JSON keyed by device name,
+pass, and line length class, so later processes replay it without re-timing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+
+import numpy as np
+import torch
+
+from . import _lib, grf
+
+PASS_NAMES = {_lib.SMK_PASS_ZFWD: "zfwd", _lib.SMK_PASS_LINE: "line", _lib.SMK_PASS_XPASS: "xpass",
+              _lib.SMK_PASS_XGEN: "xgen", _lib.SMK_PASS_ZINV: "zinv"}
+CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "tune_cache.json")
+
+
+def length_class(n: int) -> int:
+    return 0 if n <= 512 else 1 if n <= 1024 else 2 if n <= 2560 else 3
+
+
+def variants(pass_id: int, n: int) -> list:
+    lib = _lib.load()
+    out = []
+    w, t, nm = C.c_int32(), C.c_int32(), C.c_int32()
+    for v in range(lib.smk_tune_count(pass_id)):
+        _lib.check(lib.smk_tune_info(pass_id, v, C.byref(w), C.byref(t), C.byref(nm)))
+        if nm.value >= n:
+            out.append((v, w.value, t.value))
+    return out
+
+
+def _device_key() -> str:
+    return torch.cuda.get_device_name(torch.cuda.current_device())
+
+
+def apply(choices: dict):
+    """choices: {(pass_id, n): variant} -> smk_tune_set for each."""
+    lib = _lib.load()
+    for (pid, n), v in choices.items():
+        _lib.check(lib.smk_tune_set(int(pid), int(n), int(v)), "smk_tune_set")
+
+
+def load_cached(shape_passes) -> dict:
+    """Apply cached choices for [(pass_id, n), ...]; returns the ones found."""
+    try:
+        with open(CACHE) as f:
+            cache = json.load(f)
+    except (OSError, ValueError):
+        return {}
+    dev = cache.get(_device_key(), {})
+    found = {}
+    for pid, n in shape_passes:
+        key = f"{PASS_NAMES[pid]}:{length_class(n)}"
+        if key in dev:
+            found[(pid, n)] = int(dev[key])
+    apply(found)
+    return found
+
+
+def _store(choices: dict):
+    try:
+        with open(CACHE) as f:
+            cache = json.load(f)
+    except (OSError, ValueError):
+        cache = {}
+    dev = cache.setdefault(_device_key(), {})
+    for (pid, n), v in choices.items():
+        dev[f"{PASS_NAMES[pid]}:{length_class(n)}"] = int(v)
+    os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+    with open(CACHE, "w") as f:
+        json.dump(cache, f, indent=1, sort_keys=True)
+
+
+def tune_grf(nx: int, ny: int, nz: int, dcell: float = 2.19, gpu_noise: bool = True, reps: int = 2,
+             out=None, workspace=None, use_cache: bool = True) -> dict:
+    """Pick the fastest tile variant of every pass of smk_grf_boxes for this shape.
+    Returns {"choices": {pass name: (variant, W, T)}, "ms": {pass name: {variant: ms}}}."""
+    if gpu_noise:
+        passes = [(_lib.SMK_PASS_XGEN, nx, 3), (_lib.SMK_PASS_LINE, ny, 4), (_lib.SMK_PASS_ZINV, nz, 5)]
+    else:
+        passes = [(_lib.SMK_PASS_ZFWD, nz, 1), (_lib.SMK_PASS_LINE, ny, 2), (_lib.SMK_PASS_XPASS, nx, 3),
+                  (_lib.SMK_PASS_ZINV, nz, 5)]
+    if use_cache:
+        found = load_cached([(p, n) for p, n, _ in passes])
+        if len(found) == len(passes):
+            return {"choices": {PASS_NAMES[p]: found[(p, n)] for p, n, _ in passes}, "ms": {}, "cached": True}
+    cands = {p: variants(p, n) for p, n, _ in passes}
+    rounds = max(len(v) for v in cands.values())
+    if out is None:
+        out = grf.alloc_boxes(nx, ny, nz)
+    if workspace is None:
+        workspace = grf.GrfWorkspace(1)
+    amp = grf.pk_normalisation(nx, ny, nz, dcell)
+    noise = None if gpu_noise else torch.randn(nx * ny * nz, device="cuda").reshape(nx, ny, nz)
+    times = {p: {} for p, _, _ in passes}
+    for r in range(rounds):
+        cur = {}
+        for p, n, _ in passes:
+            v = cands[p][min(r, len(cands[p]) - 1)][0]
+            cur[(p, n)] = v
+        apply(cur)
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+        for e in evs:
+            e.record()
+        acc = {p: [] for p, _, _ in passes}
+        for k in range(1 + reps):
+            grf.make_boxes(nx, ny, nz, dcell, seed=1, noise=noise, amp=amp, out=out, workspace=workspace,
+                           pass_events=evs)
+            torch.cuda.synchronize()
+            if k == 0:
+                continue           # first call of a variant: launch set-up, cold caches
+            for p, n, mark in passes:
+                acc[p].append(evs[mark - 1].elapsed_time(evs[mark]))
+        for p, n, _ in passes:
+            v = cur[(p, n)]
+            times[p].setdefault(v, float(np.mean(acc[p])))
+    best = {}
+    for p, n, _ in passes:
+        v = min(times[p], key=times[p].get)
+        best[(p, n)] = v
+    apply(best)
+    _store(best)
+    info = {p: {v: (w, t) for v, w, t in cands[p]} for p, _, _ in passes}
+    return {"choices": {PASS_NAMES[p]: (best[(p, n)], *info[p][best[(p, n)]]) for p, n, _ in passes},
+            "ms": {PASS_NAMES[p]: {int(v): round(m, 3) for v, m in times[p].items()} for p, _, _ in passes},
+            "cached": False}

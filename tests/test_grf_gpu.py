@@ -160,3 +160,40 @@ def test_grf_rejects_bad_sizes(G):
     with pytest.raises(SmkError) as e:
         G.make_boxes(16, 8192, 16)            # axis longer than 4096
     assert e.value.status == SMK_ENOTSUPP
+
+
+VARIANT_AXES = {  # pass -> which axis is its line, shapes per length class
+    "zfwd": 2, "zinv": 2, "line": 1, "xpass": 0, "xgen": 0}
+CLASS_LEN = {512: 40, 1024: 600, 2560: 1536, 4096: 4000}
+
+
+@pytest.mark.parametrize("pname", ["zfwd", "line", "xpass", "xgen", "zinv"])
+def test_every_tile_variant_is_exact(G, pname):
+    """Each tile variant (W, threads) of each pass reproduces the FP64 oracle."""
+    from saclaymocks_gb300 import _lib, tune
+    pid = {v: k for k, v in tune.PASS_NAMES.items()}[pname]
+    lib = _lib.load()
+    gpu_noise = pname == "xgen"
+    for v, w, t in tune.variants(pid, 2):
+        import ctypes as C
+        nm = C.c_int32()
+        lib.smk_tune_info(pid, v, None, None, C.byref(nm))
+        n = CLASS_LEN[nm.value]
+        shape = [6, 4, 8]
+        shape[VARIANT_AXES[pname]] = n
+        nx, ny, nz = shape
+        _lib.check(lib.smk_tune_set(pid, n, v))
+        try:
+            if gpu_noise:
+                out = G.make_boxes(nx, ny, nz, 2.19, seed=17)
+                nk = ophilox.kspace_noise(nx, ny, nz, 17)
+                o64 = ograf.grf_from_modes(nk, nz, 2.19, 0.02, eta=("zz",), precision="f64")
+            else:
+                noise = np.random.RandomState(v).normal(size=shape).astype(np.float32)
+                out = G.make_boxes(nx, ny, nz, 2.19, noise=torch.from_numpy(noise).cuda())
+                o64 = ograf.grf_boxes(noise, 2.19, 0.02, eta=("zz",), precision="f64")
+            torch.cuda.synchronize()
+            _check(out.delta[0].cpu().numpy(), o64["delta"], f"{pname} variant {v} (W={w}, T={t})")
+            _check(out.eta[0].cpu().numpy(), o64["eta_zz"], f"{pname} variant {v} eta")
+        finally:
+            lib.smk_tune_set(pid, n, -1)
