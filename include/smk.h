@@ -222,6 +222,45 @@ int smk_skewers_flux_static(const SmkSkewers* sk, const int32_t* npix_host, cons
                             const float* delta_box, const float* eta_box, float* flux,
                             float* delta_out, float* eta_out, float* z_out, void* stream);
 
+/* ---------------------------------------------------------------- the (a,b,c) fit */
+/*
+ * Replaces the objective of fit_az.Fitter (py/SaclayMocks/fit_az.py:194-279: FGPA on stored
+ * delta_l + delta_s, eta_par, growth -> <F> -> dF = F/<F> - 1 -> binned P1D -> chi2) with the
+ * per-redshift-bin loss L = sum_j (<F>_j - Fbar*_j)^2 + sum_b ((P_b - P*_b)/P*_b)^2 and its
+ * exact gradient, so Migrad's finite differences become one adjoint pass.  The reductions run
+ * on the GPU (FP64 accumulators); the loss itself is assembled on the host from them.
+ * Pixels are recomputed from the fields in every pass, never stored.
+ */
+typedef struct {
+    const float* delta;     /* [n_total] delta_l + delta_s                                */
+    const float* eta;       /* [n_total] eta_par, or NULL                                 */
+    const float* G;         /* [n_total] growth, or NULL (G = 1)                          */
+    const int16_t* zbin;    /* [n_total] redshift bin of each pixel, 0..nzb-1             */
+    const int64_t* offset;  /* [n] first pixel of each skewer                             */
+    const int32_t* npix;    /* [n] pixels (1..2048)                                       */
+    const int32_t* order;   /* [n_slots] pairs of equal length, smk_fit_schedule (device) */
+    int64_t n_slots;
+    int64_t n_total;
+    int32_t nzb, nkb;       /* redshift bins, log-k bins (1..64 each)                     */
+    const double* kedges;   /* [nkb+1] k bin edges, h/Mpc (device)                        */
+    double dx;              /* pixel size, Mpc/h                                          */
+} SmkFitProblem;
+
+/* Host: pairs of equal-length skewers for the fit kernels (order_out: 2n + 16 ints). */
+int smk_fit_schedule(int64_t n, const int32_t* npix_host, int32_t* order_out, int64_t* n_slots_out);
+/* Length (doubles) of the accumulator array: [nzb] sum F per z bin, [1] sum F,
+ * [nkb] sum |X|^2 dx/N per k bin, [nzb][3] A, [nzb][3] B, [1] S. */
+int smk_fit_acc_len(int32_t nzb, int32_t nkb);
+/* Forward: zeroes acc, fills sum F per z bin, sum F, P1D power sums per k bin.
+ * theta: device [nzb][3] (a, b, c).  Workspace: 256 bytes. */
+int smk_fit_forward(const SmkFitProblem* fp, const float* theta, double* acc, void* workspace,
+                    size_t workspace_bytes, void* stream);
+/* Backward (after smk_fit_forward on the same acc): with gM_j = dL/d<F>_j / n_j and
+ * gP_b = dL/dP_b / count_b (device), fills A_j = sum (gM_j + gdF/<F>) dF/dtheta_j,
+ * B_j = sum dF/dtheta_j, S = sum gdF F; the gradient is A_j - S B_j / (n_total <F>^2). */
+int smk_fit_backward(const SmkFitProblem* fp, const float* theta, double* acc, const double* gM,
+                     const double* gP, void* workspace, size_t workspace_bytes, void* stream);
+
 /* ---------------------------------------------------------------- FGPA (util.fgpa) */
 /*
  * Replaces util.fgpa (py/SaclayMocks/util.py:421-433) as called from

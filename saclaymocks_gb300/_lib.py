@@ -62,6 +62,13 @@ class SmkSpectraParams(C.Structure):
                 ("growth24", C.c_float)]
 
 
+class SmkFitProblem(C.Structure):
+    _fields_ = [("delta", C.c_void_p), ("eta", C.c_void_p), ("G", C.c_void_p), ("zbin", C.c_void_p),
+                ("offset", C.c_void_p), ("npix", C.c_void_p), ("order", C.c_void_p),
+                ("n_slots", C.c_int64), ("n_total", C.c_int64), ("nzb", C.c_int32), ("nkb", C.c_int32),
+                ("kedges", C.c_void_p), ("dx", C.c_double)]
+
+
 # (name, restype, argtypes) of every exported entry point
 _SIGS = [
     ("smk_strerror", C.c_char_p, [C.c_int]),
@@ -90,6 +97,12 @@ _SIGS = [
     ("smk_skewers_flux_static", C.c_int, [C.POINTER(SmkSkewers), C.c_void_p, C.POINTER(SmkSpectraParams),
                                           C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_void_p]),
+    ("smk_fit_schedule", C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]),
+    ("smk_fit_acc_len", C.c_int, [C.c_int32, C.c_int32]),
+    ("smk_fit_forward", C.c_int, [C.POINTER(SmkFitProblem), C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_size_t, C.c_void_p]),
+    ("smk_fit_backward", C.c_int, [C.POINTER(SmkFitProblem), C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     ("smk_fgpa", C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p,
                            C.c_float, C.c_void_p, C.c_float, C.c_void_p, C.c_float, C.c_void_p,
                            C.c_void_p]),

@@ -1,0 +1,512 @@
+// The (a,b,c) fit on GB300: mean flux per redshift bin, binned 1D power spectrum of
+// dF = F/<F> - 1, and the exact adjoint of the loss
+//     L = sum_j (<F>_j - Fbar*_j)^2 + sum_b ((P_b - P*_b)/P*_b)^2
+// with per-bin FGPA parameters theta_j = (a_j, b_j, c_j) (the fit of
+// py/SaclayMocks/fit_az.py:194-279, with gradients instead of Migrad's finite differences).
+//
+// Pixels are never stored: every kernel recomputes F = exp(-a exp(b G (delta + c eta))) from
+// the fixed fields (delta = delta_l + delta_s, eta_par, G, redshift bin) and the parameters.
+//   fit_flux_kernel     F per pixel -> sum F per z bin and over all pixels (FP64)
+//   fit_p1d_kernel      per pair of equal-length skewers: dF, length-N DFT by Bluestein's chirp
+//                       transform on the FFT engine, |X_m|^2 dx/N binned in log-k (FP64)
+//   fit_adjoint_kernel  per pair: recompute X, back-propagate the P1D weights through the
+//                       inverse DFT (Bluestein again), then accumulate per bin
+//                       A_j = sum (gM_j + gdF/<F>) dF/dtheta_j, B_j = sum dF/dtheta_j and
+//                       S = sum gdF * F, so that dL/dtheta_j = A_j - S B_j / (n <F>^2)
+//                       (the coupling through the global mean <F> needs no second pass).
+#include <algorithm>
+#include <vector>
+
+#include "smk_fft.cuh"
+
+namespace smk {
+
+constexpr int FIT_T = 256;
+constexpr int FIT_MAX_BINS = 64;
+
+struct FitArgs {
+    const float* delta;
+    const float* eta;      // may be null (no RSD)
+    const float* G;        // may be null (G = 1)
+    const int16_t* zbin;   // [npix_total], 0..nzb-1
+    const int64_t* offset;
+    const int32_t* npix;
+    const int32_t* order;  // pairs of equal length (-1: empty)
+    int64_t n_items;
+    int64_t n_total;       // pixels
+    int nzb, nkb;
+    const float* theta;    // [nzb][3]
+    const double* kedges;  // [nkb + 1] log-k edges (h/Mpc)
+    double dx;
+    double* acc;           // accumulators, layout in smk_fit_acc_layout
+    const double* gM;      // backward: dL/d<F>_j / n_j            [nzb]
+    const double* gP;      // backward: dL/dP_b / count_b          [nkb]
+    unsigned long long* counter;
+    FftPlan plans[2];      // M = 2048, 4096
+};
+
+// accumulator layout (doubles)
+__host__ __device__ inline int acc_fsum(int) { return 0; }                       // [nzb]
+__host__ __device__ inline int acc_ftot(int nzb) { return nzb; }                 // [1]
+__host__ __device__ inline int acc_psum(int nzb) { return nzb + 1; }             // [nkb]
+__host__ __device__ inline int acc_A(int nzb, int nkb) { return nzb + 1 + nkb; }  // [nzb][3]
+__host__ __device__ inline int acc_B(int nzb, int nkb) { return 2 * nzb + 1 + nkb + 2 * nzb; }  // [nzb][3]
+__host__ __device__ inline int acc_S(int nzb, int nkb) { return 7 * nzb + 1 + nkb; }  // [1]
+__host__ __device__ inline int acc_len(int nzb, int nkb) { return 7 * nzb + 2 + nkb; }
+
+__device__ __forceinline__ float flux_of(const FitArgs& a, int64_t o, const float* th, float* tau1, float* g) {
+    const int j = a.zbin[o];
+    const float pa = th[3 * j], pb = th[3 * j + 1], pc = th[3 * j + 2];
+    const float e = a.eta ? __ldg(a.eta + o) : 0.f;
+    const float G = a.G ? __ldg(a.G + o) : 1.f;
+    const float gg = __ldg(a.delta + o) + pc * e;
+    const float t = expf(pb * G * gg);
+    *tau1 = t;
+    *g = gg;
+    return expf(-pa * t);
+}
+
+// ------------------------------------------------------------------ pass 1: mean flux
+__global__ void __launch_bounds__(FIT_T) fit_flux_kernel(const FitArgs a) {
+    __shared__ double sb[FIT_MAX_BINS + 1];
+    __shared__ float th[3 * FIT_MAX_BINS];
+    for (int i = threadIdx.x; i <= a.nzb; i += FIT_T) sb[i] = 0.0;
+    for (int i = threadIdx.x; i < 3 * a.nzb; i += FIT_T) th[i] = a.theta[i];
+    __syncthreads();
+    // per-thread FP32 partials over a short run of pixels, FP64 in shared memory
+    for (int64_t base = (blockIdx.x * (int64_t)FIT_T + threadIdx.x) * 16; base < a.n_total;
+         base += (int64_t)gridDim.x * FIT_T * 16) {
+        const int64_t end = min(base + 16, a.n_total);
+        int jcur = a.zbin[base];
+        float part = 0.f, tot = 0.f;
+        for (int64_t o = base; o < end; ++o) {
+            float t1, g;
+            const float F = flux_of(a, o, th, &t1, &g);
+            const int j = a.zbin[o];
+            if (j != jcur) {
+                atomicAdd(&sb[jcur], (double)part);
+                part = 0.f;
+                jcur = j;
+            }
+            part += F;
+            tot += F;
+        }
+        atomicAdd(&sb[jcur], (double)part);
+        atomicAdd(&sb[a.nzb], (double)tot);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i <= a.nzb; i += FIT_T) atomicAdd(a.acc + i, sb[i]);
+}
+
+// ------------------------------------------------------------------ Bluestein DFT helpers
+// chirp w_n = exp(-i pi n^2 / N) = exp(-2 pi i r / 2N), r = n^2 mod 2N (exact integers)
+__device__ __forceinline__ float2 chirp(int n, int N) {
+    const long long r = ((long long)n * n) % (2LL * N);
+    return twiddle((int)r, 2 * N);
+}
+
+// smallest power of two >= 2N - 1 (N <= 2048) and its plan slot
+__device__ __forceinline__ int bluestein_m(int N, int* slot) {
+    const int M = (2 * N - 1 <= 2048) ? 2048 : 4096;
+    *slot = M == 2048 ? 0 : 1;
+    return M;
+}
+
+// Unnormalised length-N DFT of the complex sequence held in s1[0..N) (natural order),
+// forward (e^{-}) or inverse (e^{+}); result left in s1[0..N) in natural order.  s2 is
+// scratch of M elements; tw the twiddle table of M.  Block-synchronous.
+template <bool INV>
+__device__ void bluestein(float2* s1, float2* s2, const float2* tw, int N, int M, const FftPlan& pl) {
+    // a_n = x_n w_n (INV: x_n conj(w_n)); b_d = conj(w_d) (INV: w_d) for |d| < N, wrapped
+    for (int n = threadIdx.x; n < M; n += FIT_T) {
+        if (n < N) {
+            const float2 w = chirp(n, N);
+            s1[n] = INV ? cmulc(s1[n], w) : cmul(s1[n], w);
+        } else {
+            s1[n] = make_float2(0.f, 0.f);
+        }
+        const int d = n < N ? n : (n > M - N ? M - n : -1);
+        if (d >= 0) {
+            const float2 w = chirp(d, N);
+            s2[n] = INV ? w : make_float2(w.x, -w.y);
+        } else {
+            s2[n] = make_float2(0.f, 0.f);
+        }
+    }
+    __syncthreads();
+    fft_tile<false, 1, 1, FIT_T>(s1, tw, pl);
+    fft_tile<false, 1, 1, FIT_T>(s2, tw, pl);
+    for (int n = threadIdx.x; n < M; n += FIT_T) s1[n] = cmul(s1[n], s2[n]);  // digit-reversed, same order
+    __syncthreads();
+    fft_tile<true, 1, 1, FIT_T>(s1, tw, pl);
+    const float inv_m = 1.0f / (float)M;
+    for (int k = threadIdx.x; k < N; k += FIT_T) {
+        const float2 w = chirp(k, N);
+        const float2 c = cscale(s1[k], inv_m);
+        s1[k] = INV ? cmulc(c, w) : cmul(c, w);
+    }
+    __syncthreads();
+}
+
+// bin of frequency m of a length-N spectrum: numpy's rfftfreq(N)*2*k_ny in FP64 and
+// searchsorted(edges, k, 'right') - 1 with the last edge inclusive; -1 outside
+__device__ __forceinline__ int kbin(int m, int N, double kfac, const double* edges, int nkb) {
+    const double k = ((double)m * (1.0 / (double)N)) * kfac;
+    if (k < edges[0] || k > edges[nkb]) return -1;
+    if (k == edges[nkb]) return nkb - 1;
+    int lo = 0, hi = nkb;  // edges[lo] <= k < edges[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (edges[mid] <= k) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+struct PairSetup {
+    int sid[2];
+    int N;
+    int64_t off[2];
+};
+
+// Load the pair (dF of both skewers into s1 as re/im); returns via shared `ps`.
+__device__ void load_pair(const FitArgs& a, const float* th, float fbar_inv, const PairSetup& ps, float2* s1) {
+    for (int i = threadIdx.x; i < ps.N; i += FIT_T) {
+        float v[2] = {0.f, 0.f};
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+            if (ps.sid[t] >= 0) {
+                float t1, g;
+                v[t] = flux_of(a, ps.off[t] + i, th, &t1, &g) * fbar_inv - 1.0f;
+            }
+        }
+        s1[i] = make_float2(v[0], v[1]);
+    }
+    __syncthreads();
+}
+
+__device__ bool next_pair(const FitArgs& a, long long* item_sh, PairSetup* ps) {
+    if (threadIdx.x == 0) *item_sh = (long long)atomicAdd(a.counter, 1ULL);
+    __syncthreads();
+    const long long item = *item_sh;
+    if (item >= a.n_items) return false;
+    if (threadIdx.x < 2) {
+        const int sid = a.order[2 * item + threadIdx.x];
+        ps->sid[threadIdx.x] = sid;
+        ps->off[threadIdx.x] = sid >= 0 ? a.offset[sid] : 0;
+        if (threadIdx.x == 0) ps->N = a.npix[sid];
+    }
+    __syncthreads();
+    return true;
+}
+
+// Add `v` to sbins[bin] for every lane: lanes hold consecutive frequencies so equal bins form
+// contiguous runs; each run is summed by a segmented shuffle scan and its first lane issues
+// one shared-memory FP64 atomic (bin < 0: nothing).
+__device__ __forceinline__ void warp_bin_add(double* sbins, int bin, float v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const float v2 = __shfl_down_sync(0xffffffffu, v, off);
+        const int b2 = __shfl_down_sync(0xffffffffu, bin, off);
+        if (lane + off < 32 && b2 == bin) v += v2;
+    }
+    const int bprev = __shfl_up_sync(0xffffffffu, bin, 1);
+    if (bin >= 0 && (lane == 0 || bprev != bin)) atomicAdd(&sbins[bin], (double)v);
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// ------------------------------------------------------------------ pass 2: binned P1D
+__global__ void __launch_bounds__(FIT_T) fit_p1d_kernel(const FitArgs a) {
+    extern __shared__ float2 smem[];
+    float2* s1 = smem;
+    float2* s2 = smem + FFT_MAX_N;
+    float2* tw = smem + 2 * FFT_MAX_N;
+    __shared__ double psum[FIT_MAX_BINS];
+    __shared__ double edges[FIT_MAX_BINS + 1];
+    __shared__ float th[3 * FIT_MAX_BINS];
+    __shared__ long long item_sh;
+    __shared__ PairSetup ps;
+    for (int i = threadIdx.x; i < a.nkb; i += FIT_T) psum[i] = 0.0;
+    for (int i = threadIdx.x; i <= a.nkb; i += FIT_T) edges[i] = a.kedges[i];
+    for (int i = threadIdx.x; i < 3 * a.nzb; i += FIT_T) th[i] = a.theta[i];
+    const float fbar_inv = (float)((double)a.n_total / a.acc[acc_ftot(a.nzb)]);
+    const double kfac = 2.0 * (3.14159265358979323846 / a.dx);
+    int curM = 0;
+    while (next_pair(a, &item_sh, &ps)) {
+        const int N = ps.N;
+        int slot;
+        const int M = bluestein_m(N, &slot);
+        if (M != curM) {
+            fill_twiddles<FIT_T>(tw, M);
+            curM = M;
+        }
+        load_pair(a, th, fbar_inv, ps, s1);
+        bluestein<false>(s1, s2, tw, N, M, a.plans[slot]);
+        // X1_m = (Z_m + Z*_{N-m})/2, X2_m = (Z_m - Z*_{N-m})/(2i), m = 0..N/2
+        const float norm = (float)(a.dx / (double)N);
+        const int half = N / 2;
+        for (int m0 = 0; m0 <= half; m0 += FIT_T) {    // block-uniform trip count
+            const int m = m0 + (int)threadIdx.x;
+            int b = -1;
+            float p = 0.f;
+            if (m <= half) {
+                b = kbin(m, N, kfac, edges, a.nkb);
+                const float2 zk = s1[m], zm = s1[m == 0 ? 0 : N - m];
+                const float x1r = 0.5f * (zk.x + zm.x), x1i = 0.5f * (zk.y - zm.y);
+                const float x2r = 0.5f * (zk.y + zm.y), x2i = -0.5f * (zk.x - zm.x);
+                p = x1r * x1r + x1i * x1i;
+                if (ps.sid[1] >= 0) p += x2r * x2r + x2i * x2i;
+                p *= norm;
+            }
+            warp_bin_add(psum, b, p);
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < a.nkb; i += FIT_T) atomicAdd(a.acc + acc_psum(a.nzb) + i, psum[i]);
+}
+
+// ------------------------------------------------------------------ backward
+__global__ void __launch_bounds__(FIT_T) fit_adjoint_kernel(const FitArgs a) {
+    extern __shared__ float2 smem[];
+    float2* s1 = smem;
+    float2* s2 = smem + FFT_MAX_N;
+    float2* tw = smem + 2 * FFT_MAX_N;
+    __shared__ double sA[3 * FIT_MAX_BINS], sB[3 * FIT_MAX_BINS], sS;
+    __shared__ double edges[FIT_MAX_BINS + 1], gP[FIT_MAX_BINS], gM[FIT_MAX_BINS];
+    __shared__ float th[3 * FIT_MAX_BINS];
+    __shared__ long long item_sh;
+    __shared__ PairSetup ps;
+    for (int i = threadIdx.x; i < 3 * a.nzb; i += FIT_T) {
+        sA[i] = 0.0;
+        sB[i] = 0.0;
+        th[i] = a.theta[i];
+    }
+    for (int i = threadIdx.x; i <= a.nkb; i += FIT_T) edges[i] = a.kedges[i];
+    for (int i = threadIdx.x; i < a.nkb; i += FIT_T) gP[i] = a.gP[i];
+    for (int i = threadIdx.x; i < a.nzb; i += FIT_T) gM[i] = a.gM[i];
+    if (threadIdx.x == 0) sS = 0.0;
+    const double fbar = a.acc[acc_ftot(a.nzb)] / (double)a.n_total;
+    const float fbar_inv = (float)(1.0 / fbar);
+    const double kfac = 2.0 * (3.14159265358979323846 / a.dx);
+    int curM = 0;
+    while (next_pair(a, &item_sh, &ps)) {
+        const int N = ps.N;
+        int slot;
+        const int M = bluestein_m(N, &slot);
+        if (M != curM) {
+            fill_twiddles<FIT_T>(tw, M);
+            curM = M;
+        }
+        load_pair(a, th, fbar_inv, ps, s1);
+        bluestein<false>(s1, s2, tw, N, M, a.plans[slot]);
+        // V_t (Hermitian): V_m = w_m X_m (0<m<N/2), V_{N-m} = conj; V_0, V_{N/2} = 2 Re(w X);
+        // packed W = V_1 + i V_2; the unnormalised inverse DFT of W is gdF_1 + i gdF_2.
+        const float norm = (float)(a.dx / (double)N);
+        for (int m = threadIdx.x; m <= N / 2; m += FIT_T) {
+            const float2 zk = s1[m], zm = s1[m == 0 ? 0 : N - m];
+            const int b = kbin(m, N, kfac, edges, a.nkb);
+            const float wgt = b >= 0 ? (float)gP[b] * norm : 0.f;
+            float2 x1 = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+            float2 x2 = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+            if (ps.sid[1] < 0) x2 = make_float2(0.f, 0.f);
+            x1 = cscale(x1, wgt);
+            x2 = cscale(x2, wgt);
+            // results written to s2 first (s1 still read by other threads)
+            if (m == 0 || 2 * m == N) {
+                s2[m] = make_float2(2.f * x1.x, 2.f * x2.x);
+            } else {
+                s2[m] = make_float2(x1.x - x2.y, x1.y + x2.x);          // V1_m + i V2_m
+                s2[N - m] = make_float2(x1.x + x2.y, x2.x - x1.y);      // conj(V1_m) + i conj(V2_m)
+            }
+        }
+        __syncthreads();
+        for (int n = threadIdx.x; n < N; n += FIT_T) s1[n] = s2[n];
+        __syncthreads();
+        bluestein<true>(s1, s2, tw, N, M, a.plans[slot]);
+        // per pixel: gF~ = gM_j + gdF / <F>; dF/da = -tau1 F, dF/db = -a tau1 G g F,
+        // dF/dc = -a tau1 b G eta F
+        // per-thread FP32 partials for the current redshift bin, flushed to the block's FP64
+        // accumulators when the bin changes and, warp-reduced, at the end of the pair
+        float acc6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, accS = 0.f;
+        int jw = -1;
+        for (int i = threadIdx.x; i < 2 * N; i += FIT_T) {
+            const int t = i < N ? 0 : 1;
+            const int ii = i - t * N;
+            if (ps.sid[t] < 0) continue;
+            const int64_t o = ps.off[t] + ii;
+            float t1, g;
+            const float F = flux_of(a, o, th, &t1, &g);
+            const float gdF = t ? s1[ii].y : s1[ii].x;
+            const int j = a.zbin[o];
+            if (jw >= 0 && j != jw) {
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    atomicAdd(&sA[3 * jw + q], (double)acc6[q]);
+                    atomicAdd(&sB[3 * jw + q], (double)acc6[3 + q]);
+                    acc6[q] = acc6[3 + q] = 0.f;
+                }
+            }
+            jw = j;
+            const float pa = th[3 * j], pb = th[3 * j + 1];
+            const float e = a.eta ? __ldg(a.eta + o) : 0.f;
+            const float G = a.G ? __ldg(a.G + o) : 1.f;
+            const float dFa = -t1 * F;
+            const float dFb = -pa * t1 * G * g * F;
+            const float dFc = -pa * t1 * pb * G * e * F;
+            const float gF = (float)gM[j] + gdF * fbar_inv;
+            acc6[0] = fmaf(gF, dFa, acc6[0]);
+            acc6[1] = fmaf(gF, dFb, acc6[1]);
+            acc6[2] = fmaf(gF, dFc, acc6[2]);
+            acc6[3] += dFa;
+            acc6[4] += dFb;
+            acc6[5] += dFc;
+            accS = fmaf(gdF, F, accS);
+        }
+        const float wS = warp_sum(accS);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&sS, (double)wS);
+        for (;;) {  // warp-uniform loop over the distinct bins still held by the lanes
+            const unsigned act = __ballot_sync(0xffffffffu, jw >= 0);
+            if (!act) break;
+            const int jl = __shfl_sync(0xffffffffu, jw, __ffs(act) - 1);
+            const bool mine = jw == jl;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                const float v = warp_sum(mine ? acc6[q] : 0.f);
+                if ((threadIdx.x & 31) == 0) atomicAdd(q < 3 ? &sA[3 * jl + q] : &sB[3 * jl + q - 3], (double)v);
+            }
+            if (mine) jw = -1;
+        }
+        __syncthreads();
+    }
+    double* A = a.acc + acc_A(a.nzb, a.nkb);
+    double* B = a.acc + acc_B(a.nzb, a.nkb);
+    for (int i = threadIdx.x; i < 3 * a.nzb; i += FIT_T) {
+        atomicAdd(A + i, sA[i]);
+        atomicAdd(B + i, sB[i]);
+    }
+    if (threadIdx.x == 0) atomicAdd(a.acc + acc_S(a.nzb, a.nkb), sS);
+}
+
+static int fit_grid(const void* kernel, size_t smem, int64_t items, int* grid) {
+    int dev = 0, nsm = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return check_launch("cudaFuncSetAttribute(fit)");
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, FIT_T, smem) != cudaSuccess)
+        return check_launch("occupancy(fit)");
+    *grid = (int)std::max<int64_t>(1, std::min<int64_t>(items, (int64_t)std::max(per_sm, 1) * nsm));
+    return SMK_OK;
+}
+
+}  // namespace smk
+
+using namespace smk;
+
+extern "C" {
+
+int smk_fit_acc_len(int32_t nzb, int32_t nkb) { return acc_len(nzb, nkb); }
+
+int smk_fit_schedule(int64_t n, const int32_t* npix_host, int32_t* order_out, int64_t* n_slots_out) {
+    if (n < 0 || (n > 0 && (!npix_host || !order_out)) || !n_slots_out)
+        return fail(SMK_EINVAL, "smk_fit_schedule: null argument");
+    std::vector<std::pair<int32_t, int32_t>> key((size_t)n);
+    for (int64_t s = 0; s < n; ++s) {
+        if (npix_host[s] < 1 || npix_host[s] > FFT_MAX_N / 2)
+            return fail(SMK_ENOTSUPP, "smk_fit_schedule: skewer %lld has %d pixels (1..%d)", (long long)s,
+                        npix_host[s], FFT_MAX_N / 2);
+        key[(size_t)s] = {npix_host[s], (int32_t)s};
+    }
+    std::stable_sort(key.begin(), key.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
+    int64_t k = 0;
+    for (size_t i = 0; i < key.size();) {
+        size_t j = i;
+        while (j < key.size() && key[j].first == key[i].first) ++j;
+        for (size_t q = i; q < j; ++q) order_out[k++] = key[q].second;
+        if ((j - i) & 1) order_out[k++] = -1;
+        i = j;
+    }
+    *n_slots_out = k;
+    return SMK_OK;
+}
+
+static int fit_args(const SmkFitProblem* fp, const float* theta, double* acc, const double* gM, const double* gP,
+                    unsigned long long* counter, FitArgs* a) {
+    if (!fp || !theta || !acc || !counter) return fail(SMK_EINVAL, "smk_fit: null argument");
+    if (!fp->delta || !fp->zbin || !fp->offset || !fp->npix || !fp->order || !fp->kedges)
+        return fail(SMK_EINVAL, "smk_fit: null problem array");
+    if (fp->nzb < 1 || fp->nzb > FIT_MAX_BINS || fp->nkb < 1 || fp->nkb > FIT_MAX_BINS || !(fp->dx > 0))
+        return fail(SMK_EINVAL, "smk_fit: 1..%d redshift and k bins, dx > 0", FIT_MAX_BINS);
+    a->delta = fp->delta;
+    a->eta = fp->eta;
+    a->G = fp->G;
+    a->zbin = fp->zbin;
+    a->offset = fp->offset;
+    a->npix = fp->npix;
+    a->order = fp->order;
+    a->n_items = fp->n_slots / 2;
+    a->n_total = fp->n_total;
+    a->nzb = fp->nzb;
+    a->nkb = fp->nkb;
+    a->theta = theta;
+    a->kedges = fp->kedges;
+    a->dx = fp->dx;
+    a->acc = acc;
+    a->gM = gM;
+    a->gP = gP;
+    a->counter = counter;
+    make_plan(2048, &a->plans[0]);
+    make_plan(4096, &a->plans[1]);
+    return SMK_OK;
+}
+
+int smk_fit_forward(const SmkFitProblem* fp, const float* theta, double* acc, void* workspace,
+                    size_t workspace_bytes, void* stream) {
+    if (!workspace || workspace_bytes < 256) return fail(SMK_EWORKSPACE, "smk_fit_forward: 256-byte workspace");
+    FitArgs a;
+    int rc = fit_args(fp, theta, acc, nullptr, nullptr, (unsigned long long*)workspace, &a);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemsetAsync(acc, 0, sizeof(double) * acc_len(a.nzb, a.nkb), st) != cudaSuccess ||
+        cudaMemsetAsync(workspace, 0, 8, st) != cudaSuccess)
+        return check_launch("smk_fit_forward: memset");
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int g1 = (int)std::min<int64_t>((a.n_total + FIT_T * 16 - 1) / (FIT_T * 16), 8LL * nsm);
+    fit_flux_kernel<<<std::max(g1, 1), FIT_T, 0, st>>>(a);
+    if ((rc = check_launch("fit_flux_kernel"))) return rc;
+    const size_t smem = 3 * FFT_MAX_N * sizeof(float2);
+    int grid = 0;
+    if ((rc = fit_grid((const void*)fit_p1d_kernel, smem, a.n_items, &grid))) return rc;
+    fit_p1d_kernel<<<grid, FIT_T, smem, st>>>(a);
+    return check_launch("fit_p1d_kernel");
+}
+
+int smk_fit_backward(const SmkFitProblem* fp, const float* theta, double* acc, const double* gM,
+                     const double* gP, void* workspace, size_t workspace_bytes, void* stream) {
+    if (!workspace || workspace_bytes < 256) return fail(SMK_EWORKSPACE, "smk_fit_backward: 256-byte workspace");
+    if (!gM || !gP) return fail(SMK_EINVAL, "smk_fit_backward: null weights");
+    FitArgs a;
+    int rc = fit_args(fp, theta, acc, gM, gP, (unsigned long long*)workspace, &a);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int off = acc_A(a.nzb, a.nkb);
+    if (cudaMemsetAsync(acc + off, 0, sizeof(double) * (acc_len(a.nzb, a.nkb) - off), st) != cudaSuccess ||
+        cudaMemsetAsync(workspace, 0, 8, st) != cudaSuccess)
+        return check_launch("smk_fit_backward: memset");
+    const size_t smem = 3 * FFT_MAX_N * sizeof(float2);
+    int grid = 0;
+    if ((rc = fit_grid((const void*)fit_adjoint_kernel, smem, a.n_items, &grid))) return rc;
+    fit_adjoint_kernel<<<grid, FIT_T, smem, st>>>(a);
+    return check_launch("fit_adjoint_kernel");
+}
+
+}  // extern "C"

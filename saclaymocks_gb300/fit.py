@@ -1,0 +1,201 @@
+"""The (a,b,c) fit on the GPU with an adjoint gradient (host side of smk_fit_*).
+
+The reference fits a(z) with iminuit's Migrad on fit_az.Fitter.chi2 (py/SaclayMocks/fit_az.py
+:194-279): every call recomputes the FGPA of all stored pixels, <F>, dF = F/<F> - 1 per
+spectrum and the binned P1D, and Migrad takes its derivatives by finite differences.  Here the
+same kind of objective, per redshift bin j with parameters theta_j = (a_j, b_j, c_j),
+
+    L(theta) = sum_j (<F>_j - Fbar*_j)^2 + sum_b ((P_b - P*_b) / P*_b)^2,
+
+is evaluated by two GPU passes (mean flux per z bin; P1D of dF by Bluestein DFTs per pair of
+equal-length skewers) and differentiated exactly by one adjoint pass that recomputes the
+pixels instead of storing them.  Reductions are FP64; the loss and its gradient are assembled
+in FP64 on the host from the reductions.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .grf import stream_handle
+
+
+def bin_index(x, edges):
+    """scipy binned_statistic bins: [e_i, e_i+1), the last one closed; -1 outside."""
+    x = np.asarray(x)
+    nb = len(edges) - 1
+    idx = np.searchsorted(edges, x, side="right") - 1
+    idx = np.where(x == edges[-1], nb - 1, idx)
+    return np.where((idx >= 0) & (idx < nb), idx, -1)
+
+
+class FitProblem:
+    """Fixed fields of the fit on the GPU: per-pixel delta (= delta_l + delta_s), eta_par,
+    growth G and redshift, skewer lengths (packed layout), z and log-k bin edges."""
+
+    def __init__(self, delta, eta, G, z, lengths, zedges, kedges, dx=0.2, device="cuda"):
+        dv = torch.device(device)
+        self.device = dv
+        to_dev = lambda x, dt: None if x is None else torch.as_tensor(x).to(device=dv, dtype=dt).contiguous()  # noqa: E731
+        self.delta = to_dev(delta, torch.float32)
+        self.eta = to_dev(eta, torch.float32)
+        self.G = to_dev(G, torch.float32)
+        self.zedges = np.asarray(zedges, np.float64)
+        self.kedges = np.asarray(kedges, np.float64)
+        self.nzb, self.nkb = len(self.zedges) - 1, len(self.kedges) - 1
+        zt = torch.as_tensor(z).to(device=dv, dtype=torch.float64)
+        zb = torch.searchsorted(torch.as_tensor(self.zedges, device=dv), zt, right=True) - 1
+        self.zbin = zb.clamp(0, self.nzb - 1).to(torch.int16).contiguous()
+        self.lengths = np.ascontiguousarray(lengths, np.int32)
+        self.offset = np.concatenate([[0], np.cumsum(self.lengths[:-1], dtype=np.int64)]).astype(np.int64)
+        self.n_total = int(self.lengths.astype(np.int64).sum())
+        self.dx = float(dx)
+        lib = _lib.load()
+        order = np.empty(2 * len(self.lengths) + 16, np.int32)
+        ns = C.c_int64()
+        _lib.check(lib.smk_fit_schedule(len(self.lengths), self.lengths.ctypes.data, order.ctypes.data,
+                                        C.byref(ns)), "smk_fit_schedule")
+        self.d_order = torch.from_numpy(order[:ns.value].copy()).to(dv)
+        self.d_off = torch.from_numpy(self.offset).to(dv)
+        self.d_npix = torch.from_numpy(self.lengths).to(dv)
+        self.d_kedges = torch.from_numpy(self.kedges).to(dv)
+        self.acc = torch.zeros(lib.smk_fit_acc_len(self.nzb, self.nkb), dtype=torch.float64, device=dv)
+        self.ws = torch.zeros(32, dtype=torch.int64, device=dv)
+        self.d_gM = torch.zeros(self.nzb, dtype=torch.float64, device=dv)
+        self.d_gP = torch.zeros(self.nkb, dtype=torch.float64, device=dv)
+        self.d_theta = torch.zeros((self.nzb, 3), dtype=torch.float32, device=dv)
+        # fixed counts: pixels per z bin, (skewer, mode) pairs per k bin
+        self.cnt_z = torch.bincount(self.zbin.long(), minlength=self.nzb).double().cpu().numpy()
+        cnt_k = np.zeros(self.nkb)
+        for N, mult in zip(*np.unique(self.lengths, return_counts=True)):
+            k = np.fft.rfftfreq(int(N)) * 2 * (np.pi / self.dx)
+            b = bin_index(k, self.kedges)
+            cnt_k += mult * np.bincount(b[b >= 0], minlength=self.nkb)
+        self.cnt_k = cnt_k
+        self.fp = _lib.SmkFitProblem(
+            delta=self.delta.data_ptr(), eta=self.eta.data_ptr() if self.eta is not None else None,
+            G=self.G.data_ptr() if self.G is not None else None, zbin=self.zbin.data_ptr(),
+            offset=self.d_off.data_ptr(), npix=self.d_npix.data_ptr(), order=self.d_order.data_ptr(),
+            n_slots=ns.value, n_total=self.n_total, nzb=self.nzb, nkb=self.nkb,
+            kedges=self.d_kedges.data_ptr(), dx=self.dx)
+
+    # ---------------------------------------------------------------- passes
+    def _set_theta(self, theta):
+        t = torch.as_tensor(np.asarray(theta, np.float32).reshape(self.nzb, 3))
+        self.d_theta.copy_(t)
+
+    def reductions(self, theta):
+        """(<F>_j, P_b, <F>) in FP64 from the GPU forward passes."""
+        lib = _lib.load()
+        self._set_theta(theta)
+        _lib.check(lib.smk_fit_forward(C.byref(self.fp), self.d_theta.data_ptr(), self.acc.data_ptr(),
+                                       self.ws.data_ptr(), self.ws.numel() * 8, stream_handle()),
+                   "smk_fit_forward")
+        acc = self.acc.cpu().numpy()
+        nzb, nkb = self.nzb, self.nkb
+        with np.errstate(invalid="ignore", divide="ignore"):
+            mz = acc[:nzb] / self.cnt_z
+            pk = acc[nzb + 1:nzb + 1 + nkb] / self.cnt_k
+        return mz, pk, acc[nzb] / self.n_total
+
+    def loss(self, theta, target_mz, target_pk) -> float:
+        mz, pk, _ = self.reductions(theta)
+        return float(((mz - target_mz) ** 2).sum() + (((pk - target_pk) / target_pk) ** 2).sum())
+
+    def forward(self, theta, target_mz, target_pk):
+        """Loss and the state the adjoint pass needs (small host arrays, no pixels)."""
+        mz, pk, fbar = self.reductions(theta)
+        L = float(((mz - target_mz) ** 2).sum() + (((pk - target_pk) / target_pk) ** 2).sum())
+        state = dict(theta=np.asarray(theta, np.float64).reshape(self.nzb, 3).copy(), mz=mz, pk=pk,
+                     fbar=fbar, target_mz=target_mz, target_pk=target_pk)
+        return L, state
+
+    def backward(self, state):
+        """dL/dtheta [nzb, 3] by the adjoint pass; the pixels are recomputed on the GPU.  The
+        accumulators must still hold this state's forward reductions (<F>)."""
+        lib = _lib.load()
+        mz, pk = state["mz"], state["pk"]
+        gM = 2 * (mz - state["target_mz"]) / self.cnt_z
+        gP = 2 * (pk - state["target_pk"]) / state["target_pk"] ** 2 / self.cnt_k
+        self.d_gM.copy_(torch.from_numpy(np.nan_to_num(gM)))
+        self.d_gP.copy_(torch.from_numpy(np.nan_to_num(gP)))
+        self._set_theta(state["theta"])
+        _lib.check(lib.smk_fit_backward(C.byref(self.fp), self.d_theta.data_ptr(), self.acc.data_ptr(),
+                                        self.d_gM.data_ptr(), self.d_gP.data_ptr(), self.ws.data_ptr(),
+                                        self.ws.numel() * 8, stream_handle()), "smk_fit_backward")
+        acc = self.acc.cpu().numpy()
+        nzb, nkb = self.nzb, self.nkb
+        A = acc[nzb + 1 + nkb:nzb + 1 + nkb + 3 * nzb].reshape(nzb, 3)
+        B = acc[4 * nzb + 1 + nkb:7 * nzb + 1 + nkb].reshape(nzb, 3)
+        S = acc[7 * nzb + 1 + nkb]
+        return A - S * B / (self.n_total * state["fbar"] ** 2)
+
+    def loss_grad(self, theta, target_mz, target_pk):
+        """(L, dL/dtheta [nzb, 3]) by the forward passes + one adjoint pass."""
+        L, state = self.forward(theta, target_mz, target_pk)
+        return L, self.backward(state)
+
+    def fd_grad(self, theta, target_mz, target_pk, h=1e-4):
+        """Central finite differences of the GPU loss (relative step h): the derivative-free
+        way Migrad proceeds, 2 * 3 * nzb loss evaluations."""
+        theta = np.asarray(theta, np.float64).reshape(self.nzb, 3)
+        g = np.zeros_like(theta)
+        for j in range(self.nzb):
+            for p in range(3):
+                st = h * max(abs(theta[j, p]), 1e-3)
+                tp, tm = theta.copy(), theta.copy()
+                tp[j, p] += st
+                tm[j, p] -= st
+                g[j, p] = (self.loss(tp, target_mz, target_pk) - self.loss(tm, target_mz, target_pk)) / (2 * st)
+        return g
+
+
+class FgpaP1DLoss(torch.autograd.Function):
+    """L(theta) as a torch autograd Function: forward = GPU reductions (saves only the bin
+    means and <F>), backward = the adjoint pass, which recomputes every pixel."""
+
+    @staticmethod
+    def forward(ctx, theta, problem, target_mz, target_pk):
+        L, state = problem.forward(theta.detach().cpu().numpy(), target_mz, target_pk)
+        ctx.problem = problem
+        ctx.state = state
+        return theta.new_tensor(L)
+
+    @staticmethod
+    def backward(ctx, gL):
+        g = ctx.problem.backward(ctx.state)
+        return gL * torch.as_tensor(g, dtype=gL.dtype, device=gL.device), None, None, None
+
+
+def adam_fit(problem: FitProblem, theta0, target_mz, target_pk, steps=50, lr=0.02, grad="adjoint",
+             h=1e-4):
+    """Adam on log-parameters (all of a, b, c are positive).  grad: "adjoint" or "fd".
+    Returns (theta, losses, seconds, gradient evaluations)."""
+    theta0 = np.asarray(theta0, np.float64).reshape(problem.nzb, 3)
+    x = np.log(theta0)
+    m = np.zeros_like(x)
+    v = np.zeros_like(x)
+    b1, b2, eps = 0.9, 0.999, 1e-12
+    losses = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for it in range(1, steps + 1):
+        th = np.exp(x)
+        if grad == "adjoint":
+            L, g = problem.loss_grad(th, target_mz, target_pk)
+        else:
+            L = problem.loss(th, target_mz, target_pk)
+            g = problem.fd_grad(th, target_mz, target_pk, h)
+        losses.append(L)
+        gx = g * th                      # d/dlog(theta)
+        m = b1 * m + (1 - b1) * gx
+        v = b2 * v + (1 - b2) * gx * gx
+        mh = m / (1 - b1 ** it)
+        vh = v / (1 - b2 ** it)
+        x = x - lr * mh / (np.sqrt(vh) + eps)
+    torch.cuda.synchronize()
+    return np.exp(x), losses, time.perf_counter() - t0, steps

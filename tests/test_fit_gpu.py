@@ -1,0 +1,78 @@
+"""The (a,b,c) fit on the GPU: reductions, loss, adjoint gradient and the Adam fit against the
+oracle's FP64 restatement (oracle/fit.py, whose chi2 form is pinned to fit_az.Fitter.chi2)."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from oracle import fit as ofit      # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def problem_pair():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from saclaymocks_gb300 import fit
+    rng = np.random.RandomState(0)
+    lengths = rng.randint(40, 1100, size=64)
+    lengths[:6] = lengths[6:12]             # some equal lengths -> paired skewers
+    lengths[20] = 2048                      # longest supported: Bluestein M = 4096
+    n = int(lengths.sum())
+    delta = (rng.normal(0, 1, n)).astype(np.float32)
+    eta = (rng.normal(0, 0.4, n)).astype(np.float32)
+    G = rng.uniform(0.8, 1.0, n).astype(np.float32)
+    z = np.concatenate([np.sort(rng.uniform(1.8, 3.6, 1)) + np.linspace(0, 0.3, L) for L in lengths])
+    z = np.clip(z, 1.8, 3.6)
+    zedges = np.linspace(1.8, 3.6, 11)
+    kedges = np.logspace(np.log10(0.05), np.log10(15.0), 33)
+    gp = fit.FitProblem(delta, eta, G, z, lengths, zedges, kedges, 0.2)
+    op = ofit.ZBinProblem(delta.astype(np.float64), eta.astype(np.float64), G.astype(np.float64), z,
+                          lengths, zedges, kedges, 0.2)
+    truth = np.tile([0.1, 1.58, 0.6], (10, 1))
+    mz, pk, *_ = op.reductions(op.flux(truth))
+    return gp, op, mz, pk
+
+
+def test_reductions_match_oracle(problem_pair):
+    gp, op, _, _ = problem_pair
+    theta = np.tile([0.13, 1.4, 0.5], (10, 1)) * np.linspace(0.9, 1.1, 10)[:, None]
+    mz, pk, fbar = gp.reductions(theta)
+    omz, opk, ofbar, *_ = op.reductions(op.flux(theta))
+    np.testing.assert_allclose(mz, omz, rtol=2e-6)
+    np.testing.assert_allclose(fbar, ofbar, rtol=2e-6)
+    np.testing.assert_allclose(pk, opk, rtol=2e-4)
+
+
+def test_adjoint_gradient_matches_oracle_and_fd(problem_pair):
+    gp, op, mz, pk = problem_pair
+    theta = np.tile([0.15, 1.3, 0.4], (10, 1))
+    L, g = gp.loss_grad(theta, mz, pk)
+    oL, og = op.loss_grad(theta, mz, pk)
+    assert L == pytest.approx(oL, rel=1e-4)
+    scale = np.abs(og).max()
+    np.testing.assert_allclose(g, og, rtol=0, atol=2e-4 * scale)
+    gfd = gp.fd_grad(theta, mz, pk, h=1e-3)
+    np.testing.assert_allclose(g, gfd, rtol=0, atol=5e-3 * scale)
+
+
+def test_autograd_function(problem_pair):
+    from saclaymocks_gb300 import fit
+    gp, op, mz, pk = problem_pair
+    th = torch.tensor(np.tile([0.12, 1.5, 0.55], (10, 1)), dtype=torch.float64, requires_grad=True)
+    L = fit.FgpaP1DLoss.apply(th, gp, mz, pk)
+    L.backward()
+    _, og = op.loss_grad(th.detach().numpy(), mz, pk)
+    np.testing.assert_allclose(th.grad.numpy(), og, rtol=0, atol=2e-4 * np.abs(og).max())
+
+
+def test_adjoint_and_fd_fits_agree(problem_pair):
+    """Adam from (0.15, 1.3, 0.4) with adjoint and with finite-difference gradients: same
+    parameters to 1e-4 relative after the same iterations, and the loss goes down."""
+    from saclaymocks_gb300 import fit
+    gp, op, mz, pk = problem_pair
+    th0 = np.tile([0.15, 1.3, 0.4], (10, 1))
+    ta, la, _, _ = fit.adam_fit(gp, th0, mz, pk, steps=15, lr=0.02, grad="adjoint")
+    tf, lf, _, _ = fit.adam_fit(gp, th0, mz, pk, steps=15, lr=0.02, grad="fd", h=1e-4)
+    assert la[-1] < 0.5 * la[0]
+    np.testing.assert_allclose(ta, tf, rtol=1e-4)
