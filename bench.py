@@ -239,6 +239,9 @@ def run_ours(args, cfg):
         dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
     e2e_s = float(e2e_t.item())
 
+    fit_res = None
+    if not args.no_fit and rank == 0:
+        fit_res = fit_leg(args, runner, out, table, cfg)
     if rank != 0:
         return
     peak, peak_kind = hbm_peak()
@@ -273,7 +276,8 @@ def run_ours(args, cfg):
                    "ms_per_step": e2e_s * 1e3},
            "gpu_launches": args.steps * 4,
            "tile_variants": tuned,
-           "clocks": clk.summary()}
+           "clocks": clk.summary(),
+           "fit": fit_res}
     if not args.no_cpu:
         workers = os.cpu_count() or 1
         r = cpu_baseline(cfg, 64 if not args.small else 8, workers)
@@ -281,6 +285,44 @@ def run_ours(args, cfg):
         res["cpu_baseline"] = {"value": v, "unit": "cells/s", "cores": workers, "kind": "port",
                                "sample": r["sample"]}
     print(json.dumps(res))
+
+
+def fit_leg(args, runner, out, table, cfg):
+    """The (a,b,c) fit on this chunk's skewers: 10 z bins (1.8-3.6) x (a, b, c), 32 log-k P1D
+    bins; targets from theta* = (0.1, 1.58, 0.6); adjoint vs finite-difference gradients, and
+    the same Adam fit (from (0.15, 1.3, 0.4)) with both."""
+    import numpy as np
+    import torch
+
+    from saclaymocks_gb300 import fit
+    nx, ny, nz = cfg["nx"], cfg["ny"], cfg["nz"]
+    _, dtot, eta, z = runner.run(out.delta_pad[0], out.eta_pad[0], nx=nx, ny=ny, nz=nz, pitch=out.pitch,
+                                 dcell=cfg["dcell"], want_fields=True)
+    prob = fit.FitProblem(dtot, eta, None, z, table.npix, np.linspace(1.8, 3.6, 11),
+                          np.logspace(np.log10(0.05), np.log10(15.0), 33), 0.2)
+    del dtot, eta, z
+    truth = np.tile([0.1, 1.58, 0.6], (10, 1))
+    mz, pk, _ = prob.reductions(truth)
+    th0 = np.tile([0.15, 1.3, 0.4], (10, 1))
+    prob.loss_grad(th0, mz, pk)                       # warm-up (launch set-up)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        prob.loss_grad(th0, mz, pk)
+    t_adj = (time.perf_counter() - t0) / 3
+    t0 = time.perf_counter()
+    prob.fd_grad(th0, mz, pk, h=1e-4)
+    t_fd = time.perf_counter() - t0
+    steps = args.fit_steps
+    ta, la, sa, _ = fit.adam_fit(prob, th0, mz, pk, steps=steps, lr=0.02, grad="adjoint")
+    res = {"params": "10 z bins x (a,b,c)", "pixels": prob.n_total, "adjoint_s_per_grad": t_adj,
+           "fd_s_per_grad": t_fd, "grad_speedup": t_fd / t_adj, "adam_steps": steps,
+           "adjoint_fit_s": sa, "loss_start": la[0], "loss_end": la[-1]}
+    if steps * t_fd < 120:
+        tf, lf, sf, _ = fit.adam_fit(prob, th0, mz, pk, steps=steps, lr=0.02, grad="fd", h=1e-4)
+        res.update({"fd_fit_s": sf, "fit_speedup": sf / sa,
+                    "max_rel_param_diff": float(np.max(np.abs(ta - tf) / np.abs(tf)))})
+    return res
 
 
 def run_grf_only(args, shape):
@@ -322,6 +364,8 @@ def main():
     ap.add_argument("--small", action="store_true", help="256^3 box + 2000 skewers (quick check)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-tune", action="store_true", help="built-in tile variants, no autotuning")
+    ap.add_argument("--no-fit", action="store_true", help="skip the (a,b,c) fit leg")
+    ap.add_argument("--fit-steps", type=int, default=20, help="Adam steps of the fit leg")
     ap.add_argument("--grf-shape", default=None,
                     help="NX,NY,NZ: time only the GRF boxes of this shape (profiling case)")
     args = ap.parse_args()

@@ -124,6 +124,7 @@ class FitProblem:
         self.d_gM.copy_(torch.from_numpy(np.nan_to_num(gM)))
         self.d_gP.copy_(torch.from_numpy(np.nan_to_num(gP)))
         self._set_theta(state["theta"])
+        self.acc[self.nzb] = state["fbar"] * self.n_total   # <F> of this state's forward pass
         _lib.check(lib.smk_fit_backward(C.byref(self.fp), self.d_theta.data_ptr(), self.acc.data_ptr(),
                                         self.d_gM.data_ptr(), self.d_gP.data_ptr(), self.ws.data_ptr(),
                                         self.ws.numel() * 8, stream_handle()), "smk_fit_backward")
