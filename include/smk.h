@@ -57,6 +57,13 @@ int smk_fft_supported(int32_t n);
 #define SMK_PK_ANALYTIC 0  /* P(k) = amp * k / (1 + (k/k0)^2)^2, evaluated in the kernel   */
 #define SMK_PK_GRID 1      /* sqrt(P/Vcell) read from a float32 [nx][ny][nz/2+1] grid       */
 
+#define SMK_ETA_ZZ 0 /* eta components k_i k_j / k^2 delta_k (bin/make_boxes.py:315-391) */
+#define SMK_ETA_XX 1
+#define SMK_ETA_YY 2
+#define SMK_ETA_XY 3
+#define SMK_ETA_XZ 4
+#define SMK_ETA_YZ 5
+
 typedef struct {
     int32_t nx, ny, nz;   /* cells; nz even; every axis passes smk_fft_supported            */
     int32_t batch;        /* independent boxes in one launch (>= 1)                          */
@@ -72,6 +79,7 @@ typedef struct {
     int32_t want_eta;     /* 1: also produce eta_zz = irfftn(kz^2/k^2 delta_k)               */
     void* const* pass_events; /* optional cudaEvent_t[6]: recorded on the stream before the    */
     int32_t n_pass_events;    /* first HBM pass and after each of the five (0: none)          */
+    int32_t eta_comp;     /* SMK_ETA_*: which eta_ij the eta box holds (default 0 = zz)      */
 } SmkGrfParams;
 
 /* Row pitch (floats) of the padded box layout for a z extent nz. */
@@ -123,6 +131,9 @@ int smk_tune_get(int32_t pass, int32_t n);
 #define SMK_INTERP_TRILINEAR 0 /* 8-corner read, periodic, cell centres at (i+0.5)dcell */
 #define SMK_INTERP_PIXELS 1    /* no box read: delta_l, eta_par, z given per pixel      */
                                /* (the merge_spectra input, bin/merge_spectra.py:282-300) */
+#define SMK_INTERP_GAUSS343 2  /* the reference's read: Gaussian weights over the 7^3   */
+                               /* cells around the pixel, eta_par = r_i r_j eta_ij / r^2  */
+                               /* from six eta boxes (bin/make_spectra.py:39-139)         */
 
 #define SMK_SS_NONE 0     /* no small-scale field                                      */
 #define SMK_SS_HOST 1     /* white noise given per skewer (length nz_s)                 */
@@ -154,7 +165,9 @@ typedef struct {
     int32_t nx, ny, nz;
     int64_t pitch;         /* floats between consecutive (x,y) rows of the boxes          */
     double dcell;
-    int32_t interp;        /* SMK_INTERP_TRILINEAR                                        */
+    int32_t interp;        /* SMK_INTERP_TRILINEAR / PIXELS / GAUSS343                    */
+    const float* eta6[6];  /* GAUSS343: eta_xx, yy, zz, xy, xz, yz boxes (all or none)     */
+    double obs[3];         /* GAUSS343: observer position, box-corner frame, Mpc/h         */
     /* small scales (bin/merge_spectra.py:303-331) */
     int32_t ss_mode;       /* SMK_SS_NONE / SMK_SS_HOST / SMK_SS_PHILOX                   */
     int32_t ss_nz;         /* FFT length (power of two 256..4096) or 0: 256*2^n >= npix+50 */

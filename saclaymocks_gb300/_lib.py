@@ -20,10 +20,11 @@ SMK_ENULLBOX = -5
 
 SMK_NOISE_HOST, SMK_NOISE_PHILOX = 0, 1
 SMK_PK_ANALYTIC, SMK_PK_GRID = 0, 1
-SMK_INTERP_TRILINEAR, SMK_INTERP_PIXELS = 0, 1
+SMK_INTERP_TRILINEAR, SMK_INTERP_PIXELS, SMK_INTERP_GAUSS343 = 0, 1, 2
 SMK_SS_NONE, SMK_SS_HOST, SMK_SS_PHILOX = 0, 1, 2
 SMK_ABC_CONST, SMK_ABC_POWERLAW, SMK_ABC_TABLE = 0, 1, 2
 SMK_G_ONE, SMK_G_MERGE = 0, 1
+SMK_ETA = {"zz": 0, "xx": 1, "yy": 2, "xy": 3, "xz": 4, "yz": 5}
 SMK_PASS_ZFWD, SMK_PASS_LINE, SMK_PASS_XPASS, SMK_PASS_XGEN, SMK_PASS_ZINV = 0, 1, 2, 3, 4
 
 
@@ -40,7 +41,7 @@ class SmkGrfParams(C.Structure):
                 ("dcell", C.c_double), ("pk_mode", C.c_int32), ("k0", C.c_double),
                 ("amp", C.c_double), ("pk_grid", C.c_void_p), ("noise_mode", C.c_int32),
                 ("noise", C.c_void_p), ("seed", C.c_uint64), ("want_eta", C.c_int32),
-                ("pass_events", C.c_void_p), ("n_pass_events", C.c_int32)]
+                ("pass_events", C.c_void_p), ("n_pass_events", C.c_int32), ("eta_comp", C.c_int32)]
 
 
 class SmkSkewers(C.Structure):
@@ -52,8 +53,8 @@ class SmkSkewers(C.Structure):
 
 class SmkSpectraParams(C.Structure):
     _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("pitch", C.c_int64),
-                ("dcell", C.c_double), ("interp", C.c_int32),
-                ("ss_mode", C.c_int32), ("ss_nz", C.c_int32), ("ss_scale", C.c_void_p),
+                ("dcell", C.c_double), ("interp", C.c_int32), ("eta6", C.c_void_p * 6),
+                ("obs", C.c_double * 3), ("ss_mode", C.c_int32), ("ss_nz", C.c_int32), ("ss_scale", C.c_void_p),
                 ("ss_noise", C.c_void_p), ("ss_noise_offset", C.c_void_p), ("seed", C.c_uint64),
                 ("abc_mode", C.c_int32), ("a", C.c_float), ("b", C.c_float), ("c", C.c_float),
                 ("a_zref1", C.c_float), ("a_power", C.c_float), ("abc_tab", C.c_void_p),

@@ -154,6 +154,8 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         return fail(SMK_EINVAL, "smk_grf_boxes: need nx, ny >= 2, nz >= 2 even, batch >= 1");
     if (!(p->dcell > 0)) return fail(SMK_EINVAL, "smk_grf_boxes: dcell must be > 0");
     if (p->want_eta && !eta) return fail(SMK_EINVAL, "smk_grf_boxes: want_eta needs an eta box");
+    if (p->eta_comp < SMK_ETA_ZZ || p->eta_comp > SMK_ETA_YZ)
+        return fail(SMK_EINVAL, "smk_grf_boxes: unknown eta_comp");
     if (p->noise_mode != SMK_NOISE_HOST && p->noise_mode != SMK_NOISE_PHILOX)
         return fail(SMK_EINVAL, "smk_grf_boxes: unknown noise_mode");
     if (p->noise_mode == SMK_NOISE_HOST && !p->noise) return fail(SMK_EINVAL, "smk_grf_boxes: null noise");
@@ -230,6 +232,7 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         ga.sig_c = (float)sqrt(0.5 * ncell);
         ga.sig_r = (float)sqrt(ncell);
         ga.seed = p->seed;
+        ga.eta_comp = p->eta_comp;
         if ((rc = run_xgen(variant_for(PASS_XGEN, p->nx), ga, st))) return rc;
         if ((rc = mark(3))) return rc;
     } else {
@@ -263,6 +266,7 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         xa.kfac = kfac;
         xa.inv_k0 = p->pk_mode == SMK_PK_ANALYTIC ? (float)(1.0 / p->k0) : 0.f;
         xa.inv_vcell = inv_vcell;
+        xa.eta_comp = p->eta_comp;
         if ((rc = run_xpass(variant_for(PASS_XPASS, p->nx), xa, st))) return rc;
         if ((rc = mark(3))) return rc;
     }

@@ -166,7 +166,20 @@ struct XArgs {
     double amp_host;
     double kfac;           // 2 * pi / dcell (2 k_Nyquist)
     float inv_k0, inv_vcell;
+    int eta_comp;          // SMK_ETA_*: eta_ij = k_i k_j / k^2 delta_k
 };
+
+// k_i k_j of the eta component (SMK_ETA_*), float32 product as numpy forms kx*ky
+__device__ __forceinline__ float eta_num(int comp, float kx, float ky, float kz) {
+    switch (comp) {
+        case SMK_ETA_XX: return __fmul_rn(kx, kx);
+        case SMK_ETA_YY: return __fmul_rn(ky, ky);
+        case SMK_ETA_XY: return __fmul_rn(kx, ky);
+        case SMK_ETA_XZ: return __fmul_rn(kx, kz);
+        case SMK_ETA_YZ: return __fmul_rn(ky, kz);
+        default: return __fmul_rn(kz, kz);
+    }
+}
 
 __device__ __forceinline__ float kaxis(int i, int n, double kfac, bool full) {
     // numpy fftfreq / rfftfreq times 2 k_ny, rounded to float32 (bin/make_boxes.py:299-302)
@@ -232,7 +245,7 @@ __global__ void __launch_bounds__(C::T, 1) xpass_kernel(const XArgs a) {
             s[idx] = d;
             if (pb && w < cols) {
                 const float kk1 = (kk == 0.0f) ? 1.0f : kk;  // k^2[0,0,0] = 1 (bin/make_boxes.py:306)
-                pb[e * estride + w] = cscale(d, __fdiv_rn(__fmul_rn(kz, kz), kk1));
+                pb[e * estride + w] = cscale(d, __fdiv_rn(eta_num(a.eta_comp, kxv, ky, kz), kk1));
             }
         }
         __syncthreads();
@@ -274,6 +287,7 @@ struct XGenArgs {
     float inv_k0, inv_vcell;
     float sig_c, sig_r;    // sqrt(N/2), sqrt(N)
     uint64_t seed;
+    int eta_comp;
 };
 
 // smem: s[n*W] | tw[n] | kx[n] | ix[n] | kzt[nzh]
@@ -359,7 +373,7 @@ __global__ void __launch_bounds__(C::T, 1) xgen_kernel(const XGenArgs a) {
                     }
                     d = cscale(X, sc);
                     const float kk1 = (kk == 0.0f) ? 1.0f : kk;
-                    et = cscale(d, __fdividef(kz_ * kz_, kk1));
+                    et = cscale(d, __fdividef(eta_num(a.eta_comp, kxv, ky, kz_), kk1));
                 }
                 s[e * W + c0 + h] = d;
                 s[e * W + WC + c0 + h] = et;

@@ -28,6 +28,8 @@ struct SkArgs {
     const int32_t* order;
     int64_t n_items;
     int interp;
+    const float* eta6[6];     // SMK_INTERP_GAUSS343: eta_xx, yy, zz, xy, xz, yz boxes (or null)
+    double obs[3];            // SMK_INTERP_GAUSS343: observer, box-corner frame (Mpc/h)
     const float* pix_delta;
     const float* pix_eta;
     const float* pix_z;
@@ -81,7 +83,14 @@ struct SkewerGeo {
     int i0[3];        // cell index of the first pixel's lower corner, wrapped
     long long f0[3];  // fraction of the first pixel above i0, 2^-32 units
     long long step[3];// pixel step, 2^-32 cell units
+    long long i0u[3]; // i0 before wrapping (unwrapped line of sight, for the eta projection)
 };
+
+// Gaussian-weighted read of the (2*GR+1)^3 cells around the pixel (ReadSpec of
+// bin/make_spectra.py:39-68, 104-129): for the cell holding p (index floor(p/dcell)), weights
+// exp(-|r_cell - p|^2 / (2 dcell^2)) = prod_d exp(-(c_d + 0.5 - f_d)^2 / 2), one 1D factor per
+// axis; value = sum(w rho) / sum(w), with periodic wrap.
+constexpr int GR = 3;
 
 __global__ void __launch_bounds__(SK_T, 2) skewer_kernel(const SkArgs a) {
     extern __shared__ float2 smem[];
@@ -105,11 +114,12 @@ __global__ void __launch_bounds__(SK_T, 2) skewer_kernel(const SkArgs a) {
             sk_id[t] = sid;
             sk_np[t] = sid >= 0 ? a.npix[sid] : 0;
             sk_off[t] = sid >= 0 ? a.offset[sid] : 0;
-            if (sid >= 0 && a.interp == SMK_INTERP_TRILINEAR) {
+            if (sid >= 0 && a.interp != SMK_INTERP_PIXELS) {
                 for (int d = 0; d < 3; ++d) {
                     const double u0 = (double)a.start[3 * sid + d] / a.dcell - 0.5;
                     const double fl = floor(u0);
                     geo[t].i0[d] = wrap((int64_t)fl, dims[d]);
+                    geo[t].i0u[d] = (long long)fl;
                     geo[t].f0[d] = __double2ll_rn((u0 - fl) * 4294967296.0);
                     geo[t].step[d] = __double2ll_rn(a.dpix * (double)a.dir[3 * sid + d] / a.dcell * 4294967296.0);
                 }
@@ -191,6 +201,67 @@ __global__ void __launch_bounds__(SK_T, 2) skewer_kernel(const SkArgs a) {
                 dl = __ldg(a.pix_delta + o);
                 et = a.pix_eta ? __ldg(a.pix_eta + o) : 0.f;
                 z = __ldg(a.pix_z + o);
+            } else if (a.interp == SMK_INTERP_GAUSS343) {
+                const SkewerGeo& g = geo[t];
+                int ci[3];
+                float ew[3][2 * GR + 1];
+                double rpos[3];
+                float fux = 0.f;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    // p/dcell = i0 + q 2^-32 + 0.5: shift by half a cell to get floor(p/dcell)
+                    const long long q = g.f0[d] + (long long)i * g.step[d] + (1LL << 31);
+                    const float fu = (float)(unsigned)(q & 0xffffffffLL) * 2.3283064365386963e-10f;
+                    ci[d] = wrap((int64_t)g.i0[d] + (q >> 32), dims[d]);
+                    rpos[d] = ((double)(g.i0u[d] + (q >> 32)) + (double)fu) * a.dcell - a.obs[d];
+                    if (d == 0) fux = fu;
+#pragma unroll
+                    for (int c = -GR; c <= GR; ++c) {
+                        const float x = (float)c + 0.5f - fu;
+                        ew[d][c + GR] = expf(-0.5f * x * x);
+                    }
+                }
+                float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+                for (int c = 0; c < 2 * GR + 1; ++c) {
+                    sx += ew[0][c];
+                    sy += ew[1][c];
+                    sz += ew[2][c];
+                }
+                const bool rsd = a.eta6[0] != nullptr;
+                float acc[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                for (int cx = -GR; cx <= GR; ++cx) {
+                    const int ixw = wrap((int64_t)ci[0] + cx, dims[0]);
+                    for (int cy = -GR; cy <= GR; ++cy) {
+                        const int iyw = wrap((int64_t)ci[1] + cy, dims[1]);
+                        const float wxy = ew[0][cx + GR] * ew[1][cy + GR];
+                        const int64_t row = ((int64_t)ixw * a.ny + iyw) * a.pitch;
+#pragma unroll
+                        for (int cz = -GR; cz <= GR; ++cz) {
+                            const int izw = ci[2] + cz < 0 ? ci[2] + cz + dims[2]
+                                          : (ci[2] + cz >= dims[2] ? ci[2] + cz - dims[2] : ci[2] + cz);
+                            const float w = wxy * ew[2][cz + GR];
+                            acc[0] = fmaf(w, __ldg(a.delta + row + izw), acc[0]);
+                            if (rsd) {
+#pragma unroll
+                                for (int f = 0; f < 6; ++f) acc[1 + f] = fmaf(w, __ldg(a.eta6[f] + row + izw), acc[1 + f]);
+                            }
+                        }
+                    }
+                }
+                const float inv = 1.0f / (sx * sy * sz);
+                dl = acc[0] * inv;
+                et = 0.f;
+                if (rsd) {
+                    const double X = rpos[0], Y = rpos[1], Z = rpos[2];
+                    const double RR = X * X + Y * Y + Z * Z;
+                    const double e = (X * acc[1] * X + Y * acc[2] * Y + Z * acc[3] * Z + 2 * X * acc[4] * Y +
+                                      2 * X * acc[5] * Z + 2 * Y * acc[6] * Z) / RR;
+                    et = (float)e * inv;
+                }
+                // redshift from the wrapped x coordinate x / dcell = ci_x + fu_x (as the trilinear read)
+                const float xc = (float)ci[0] + fux;
+                z = a.z_lo + (a.z_hi - a.z_lo) * (xc / nxf);
             } else {
                 const SkewerGeo& g = geo[t];
                 int c0[3], c1[3];
@@ -266,14 +337,18 @@ int smk_skewers_flux(const SmkSkewers* sk, const SmkSpectraParams* p, const floa
                      const float* eta_box, float* flux, float* delta_out, float* eta_out, float* z_out,
                      void* workspace, size_t workspace_bytes, void* stream) {
     if (!sk || !p || !flux) return fail(SMK_EINVAL, "smk_skewers_flux: null argument");
-    if (p->interp == SMK_INTERP_TRILINEAR && !delta_box)
-        return fail(SMK_EINVAL, "smk_skewers_flux: trilinear read needs the delta box");
+    if (p->interp != SMK_INTERP_PIXELS && !delta_box)
+        return fail(SMK_EINVAL, "smk_skewers_flux: a box read needs the delta box");
+    if (p->interp == SMK_INTERP_GAUSS343) {
+        const int nset = !!p->eta6[0] + !!p->eta6[1] + !!p->eta6[2] + !!p->eta6[3] + !!p->eta6[4] + !!p->eta6[5];
+        if (nset != 0 && nset != 6) return fail(SMK_EINVAL, "smk_skewers_flux: give all six eta_ij boxes or none");
+    }
     if (p->interp == SMK_INTERP_PIXELS && (!sk->pix_delta || !sk->pix_z))
         return fail(SMK_EINVAL, "smk_skewers_flux: SMK_INTERP_PIXELS needs pix_delta and pix_z");
     if (sk->n < 0 || sk->n_slots < 0 || (sk->n_slots & 1)) return fail(SMK_EINVAL, "smk_skewers_flux: bad counts");
     if (sk->n_slots == 0) return SMK_OK;
     if (!sk->npix || !sk->offset || !sk->order) return fail(SMK_EINVAL, "smk_skewers_flux: null skewer table array");
-    if (p->interp == SMK_INTERP_TRILINEAR) {
+    if (p->interp == SMK_INTERP_TRILINEAR || p->interp == SMK_INTERP_GAUSS343) {
         if (!sk->start || !sk->dir) return fail(SMK_EINVAL, "smk_skewers_flux: null start/dir");
         if (p->nx < 1 || p->ny < 1 || p->nz < 1 || p->pitch < p->nz || !(p->dcell > 0) || !(sk->dpix > 0))
             return fail(SMK_EINVAL, "smk_skewers_flux: bad box geometry");
@@ -307,6 +382,8 @@ int smk_skewers_flux(const SmkSkewers* sk, const SmkSpectraParams* p, const floa
     a.order = sk->order;
     a.n_items = sk->n_slots / 2;
     a.interp = p->interp;
+    for (int f = 0; f < 6; ++f) a.eta6[f] = p->eta6[f];
+    for (int d = 0; d < 3; ++d) a.obs[d] = p->obs[d];
     a.pix_delta = sk->pix_delta;
     a.pix_eta = sk->pix_eta;
     a.pix_z = sk->pix_z;

@@ -131,6 +131,8 @@ class SpectraConfig:
     z_lo: float = 1.8
     z_hi: float = 3.6
     growth: int = _lib.SMK_G_ONE
+    read: str = "trilinear"           # "trilinear" or "gauss343" (the reference's 7^3 read)
+    observer: tuple = (0.0, 0.0, 0.0)  # gauss343: observer in the box-corner frame (Mpc/h)
 
 
 class SkewerRunner:
@@ -158,7 +160,7 @@ class SkewerRunner:
         self.ws = torch.zeros(32, dtype=torch.int64, device=dv)
         self.pixels = pixels     # (delta_l, eta_par or None, z) packed CUDA tensors for SMK_INTERP_PIXELS
 
-    def structs(self, nx, ny, nz, pitch, dcell, noise=None):
+    def structs(self, nx, ny, nz, pitch, dcell, noise=None, eta6=None):
         cfg = self.cfg
         sk = _lib.SmkSkewers()
         sk.n = self.table.n
@@ -171,6 +173,15 @@ class SkewerRunner:
         sk.n_slots = self.n_slots
         p = _lib.SmkSpectraParams()
         p.interp = _lib.SMK_INTERP_TRILINEAR
+        if cfg.read == "gauss343":
+            p.interp = _lib.SMK_INTERP_GAUSS343
+            p.obs[:] = [float(v) for v in cfg.observer]
+            if eta6 is not None:
+                if len(eta6) != 6:
+                    raise ValueError("eta6: six boxes eta_xx, yy, zz, xy, xz, yz")
+                p.eta6[:] = [t.data_ptr() for t in eta6]
+        elif cfg.read != "trilinear":
+            raise ValueError(f"unknown read {cfg.read!r}")
         if self.pixels is not None:
             p.interp = _lib.SMK_INTERP_PIXELS
             sk.pix_delta = self.pixels[0].data_ptr()
@@ -196,11 +207,13 @@ class SkewerRunner:
         return sk, p
 
     def run(self, delta_box=None, eta_box=None, *, nx=1, ny=1, nz=1, pitch=1, dcell=1.0,
-            noise=None, want_fields=False, flux=None, stream=None):
+            noise=None, want_fields=False, flux=None, stream=None, eta6=None):
         """Launch the fused kernel; boxes are padded CUDA tensors [nx, ny, pitch] (or None in
-        pixel mode).  noise = (packed float32 tensor, int64 offsets tensor) for SMK_SS_HOST."""
+        pixel mode).  noise = (packed float32 tensor, int64 offsets tensor) for SMK_SS_HOST.
+        eta6: for read="gauss343", the six eta_ij boxes (xx, yy, zz, xy, xz, yz) whose
+        projection on the line of sight from cfg.observer gives eta_par (None: no RSD)."""
         lib = _lib.load()
-        sk, p = self.structs(nx, ny, nz, pitch, dcell, noise)
+        sk, p = self.structs(nx, ny, nz, pitch, dcell, noise, eta6)
         npx = self.table.total_pixels
         dv = self.device
         if flux is None:

@@ -185,3 +185,98 @@ def test_pixel_mode_matches_merge_spectra_golden(env, golden, tag):
     ds = dtot.cpu().numpy().reshape(n_sp, npx) - f["delta_l_in"][order]
     np.testing.assert_allclose(ds, f["delta_s"], rtol=0, atol=2e-6)
     np.testing.assert_allclose(F, f["flux"], rtol=0, atol=F_ATOL)
+
+
+# ----------------------------------------------------------------------------- Gaussian 7^3 read
+ETA6 = ("xx", "yy", "zz", "xy", "xz", "yz")
+
+
+def _padded(box, pitch):
+    nx, ny, nz = box.shape
+    t = torch.zeros((nx, ny, pitch), dtype=torch.float32)
+    t[:, :, :nz] = torch.from_numpy(np.ascontiguousarray(box, np.float32))
+    return t.cuda()
+
+
+def _readspec_table(spectra, r):
+    pos = r["pos"]                                            # (n, 60, 3), corner frame
+    d = pos[:, 1] - pos[:, 0]
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return spectra.SkewerTable(pos[:, 0].copy(), d, np.full(len(pos), pos.shape[1], np.int32), dpix=0.2)
+
+
+def _gauss_run(env, table, cfg, delta_box, eta6, nxyz, pitch, dx):
+    _, _, spectra = env
+    run = spectra.SkewerRunner(table, cfg)
+    F, dl, et, z = run.run(delta_box, None, nx=nxyz[0], ny=nxyz[1], nz=nxyz[2], pitch=pitch, dcell=dx,
+                           want_fields=True, eta6=eta6)
+    torch.cuda.synchronize()
+    return spectra.split(dl, table), spectra.split(et, table)
+
+
+def test_gauss343_read_of_reference_boxes_matches_readspec(env, golden):
+    """SMK_INTERP_GAUSS343 on the reference's own delta and eta_ij boxes against ReadSpec
+    (bin/make_spectra.py:39-139) run by the reference: delta_l and eta_par per pixel."""
+    _lib, grf, spectra = env
+    g, r = golden("grf_cube16.npz"), golden("readspec.npz")
+    n, dx, R0 = int(g["NX"]), float(g["DX"]), float(r["R0"])
+    L = n * dx
+    pitch = grf.pitch_of(n)
+    cfg = spectra.SpectraConfig(read="gauss343", observer=(L / 2, L / 2, L / 2 - R0))
+    t = _readspec_table(spectra, r)
+    dl, et = _gauss_run(env, t, cfg, _padded(g["delta"], pitch), [_padded(g["eta_" + c], pitch) for c in ETA6],
+                        (n, n, n), pitch, dx)
+    sig = float(np.std(g["delta"]))
+    for s in range(len(dl)):
+        np.testing.assert_allclose(dl[s], r["delta_l"][s], rtol=0, atol=5e-6 * sig)
+        np.testing.assert_allclose(et[s], r["eta_par"][s], rtol=0, atol=5e-6 * sig)
+
+
+def test_gauss343_on_gpu_boxes_matches_readspec(env, golden):
+    """The full chain: delta and the six eta_ij boxes made on the GPU from the reference's
+    noise (eta_comp per component), then the Gaussian read, against ReadSpec's output."""
+    _lib, grf, spectra = env
+    g, r = golden("grf_cube16.npz"), golden("readspec.npz")
+    n, dx, R0 = int(g["NX"]), float(g["DX"]), float(r["R0"])
+    L = n * dx
+    noise = torch.from_numpy(ograf.draw_noise(n, n, n, int(g["seed"]))).cuda()
+    outs = [grf.make_boxes(n, n, n, dx, noise=noise, k0=float(g["k0"]), eta_comp=c) for c in ETA6]
+    torch.cuda.synchronize()
+    for c, o in zip(ETA6, outs):
+        e = o.eta[0].cpu().numpy()
+        assert np.abs(e - g["eta_" + c]).max() < 1e-5 * np.std(g["delta"]), c
+    cfg = spectra.SpectraConfig(read="gauss343", observer=(L / 2, L / 2, L / 2 - R0))
+    t = _readspec_table(spectra, r)
+    dl, et = _gauss_run(env, t, cfg, outs[0].delta_pad[0], [o.eta_pad[0] for o in outs], (n, n, n),
+                        outs[0].pitch, dx)
+    sig = float(np.std(g["delta"]))
+    for s in range(len(dl)):
+        np.testing.assert_allclose(dl[s], r["delta_l"][s], rtol=0, atol=1e-5 * sig)
+        np.testing.assert_allclose(et[s], r["eta_par"][s], rtol=0, atol=1e-5 * sig)
+
+
+def test_gauss343_periodic_wrap_vs_oracle(env, boxes):
+    """Tilted skewers leaving the box: the 7^3 neighbourhoods wrap periodically; eta_par
+    projected on the unwrapped observer->pixel vector; no RSD boxes gives eta_par = 0."""
+    _lib, grf, spectra = env
+    nx, ny, nz, dx = boxes["nx"], boxes["ny"], boxes["nz"], boxes["dx"]
+    t = spectra.skewers_cone(12, (nx * dx, ny * dx, nz * dx), seed=4, max_angle_deg=35.0)
+    t = spectra.SkewerTable(t.start, t.direction, np.minimum(t.npix, 500).astype(np.int32), dpix=t.dpix)
+    rs = np.random.RandomState(9)
+    eta6 = [rs.normal(size=(nx, ny, nz)).astype(np.float32) for _ in ETA6]
+    pitch = boxes["out"].pitch
+    obs = (0.3 * nx * dx, 0.6 * ny * dx, -120.0)
+    cfg = spectra.SpectraConfig(read="gauss343", observer=obs)
+    dl, et = _gauss_run(env, t, cfg, boxes["out"].delta_pad[0], [_padded(e, pitch) for e in eta6],
+                        (nx, ny, nz), pitch, dx)
+    dl0, et0 = _gauss_run(env, t, cfg, boxes["out"].delta_pad[0], None, (nx, ny, nz), pitch, dx)
+    sig = float(np.std(boxes["d"]))
+    for s in range(t.n):
+        i = np.arange(t.npix[s])
+        pos = t.start[s].astype(np.float64) + (i * t.dpix)[:, None] * t.direction[s].astype(np.float64)
+        vals = osk.gauss343([boxes["d"]] + [e.astype(np.float64) for e in eta6], pos, dx)
+        ep = osk.eta_par_projection(dict(zip(ETA6, vals[1:])), pos - np.asarray(obs))
+        np.testing.assert_allclose(dl[s], vals[0], rtol=0, atol=1e-5 * sig)
+        np.testing.assert_allclose(et[s], ep, rtol=0, atol=1e-5)
+        np.testing.assert_array_equal(dl0[s], dl[s])
+        assert not np.any(et0[s])
