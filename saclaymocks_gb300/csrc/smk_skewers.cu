@@ -228,6 +228,9 @@ __global__ void __launch_bounds__(SK_T, 2) skewer_kernel(const SkArgs a) {
                     sy += ew[1][c];
                     sz += ew[2][c];
                 }
+                int izs[2 * GR + 1];
+#pragma unroll
+                for (int c = 0; c < 2 * GR + 1; ++c) izs[c] = wrap((int64_t)ci[2] + c - GR, dims[2]);
                 const bool rsd = a.eta6[0] != nullptr;
                 float acc[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
                 for (int cx = -GR; cx <= GR; ++cx) {
@@ -238,8 +241,7 @@ __global__ void __launch_bounds__(SK_T, 2) skewer_kernel(const SkArgs a) {
                         const int64_t row = ((int64_t)ixw * a.ny + iyw) * a.pitch;
 #pragma unroll
                         for (int cz = -GR; cz <= GR; ++cz) {
-                            const int izw = ci[2] + cz < 0 ? ci[2] + cz + dims[2]
-                                          : (ci[2] + cz >= dims[2] ? ci[2] + cz - dims[2] : ci[2] + cz);
+                            const int izw = izs[cz + GR];
                             const float w = wxy * ew[2][cz + GR];
                             acc[0] = fmaf(w, __ldg(a.delta + row + izw), acc[0]);
                             if (rsd) {
