@@ -177,7 +177,9 @@ def run_ours(args, cfg):
     runner = chunk._prepare(table.start, table.direction, table.npix)
     boxes, ws = chunk.boxes, chunk.ws
     tuned = None
-    if not args.no_tune:
+    if args.variants:
+        tuned = set_variants(args.variants, cfg["nx"], cfg["ny"], cfg["nz"])
+    elif not args.no_tune:
         from saclaymocks_gb300 import tune
         tuned = tune.tune_grf(cfg["nx"], cfg["ny"], cfg["nz"], cfg["dcell"], out=boxes, workspace=ws)
     nx, ny, nz = cfg["nx"], cfg["ny"], cfg["nz"]
@@ -312,22 +314,36 @@ def fit_leg(args, runner, out, table, cfg):
     t_adj = (time.perf_counter() - t0) / 3
     _, g_adj = prob.loss_grad(th0, mz, pk)
     t0 = time.perf_counter()
-    g_fd = prob.fd_grad(th0, mz, pk, h=3e-2, points=4)
+    g_fd = prob.fd_grad(th0, mz, pk, h=1e-2, points=4)
     t_fd = time.perf_counter() - t0
     rel = np.abs(g_fd - g_adj) / np.abs(g_adj)
     steps = args.fit_steps
     ta, la, sa, _ = fit.adam_fit(prob, th0, mz, pk, steps=steps, lr=0.02, grad="adjoint", eps_rel=1e-2)
     res = {"params": "10 z bins x (a,b,c)", "pixels": prob.n_total, "adjoint_s_per_grad": t_adj,
-           "fd": "4-point stencil, relative step 3e-2 (120 loss evaluations per gradient)",
+           "fd": "4-point stencil, relative step 1e-2 (120 loss evaluations per gradient)",
            "fd_s_per_grad": t_fd, "grad_speedup": t_fd / t_adj,
            "grad_rel_diff_median": float(np.median(rel)), "grad_rel_diff_max": float(rel.max()),
            "adam_steps": steps, "adjoint_fit_s": sa, "loss_start": la[0], "loss_end": la[-1]}
     if steps * t_fd < 150:
-        tf, lf, sf, _ = fit.adam_fit(prob, th0, mz, pk, steps=steps, lr=0.02, grad="fd", h=3e-2, points=4,
+        tf, lf, sf, _ = fit.adam_fit(prob, th0, mz, pk, steps=steps, lr=0.02, grad="fd", h=1e-2, points=4,
                                      eps_rel=1e-2)
         res.update({"fd_fit_s": sf, "fit_speedup": sf / sa,
                     "max_rel_param_diff": float(np.max(np.abs(ta - tf) / np.abs(tf)))})
     return res
+
+
+def set_variants(spec, nx, ny, nz):
+    """--variants xgen=5,line=5,zinv=4: fixed tile variants per GRF pass instead of tuning
+    (so a profile replays the tile choice of an earlier tuned run)."""
+    from saclaymocks_gb300 import _lib, tune
+    ids = {"zfwd": (_lib.SMK_PASS_ZFWD, nz), "line": (_lib.SMK_PASS_LINE, ny), "xpass": (_lib.SMK_PASS_XPASS, nx),
+           "xgen": (_lib.SMK_PASS_XGEN, nx), "zinv": (_lib.SMK_PASS_ZINV, nz)}
+    choices = {}
+    for item in spec.split(","):
+        name, v = item.split("=")
+        choices[ids[name.strip()]] = int(v)
+    tune.apply(choices)
+    return {"fixed": spec}
 
 
 def run_grf_only(args, shape):
@@ -341,7 +357,9 @@ def run_grf_only(args, shape):
     ws = grf.GrfWorkspace(1)
     amp = grf.pk_normalisation(nx, ny, nz)
     tuned = None
-    if not args.no_tune:
+    if args.variants:
+        tuned = set_variants(args.variants, nx, ny, nz)
+    elif not args.no_tune:
         from saclaymocks_gb300 import tune
         tuned = tune.tune_grf(nx, ny, nz, out=boxes, workspace=ws, use_cache=False)
     for _ in range(args.warmup):
@@ -369,6 +387,8 @@ def main():
     ap.add_argument("--small", action="store_true", help="256^3 box + 2000 skewers (quick check)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-tune", action="store_true", help="built-in tile variants, no autotuning")
+    ap.add_argument("--variants", default=None,
+                    help="fixed tile variants, e.g. xgen=5,line=5,zinv=4 (no autotuning)")
     ap.add_argument("--no-fit", action="store_true", help="skip the (a,b,c) fit leg")
     ap.add_argument("--fit-steps", type=int, default=20, help="Adam steps of the fit leg")
     ap.add_argument("--grf-shape", default=None,
