@@ -244,6 +244,10 @@ def run_ours(args, cfg):
     fit_res = None
     if not args.no_fit and rank == 0:
         fit_res = fit_leg(args, runner, out, table, cfg)
+    batch_res = None
+    if not args.no_batching and rank == 0 and not args.small:
+        del runner
+        batch_res = batching_leg()
     if rank != 0:
         return
     peak, peak_kind = hbm_peak()
@@ -279,7 +283,8 @@ def run_ours(args, cfg):
            "gpu_launches": args.steps * 4,
            "tile_variants": tuned,
            "clocks": clk.summary(),
-           "fit": fit_res}
+           "fit": fit_res,
+           "batching": batch_res}
     if not args.no_cpu:
         workers = os.cpu_count() or 1
         r = cpu_baseline(cfg, 64 if not args.small else 8, workers)
@@ -329,6 +334,92 @@ def fit_leg(args, runner, out, table, cfg):
                                      eps_rel=1e-2)
         res.update({"fd_fit_s": sf, "fit_speedup": sf / sa,
                     "max_rel_param_diff": float(np.max(np.abs(ta - tf) / np.abs(tf)))})
+    return res
+
+
+def batching_leg(cfg_seed=2):
+    """Batched and graph-captured launches: 64 boxes of 128^3 (seeds 100..163) in one batched
+    call vs 64 single-box calls (plain and replayed from a CUDA graph); a 1024^3 box pair with
+    5e4 skewers of log-uniform length 64..2048 pixels through the persistent paired-skewer
+    kernel vs one skewer per work item, and the skewer launch replayed from a CUDA graph."""
+    import numpy as np
+    import torch
+
+    from saclaymocks_gb300 import _lib, grf, spectra
+
+    def timed(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    res = {}
+    n, B = 128, 64
+    amp = grf.pk_normalisation(n, n, n)
+    big = grf.alloc_boxes(n, n, n, batch=B)
+    wsb = grf.GrfWorkspace(B)
+    one = grf.alloc_boxes(n, n, n, batch=1)
+    ws1 = grf.GrfWorkspace(1)
+    t_batch = timed(lambda: grf.make_boxes(n, n, n, seed=100, batch=B, amp=amp, out=big, workspace=wsb))
+
+    def singles():
+        for b in range(B):
+            grf.make_boxes(n, n, n, seed=100 + b, amp=amp, out=one, workspace=ws1)
+    t_single = timed(singles)
+    stream = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    singles()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g, stream=stream):
+        singles()
+    t_graph = timed(g.replay)
+    o1 = grf.make_boxes(n, n, n, seed=100 + 37, amp=amp, out=one, workspace=ws1)
+    ob = grf.make_boxes(n, n, n, seed=100, batch=B, amp=amp, out=big, workspace=wsb)
+    torch.cuda.synchronize()
+    same = bool(torch.equal(ob.delta[37], o1.delta[0]) and torch.equal(ob.eta[37], o1.eta[0]))
+    cells = B * n ** 3
+    res["grf_64x128^3"] = {"batched_ms": t_batch, "single_calls_ms": t_single, "graph_replay_ms": t_graph,
+                           "batched_cells_per_s": cells / (t_batch * 1e-3),
+                           "batched_member_equals_single_call": same}
+    del big, wsb, one, ws1, g, o1, ob
+    torch.cuda.empty_cache()
+
+    n = 1024
+    L = n * 2.19
+    boxes = grf.alloc_boxes(n, n, n)
+    ws = grf.GrfWorkspace(1)
+    amp = grf.pk_normalisation(n, n, n)
+    t_grf = timed(lambda: grf.make_boxes(n, n, n, seed=cfg_seed, amp=amp, out=boxes, workspace=ws), reps=3)
+    out = grf.make_boxes(n, n, n, seed=cfg_seed, amp=amp, out=boxes, workspace=ws)
+    table = spectra.skewers_cone(50_000, (L, L, L), seed=cfg_seed, npix_range=(64, 2048), log_uniform=True)
+    scfg = spectra.SpectraConfig(ss_mode=_lib.SMK_SS_PHILOX, ss_nz=0, pmiss=spectra.pmiss_gauss(0.05, 2.0),
+                                 seed=cfg_seed, abc_mode=_lib.SMK_ABC_POWERLAW, a=0.1, a_zref1=3.2,
+                                 a_power=4.5, b=1.58, c=0.6)
+    kw = dict(nx=n, ny=n, nz=n, pitch=out.pitch, dcell=2.19)
+    paired = spectra.SkewerRunner(table, scfg)
+    single = spectra.SkewerRunner(table, scfg, pair=False)
+    fp = torch.empty(table.total_pixels, device="cuda")
+    fs = torch.empty(table.total_pixels, device="cuda")
+    t_pair = timed(lambda: paired.run(out.delta_pad[0], out.eta_pad[0], flux=fp, **kw), reps=10)
+    t_one = timed(lambda: single.run(out.delta_pad[0], out.eta_pad[0], flux=fs, **kw), reps=10)
+    gs = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(gs, stream=stream):
+        paired.run(out.delta_pad[0], out.eta_pad[0], flux=fp, **kw)
+    t_sgraph = timed(gs.replay, reps=10)
+    paired.run(out.delta_pad[0], out.eta_pad[0], flux=fp, **kw)
+    single.run(out.delta_pad[0], out.eta_pad[0], flux=fs, **kw)
+    torch.cuda.synchronize()
+    px = table.total_pixels
+    res["grf_1024^3_ms"] = t_grf
+    res["skewers_5e4_loguniform_64_2048"] = {
+        "pixels": px, "paired_ms": t_pair, "one_per_item_ms": t_one, "graph_replay_ms": t_sgraph,
+        "paired_pixels_per_s": px / (t_pair * 1e-3), "paired_speedup": t_one / t_pair,
+        "max_abs_flux_diff_paired_vs_single": float((fp - fs).abs().max())}
     return res
 
 
@@ -387,6 +478,7 @@ def main():
     ap.add_argument("--small", action="store_true", help="256^3 box + 2000 skewers (quick check)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-tune", action="store_true", help="built-in tile variants, no autotuning")
+    ap.add_argument("--no-batching", action="store_true", help="skip the batched / graph-replay leg")
     ap.add_argument("--variants", default=None,
                     help="fixed tile variants, e.g. xgen=5,line=5,zinv=4 (no autotuning)")
     ap.add_argument("--no-fit", action="store_true", help="skip the (a,b,c) fit leg")

@@ -17,6 +17,8 @@
 // butterfly at a time and the block synchronises only between stages.
 #pragma once
 
+#include <type_traits>
+
 #include "smk_common.cuh"
 
 namespace smk {
@@ -33,9 +35,21 @@ struct FftPlan {
     uint32_t magic[FFT_MAX_STAGES];  // floor(2^32/m) + 1: x / m == umulhi(x, magic) for x < 2^16
 };
 
-// Host: radix plan of n (8s first, then 4s/2 for the rest of the power of two, 3s, 5s).
+// Host: radix plan of n (16s first, one of them 32 when a single factor 2 is left, else
+// 8/4/2 for the rest of the power of two, then 3s, 5s).
 // Returns false unless 2 <= n <= FFT_MAX_N and n = 2^a 3^b 5^c.
-bool make_plan(int n, FftPlan* p);
+bool make_plan(int n, FftPlan* p, int rmax = 16);
+
+// Largest radix a kernel of T threads per block runs in registers without spilling (the
+// register budget per thread is 65536 / T): radix 32 for <= 256 threads, 16 for 512, 8 above.
+__host__ __device__ constexpr int fft_max_radix(int T) { return T >= 1024 ? 8 : (T >= 512 ? 16 : 32); }
+
+// True when every stage radix of the plan is <= rmax (the kernel compiled that radix).
+inline bool plan_fits(const FftPlan& p, int rmax) {
+    for (int s = 0; s < p.nst; ++s)
+        if (p.r[s] > rmax) return false;
+    return true;
+}
 
 __device__ __forceinline__ int div_m(const FftPlan& pl, int st, int x) {
     return pl.m[st] == 1 ? x : (int)__umulhi((unsigned)x, pl.magic[st]);
@@ -67,7 +81,7 @@ __device__ __forceinline__ int slot_of_freq(const FftPlan& pl, int k) {
 
 // ------------------------------------------------------------------ R-point DFTs
 template <bool INV>
-__device__ __forceinline__ float2 mul_mi(float2 a) {  // * (-i) forward, * (+i) inverse
+__host__ __device__ __forceinline__ float2 mul_mi(float2 a) {  // * (-i) forward, * (+i) inverse
     return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
 
@@ -76,7 +90,7 @@ struct Dft;
 
 template <bool INV>
 struct Dft<2, INV> {
-    __device__ __forceinline__ static void run(float2* v) {
+    __host__ __device__ __forceinline__ static void run(float2* v) {
         const float2 a = v[0], b = v[1];
         v[0] = cadd(a, b);
         v[1] = csub(a, b);
@@ -85,7 +99,7 @@ struct Dft<2, INV> {
 
 template <bool INV>
 struct Dft<3, INV> {
-    __device__ __forceinline__ static void run(float2* v) {
+    __host__ __device__ __forceinline__ static void run(float2* v) {
         const float h = 0.86602540378443864676f;  // sin(2 pi / 3)
         const float2 a = cadd(v[1], v[2]);
         const float2 b = csub(v[1], v[2]);
@@ -99,7 +113,7 @@ struct Dft<3, INV> {
 
 template <bool INV>
 struct Dft<4, INV> {
-    __device__ __forceinline__ static void run(float2* v) {
+    __host__ __device__ __forceinline__ static void run(float2* v) {
         const float2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
         const float2 t2 = cadd(v[1], v[3]), t3 = mul_mi<INV>(csub(v[1], v[3]));
         v[0] = cadd(t0, t2);
@@ -111,7 +125,7 @@ struct Dft<4, INV> {
 
 template <bool INV>
 struct Dft<5, INV> {
-    __device__ __forceinline__ static void run(float2* v) {
+    __host__ __device__ __forceinline__ static void run(float2* v) {
         const float c1 = 0.30901699437494742410f;   // cos(2 pi / 5)
         const float c2 = -0.80901699437494742410f;  // cos(4 pi / 5)
         const float s1 = 0.95105651629515357212f;   // sin(2 pi / 5)
@@ -133,7 +147,7 @@ struct Dft<5, INV> {
 
 template <bool INV>
 struct Dft<8, INV> {
-    __device__ __forceinline__ static void run(float2* v) {
+    __host__ __device__ __forceinline__ static void run(float2* v) {
         const float h = 0.70710678118654752440f;  // 1/sqrt(2)
         float2 a[4], b[4];
 #pragma unroll
@@ -160,6 +174,97 @@ struct Dft<8, INV> {
         }
     }
 };
+
+// ------------------------------------------------------------------ composite R-point DFTs
+// Compile-time unrolling: f(integral_constant<int, i>) for i = B .. E-1.
+template <int B, int E, class F>
+__host__ __device__ __forceinline__ void static_for(F&& f) {
+    if constexpr (B < E) {
+        f(std::integral_constant<int, B>{});
+        static_for<B + 1, E>(f);
+    }
+}
+
+// cos / sin of 2 pi m / R by octant reduction and Taylor series in double; used only to
+// initialise constexpr twiddle constants (evaluated by the compiler, never at run time).
+__host__ __device__ constexpr double taylor_cos(double t) {
+    double term = 1.0, sum = 1.0;
+    for (int k = 1; k < 14; ++k) {
+        term *= -t * t / ((2.0 * k - 1.0) * (2.0 * k));
+        sum += term;
+    }
+    return sum;
+}
+__host__ __device__ constexpr double taylor_sin(double t) {
+    double term = t, sum = t;
+    for (int k = 1; k < 14; ++k) {
+        term *= -t * t / ((2.0 * k) * (2.0 * k + 1.0));
+        sum += term;
+    }
+    return sum;
+}
+// (cos, sin)(2 pi m / R): reduce m/R to [0, 1/8] with the symmetries of the circle
+__host__ __device__ constexpr double unit_cos(int m, int R) {
+    m %= R;
+    if (m < 0) m += R;
+    if (2 * m > R) m = R - m;                        // cos(2pi - a) = cos(a)
+    if (4 * m > R) return -unit_cos(R - 2 * m, 2 * R);  // cos(pi - a) = -cos(a)
+    const double PI = 3.14159265358979323846;
+    if (8 * m > R) return taylor_sin(2.0 * PI * (double)(R - 4 * m) / (4.0 * R));  // cos(a) = sin(pi/2 - a)
+    return taylor_cos(2.0 * PI * (double)m / (double)R);
+}
+__host__ __device__ constexpr double unit_sin(int m, int R) { return unit_cos(4 * m - R, 4 * R); }  // sin a = cos(a - pi/2)
+
+// v * exp(-+ 2 pi i m / R) with m, R compile-time; trivial factors fold away.
+template <int M, int R, bool INV>
+__host__ __device__ __forceinline__ float2 ctw(float2 v) {
+    constexpr int m = ((M % R) + R) % R;
+    if constexpr (m == 0) {
+        return v;
+    } else if constexpr (4 * m == R) {
+        return mul_mi<INV>(v);
+    } else if constexpr (2 * m == R) {
+        return make_float2(-v.x, -v.y);
+    } else if constexpr (4 * m == 3 * R) {
+        return mul_mi<!INV>(v);
+    } else {
+        constexpr float c = (float)unit_cos(m, R);
+        constexpr float sn = INV ? (float)unit_sin(m, R) : -(float)unit_sin(m, R);
+        return make_float2(c * v.x - sn * v.y, c * v.y + sn * v.x);
+    }
+}
+
+template <int R>
+struct DftSplit;  // R = R1 * R2 for the composite radices
+template <> struct DftSplit<16> { static constexpr int R1 = 4, R2 = 4; };
+template <> struct DftSplit<32> { static constexpr int R1 = 8, R2 = 4; };
+
+// Composite R-point DFT in registers, natural order in and out: with j = j1 R2 + j2 and
+// k = k1 + R1 k2, X_k = sum_j2 w_R2^(j2 k2) w_R^(j2 k1) sum_j1 w_R1^(j1 k1) x_j.
+template <int R, bool INV>
+struct DftComposite {
+    __host__ __device__ __forceinline__ static void run(float2* v) {
+        constexpr int R1 = DftSplit<R>::R1, R2 = DftSplit<R>::R2;
+        float2 a[R];
+        static_for<0, R2>([&](auto j2c) {
+            constexpr int j2 = decltype(j2c)::value;
+            float2 t[R1];
+            static_for<0, R1>([&](auto j1c) { t[decltype(j1c)::value] = v[decltype(j1c)::value * R2 + j2]; });
+            Dft<R1, INV>::run(t);
+            static_for<0, R1>([&](auto k1c) {
+                constexpr int k1 = decltype(k1c)::value;
+                a[k1 * R2 + j2] = ctw<j2 * k1, R, INV>(t[k1]);
+            });
+        });
+        static_for<0, R1>([&](auto k1c) {
+            constexpr int k1 = decltype(k1c)::value;
+            Dft<R2, INV>::run(a + k1 * R2);
+            static_for<0, R2>([&](auto k2c) { v[k1 + R1 * decltype(k2c)::value] = a[k1 * R2 + decltype(k2c)::value]; });
+        });
+    }
+};
+template <bool INV> struct Dft<16, INV> : DftComposite<16, INV> {};
+template <bool INV> struct Dft<32, INV> : DftComposite<32, INV> {};
 
 // ------------------------------------------------------------------ one in-place stage
 template <int R, bool INV, int W, int SN, int T>
@@ -196,9 +301,15 @@ __device__ __forceinline__ void fft_stage(float2* __restrict__ s, const float2* 
     __syncthreads();
 }
 
-template <bool INV, int W, int SN, int T>
+template <bool INV, int W, int SN, int T, int RMAX>
 __device__ __forceinline__ void fft_stage_any(float2* s, const float2* tw, const FftPlan& pl, int st) {
     switch (pl.r[st]) {
+        case 32:
+            if constexpr (RMAX >= 32) fft_stage<32, INV, W, SN, T>(s, tw, pl, st);
+            break;
+        case 16:
+            if constexpr (RMAX >= 16) fft_stage<16, INV, W, SN, T>(s, tw, pl, st);
+            break;
         case 8: fft_stage<8, INV, W, SN, T>(s, tw, pl, st); break;
         case 4: fft_stage<4, INV, W, SN, T>(s, tw, pl, st); break;
         case 2: fft_stage<2, INV, W, SN, T>(s, tw, pl, st); break;
@@ -209,14 +320,15 @@ __device__ __forceinline__ void fft_stage_any(float2* s, const float2* tw, const
 
 // Full transform of the W lines of the tile: forward natural -> digit-reversed, inverse
 // digit-reversed -> natural (unnormalised).  The caller synchronises after filling s; on
-// return the block is synchronised.
-template <bool INV, int W, int SN, int T>
+// return the block is synchronised.  The plan's radices must be <= RMAX (plan_fits; the
+// launchers check it), larger radices are not compiled into the kernel.
+template <bool INV, int W, int SN, int T, int RMAX = fft_max_radix(T)>
 __device__ __forceinline__ void fft_tile(float2* __restrict__ s, const float2* __restrict__ tw,
                                          const FftPlan& pl) {
     if (!INV) {
-        for (int st = 0; st < pl.nst; ++st) fft_stage_any<false, W, SN, T>(s, tw, pl, st);
+        for (int st = 0; st < pl.nst; ++st) fft_stage_any<false, W, SN, T, RMAX>(s, tw, pl, st);
     } else {
-        for (int st = pl.nst - 1; st >= 0; --st) fft_stage_any<true, W, SN, T>(s, tw, pl, st);
+        for (int st = pl.nst - 1; st >= 0; --st) fft_stage_any<true, W, SN, T, RMAX>(s, tw, pl, st);
     }
 }
 

@@ -134,11 +134,11 @@ __device__ void bluestein(float2* s1, float2* s2, const float2* tw, int N, int M
         }
     }
     __syncthreads();
-    fft_tile<false, 1, 1, FIT_T>(s1, tw, pl);
-    fft_tile<false, 1, 1, FIT_T>(s2, tw, pl);
+    fft_tile<false, 1, 1, FIT_T, 16>(s1, tw, pl);
+    fft_tile<false, 1, 1, FIT_T, 16>(s2, tw, pl);
     for (int n = threadIdx.x; n < M; n += FIT_T) s1[n] = cmul(s1[n], s2[n]);  // digit-reversed, same order
     __syncthreads();
-    fft_tile<true, 1, 1, FIT_T>(s1, tw, pl);
+    fft_tile<true, 1, 1, FIT_T, 16>(s1, tw, pl);
     const float inv_m = 1.0f / (float)M;
     for (int k = threadIdx.x; k < N; k += FIT_T) {
         const float2 w = chirp(k, N);
@@ -462,8 +462,8 @@ static int fit_args(const SmkFitProblem* fp, const float* theta, double* acc, co
     a->gM = gM;
     a->gP = gP;
     a->counter = counter;
-    make_plan(2048, &a->plans[0]);
-    make_plan(4096, &a->plans[1]);
+    make_plan(2048, &a->plans[0], 16);
+    make_plan(4096, &a->plans[1], 16);
     return SMK_OK;
 }
 

@@ -169,8 +169,15 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
     } else {
         return fail(SMK_EINVAL, "smk_grf_boxes: unknown pk_mode");
     }
-    FftPlan plx, ply, plz;
-    if (!make_plan(p->nx, &plx) || !make_plan(p->ny, &ply) || !make_plan(p->nz, &plz))
+    // tile variant of every pass, and each pass's radix plan within its register budget
+    const bool gpu_noise = p->noise_mode == SMK_NOISE_PHILOX;
+    const int pass_x = gpu_noise ? PASS_XGEN : PASS_XPASS;
+    const int vx = variant_for(pass_x, p->nx), vy = variant_for(PASS_LINE, p->ny);
+    const int vzf = variant_for(PASS_ZFWD, p->nz), vzi = variant_for(PASS_ZINV, p->nz);
+    auto rmax = [](int pass, int v) { return fft_max_radix(variant_table(pass)[v].t); };
+    FftPlan plx, ply, plzf, plzi;
+    if (!make_plan(p->nx, &plx, rmax(pass_x, vx)) || !make_plan(p->ny, &ply, rmax(PASS_LINE, vy)) ||
+        !make_plan(p->nz, &plzf, rmax(PASS_ZFWD, vzf)) || !make_plan(p->nz, &plzi, rmax(PASS_ZINV, vzi)))
         return fail(SMK_ENOTSUPP, "smk_grf_boxes: %dx%dx%d has an axis outside 2..4096 or not 2^a3^b5^c",
                     p->nx, p->ny, p->nz);
     cudaStream_t st = (cudaStream_t)stream;
@@ -207,7 +214,7 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
     ya.ncol = nzh;
     const int64_t rows_per_box = (int64_t)p->nx * p->ny;
     const float inv_vcell = 1.0f / (float)(p->dcell * p->dcell * p->dcell);
-    if (p->noise_mode == SMK_NOISE_PHILOX) {
+    if (gpu_noise) {
         // Fourier modes drawn in the x pass: no forward z / y passes
         if ((rc = mark(1)) || (rc = mark(2))) return rc;
         XGenArgs ga;
@@ -233,20 +240,20 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         ga.sig_r = (float)sqrt(ncell);
         ga.seed = p->seed;
         ga.eta_comp = p->eta_comp;
-        if ((rc = run_xgen(variant_for(PASS_XGEN, p->nx), ga, st))) return rc;
+        if ((rc = run_xgen(vx, ga, st))) return rc;
         if ((rc = mark(3))) return rc;
     } else {
         // 1. r2c along z of the caller's noise
         ZFwdArgs za;
-        za.pl = plz;
+        za.pl = plzf;
         za.batch = p->batch;
         za.pitch = pitch;
         za.noise = p->noise;
         za.out = delta;
-        if ((rc = run_zfwd(variant_for(PASS_ZFWD, p->nz), za, rows_per_box, st))) return rc;
+        if ((rc = run_zfwd(vzf, za, rows_per_box, st))) return rc;
         if ((rc = mark(1))) return rc;
         // 2. c2c along y, forward (the y spectrum stays in digit-reversed order)
-        if ((rc = run_line(variant_for(PASS_LINE, p->ny), ya, false, st))) return rc;
+        if ((rc = run_line(vy, ya, false, st))) return rc;
         if ((rc = mark(2))) return rc;
         // 3. x: forward, P(k) scaling + eta split, inverse
         XArgs xa;
@@ -267,18 +274,18 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         xa.inv_k0 = p->pk_mode == SMK_PK_ANALYTIC ? (float)(1.0 / p->k0) : 0.f;
         xa.inv_vcell = inv_vcell;
         xa.eta_comp = p->eta_comp;
-        if ((rc = run_xpass(variant_for(PASS_XPASS, p->nx), xa, st))) return rc;
+        if ((rc = run_xpass(vx, xa, st))) return rc;
         if ((rc = mark(3))) return rc;
     }
 
     // 4. c2c along y, inverse, on delta (and eta)
     ya.nbuf = p->want_eta ? 2 : 1;
-    if ((rc = run_line(variant_for(PASS_LINE, p->ny), ya, true, st))) return rc;
+    if ((rc = run_line(vy, ya, true, st))) return rc;
     if ((rc = mark(4))) return rc;
 
     // 5. c2r along z, / N, statistics
     ZInvArgs ia;
-    ia.pl = plz;
+    ia.pl = plzi;
     ia.batch = p->batch;
     ia.buf[0] = delta;
     ia.buf[1] = eta;
@@ -286,7 +293,7 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
     ia.pitch = pitch;
     ia.scale = (float)(1.0 / ((double)p->nx * p->ny * p->nz));
     ia.stats = stats;
-    if ((rc = run_zinv(variant_for(PASS_ZINV, p->nz), ia, rows_per_box, st))) return rc;
+    if ((rc = run_zinv(vzi, ia, rows_per_box, st))) return rc;
     return mark(5);
 }
 

@@ -549,6 +549,7 @@ static size_t zpass_smem(int n) {
 
 template <class C>
 static int launch_zfwd(ZFwdArgs a, int64_t rows_per_box, cudaStream_t st) {
+    if (!plan_fits(a.pl, fft_max_radix(C::T))) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "zfwd_kernel");
     a.zt.init(rows_per_box, C::W);
     const size_t smem = zpass_smem<C>(a.pl.n);
     const int64_t ntiles = a.zt.tiles_per_box * a.batch;
@@ -560,6 +561,7 @@ static int launch_zfwd(ZFwdArgs a, int64_t rows_per_box, cudaStream_t st) {
 
 template <class C>
 static int launch_zinv(ZInvArgs a, int64_t rows_per_box, cudaStream_t st) {
+    if (!plan_fits(a.pl, fft_max_radix(C::T))) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "zinv_kernel");
     a.zt.init(rows_per_box, C::W);
     const size_t smem = zpass_smem<C>(a.pl.n);
     const int64_t ntiles = a.zt.tiles_per_box * a.batch * a.nbuf;
@@ -571,6 +573,7 @@ static int launch_zinv(ZInvArgs a, int64_t rows_per_box, cudaStream_t st) {
 
 template <class C>
 static int launch_line(const LineArgs& a, bool inv, cudaStream_t st) {
+    if (!plan_fits(a.pl, fft_max_radix(C::T))) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "line_kernel");
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2);
     const int64_t ntiles = a.n_outer * ceil_div(a.ncol, C::W) * a.nbuf;
     int grid = 0, rc;
@@ -586,6 +589,7 @@ static int launch_line(const LineArgs& a, bool inv, cudaStream_t st) {
 
 template <class C>
 static int launch_xpass(const XArgs& a, cudaStream_t st) {
+    if (!plan_fits(a.pl, fft_max_radix(C::T))) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xpass_kernel");
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 + (C::W + 1) * 4;
     const int64_t ntiles = (int64_t)a.batch * a.ny * ceil_div(a.nzh, C::W);
     int grid = 0, rc;
@@ -596,6 +600,7 @@ static int launch_xpass(const XArgs& a, cudaStream_t st) {
 
 template <class C>
 static int launch_xgen(const XGenArgs& a, cudaStream_t st) {
+    if (!plan_fits(a.pl, fft_max_radix(C::T))) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xgen_kernel");
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 +
                         (size_t)a.nzh * 4 + 16;
     const int64_t ntiles = (int64_t)a.batch * a.ny * ceil_div(a.nzh, C::W / 2);
@@ -611,15 +616,16 @@ struct TileVariant {
 };
 // z passes (zfwd, zinv): W = row pairs per tile
 #define SMK_Z_VARIANTS(X) X(16, 256, 512) X(8, 256, 512) X(16, 512, 1024) X(8, 512, 1024) \
-    X(8, 512, 2560) X(4, 512, 2560) X(8, 1024, 2560) X(4, 256, 2560) X(4, 512, 4096) X(2, 512, 4096)
+    X(8, 512, 2560) X(4, 512, 2560) X(8, 1024, 2560) X(4, 256, 2560) X(4, 512, 4096) X(2, 512, 4096) \
+    X(8, 256, 2560)
 // y pass (line): W = columns per tile
 #define SMK_LINE_VARIANTS(X) X(16, 256, 512) X(32, 256, 512) X(16, 512, 1024) X(16, 1024, 1024) \
-    X(8, 512, 2560) X(8, 1024, 2560) X(4, 512, 4096) X(4, 1024, 4096)
+    X(8, 512, 2560) X(8, 1024, 2560) X(4, 512, 4096) X(4, 1024, 4096) X(8, 256, 2560)
 // x pass of host noise: W = columns per tile
 #define SMK_X_VARIANTS(X) X(16, 256, 512) X(16, 512, 1024) X(8, 512, 2560) X(4, 512, 4096)
 // x pass of GPU noise: W = lines per tile (W/2 delta columns + W/2 eta columns)
 #define SMK_XGEN_VARIANTS(X) X(32, 256, 512) X(16, 256, 512) X(16, 512, 1024) X(16, 1024, 1024) \
-    X(8, 512, 2560) X(8, 1024, 2560) X(4, 512, 4096) X(4, 1024, 4096)
+    X(8, 512, 2560) X(8, 1024, 2560) X(4, 512, 4096) X(4, 1024, 4096) X(8, 256, 2560)
 
 enum { PASS_ZFWD = 0, PASS_LINE = 1, PASS_XPASS = 2, PASS_XGEN = 3, PASS_ZINV = 4, NPASS = 5 };
 

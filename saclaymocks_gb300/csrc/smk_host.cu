@@ -27,17 +27,29 @@ int check_launch(const char* what) {
     return SMK_OK;
 }
 
-bool make_plan(int n, FftPlan* p) {
+bool make_plan(int n, FftPlan* p, int rmax) {
     if (n < 2 || n > FFT_MAX_N) return false;
     int m = n, p2 = 0, p3 = 0, p5 = 0;
     while (m % 2 == 0) { m /= 2; ++p2; }
     while (m % 3 == 0) { m /= 3; ++p3; }
     while (m % 5 == 0) { m /= 5; ++p5; }
     if (m != 1) return false;
+    // rmax >= 16: radix-16 stages (a radix-32 one when one factor 2 is left over and
+    // rmax >= 32), then 8, 4 or 2 for the rest of the power of two; rmax 8: 8s, then 4s / 2.
+    // 3s and 5s follow.
     int rad[32], nr = 0;
-    while (p2 >= 3 && p2 - 3 != 1) { rad[nr++] = 8; p2 -= 3; }
-    while (p2 >= 2) { rad[nr++] = 4; p2 -= 2; }
-    if (p2 == 1) rad[nr++] = 2;
+    if (rmax >= 16) {
+        while (p2 >= 4) { rad[nr++] = 16; p2 -= 4; }
+        if (p2 == 1 && nr > 0 && rmax >= 32) {
+            rad[0] = 32;
+        } else if (p2 > 0) {
+            rad[nr++] = 1 << p2;
+        }
+    } else {
+        while (p2 >= 3 && p2 - 3 != 1) { rad[nr++] = 8; p2 -= 3; }
+        while (p2 >= 2) { rad[nr++] = 4; p2 -= 2; }
+        if (p2 == 1) rad[nr++] = 2;
+    }
     for (int i = 0; i < p3; ++i) rad[nr++] = 3;
     for (int i = 0; i < p5; ++i) rad[nr++] = 5;
     if (nr > FFT_MAX_STAGES) return false;

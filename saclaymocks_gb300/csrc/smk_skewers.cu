@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(SK_T, 2) skewer_kernel(const SkArgs a) {
                 for (int e = threadIdx.x; e < nzz; e += SK_T)
                     s[e] = make_float2(__ldg(n0 + e), n1 ? __ldg(n1 + e) : 0.f);
                 __syncthreads();
-                fft_tile<false, 1, 1, SK_T>(s, tw, pl);
+                fft_tile<false, 1, 1, SK_T, 16>(s, tw, pl);
                 for (int e = threadIdx.x; e < nzz; e += SK_T) {
                     const int f = freq_of_slot(pl, e);
                     s[e] = cscale(s[e], __ldg(S + (f <= half ? f : nzz - f)));
@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(SK_T, 2) skewer_kernel(const SkArgs a) {
                 }
                 __syncthreads();
             }
-            fft_tile<true, 1, 1, SK_T>(s, tw, pl);
+            fft_tile<true, 1, 1, SK_T, 16>(s, tw, pl);
             inv_nz = 1.0f / (float)nzz;
         }
         // pixels of both skewers
@@ -402,7 +402,7 @@ int smk_skewers_flux(const SmkSkewers* sk, const SmkSpectraParams* p, const floa
     a.ss_noise = p->ss_noise;
     a.ss_noise_offset = p->ss_noise_offset;
     a.seed = p->seed;
-    for (int j = 0; j < SK_NCLASS; ++j) make_plan(256 << j, &a.plans[j]);
+    for (int j = 0; j < SK_NCLASS; ++j) make_plan(256 << j, &a.plans[j], 16);
     a.abc_mode = p->abc_mode;
     a.a = p->a;
     a.b = p->b;

@@ -71,14 +71,21 @@ class SkewerTable:
     def total_pixels(self) -> int:
         return int(self.npix.astype(np.int64).sum())
 
-    def schedule(self, ss_nz: int) -> np.ndarray:
-        """Work schedule of smk_skewers_flux (pairs of equal small-scale FFT length)."""
+    def schedule(self, ss_nz: int, pair: bool = True) -> np.ndarray:
+        """Work schedule of smk_skewers_flux (pairs of equal small-scale FFT length).
+        pair=False gives every skewer a work item of its own (the other slot empty): the
+        one-skewer-per-block layout, kept as the baseline the paired schedule is measured
+        against."""
         lib = _lib.load()
         order = np.empty(2 * self.n + 16, dtype=np.int32)
         nslots = C.c_int64(0)
         _lib.check(lib.smk_skewer_schedule(self.n, self.npix.ctypes.data, int(ss_nz),
                                            order.ctypes.data, C.byref(nslots)), "smk_skewer_schedule")
-        return order[:nslots.value].copy()
+        order = order[:nslots.value].copy()
+        if not pair:
+            ids = order[order >= 0]
+            order = np.stack([ids, np.full_like(ids, -1)], 1).ravel().copy()
+        return order
 
 
 def skewers_parallel_z(n: int, nx: int, ny: int, npix: int, dcell: float, seed: int = 0,
@@ -138,11 +145,11 @@ class SpectraConfig:
 class SkewerRunner:
     """Device copies of a skewer table + schedule + tables, reusable across calls."""
 
-    def __init__(self, table: SkewerTable, cfg: SpectraConfig, device="cuda", pixels=None):
+    def __init__(self, table: SkewerTable, cfg: SpectraConfig, device="cuda", pixels=None, pair: bool = True):
         self.table = table
         self.cfg = cfg
         self.device = torch.device(device)
-        order = table.schedule(cfg.ss_nz if cfg.ss_mode != _lib.SMK_SS_NONE else -1)
+        order = table.schedule(cfg.ss_nz if cfg.ss_mode != _lib.SMK_SS_NONE else -1, pair=pair)
         dv = self.device
         self.d_start = torch.from_numpy(table.start).to(dv)
         self.d_dir = torch.from_numpy(table.direction).to(dv)

@@ -197,3 +197,36 @@ def test_every_tile_variant_is_exact(G, pname):
             _check(out.eta[0].cpu().numpy(), o64["eta_zz"], f"{pname} variant {v} eta")
         finally:
             lib.smk_tune_set(pid, n, -1)
+
+
+def test_philox_batch_member_equals_single_call(G):
+    """One batched call of B boxes (box b drawn from seed + b) gives the same boxes, bit for
+    bit, as B single-box calls with seeds seed + b."""
+    nx, ny, nz, B, seed = 20, 18, 24, 4, 100
+    out = G.make_boxes(nx, ny, nz, 2.19, seed=seed, batch=B)
+    for b in range(B):
+        one = G.make_boxes(nx, ny, nz, 2.19, seed=seed + b)
+        torch.cuda.synchronize()
+        assert torch.equal(out.delta[b], one.delta[0])
+        assert torch.equal(out.eta[b], one.eta[0])
+
+
+def test_grf_replayed_from_a_cuda_graph_equals_eager(G):
+    """smk_grf_boxes is stream-ordered and sync-free, so it can be captured in a CUDA graph;
+    a replay reproduces the eager call bit for bit."""
+    nx, ny, nz = 24, 20, 30
+    amp = G.pk_normalisation(nx, ny, nz)
+    eager = G.make_boxes(nx, ny, nz, 2.19, seed=9, amp=amp)
+    out = G.alloc_boxes(nx, ny, nz)
+    ws = G.GrfWorkspace(1)
+    G.make_boxes(nx, ny, nz, 2.19, seed=9, amp=amp, out=out, workspace=ws)   # launch set-up outside capture
+    torch.cuda.synchronize()
+    out[0].zero_()
+    out[1].zero_()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        G.make_boxes(nx, ny, nz, 2.19, seed=9, amp=amp, out=out, workspace=ws)
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(out[0][..., :nz], eager.delta)
+    assert torch.equal(out[1][..., :nz], eager.eta)

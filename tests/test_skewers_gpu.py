@@ -280,3 +280,37 @@ def test_gauss343_periodic_wrap_vs_oracle(env, boxes):
         np.testing.assert_allclose(et[s], ep, rtol=0, atol=1e-5)
         np.testing.assert_array_equal(dl0[s], dl[s])
         assert not np.any(et0[s])
+
+
+def test_one_skewer_per_item_schedule_matches_paired(env, boxes):
+    """The one-skewer-per-work-item schedule (the baseline of the paired one) gives the same
+    flux up to float32 rounding of the packed complex FFT."""
+    _lib, _, spectra = env
+    L = np.array([boxes["nx"], boxes["ny"], boxes["nz"]]) * boxes["dx"]
+    t = spectra.skewers_cone(33, L, seed=5, npix_range=(60, 700), log_uniform=True)
+    cfg = spectra.SpectraConfig(ss_mode=_lib.SMK_SS_PHILOX, ss_nz=0, seed=3)
+    out = boxes["out"]
+    kw = dict(nx=boxes["nx"], ny=boxes["ny"], nz=boxes["nz"], pitch=out.pitch, dcell=boxes["dx"])
+    fp = spectra.SkewerRunner(t, cfg).run(out.delta_pad[0], out.eta_pad[0], **kw)
+    fs = spectra.SkewerRunner(t, cfg, pair=False).run(out.delta_pad[0], out.eta_pad[0], **kw)
+    torch.cuda.synchronize()
+    assert float((fp - fs).abs().max()) <= F_ATOL
+
+
+def test_skewer_launch_replayed_from_a_cuda_graph_equals_eager(env, boxes):
+    _lib, _, spectra = env
+    L = np.array([boxes["nx"], boxes["ny"], boxes["nz"]]) * boxes["dx"]
+    t = spectra.skewers_cone(40, L, seed=6, npix_range=(100, 500))
+    cfg = spectra.SpectraConfig(ss_mode=_lib.SMK_SS_PHILOX, ss_nz=1024, seed=4)
+    out = boxes["out"]
+    kw = dict(nx=boxes["nx"], ny=boxes["ny"], nz=boxes["nz"], pitch=out.pitch, dcell=boxes["dx"])
+    run = spectra.SkewerRunner(t, cfg)
+    eager = run.run(out.delta_pad[0], out.eta_pad[0], **kw).clone()
+    flux = torch.zeros_like(eager)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        run.run(out.delta_pad[0], out.eta_pad[0], flux=flux, **kw)
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(flux, eager)
