@@ -423,6 +423,152 @@ def batching_leg(cfg_seed=2):
     return res
 
 
+def precision_leg(n=1536, seed=3, nsk=100_000, npix=1024, dcell=2.19, k0=0.02, nbins=64, slab=64):
+    """FP32 GPU path against an FP64 restatement of the same arithmetic (cuFFT double through
+    torch.fft) on the same white noise: delta / eta_zz boxes (relative RMS, max |err| / sigma),
+    P(k) of delta in `nbins` linear |k| bins (P32/P64 - 1 per bin), and the flux of `nsk`
+    skewers of `npix` pixels (trilinear read, FGPA with a(z) power law, no small scales):
+    mean F and the binned P1D of F/<F> - 1.  Host-noise mode, i.e. all five HBM passes."""
+    import math
+
+    import numpy as np
+    import torch
+
+    from saclaymocks_gb300 import _lib, grf, spectra
+    torch.cuda.empty_cache()
+    dv = torch.device("cuda")
+    f64 = torch.float64
+    gen = torch.Generator(device=dv)
+    gen.manual_seed(seed)
+    noise = torch.randn((n, n, n), generator=gen, device=dv, dtype=torch.float32)
+    amp = grf.pk_normalisation(n, n, n, dcell, k0)
+    out = grf.make_boxes(n, n, n, dcell, noise=noise, amp=amp, k0=k0)
+    torch.cuda.synchronize()
+    spec = torch.fft.rfftn(noise.to(f64))
+    del noise
+    kf = 2.0 * math.pi / dcell
+    kx = torch.fft.fftfreq(n, device=dv, dtype=f64).mul_(kf).view(n, 1, 1)
+    ky = torch.fft.fftfreq(n, device=dv, dtype=f64).mul_(kf).view(1, n, 1)
+    kz = torch.fft.rfftfreq(n, device=dv, dtype=f64).mul_(kf).view(1, 1, -1)
+    nzh = n // 2 + 1
+    kmax = math.sqrt(3.0) * math.pi / dcell
+    wz = torch.full((1, 1, nzh), 2.0, device=dv, dtype=f64)
+    wz[..., 0] = 1.0
+    if n % 2 == 0:
+        wz[..., -1] = 1.0
+
+    def kgrid(i0, i1):
+        return kx[i0:i1] ** 2 + ky ** 2 + kz ** 2
+
+    def binned_power(sp):
+        num = torch.zeros(nbins, device=dv, dtype=f64)
+        cnt = torch.zeros(nbins, device=dv, dtype=f64)
+        for i0 in range(0, n, slab):
+            k = kgrid(i0, i0 + slab).sqrt_()
+            b = (k / kmax * nbins).long().clamp_(0, nbins - 1)
+            w = wz.expand_as(k)
+            num.index_add_(0, b.flatten(), (sp[i0:i0 + slab].abs() ** 2 * w).flatten())
+            cnt.index_add_(0, b.flatten(), w.flatten())
+        return num / cnt.clamp(min=1), cnt
+    for i0 in range(0, n, slab):
+        k = kgrid(i0, i0 + slab).sqrt_()
+        spec[i0:i0 + slab] *= (amp * k / (1.0 + (k / k0) ** 2) ** 2 / dcell ** 3).sqrt_()
+    p64, cnt = binned_power(spec)
+    d64 = torch.fft.irfftn(spec, s=(n, n, n))
+    for i0 in range(0, n, slab):
+        kk = kgrid(i0, i0 + slab)
+        if i0 == 0:
+            kk[0, 0, 0] = 1.0
+        spec[i0:i0 + slab] *= kz ** 2 / kk
+    e64 = torch.fft.irfftn(spec, s=(n, n, n))
+    del spec
+    torch.cuda.empty_cache()
+
+    def box_err(a32, a64):
+        se = sa = 0.0
+        mx = 0.0
+        for i0 in range(0, n, slab):
+            d = a32[i0:i0 + slab].to(f64) - a64[i0:i0 + slab]
+            se += float((d * d).sum())
+            sa += float((a64[i0:i0 + slab] ** 2).sum())
+            mx = max(mx, float(d.abs().max()))
+        sig = math.sqrt(sa / n ** 3)
+        return {"rel_rms": math.sqrt(se / sa), "max_abs_over_sigma": mx / sig}
+    res = {"box": f"{n}^3", "delta": box_err(out.delta[0], d64), "eta_zz": box_err(out.eta[0], e64)}
+    sp32 = torch.fft.rfftn(out.delta[0].to(f64))
+    p32, _ = binned_power(sp32)
+    del sp32
+    torch.cuda.empty_cache()
+    ok = cnt > 0
+    ratio = (p32[ok] / p64[ok] - 1.0).abs()
+    res["pk_bins"] = int(ok.sum())
+    res["pk_max_rel_diff"] = float(ratio.max())
+    res["pk_median_rel_diff"] = float(ratio.median())
+
+    # skewers: GPU kernel on the FP32 boxes vs FP64 trilinear read + FGPA on the FP64 boxes
+    L = n * dcell
+    table = spectra.skewers_cone(nsk, (L, L, L), seed=seed, npix_range=(npix, npix))
+    scfg = spectra.SpectraConfig(ss_mode=_lib.SMK_SS_NONE, abc_mode=_lib.SMK_ABC_POWERLAW, a=0.1,
+                                 a_zref1=3.2, a_power=4.5, b=1.58, c=0.6, z_lo=1.8, z_hi=3.6)
+    run = spectra.SkewerRunner(table, scfg)
+    F32 = run.run(out.delta_pad[0], out.eta_pad[0], nx=n, ny=n, nz=n, pitch=out.pitch, dcell=dcell)
+    st = torch.from_numpy(table.start).to(dv).to(f64)
+    di = torch.from_numpy(table.direction).to(dv).to(f64)
+    F64 = torch.empty(table.total_pixels, device=dv, dtype=f64)
+    i = torch.arange(npix, device=dv, dtype=f64) * table.dpix
+    dflat, eflat = d64.view(-1), e64.view(-1)
+    per = max(1, 20_000_000 // npix)
+    for s0 in range(0, nsk, per):
+        pos = st[s0:s0 + per, None, :] + i[None, :, None] * di[s0:s0 + per, None, :]
+        u = pos / dcell - 0.5
+        fl = torch.floor(u)
+        fr = u - fl
+        c0 = torch.remainder(fl.long(), n)
+        c1 = torch.remainder(c0 + 1, n)
+        val_d = torch.zeros(pos.shape[:2], device=dv, dtype=f64)
+        val_e = torch.zeros_like(val_d)
+        for cx in (0, 1):
+            wx = fr[..., 0] if cx else 1 - fr[..., 0]
+            ix = c1[..., 0] if cx else c0[..., 0]
+            for cy in (0, 1):
+                wy = fr[..., 1] if cy else 1 - fr[..., 1]
+                iy = c1[..., 1] if cy else c0[..., 1]
+                for cz in (0, 1):
+                    wzz = fr[..., 2] if cz else 1 - fr[..., 2]
+                    iz = c1[..., 2] if cz else c0[..., 2]
+                    idx = (ix * n + iy) * n + iz
+                    w = wx * wy * wzz
+                    val_d += w * dflat[idx]
+                    val_e += w * eflat[idx]
+        xc = torch.remainder(pos[..., 0] / dcell, n)
+        z = 1.8 + 1.8 * xc / n
+        a = 0.1 * ((1.0 + z) / 3.2) ** 4.5
+        F = torch.exp(-a * torch.exp(1.58 * (val_d + 0.6 * val_e)))
+        F64[s0 * npix:(s0 + per) * npix] = F.flatten()
+    del d64, e64
+    F32d = F32.to(f64)
+    res["skewers"] = f"{nsk} x {npix} pixels"
+    res["flux_max_abs_diff"] = float((F32d - F64).abs().max())
+    m32, m64 = float(F32d.mean()), float(F64.mean())
+    res["mean_flux_rel_diff"] = abs(m32 / m64 - 1.0)
+    dF32 = (F32d / m32 - 1.0).view(nsk, npix)
+    dF64 = (F64 / m64 - 1.0).view(nsk, npix)
+    q32 = (torch.fft.rfft(dF32, dim=1).abs() ** 2).mean(0)
+    q64 = (torch.fft.rfft(dF64, dim=1).abs() ** 2).mean(0)
+    kk = np.fft.rfftfreq(npix) * 2 * np.pi / table.dpix
+    edges = np.logspace(np.log10(kk[1]), np.log10(kk[-1] * 1.0001), 33)
+    b = np.searchsorted(edges, kk, side="right") - 1
+    rel = []
+    q32n, q64n = q32.cpu().numpy(), q64.cpu().numpy()
+    for j in range(32):
+        sel = b == j
+        if sel.any():
+            rel.append(abs(q32n[sel].mean() / q64n[sel].mean() - 1.0))
+    res["p1d_bins"] = len(rel)
+    res["p1d_max_rel_diff"] = float(max(rel))
+    return res
+
+
 def set_variants(spec, nx, ny, nz):
     """--variants xgen=5,line=5,zinv=4: fixed tile variants per GRF pass instead of tuning
     (so a profile replays the tile choice of an earlier tuned run)."""
@@ -444,7 +590,8 @@ def run_grf_only(args, shape):
 
     from saclaymocks_gb300 import grf
     nx, ny, nz = shape
-    boxes = grf.alloc_boxes(nx, ny, nz)
+    want_eta = not args.no_eta
+    boxes = grf.alloc_boxes(nx, ny, nz, want_eta=want_eta)
     ws = grf.GrfWorkspace(1)
     amp = grf.pk_normalisation(nx, ny, nz)
     tuned = None
@@ -454,13 +601,14 @@ def run_grf_only(args, shape):
         from saclaymocks_gb300 import tune
         tuned = tune.tune_grf(nx, ny, nz, out=boxes, workspace=ws, use_cache=False)
     for _ in range(args.warmup):
-        grf.make_boxes(nx, ny, nz, seed=1, amp=amp, out=boxes, workspace=ws)
+        grf.make_boxes(nx, ny, nz, seed=1, amp=amp, out=boxes, workspace=ws, want_eta=want_eta)
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(args.steps)]
     for e in [x for row in evs for x in row]:
         e.record()
     torch.cuda.synchronize()
     for k in range(args.steps):
-        out = grf.make_boxes(nx, ny, nz, seed=1, amp=amp, out=boxes, workspace=ws, pass_events=evs[k])
+        out = grf.make_boxes(nx, ny, nz, seed=1, amp=amp, out=boxes, workspace=ws, pass_events=evs[k],
+                             want_eta=want_eta)
     torch.cuda.synchronize()
     out.check()
     pass_ms = np.mean([[evs[k][i].elapsed_time(evs[k][i + 1]) for i in range(5)]
@@ -479,6 +627,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-tune", action="store_true", help="built-in tile variants, no autotuning")
     ap.add_argument("--no-batching", action="store_true", help="skip the batched / graph-replay leg")
+    ap.add_argument("--no-eta", action="store_true", help="--grf-shape: delta box only")
+    ap.add_argument("--precision", default=None, const="1536,100000,1024", nargs="?",
+                    help="only the FP32-vs-FP64 precision report: N,skewers,pixels (default 1536^3, 1e5 x 1024)")
     ap.add_argument("--variants", default=None,
                     help="fixed tile variants, e.g. xgen=5,line=5,zinv=4 (no autotuning)")
     ap.add_argument("--no-fit", action="store_true", help="skip the (a,b,c) fit leg")
@@ -489,6 +640,10 @@ def main():
     cfg = SMALL if args.small else PRODUCTION
     if args.grf_shape:
         run_grf_only(args, [int(x) for x in args.grf_shape.split(",")])
+        return
+    if args.precision:
+        n, nsk, npix = (int(x) for x in args.precision.split(","))
+        print(json.dumps({"precision": precision_leg(n=n, nsk=nsk, npix=npix)}))
         return
     if args.impl == "reference":
         run_reference(args, cfg)

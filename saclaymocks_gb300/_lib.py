@@ -89,6 +89,7 @@ _SIGS = [
                                 C.POINTER(C.c_int32)]),
     ("smk_tune_set", C.c_int, [C.c_int32, C.c_int32, C.c_int32]),
     ("smk_tune_get", C.c_int, [C.c_int32, C.c_int32]),
+    ("smk_tune_xgen_split", C.c_int, [C.c_int32]),
     ("smk_skewer_schedule", C.c_int, [C.c_int64, C.c_void_p, C.c_int32, C.c_void_p,
                                       C.POINTER(C.c_int64)]),
     ("smk_skewers_workspace_size", C.c_size_t, [C.POINTER(SmkSkewers), C.POINTER(SmkSpectraParams)]),

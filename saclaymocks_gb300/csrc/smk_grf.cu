@@ -63,6 +63,8 @@ static struct ChoiceInit {
     }
 } g_choice_init;
 
+static std::atomic<int> g_xgen_split{-1};  // -1: by footprint, 0: never, 1: always
+
 static int length_class(int n) { return n <= 512 ? 0 : n <= 1024 ? 1 : n <= 2560 ? 2 : 3; }
 
 const TileVariant* variant_table(int pass) {
@@ -240,7 +242,19 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         ga.sig_r = (float)sqrt(ncell);
         ga.seed = p->seed;
         ga.eta_comp = p->eta_comp;
+        // A tile writes all nx rows of its columns, so one wave of tiles touches rows spread over
+        // the whole of each output box.  Past ~64 GiB for the two boxes together (2 x 40 GB at
+        // 2560x2560x1536) that spread outruns the GPU's address-translation reach and the pass
+        // slows by 1.7x; writing delta and eta in two launches keeps each wave within one box.
+        const double pair_bytes = 2.0 * 4.0 * (double)p->batch * p->nx * p->ny * (double)pitch;
+        const int sm = g_xgen_split.load();
+        const bool split = p->want_eta && (sm < 0 ? pair_bytes > 64.0 * (1ull << 30) : sm == 1);
+        ga.fields = !p->want_eta ? XGEN_DELTA : (split ? XGEN_DELTA : XGEN_BOTH);
         if ((rc = run_xgen(vx, ga, st))) return rc;
+        if (split) {
+            ga.fields = XGEN_ETA;
+            if ((rc = run_xgen(vx, ga, st))) return rc;
+        }
         if ((rc = mark(3))) return rc;
     } else {
         // 1. r2c along z of the caller's noise
@@ -295,6 +309,11 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
     ia.stats = stats;
     if ((rc = run_zinv(vzi, ia, rows_per_box, st))) return rc;
     return mark(5);
+}
+
+int smk_tune_xgen_split(int32_t mode) {
+    if (mode < -1 || mode > 1) return fail(SMK_EINVAL, "smk_tune_xgen_split: mode must be -1, 0 or 1");
+    return g_xgen_split.exchange(mode);
 }
 
 int smk_tune_count(int32_t pass) { return variant_count(pass); }

@@ -288,12 +288,17 @@ struct XGenArgs {
     float sig_c, sig_r;    // sqrt(N/2), sqrt(N)
     uint64_t seed;
     int eta_comp;
+    int fields;            // XGEN_BOTH: W/2 delta + W/2 eta lines per tile; XGEN_DELTA / XGEN_ETA:
+                           // W lines of one field (two launches; see xgen_split)
 };
+enum { XGEN_BOTH = 0, XGEN_DELTA = 1, XGEN_ETA = 2 };
 
 // smem: s[n*W] | tw[n] | kx[n] | ix[n] | kzt[nzh]
 template <class C>
 __global__ void __launch_bounds__(C::T, 1) xgen_kernel(const XGenArgs a) {
-    constexpr int W = C::W, WC = W / 2, NP = WC / 2, T = C::T;
+    constexpr int W = C::W, T = C::T;
+    const int WC = a.fields == XGEN_BOTH ? W / 2 : W;   // k_z columns per tile
+    const int NP = WC / 2;
     extern __shared__ float2 smem[];
     const int n = a.pl.n;  // == nx
     float2* s = smem;
@@ -372,11 +377,17 @@ __global__ void __launch_bounds__(C::T, 1) xgen_kernel(const XGenArgs a) {
                         sc = sqrtf(__fdividef(amp * k, den * den) * a.inv_vcell);
                     }
                     d = cscale(X, sc);
-                    const float kk1 = (kk == 0.0f) ? 1.0f : kk;
-                    et = cscale(d, __fdividef(eta_num(a.eta_comp, kxv, ky, kz_), kk1));
+                    if (a.fields != XGEN_DELTA) {
+                        const float kk1 = (kk == 0.0f) ? 1.0f : kk;
+                        et = cscale(d, __fdividef(eta_num(a.eta_comp, kxv, ky, kz_), kk1));
+                    }
                 }
-                s[e * W + c0 + h] = d;
-                s[e * W + WC + c0 + h] = et;
+                if (a.fields == XGEN_BOTH) {
+                    s[e * W + c0 + h] = d;
+                    s[e * W + WC + c0 + h] = et;
+                } else {
+                    s[e * W + c0 + h] = a.fields == XGEN_DELTA ? d : et;
+                }
             }
         }
         __syncthreads();
@@ -385,9 +396,9 @@ __global__ void __launch_bounds__(C::T, 1) xgen_kernel(const XGenArgs a) {
         const int64_t off = b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)cb * WC;
         for (int idx = threadIdx.x; idx < n * W; idx += T) {
             const int e = idx / W, l = idx % W;
-            const int c = l % WC;
+            const int c = l < WC ? l : l - WC;
             if (c < cols) {
-                float2* dst = l < WC ? a.A : a.B;
+                float2* dst = a.fields == XGEN_BOTH ? (l < WC ? a.A : a.B) : (a.fields == XGEN_DELTA ? a.A : a.B);
                 if (dst) dst[off + e * estride + c] = s[idx];
             }
         }
@@ -603,7 +614,7 @@ static int launch_xgen(const XGenArgs& a, cudaStream_t st) {
     if (!plan_fits(a.pl, fft_max_radix(C::T))) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xgen_kernel");
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 +
                         (size_t)a.nzh * 4 + 16;
-    const int64_t ntiles = (int64_t)a.batch * a.ny * ceil_div(a.nzh, C::W / 2);
+    const int64_t ntiles = (int64_t)a.batch * a.ny * ceil_div(a.nzh, a.fields == XGEN_BOTH ? C::W / 2 : C::W);
     int grid = 0, rc;
     if ((rc = persistent_grid(xgen_kernel<C>, C::T, smem, ntiles, &grid))) return rc;
     xgen_kernel<C><<<grid, C::T, smem, st>>>(a);
