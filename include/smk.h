@@ -127,9 +127,10 @@ int smk_tune_set(int32_t pass, int32_t n, int32_t variant);
 int smk_tune_get(int32_t pass, int32_t n);
 /* GPU-noise x pass: write delta and eta in one launch (mode 0), in two launches of one field
  * each (1), or by footprint (-1, the default: two launches when the delta + eta boxes span
- * more than 64 GiB, where one launch's spread of rows outruns address translation).  Returns
- * the previous mode.  No reference counterpart (a tuning knob of this library). */
-int smk_tune_xgen_split(int32_t mode);
+ * more than 64 GiB, where one launch's spread of rows outruns address translation).  The
+ * previous mode goes to *previous (if not null).  No reference counterpart (a tuning knob of
+ * this library). */
+int smk_tune_xgen_split(int32_t mode, int32_t* previous);
 
 /* ---------------------------------------------------------------- skewers (make_spectra +
  *                                                                   merge_spectra) */

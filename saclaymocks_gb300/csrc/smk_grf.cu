@@ -311,9 +311,11 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
     return mark(5);
 }
 
-int smk_tune_xgen_split(int32_t mode) {
+int smk_tune_xgen_split(int32_t mode, int32_t* previous) {
     if (mode < -1 || mode > 1) return fail(SMK_EINVAL, "smk_tune_xgen_split: mode must be -1, 0 or 1");
-    return g_xgen_split.exchange(mode);
+    const int old = g_xgen_split.exchange(mode);
+    if (previous) *previous = old;
+    return SMK_OK;
 }
 
 int smk_tune_count(int32_t pass) { return variant_count(pass); }

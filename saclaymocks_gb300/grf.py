@@ -158,6 +158,16 @@ def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: flo
                     dcell=float(dcell))
 
 
+def grf_launches(nx: int, ny: int, nz: int, batch: int = 1, want_eta: bool = True, gpu_noise: bool = True) -> int:
+    """Kernel launches of one smk_grf_boxes call with the default split rule (GPU noise: x pass
+    once, or twice when delta + eta span more than 64 GiB; then y inverse and z inverse; host
+    noise: z forward, y forward, x, y inverse, z inverse)."""
+    if not gpu_noise:
+        return 5
+    pair = 2 * 4 * batch * nx * ny * pitch_of(nz)
+    return (2 if want_eta and pair > 64 * 2 ** 30 else 1) + 2
+
+
 def pk_normalisation(nx: int, ny: int, nz: int, dcell: float = 2.19, k0: float = 0.02) -> float:
     """A with E[var delta] = 1 for the analytic spectrum, summed on the GPU in FP64."""
     lib = _lib.load()

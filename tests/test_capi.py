@@ -99,3 +99,14 @@ def test_argument_validation_needs_no_gpu(lib):
 def test_missing_library_fails_loudly(tmp_path):
     with pytest.raises(_lib.SmkError):
         _lib.load(str(tmp_path / "libsmk.so"))
+
+
+def test_xgen_split_knob(lib):
+    """smk_tune_xgen_split is host-only state: bad modes are rejected, the previous mode comes
+    back through the out pointer."""
+    prev = C.c_int32(7)
+    assert lib.smk_tune_xgen_split(3, C.byref(prev)) == _lib.SMK_EINVAL
+    assert lib.smk_tune_xgen_split(1, C.byref(prev)) == _lib.SMK_OK
+    assert prev.value == -1
+    assert _lib.xgen_split(-1) == 1
+    assert _lib.xgen_split(-1) == -1

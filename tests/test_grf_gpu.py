@@ -236,16 +236,15 @@ def test_xgen_split_launches_equal_one_launch(G):
     """The GPU-noise x pass written as two one-field launches (the large-box form) gives the
     same boxes, bit for bit, as the one-launch form."""
     from saclaymocks_gb300 import _lib
-    lib = _lib.load()
     nx, ny, nz = 40, 24, 36
-    prev = lib.smk_tune_xgen_split(0)
+    prev = _lib.xgen_split(0)
     try:
         one = G.make_boxes(nx, ny, nz, 2.19, seed=21, batch=2)
-        lib.smk_tune_xgen_split(1)
+        _lib.xgen_split(1)
         two = G.make_boxes(nx, ny, nz, 2.19, seed=21, batch=2)
         torch.cuda.synchronize()
     finally:
-        lib.smk_tune_xgen_split(prev)
+        _lib.xgen_split(prev)
     assert torch.equal(one.delta, two.delta)
     assert torch.equal(one.eta, two.eta)
     delta_only = G.make_boxes(nx, ny, nz, 2.19, seed=21, batch=2, want_eta=False)
