@@ -93,17 +93,20 @@ enum : uint32_t { STREAM_KMODE = 0x4Bu, STREAM_SKEWER = 0x53u };
 
 // Four N(0,1) deviates from one Philox block: Box-Muller on (u0,u1) and (u2,u3) with
 // u = ((x >> 8) + 1) * 2^-24 in (0, 1] for the radius and (x >> 8) * 2^-23 in [0, 2)
-// as the angle in units of pi (both exact in float32).
+// as the angle in units of pi (both exact in float32).  The angle is evaluated as
+// pi (t - 1) in [-pi, pi) with the hardware sine/cosine (absolute error < 4e-7 there) and
+// the signs flipped back; the radius uses the reciprocal square root.
 __device__ __forceinline__ void gauss4(u32x4 r, float g[4]) {
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const float u1 = (float)((r.v[2 * h] >> 8) + 1u) * 5.9604644775390625e-08f;  // 2^-24
         const float t = (float)(r.v[2 * h + 1] >> 8) * 1.1920928955078125e-07f;       // 2^-23
-        const float rad = sqrtf(-2.0f * logf(u1));
+        const float x = -2.0f * logf(u1);
+        const float rad = x > 0.0f ? x * rsqrtf(x) : 0.0f;
         float s, c;
-        sincospif(t, &s, &c);
-        g[2 * h] = rad * c;
-        g[2 * h + 1] = rad * s;
+        __sincosf(fmaf(t, 3.14159265358979f, -3.14159265358979f), &s, &c);
+        g[2 * h] = -rad * c;
+        g[2 * h + 1] = -rad * s;
     }
 }
 

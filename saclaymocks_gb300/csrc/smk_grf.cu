@@ -48,7 +48,7 @@ int sm_count() {
 }
 
 // ------------------------------------------------------------------ tile-variant tables
-#define X(W, T, N) {W, T, N},
+#define X(W, T, N, R, B) {W, T, N, R, B},
 static const TileVariant kZVar[] = {SMK_Z_VARIANTS(X)};
 static const TileVariant kLineVar[] = {SMK_LINE_VARIANTS(X)};
 static const TileVariant kXVar[] = {SMK_X_VARIANTS(X)};
@@ -176,7 +176,7 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
     const int pass_x = gpu_noise ? PASS_XGEN : PASS_XPASS;
     const int vx = variant_for(pass_x, p->nx), vy = variant_for(PASS_LINE, p->ny);
     const int vzf = variant_for(PASS_ZFWD, p->nz), vzi = variant_for(PASS_ZINV, p->nz);
-    auto rmax = [](int pass, int v) { return fft_max_radix(variant_table(pass)[v].t); };
+    auto rmax = [](int pass, int v) { return variant_table(pass)[v].rmax; };
     FftPlan plx, ply, plzf, plzi;
     if (!make_plan(p->nx, &plx, rmax(pass_x, vx)) || !make_plan(p->ny, &ply, rmax(PASS_LINE, vy)) ||
         !make_plan(p->nz, &plzf, rmax(PASS_ZFWD, vzf)) || !make_plan(p->nz, &plzi, rmax(PASS_ZINV, vzi)))

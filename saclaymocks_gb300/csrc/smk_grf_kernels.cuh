@@ -20,9 +20,11 @@
 
 namespace smk {
 
-template <int W_, int T_>
+// W lines (or row pairs) per tile, T threads, largest FFT radix R in registers, at least B
+// resident blocks per SM requested from the register allocator.
+template <int W_, int T_, int R_ = fft_max_radix(T_), int B_ = 1>
 struct TileCfg {
-    static constexpr int W = W_, T = T_;
+    static constexpr int W = W_, T = T_, RMAX = R_, MINB = B_;
 };
 
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
@@ -71,7 +73,7 @@ struct ZFwdArgs {
 // r2c along z of the caller's white noise (two rows per complex line).
 // smem: s[n*SN] | tw[n] | sof[n] (slot of each frequency)
 template <class C>
-__global__ void __launch_bounds__(C::T, 1) zfwd_kernel(const ZFwdArgs a) {
+__global__ void __launch_bounds__(C::T, C::MINB) zfwd_kernel(const ZFwdArgs a) {
     constexpr int W = C::W, SN = W + 1, T = C::T;
     extern __shared__ float2 smem[];
     const int n = a.pl.n;
@@ -99,7 +101,7 @@ __global__ void __launch_bounds__(C::T, 1) zfwd_kernel(const ZFwdArgs a) {
         }
         cp_async_wait_all();
         __syncthreads();
-        fft_tile<false, W, SN, T>(s, tw, a.pl);
+        fft_tile<false, W, SN, T, C::RMAX>(s, tw, a.pl);
         // split the two real transforms packed as re/im and store the half spectra
         for (int idx = threadIdx.x; idx < W * nh; idx += T) {
             const int k = idx / W, w = idx % W;
@@ -126,7 +128,7 @@ struct LineArgs {
 // Forward: natural -> digit-reversed order along the axis (kept in HBM); inverse: back.
 // smem: s[n*W] | tw[n]
 template <class C, bool INV>
-__global__ void __launch_bounds__(C::T, 1) line_kernel(const LineArgs a) {
+__global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const LineArgs a) {
     constexpr int W = C::W, T = C::T;
     extern __shared__ float2 smem[];
     const int n = a.pl.n;
@@ -146,7 +148,7 @@ __global__ void __launch_bounds__(C::T, 1) line_kernel(const LineArgs a) {
         load_cols_async<W, T>(s, base, n, a.estride, cols);
         cp_async_wait_all();
         __syncthreads();
-        fft_tile<INV, W, W, T>(s, tw, a.pl);
+        fft_tile<INV, W, W, T, C::RMAX>(s, tw, a.pl);
         store_cols<W, T>(s, base, n, a.estride, cols);
         __syncthreads();
     }
@@ -190,7 +192,7 @@ __device__ __forceinline__ float kaxis(int i, int n, double kfac, bool full) {
 // smem: s[n*W] | tw[n] | kx[n] (k_x of each slot) | ix[n] (frequency index of each slot) |
 //       kt[W+1] (k_y of the tile, k_z of its columns)
 template <class C>
-__global__ void __launch_bounds__(C::T, 1) xpass_kernel(const XArgs a) {
+__global__ void __launch_bounds__(C::T, C::MINB) xpass_kernel(const XArgs a) {
     constexpr int W = C::W, T = C::T;
     extern __shared__ float2 smem[];
     const int n = a.pl.n;  // == nx
@@ -225,7 +227,7 @@ __global__ void __launch_bounds__(C::T, 1) xpass_kernel(const XArgs a) {
         if (threadIdx.x < W) kt[1 + threadIdx.x] = kaxis(cb * W + threadIdx.x, 2 * (a.nzh - 1), a.kfac, false);
         cp_async_wait_all();
         __syncthreads();
-        fft_tile<false, W, W, T>(s, tw, a.pl);
+        fft_tile<false, W, W, T, C::RMAX>(s, tw, a.pl);
         const float ky = kt[0];
         for (int idx = threadIdx.x; idx < n * W; idx += T) {
             const int e = idx / W, w = idx % W;
@@ -249,7 +251,7 @@ __global__ void __launch_bounds__(C::T, 1) xpass_kernel(const XArgs a) {
             }
         }
         __syncthreads();
-        fft_tile<true, W, W, T>(s, tw, a.pl);
+        fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
         store_cols<W, T>(s, pa, n, estride, cols);
         __syncthreads();
         if (pb) {
@@ -259,7 +261,7 @@ __global__ void __launch_bounds__(C::T, 1) xpass_kernel(const XArgs a) {
                 s[idx] = w < cols ? __ldcg(pb + e * estride + w) : make_float2(0.f, 0.f);
             }
             __syncthreads();
-            fft_tile<true, W, W, T>(s, tw, a.pl);
+            fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
             store_cols<W, T>(s, pb, n, estride, cols);
             __syncthreads();
         }
@@ -294,11 +296,13 @@ struct XGenArgs {
 enum { XGEN_BOTH = 0, XGEN_DELTA = 1, XGEN_ETA = 2 };
 
 // smem: s[n*W] | tw[n] | kx[n] | ix[n] | kzt[nzh]
-template <class C>
-__global__ void __launch_bounds__(C::T, 1) xgen_kernel(const XGenArgs a) {
+// ONE: one field per launch (a.fields = XGEN_DELTA or XGEN_ETA, W columns per tile), else
+// XGEN_BOTH (W/2 columns, each drawn once for both fields).
+template <class C, bool ONE>
+__global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
     constexpr int W = C::W, T = C::T;
-    const int WC = a.fields == XGEN_BOTH ? W / 2 : W;   // k_z columns per tile
-    const int NP = WC / 2;
+    constexpr int WC = ONE ? W : W / 2;   // k_z columns per tile
+    constexpr int NP = WC / 2;
     extern __shared__ float2 smem[];
     const int n = a.pl.n;  // == nx
     float2* s = smem;
@@ -371,18 +375,20 @@ __global__ void __launch_bounds__(C::T, 1) xgen_kernel(const XGenArgs a) {
                     if (a.pk_mode == SMK_PK_GRID) {
                         sc = __ldg(a.grid + ((int64_t)ixe * a.ny + iy) * a.nzh + kz);
                     } else {
-                        const float k = __fsqrt_rn(kk);
+                        // GPU noise has no bit-level reference: approximate square roots
+                        const float k = kk > 0.0f ? kk * rsqrtf(kk) : 0.0f;
                         const float kr = k * a.inv_k0;
                         const float den = fmaf(kr, kr, 1.0f);
-                        sc = sqrtf(__fdividef(amp * k, den * den) * a.inv_vcell);
+                        const float p = __fdividef(amp * k, den * den) * a.inv_vcell;
+                        sc = p > 0.0f ? p * rsqrtf(p) : 0.0f;
                     }
                     d = cscale(X, sc);
-                    if (a.fields != XGEN_DELTA) {
+                    if (!ONE || a.fields == XGEN_ETA) {
                         const float kk1 = (kk == 0.0f) ? 1.0f : kk;
                         et = cscale(d, __fdividef(eta_num(a.eta_comp, kxv, ky, kz_), kk1));
                     }
                 }
-                if (a.fields == XGEN_BOTH) {
+                if (!ONE) {
                     s[e * W + c0 + h] = d;
                     s[e * W + WC + c0 + h] = et;
                 } else {
@@ -391,14 +397,14 @@ __global__ void __launch_bounds__(C::T, 1) xgen_kernel(const XGenArgs a) {
             }
         }
         __syncthreads();
-        fft_tile<true, W, W, T>(s, tw, a.pl);
+        fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
         const int cols = min(WC, a.nzh - cb * WC);
         const int64_t off = b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)cb * WC;
         for (int idx = threadIdx.x; idx < n * W; idx += T) {
             const int e = idx / W, l = idx % W;
             const int c = l < WC ? l : l - WC;
             if (c < cols) {
-                float2* dst = a.fields == XGEN_BOTH ? (l < WC ? a.A : a.B) : (a.fields == XGEN_DELTA ? a.A : a.B);
+                float2* dst = !ONE ? (l < WC ? a.A : a.B) : (a.fields == XGEN_DELTA ? a.A : a.B);
                 if (dst) dst[off + e * estride + c] = s[idx];
             }
         }
@@ -450,7 +456,7 @@ __device__ __forceinline__ void flush_stats(double s1, double s2, double bad, do
 
 // smem: s[n*SN] | tw[n] | sof[n] | red[3*T/32] (doubles)
 template <class C>
-__global__ void __launch_bounds__(C::T, 1) zinv_kernel(const ZInvArgs a) {
+__global__ void __launch_bounds__(C::T, C::MINB) zinv_kernel(const ZInvArgs a) {
     constexpr int W = C::W, SN = W + 1, T = C::T;
     extern __shared__ float2 smem[];
     const int n = a.pl.n;
@@ -509,7 +515,7 @@ __global__ void __launch_bounds__(C::T, 1) zinv_kernel(const ZInvArgs a) {
             s[i2] = make_float2(x1.x + x2.y, x2.x - x1.y);   // Z_{n-k} = X1_k* + i X2_k*
         }
         __syncthreads();
-        fft_tile<true, W, SN, T>(s, tw, a.pl);
+        fft_tile<true, W, SN, T, C::RMAX>(s, tw, a.pl);
         float p1 = 0.f, p2 = 0.f, pb = 0.f;
         float* out = a.buf[buf] + grow0 * a.pitch;
         for (int rl = 0; rl < rows_here; ++rl) {
@@ -560,7 +566,7 @@ static size_t zpass_smem(int n) {
 
 template <class C>
 static int launch_zfwd(ZFwdArgs a, int64_t rows_per_box, cudaStream_t st) {
-    if (!plan_fits(a.pl, fft_max_radix(C::T))) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "zfwd_kernel");
+    if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "zfwd_kernel");
     a.zt.init(rows_per_box, C::W);
     const size_t smem = zpass_smem<C>(a.pl.n);
     const int64_t ntiles = a.zt.tiles_per_box * a.batch;
@@ -572,7 +578,7 @@ static int launch_zfwd(ZFwdArgs a, int64_t rows_per_box, cudaStream_t st) {
 
 template <class C>
 static int launch_zinv(ZInvArgs a, int64_t rows_per_box, cudaStream_t st) {
-    if (!plan_fits(a.pl, fft_max_radix(C::T))) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "zinv_kernel");
+    if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "zinv_kernel");
     a.zt.init(rows_per_box, C::W);
     const size_t smem = zpass_smem<C>(a.pl.n);
     const int64_t ntiles = a.zt.tiles_per_box * a.batch * a.nbuf;
@@ -584,7 +590,7 @@ static int launch_zinv(ZInvArgs a, int64_t rows_per_box, cudaStream_t st) {
 
 template <class C>
 static int launch_line(const LineArgs& a, bool inv, cudaStream_t st) {
-    if (!plan_fits(a.pl, fft_max_radix(C::T))) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "line_kernel");
+    if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "line_kernel");
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2);
     const int64_t ntiles = a.n_outer * ceil_div(a.ncol, C::W) * a.nbuf;
     int grid = 0, rc;
@@ -600,7 +606,7 @@ static int launch_line(const LineArgs& a, bool inv, cudaStream_t st) {
 
 template <class C>
 static int launch_xpass(const XArgs& a, cudaStream_t st) {
-    if (!plan_fits(a.pl, fft_max_radix(C::T))) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xpass_kernel");
+    if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xpass_kernel");
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 + (C::W + 1) * 4;
     const int64_t ntiles = (int64_t)a.batch * a.ny * ceil_div(a.nzh, C::W);
     int grid = 0, rc;
@@ -611,32 +617,41 @@ static int launch_xpass(const XArgs& a, cudaStream_t st) {
 
 template <class C>
 static int launch_xgen(const XGenArgs& a, cudaStream_t st) {
-    if (!plan_fits(a.pl, fft_max_radix(C::T))) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xgen_kernel");
+    if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xgen_kernel");
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 +
                         (size_t)a.nzh * 4 + 16;
-    const int64_t ntiles = (int64_t)a.batch * a.ny * ceil_div(a.nzh, a.fields == XGEN_BOTH ? C::W / 2 : C::W);
+    const bool one = a.fields != XGEN_BOTH;
+    const int64_t ntiles = (int64_t)a.batch * a.ny * ceil_div(a.nzh, one ? C::W : C::W / 2);
     int grid = 0, rc;
-    if ((rc = persistent_grid(xgen_kernel<C>, C::T, smem, ntiles, &grid))) return rc;
-    xgen_kernel<C><<<grid, C::T, smem, st>>>(a);
+    if (one) {
+        if ((rc = persistent_grid(xgen_kernel<C, true>, C::T, smem, ntiles, &grid))) return rc;
+        xgen_kernel<C, true><<<grid, C::T, smem, st>>>(a);
+    } else {
+        if ((rc = persistent_grid(xgen_kernel<C, false>, C::T, smem, ntiles, &grid))) return rc;
+        xgen_kernel<C, false><<<grid, C::T, smem, st>>>(a);
+    }
     return check_launch("xgen_kernel");
 }
 
 // ------------------------------------------------------------------ tile variants
 struct TileVariant {
     int w, t, nmax;  // columns (line pairs for z passes, lines for xgen) per tile, threads, max length
+    int rmax, minb;  // largest FFT radix, requested resident blocks per SM
 };
 // z passes (zfwd, zinv): W = row pairs per tile
-#define SMK_Z_VARIANTS(X) X(16, 256, 512) X(8, 256, 512) X(16, 512, 1024) X(8, 512, 1024) \
-    X(8, 512, 2560) X(4, 512, 2560) X(8, 1024, 2560) X(4, 256, 2560) X(4, 512, 4096) X(2, 512, 4096) \
-    X(8, 256, 2560)
+#define SMK_Z_VARIANTS(X) X(16, 256, 512, 32, 1) X(8, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 1024, 16, 1) \
+    X(8, 512, 2560, 16, 1) X(4, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) X(4, 256, 2560, 32, 1) X(4, 512, 4096, 16, 1) X(2, 512, 4096, 16, 1) \
+    X(8, 256, 2560, 32, 1) X(2, 128, 2560, 16, 4) X(4, 128, 2560, 16, 2) X(4, 256, 2560, 16, 2) \
+    X(2, 256, 4096, 16, 2)
 // y pass (line): W = columns per tile
-#define SMK_LINE_VARIANTS(X) X(16, 256, 512) X(32, 256, 512) X(16, 512, 1024) X(16, 1024, 1024) \
-    X(8, 512, 2560) X(8, 1024, 2560) X(4, 512, 4096) X(4, 1024, 4096) X(8, 256, 2560)
+#define SMK_LINE_VARIANTS(X) X(16, 256, 512, 32, 1) X(32, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(16, 1024, 1024, 8, 1) \
+    X(8, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1) X(4, 1024, 4096, 8, 1) X(8, 256, 2560, 32, 1) \
+    X(4, 128, 2560, 16, 2) X(4, 256, 2560, 16, 2) X(8, 256, 2560, 16, 1)
 // x pass of host noise: W = columns per tile
-#define SMK_X_VARIANTS(X) X(16, 256, 512) X(16, 512, 1024) X(8, 512, 2560) X(4, 512, 4096)
+#define SMK_X_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(4, 512, 4096, 16, 1)
 // x pass of GPU noise: W = lines per tile (W/2 delta columns + W/2 eta columns)
-#define SMK_XGEN_VARIANTS(X) X(32, 256, 512) X(16, 256, 512) X(16, 512, 1024) X(16, 1024, 1024) \
-    X(8, 512, 2560) X(8, 1024, 2560) X(4, 512, 4096) X(4, 1024, 4096) X(8, 256, 2560)
+#define SMK_XGEN_VARIANTS(X) X(32, 256, 512, 32, 1) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(16, 1024, 1024, 8, 1) \
+    X(8, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1) X(4, 1024, 4096, 8, 1) X(8, 256, 2560, 32, 1)
 
 enum { PASS_ZFWD = 0, PASS_LINE = 1, PASS_XPASS = 2, PASS_XGEN = 3, PASS_ZINV = 4, NPASS = 5 };
 

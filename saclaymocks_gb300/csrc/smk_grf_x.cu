@@ -5,8 +5,8 @@ namespace smk {
 
 int run_xpass(int v, const XArgs& a, cudaStream_t st) {
     int i = 0;
-#define X(W, T, N) \
-    if (v == i++) return launch_xpass<TileCfg<W, T>>(a, st);
+#define X(W, T, N, R, B) \
+    if (v == i++) return launch_xpass<TileCfg<W, T, R, B>>(a, st);
     SMK_X_VARIANTS(X)
 #undef X
     return fail(SMK_EINVAL, "xpass: no tile variant %d", v);
@@ -14,8 +14,8 @@ int run_xpass(int v, const XArgs& a, cudaStream_t st) {
 
 int run_xgen(int v, const XGenArgs& a, cudaStream_t st) {
     int i = 0;
-#define X(W, T, N) \
-    if (v == i++) return launch_xgen<TileCfg<W, T>>(a, st);
+#define X(W, T, N, R, B) \
+    if (v == i++) return launch_xgen<TileCfg<W, T, R, B>>(a, st);
     SMK_XGEN_VARIANTS(X)
 #undef X
     return fail(SMK_EINVAL, "xgen: no tile variant %d", v);
