@@ -605,6 +605,9 @@ def run_grf_only(args, shape):
     if args.xgen_split is not None:
         from saclaymocks_gb300 import _lib
         _lib.xgen_split(args.xgen_split)
+    if args.no_prefetch:
+        from saclaymocks_gb300 import _lib
+        _lib.tune_flag(_lib.SMK_TUNE_PREFETCH, 0)
     boxes = grf.alloc_boxes(nx, ny, nz, want_eta=want_eta)
     ws = grf.GrfWorkspace(1)
     amp = grf.pk_normalisation(nx, ny, nz)
@@ -642,6 +645,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="built-in tile variants, no autotuning")
     ap.add_argument("--no-batching", action="store_true", help="skip the batched / graph-replay leg")
     ap.add_argument("--no-eta", action="store_true", help="--grf-shape: delta box only")
+    ap.add_argument("--no-prefetch", action="store_true", help="--grf-shape: no L2 prefetch of the next tile")
     ap.add_argument("--xgen-split", type=int, default=None, choices=[-1, 0, 1],
                     help="--grf-shape: x pass as one launch (0), two one-field launches (1), by footprint (-1)")
     ap.add_argument("--precision", default=None, const="1536,100000,1024", nargs="?",

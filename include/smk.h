@@ -125,12 +125,17 @@ int smk_tune_count(int32_t pass);
 int smk_tune_info(int32_t pass, int32_t variant, int32_t* w, int32_t* threads, int32_t* n_max);
 int smk_tune_set(int32_t pass, int32_t n, int32_t variant);
 int smk_tune_get(int32_t pass, int32_t n);
-/* GPU-noise x pass: write delta and eta in one launch (mode 0), in two launches of one field
- * each (1), or by footprint (-1, the default: two launches when the delta + eta boxes span
- * more than 64 GiB, where one launch's spread of rows outruns address translation).  The
- * previous mode goes to *previous (if not null).  No reference counterpart (a tuning knob of
- * this library). */
-int smk_tune_xgen_split(int32_t mode, int32_t* previous);
+/* Process-wide switches of smk_grf_boxes (no reference counterpart; tuning knobs of this
+ * library).  The previous value goes to *previous (if not null).
+ *   SMK_TUNE_XGEN_SPLIT: GPU-noise x pass writing delta and eta in one launch (0), in two
+ *     launches of one field each (1), or by footprint (-1, default: two launches when the
+ *     delta + eta boxes span more than 64 GiB, where one launch's spread of rows outruns
+ *     address translation);
+ *   SMK_TUNE_PREFETCH: the y and z passes pull their next tile into L2 while transforming the
+ *     current one (1, default) or not (0). */
+#define SMK_TUNE_XGEN_SPLIT 0
+#define SMK_TUNE_PREFETCH 1
+int smk_tune_flag(int32_t flag, int32_t value, int32_t* previous);
 
 /* ---------------------------------------------------------------- skewers (make_spectra +
  *                                                                   merge_spectra) */

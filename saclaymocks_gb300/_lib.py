@@ -89,7 +89,7 @@ _SIGS = [
                                 C.POINTER(C.c_int32)]),
     ("smk_tune_set", C.c_int, [C.c_int32, C.c_int32, C.c_int32]),
     ("smk_tune_get", C.c_int, [C.c_int32, C.c_int32]),
-    ("smk_tune_xgen_split", C.c_int, [C.c_int32, C.c_void_p]),
+    ("smk_tune_flag", C.c_int, [C.c_int32, C.c_int32, C.c_void_p]),
     ("smk_skewer_schedule", C.c_int, [C.c_int64, C.c_void_p, C.c_int32, C.c_void_p,
                                       C.POINTER(C.c_int64)]),
     ("smk_skewers_workspace_size", C.c_size_t, [C.POINTER(SmkSkewers), C.POINTER(SmkSpectraParams)]),
@@ -141,12 +141,19 @@ def load(path: str | None = None):
     return lib
 
 
-def xgen_split(mode: int) -> int:
-    """smk_tune_xgen_split: set the x-pass launch mode (-1 by footprint, 0 one launch, 1 two
-    launches); returns the previous mode."""
+SMK_TUNE_XGEN_SPLIT, SMK_TUNE_PREFETCH = 0, 1
+
+
+def tune_flag(flag: int, value: int) -> int:
+    """smk_tune_flag: set a process-wide switch; returns its previous value."""
     prev = C.c_int32(0)
-    check(load().smk_tune_xgen_split(int(mode), C.byref(prev)), "smk_tune_xgen_split")
+    check(load().smk_tune_flag(int(flag), int(value), C.byref(prev)), "smk_tune_flag")
     return prev.value
+
+
+def xgen_split(mode: int) -> int:
+    """x-pass launch mode (-1 by footprint, 0 one launch, 1 two launches); returns the previous."""
+    return tune_flag(SMK_TUNE_XGEN_SPLIT, mode)
 
 
 def check(status: int, what: str = ""):

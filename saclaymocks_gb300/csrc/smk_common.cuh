@@ -61,6 +61,15 @@ __device__ __forceinline__ void cp_async(void* smem_dst, const void* gmem_src, i
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Hints that pull the next tile's bytes into L2 while the current tile is transformed: one
+// cache line, or a 16-byte-aligned run of bytes (a multiple of 16) with the bulk form.
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+    asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));
+}
+__device__ __forceinline__ void prefetch_l2_bulk(const void* p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(p), "r"(bytes) : "memory");
+}
+
 // ------------------------------------------------------------------ Philox4x32-10
 // Counter-based generator of Salmon, Moraes, Dror & Shaw, "Parallel random numbers: as
 // easy as 1, 2, 3" (SC'11): 10 rounds of the 4x32 Philox bijection keyed by the seed.

@@ -64,6 +64,7 @@ static struct ChoiceInit {
 } g_choice_init;
 
 static std::atomic<int> g_xgen_split{-1};  // -1: by footprint, 0: never, 1: always
+static std::atomic<int> g_prefetch{1};     // L2 prefetch of the next tile in the y and z passes
 
 static int length_class(int n) { return n <= 512 ? 0 : n <= 1024 ? 1 : n <= 2560 ? 2 : 3; }
 
@@ -214,6 +215,7 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
     ya.ostride = (int64_t)p->ny * cp;
     ya.estride = cp;
     ya.ncol = nzh;
+    ya.prefetch = g_prefetch.load();
     const int64_t rows_per_box = (int64_t)p->nx * p->ny;
     const float inv_vcell = 1.0f / (float)(p->dcell * p->dcell * p->dcell);
     if (gpu_noise) {
@@ -307,13 +309,22 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
     ia.pitch = pitch;
     ia.scale = (float)(1.0 / ((double)p->nx * p->ny * p->nz));
     ia.stats = stats;
+    ia.prefetch = g_prefetch.load();
     if ((rc = run_zinv(vzi, ia, rows_per_box, st))) return rc;
     return mark(5);
 }
 
-int smk_tune_xgen_split(int32_t mode, int32_t* previous) {
-    if (mode < -1 || mode > 1) return fail(SMK_EINVAL, "smk_tune_xgen_split: mode must be -1, 0 or 1");
-    const int old = g_xgen_split.exchange(mode);
+int smk_tune_flag(int32_t flag, int32_t value, int32_t* previous) {
+    int old;
+    if (flag == SMK_TUNE_XGEN_SPLIT) {
+        if (value < -1 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: XGEN_SPLIT must be -1, 0 or 1");
+        old = g_xgen_split.exchange(value);
+    } else if (flag == SMK_TUNE_PREFETCH) {
+        if (value < 0 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: PREFETCH must be 0 or 1");
+        old = g_prefetch.exchange(value);
+    } else {
+        return fail(SMK_EINVAL, "smk_tune_flag: unknown flag %d", flag);
+    }
     if (previous) *previous = old;
     return SMK_OK;
 }

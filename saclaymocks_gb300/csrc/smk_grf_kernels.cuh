@@ -123,6 +123,7 @@ struct LineArgs {
     int nbuf;
     int64_t n_outer, ostride, estride;
     int ncol;
+    int prefetch;   // pull the next tile into L2 during the transform
 };
 
 // Forward: natural -> digit-reversed order along the axis (kept in HBM); inverse: back.
@@ -148,6 +149,15 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const LineArgs a) {
         load_cols_async<W, T>(s, base, n, a.estride, cols);
         cp_async_wait_all();
         __syncthreads();
+        if (a.prefetch && tile + gridDim.x < ntiles) {
+            // the next tile of this block: one line per row segment of its W columns
+            const int64_t tn = tile + gridDim.x;
+            const int bn = (int)(tn / tpb);
+            const int64_t un = tn - bn * tpb;
+            const int64_t on = un / ncolt;
+            const float2* nb = a.base[bn] + on * a.ostride + (un - on * ncolt) * W;
+            for (int e = threadIdx.x; e < n; e += T) prefetch_l2(nb + (int64_t)e * a.estride);
+        }
         fft_tile<INV, W, W, T, C::RMAX>(s, tw, a.pl);
         store_cols<W, T>(s, base, n, a.estride, cols);
         __syncthreads();
@@ -422,6 +432,7 @@ struct ZInvArgs {
     int64_t pitch;
     float scale;
     double* stats;  // [batch][2][4] or null
+    int prefetch;   // pull the next tile into L2 during the transform
 };
 
 template <int T>
@@ -491,44 +502,76 @@ __global__ void __launch_bounds__(C::T, C::MINB) zinv_kernel(const ZInvArgs a) {
             cur = key;
         }
         const float2* in2 = reinterpret_cast<const float2*>(a.buf[buf]) + grow0 * cp;
-        // X1_k (even row) to the slot of frequency k, X2_k (odd row) to the slot of n-k;
-        // DC and Nyquist keep their real parts (re: X1, im: X2).  Rows are the fast index of
-        // the thread mapping so the permuted shared-memory slots are written W-contiguous.
-        for (int idx = threadIdx.x; idx < 2 * W * nh; idx += T) {
-            const int k = idx / (2 * W), rl = idx % (2 * W);
-            const int w = rl >> 1, odd = rl & 1;
-            const bool ok = rl < rows_here;
-            const float2* src = ok ? in2 + (int64_t)rl * cp + k : in2;
-            if (k == 0 || k == half) {
-                cp_async<4>(sf + 2 * (sof[k] * SN + w) + odd, src, ok ? 4 : 0);
-            } else {
-                cp_async<8>(s + sof[odd ? n - k : k] * SN + w, src, ok ? 8 : 0);
+        // Row pair w holds the half spectra X1 (even row) and X2 (odd row); the complex line
+        // Z_k = X1_k + i X2_k (k <= n/2), Z_{n-k} = X1_k* + i X2_k* goes to the slot of each
+        // frequency (DC and Nyquist: real parts, re from X1, im from X2).  The pair index is
+        // the fast index of the thread mapping: a warp reads W rows x (32/W) consecutive k
+        // (whole 32-byte sectors) and writes W-contiguous slots.  Four items per thread are
+        // loaded before any is used.
+        constexpr int U = 4;
+        const int items = W * nh;
+        for (int base = threadIdx.x; base < items; base += U * T) {
+            float2 x1[U], x2[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int idx = base + u * T;
+                const int w = idx % W, k = idx / W;
+                x1[u] = x2[u] = make_float2(0.f, 0.f);
+                if (idx < items) {
+                    if (2 * w < rows_here) x1[u] = __ldcs(in2 + (int64_t)(2 * w) * cp + k);
+                    if (2 * w + 1 < rows_here) x2[u] = __ldcs(in2 + (int64_t)(2 * w + 1) * cp + k);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int idx = base + u * T;
+                if (idx >= items) break;
+                const int w = idx % W, k = idx / W;
+                if (k == 0 || k == half) {
+                    s[sof[k] * SN + w] = make_float2(x1[u].x, x2[u].x);
+                } else {
+                    s[sof[k] * SN + w] = make_float2(x1[u].x - x2[u].y, x1[u].y + x2[u].x);
+                    s[sof[n - k] * SN + w] = make_float2(x1[u].x + x2[u].y, x2[u].x - x1[u].y);
+                }
             }
         }
-        cp_async_wait_all();
         __syncthreads();
-        for (int idx = threadIdx.x; idx < W * (half - 1); idx += T) {
-            const int k = 1 + idx / W, w = idx % W;
-            const int i1 = sof[k] * SN + w, i2 = sof[n - k] * SN + w;
-            const float2 x1 = s[i1], x2 = s[i2];
-            s[i1] = make_float2(x1.x - x2.y, x1.y + x2.x);   // Z_k = X1_k + i X2_k
-            s[i2] = make_float2(x1.x + x2.y, x2.x - x1.y);   // Z_{n-k} = X1_k* + i X2_k*
+        if (a.prefetch && tile + gridDim.x < ntiles && threadIdx.x < 2 * W) {
+            // the next tile of this block: its rows, one bulk prefetch per row
+            const int64_t tn = tile + gridDim.x;
+            const int bufn = (int)(tn / tpbuf);
+            const int64_t un = tn - bufn * tpbuf;
+            const int64_t bn = un / a.zt.tiles_per_box;
+            const int64_t lrn = (un - bn * a.zt.tiles_per_box) * (2 * W) + threadIdx.x;
+            if (lrn < a.zt.rows_per_box)
+                prefetch_l2_bulk(a.buf[bufn] + (bn * a.zt.rows_per_box + lrn) * a.pitch, (uint32_t)(a.pitch * 4));
         }
-        __syncthreads();
         fft_tile<true, W, SN, T, C::RMAX>(s, tw, a.pl);
+        // z_e = x1_e + i x2_e: one 8-byte shared read gives both rows' values
         float p1 = 0.f, p2 = 0.f, pb = 0.f;
         float* out = a.buf[buf] + grow0 * a.pitch;
-        for (int rl = 0; rl < rows_here; ++rl) {
-            const float* srow = sf + 2 * (rl >> 1) + (rl & 1);
-            float* orow = out + (int64_t)rl * a.pitch;
+        for (int w = 0; 2 * w < rows_here; ++w) {
+            float* r0 = out + (int64_t)(2 * w) * a.pitch;
+            float* r1 = r0 + a.pitch;
+            const bool two = 2 * w + 1 < rows_here;
             for (int e = threadIdx.x; e < n; e += T) {
-                const float v = srow[2 * e * SN] * a.scale;
-                orow[e] = v;
-                if (isfinite(v)) {
-                    p1 += v;
-                    p2 = fmaf(v, v, p2);
+                const float2 z = s[e * SN + w];
+                const float v0 = z.x * a.scale, v1 = z.y * a.scale;
+                r0[e] = v0;
+                if (isfinite(v0)) {
+                    p1 += v0;
+                    p2 = fmaf(v0, v0, p2);
                 } else {
                     pb += 1.f;
+                }
+                if (two) {
+                    r1[e] = v1;
+                    if (isfinite(v1)) {
+                        p1 += v1;
+                        p2 = fmaf(v1, v1, p2);
+                    } else {
+                        pb += 1.f;
+                    }
                 }
             }
         }

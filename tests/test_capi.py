@@ -101,12 +101,16 @@ def test_missing_library_fails_loudly(tmp_path):
         _lib.load(str(tmp_path / "libsmk.so"))
 
 
-def test_xgen_split_knob(lib):
-    """smk_tune_xgen_split is host-only state: bad modes are rejected, the previous mode comes
-    back through the out pointer."""
+def test_tune_flags(lib):
+    """smk_tune_flag is host-only state: bad flags and values are rejected, the previous value
+    comes back through the out pointer."""
     prev = C.c_int32(7)
-    assert lib.smk_tune_xgen_split(3, C.byref(prev)) == _lib.SMK_EINVAL
-    assert lib.smk_tune_xgen_split(1, C.byref(prev)) == _lib.SMK_OK
+    assert lib.smk_tune_flag(_lib.SMK_TUNE_XGEN_SPLIT, 3, C.byref(prev)) == _lib.SMK_EINVAL
+    assert lib.smk_tune_flag(9, 0, C.byref(prev)) == _lib.SMK_EINVAL
+    assert lib.smk_tune_flag(_lib.SMK_TUNE_XGEN_SPLIT, 1, C.byref(prev)) == _lib.SMK_OK
     assert prev.value == -1
     assert _lib.xgen_split(-1) == 1
     assert _lib.xgen_split(-1) == -1
+    assert _lib.tune_flag(_lib.SMK_TUNE_PREFETCH, 0) == 1
+    assert _lib.tune_flag(_lib.SMK_TUNE_PREFETCH, 1) == 0
+    assert lib.smk_tune_flag(_lib.SMK_TUNE_PREFETCH, 2, None) == _lib.SMK_EINVAL
