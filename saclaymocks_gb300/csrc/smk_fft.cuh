@@ -35,8 +35,9 @@ struct FftPlan {
     uint32_t magic[FFT_MAX_STAGES];  // floor(2^32/m) + 1: x / m == umulhi(x, magic) for x < 2^16
 };
 
-// Host: radix plan of n (16s first, one of them 32 when a single factor 2 is left, else
-// 8/4/2 for the rest of the power of two, then 3s, 5s).
+// Host: radix plan of n.  rmax >= 16: 16s first; a single factor 2 left over becomes a
+// radix-32 stage (rmax >= 32), else joins a 5 (radix 10) or a 3 (radix 6), else stays a 2;
+// rmax 8: 8s, then 4s / 2.  3s and 5s follow.
 // Returns false unless 2 <= n <= FFT_MAX_N and n = 2^a 3^b 5^c.
 bool make_plan(int n, FftPlan* p, int rmax = 16);
 
@@ -236,6 +237,8 @@ __host__ __device__ __forceinline__ float2 ctw(float2 v) {
 
 template <int R>
 struct DftSplit;  // R = R1 * R2 for the composite radices
+template <> struct DftSplit<6> { static constexpr int R1 = 3, R2 = 2; };
+template <> struct DftSplit<10> { static constexpr int R1 = 5, R2 = 2; };
 template <> struct DftSplit<16> { static constexpr int R1 = 4, R2 = 4; };
 template <> struct DftSplit<32> { static constexpr int R1 = 8, R2 = 4; };
 
@@ -263,6 +266,8 @@ struct DftComposite {
         });
     }
 };
+template <bool INV> struct Dft<6, INV> : DftComposite<6, INV> {};
+template <bool INV> struct Dft<10, INV> : DftComposite<10, INV> {};
 template <bool INV> struct Dft<16, INV> : DftComposite<16, INV> {};
 template <bool INV> struct Dft<32, INV> : DftComposite<32, INV> {};
 
@@ -309,6 +314,12 @@ __device__ __forceinline__ void fft_stage_any(float2* s, const float2* tw, const
             break;
         case 16:
             if constexpr (RMAX >= 16) fft_stage<16, INV, W, SN, T>(s, tw, pl, st);
+            break;
+        case 10:
+            if constexpr (RMAX >= 16) fft_stage<10, INV, W, SN, T>(s, tw, pl, st);
+            break;
+        case 6:
+            if constexpr (RMAX >= 16) fft_stage<6, INV, W, SN, T>(s, tw, pl, st);
             break;
         case 8: fft_stage<8, INV, W, SN, T>(s, tw, pl, st); break;
         case 4: fft_stage<4, INV, W, SN, T>(s, tw, pl, st); break;

@@ -685,7 +685,8 @@ struct TileVariant {
 #define SMK_Z_VARIANTS(X) X(16, 256, 512, 32, 1) X(8, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 1024, 16, 1) \
     X(8, 512, 2560, 16, 1) X(4, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) X(4, 256, 2560, 32, 1) X(4, 512, 4096, 16, 1) X(2, 512, 4096, 16, 1) \
     X(8, 256, 2560, 32, 1) X(2, 128, 2560, 16, 4) X(4, 128, 2560, 16, 2) X(4, 256, 2560, 16, 2) \
-    X(2, 256, 4096, 16, 2)
+    X(2, 256, 4096, 16, 2) X(8, 256, 2560, 16, 1) X(1, 64, 2560, 16, 6) X(2, 64, 2560, 16, 6) \
+    X(1, 128, 2560, 16, 4) X(2, 128, 2560, 32, 2)
 // y pass (line): W = columns per tile
 #define SMK_LINE_VARIANTS(X) X(16, 256, 512, 32, 1) X(32, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(16, 1024, 1024, 8, 1) \
     X(8, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1) X(4, 1024, 4096, 8, 1) X(8, 256, 2560, 32, 1) \
@@ -694,7 +695,8 @@ struct TileVariant {
 #define SMK_X_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(4, 512, 4096, 16, 1)
 // x pass of GPU noise: W = lines per tile (W/2 delta columns + W/2 eta columns)
 #define SMK_XGEN_VARIANTS(X) X(32, 256, 512, 32, 1) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(16, 1024, 1024, 8, 1) \
-    X(8, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1) X(4, 1024, 4096, 8, 1) X(8, 256, 2560, 32, 1)
+    X(8, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1) X(4, 1024, 4096, 8, 1) X(8, 256, 2560, 32, 1) \
+    X(8, 256, 2560, 16, 1)
 
 enum { PASS_ZFWD = 0, PASS_LINE = 1, PASS_XPASS = 2, PASS_XGEN = 3, PASS_ZINV = 4, NPASS = 5 };
 

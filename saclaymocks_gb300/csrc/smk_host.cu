@@ -42,6 +42,12 @@ bool make_plan(int n, FftPlan* p, int rmax) {
         while (p2 >= 4) { rad[nr++] = 16; p2 -= 4; }
         if (p2 == 1 && nr > 0 && rmax >= 32) {
             rad[0] = 32;
+        } else if (p2 == 1 && p5 > 0) {
+            rad[nr++] = 10;
+            --p5;
+        } else if (p2 == 1 && p3 > 0) {
+            rad[nr++] = 6;
+            --p3;
         } else if (p2 > 0) {
             rad[nr++] = 1 << p2;
         }
