@@ -63,6 +63,9 @@ int smk_fft_supported(int32_t n);
 #define SMK_ETA_XY 3
 #define SMK_ETA_XZ 4
 #define SMK_ETA_YZ 5
+#define SMK_ETA_VX 6 /* velocity components -i k_i / k^2 * vel_factor * delta_k           */
+#define SMK_ETA_VY 7 /* (bin/make_boxes.py:393-431; vel_factor = H0 * dD/dz at z = 0)     */
+#define SMK_ETA_VZ 8
 
 typedef struct {
     int32_t nx, ny, nz;   /* cells; nz even; every axis passes smk_fft_supported            */
@@ -79,7 +82,8 @@ typedef struct {
     int32_t want_eta;     /* 1: also produce eta_zz = irfftn(kz^2/k^2 delta_k)               */
     void* const* pass_events; /* optional cudaEvent_t[6]: recorded on the stream before the    */
     int32_t n_pass_events;    /* first HBM pass and after each of the five (0: none)          */
-    int32_t eta_comp;     /* SMK_ETA_*: which eta_ij the eta box holds (default 0 = zz)      */
+    int32_t eta_comp;     /* SMK_ETA_*: which eta_ij or velocity the eta box holds (0 = zz)  */
+    double vel_factor;    /* SMK_ETA_VX/VY/VZ: H0 * dD/dz(z = 0) (km/s/(Mpc/h) per unit z)    */
 } SmkGrfParams;
 
 /* Row pitch (floats) of the padded box layout for a z extent nz. */

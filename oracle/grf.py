@@ -78,6 +78,19 @@ def eta_factor(comp: str, kx, ky, kz):
     return ki[comp[0]] * ki[comp[1]] / kk
 
 
+VELOCITY_COMPONENTS = ("vx", "vy", "vz")
+
+
+def velocity_factor(comp: str, kx, ky, kz, H0: float, dgrowth0: float):
+    """-i k_i / k^2 * H0 * dD/dz(0) with numpy's promotion of the reference's expression
+    (bin/make_boxes.py:393-431): complex64 up to the H0 product, complex128 after the
+    float64 growth-rate scalar."""
+    kk = kx * kx + ky * ky + kz * kz
+    kk[0, 0, 0] = 1
+    ki = {"vx": kx, "vy": ky, "vz": kz}[comp]
+    return -1j * ki / kk * H0 * np.float64(dgrowth0)
+
+
 def grf_boxes(noise: np.ndarray, dcell: float, k0: float = 0.02, A: float | None = None,
               eta=("zz",), precision: str = "f32") -> dict:
     """delta and eta_ij boxes from a white-noise box.
@@ -96,12 +109,15 @@ def grf_boxes(noise: np.ndarray, dcell: float, k0: float = 0.02, A: float | None
 
 
 def grf_from_modes(nk: np.ndarray, NZ: int, dcell: float, k0: float = 0.02, A: float | None = None,
-                   eta=("zz",), precision: str = "f32") -> dict:
+                   eta=("zz",), precision: str = "f32", P0=None, velocity=None) -> dict:
     """The GRF step from the (unnormalised) Fourier transform nk [NX, NY, NZ//2+1] of the
-    white noise: everything of grf_boxes after the forward r2c."""
+    white noise: everything of grf_boxes after the forward r2c.  P0: a sqrt(P/Vcell) grid to
+    use instead of the analytic one (the lognormal boxes multiply by the Pln grids,
+    bin/make_boxes.py:241-275).  velocity: (H0, dD/dz(0)) adds vx, vy, vz."""
     NX, NY = nk.shape[:2]
     N = NX * NY * NZ
-    P0 = sqrt_pk_grid(NX, NY, NZ, dcell, k0, A)
+    if P0 is None:
+        P0 = sqrt_pk_grid(NX, NY, NZ, dcell, k0, A)
     kx, ky, kz = k_components(NX, NY, NZ, dcell)
     if precision == "f32":
         dk = nk.astype(np.complex64) * P0
@@ -121,6 +137,13 @@ def grf_from_modes(nk: np.ndarray, NZ: int, dcell: float, k0: float = 0.02, A: f
             out["eta_" + comp] = c2r((dk * f).astype(np.complex64))
         else:
             out["eta_" + comp] = c2r(dk * f.astype(np.float64))
+    if velocity is not None:
+        for comp in VELOCITY_COMPONENTS:
+            f = velocity_factor(comp, kx, ky, kz, *velocity)
+            if precision == "f32":
+                out[comp] = c2r((dk * f).astype(np.complex64))
+            else:
+                out[comp] = c2r(dk * f.astype(np.complex128))
     out["sigma"] = float(np.std(out["delta"].astype(np.float64)))
     return out
 

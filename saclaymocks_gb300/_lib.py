@@ -24,7 +24,7 @@ SMK_INTERP_TRILINEAR, SMK_INTERP_PIXELS, SMK_INTERP_GAUSS343 = 0, 1, 2
 SMK_SS_NONE, SMK_SS_HOST, SMK_SS_PHILOX = 0, 1, 2
 SMK_ABC_CONST, SMK_ABC_POWERLAW, SMK_ABC_TABLE = 0, 1, 2
 SMK_G_ONE, SMK_G_MERGE = 0, 1
-SMK_ETA = {"zz": 0, "xx": 1, "yy": 2, "xy": 3, "xz": 4, "yz": 5}
+SMK_ETA = {"zz": 0, "xx": 1, "yy": 2, "xy": 3, "xz": 4, "yz": 5, "vx": 6, "vy": 7, "vz": 8}
 SMK_PASS_ZFWD, SMK_PASS_LINE, SMK_PASS_XPASS, SMK_PASS_XGEN, SMK_PASS_ZINV = 0, 1, 2, 3, 4
 
 
@@ -41,7 +41,8 @@ class SmkGrfParams(C.Structure):
                 ("dcell", C.c_double), ("pk_mode", C.c_int32), ("k0", C.c_double),
                 ("amp", C.c_double), ("pk_grid", C.c_void_p), ("noise_mode", C.c_int32),
                 ("noise", C.c_void_p), ("seed", C.c_uint64), ("want_eta", C.c_int32),
-                ("pass_events", C.c_void_p), ("n_pass_events", C.c_int32), ("eta_comp", C.c_int32)]
+                ("pass_events", C.c_void_p), ("n_pass_events", C.c_int32), ("eta_comp", C.c_int32),
+                ("vel_factor", C.c_double)]
 
 
 class SmkSkewers(C.Structure):

@@ -1,15 +1,18 @@
-"""Drop-in for bin/make_boxes.py: GRF delta and eta_zz boxes on the GPU, written as the
-reference writes them (one x-plane per FITS file, bin/make_boxes.py:110-117).
+"""Drop-in for bin/make_boxes.py: the GRF boxes on the GPU, written as the reference writes
+them (bin/make_boxes.py:110-117, 241-431).
 
     python -m saclaymocks_gb300.bin.make_boxes -NX 256 -pixel 2.19 -seed 0 -outDir out
 
 Reference flags (bin/make_boxes.py:137-148) keep their meaning: -pixel, -NX/-NY/-NZ, -seed,
--rsd (eta_zz box when True), -outDir, -PkDir (if it holds the P-grid file of interpolate_pk,
-P0 = sqrt(P/Vcell) is read from it; otherwise the analytic spectrum A k/(1+(k/k0)^2)^2 with
-E[var delta] = 1 is used); -nHDU, -ncpu and -dgrowthfile are accepted and ignored (no
-lognormal or velocity boxes on this path).  Extra flags: --noise numpy|gpu (numpy: the
-reference's MT19937 plane-order draws, bit-identical input; gpu: Fourier modes drawn on the
-GPU), -k0, --no-write.
+-rsd, -outDir, -nHDU, -PkDir, -dgrowthfile.  Outputs: box-{i}.fits (one x plane per file);
+with a P-grid file in -PkDir holding Pln1..3, boxln_{1,2,3}-{i}.fits (nHDU files); with -rsd
+True, eta_{xx,yy,zz,xy,xz,yz}-{i}.fits (one x plane per file) and v{x,y,z}-{i}.fits (nHDU
+files, velocity factor H0 * dD/dz(z=0) from the growth-rate table of -dgrowthfile or
+$SACLAYMOCKS_BASE/etc/dgrowth.fits).  Without a P-grid file the analytic spectrum
+A k/(1+(k/k0)^2)^2 with E[var delta] = 1 is used (no lognormal boxes).  -ncpu is accepted and
+ignored.  Extra flags: --noise numpy|gpu (numpy: the reference's MT19937 plane-order draws,
+bit-identical input; gpu: Fourier modes drawn on the GPU), -k0, --eta-only-zz (write only the
+eta_zz box the trilinear skewer read uses), --no-write.
 """
 from __future__ import annotations
 
@@ -46,8 +49,18 @@ def parser():
     p.add_argument("-outDir", default=".")
     p.add_argument("-k0", type=float, default=0.02)
     p.add_argument("--noise", choices=["numpy", "gpu"], default="gpu")
+    p.add_argument("--eta-only-zz", action="store_true")
     p.add_argument("--no-write", action="store_true")
     return p
+
+
+H0 = 100.0   # km/s/(Mpc/h), py/SaclayMocks/constant.py:36
+
+
+def growth_rate_at_zero(path):
+    """dD/dz at z = 0: first row of the growth-rate table (bin/make_boxes.py:310-318)."""
+    from saclaymocks_gb300 import fits
+    return float(fits.read(path, 1)["dD/dz"][0])
 
 
 def pgrid_file(pkdir, NX, NY, NZ):
@@ -57,16 +70,19 @@ def pgrid_file(pkdir, NX, NY, NZ):
     return os.path.join(pkdir, f"P{NX}-{NY}-{NZ}.fits")
 
 
-def write_planes(prefix, box, dcell, sigma, seed):
-    """box-{i}.fits files: float32 [1, NY, NZ] per x plane, keys DX..NZ; sigma and seed on
-    file 0 (bin/make_boxes.py:110-117)."""
+def write_planes(prefix, box, dcell, sigma, seed, nhdu=None):
+    """{prefix}-{i}.fits files, i < nhdu (default NX: one x plane per file), each holding
+    planes [i NX/nhdu, (i+1) NX/nhdu) as float32 with keys DX..NZ; sigma and seed on file 0
+    (bin/make_boxes.py:110-117)."""
     from saclaymocks_gb300 import fits
     NX, NY, NZ = box.shape
-    for i in range(NX):
+    nhdu = NX if nhdu is None else nhdu
+    for i in range(nhdu):
         hdr = {"DX": dcell, "DY": dcell, "DZ": dcell, "NX": NX, "NY": NY, "NZ": NZ}
         if i == 0:
             hdr.update({"SIGMA": float(np.float32(sigma)), "SEED": int(seed)})
-        fits.write_image(f"{prefix}-{i}.fits", np.ascontiguousarray(box[i:i + 1]), hdr)
+        part = box[i * NX // nhdu:(i + 1) * NX // nhdu]
+        fits.write_image(f"{prefix}-{i}.fits", np.ascontiguousarray(part), hdr)
 
 
 def main(argv=None):
@@ -86,24 +102,55 @@ def main(argv=None):
             box[:, :, iz] = np.float32(rs.normal(size=[NX, NY]))
         noise = torch.from_numpy(box).cuda()
         del box
-    pk = None
+    grids = {}
     if args.PkDir:
         fn = pgrid_file(args.PkDir, NX, NY, NZ)
         if os.path.exists(fn):
-            pk = torch.from_numpy(np.ascontiguousarray(fits.read(fn, "P0"), dtype=np.float32)).cuda()
-    out = grf.make_boxes(NX, NY, NZ, args.pixel, seed=seed, noise=noise, k0=args.k0, pk_grid=pk,
-                         want_eta=rsd)
-    out.check()
-    sig = out.sigma()[0]
-    torch.cuda.synchronize()
-    print(f"boxes {NX}x{NY}x{NZ} drawn on the GPU in {time.time() - t0:.3f} s, sigma = {sig:.6f}")
-    if not args.no_write:
+            for ext in ("Pln1", "Pln2", "Pln3", "P0"):
+                try:
+                    g = fits.read(fn, ext)
+                except Exception:
+                    continue
+                grids[ext] = torch.from_numpy(np.ascontiguousarray(g, dtype=np.float32)).cuda()
+    vfac = None
+    if rsd and not args.eta_only_zz:
+        path = args.dgrowthfile or os.path.expandvars("$SACLAYMOCKS_BASE/etc/dgrowth.fits")
+        vfac = H0 * growth_rate_at_zero(path)
+    common = dict(seed=seed, noise=noise, k0=args.k0)
+    write = not args.no_write
+    if write:
         os.makedirs(args.outDir, exist_ok=True)
-        write_planes(os.path.join(args.outDir, "box"), out.delta[0].cpu().numpy(), args.pixel, sig, seed)
-        if rsd:
-            write_planes(os.path.join(args.outDir, "eta_zz"), out.eta[0].cpu().numpy(), args.pixel,
-                         out.sigma(1)[0], seed)
-        print(f"written to {args.outDir} in {time.time() - t0:.1f} s")
+    outdir = args.outDir
+
+    def emit(prefix, field, nhdu=None):
+        if write:
+            write_planes(os.path.join(outdir, prefix), field[0], args.pixel, field[1], seed, nhdu)
+
+    # lognormal boxes: raw modes x Pln grids (bin/make_boxes.py:241-275)
+    for i in (1, 2, 3):
+        if f"Pln{i}" in grids:
+            o = grf.make_boxes(NX, NY, NZ, args.pixel, pk_grid=grids[f"Pln{i}"], want_eta=False, **common)
+            o.check()
+            emit(f"boxln_{i}", (o.delta[0].cpu().numpy(), o.sigma()[0]), args.nHDU)
+    # density and the eta / velocity boxes, one GRF call per output component
+    comps = []
+    if rsd:
+        comps = ["zz"] if args.eta_only_zz else ["xx", "yy", "zz", "xy", "xz", "yz", "vx", "vy", "vz"]
+    pk = grids.get("P0")
+    out = None
+    for j, c in enumerate(comps or [None]):
+        o = grf.make_boxes(NX, NY, NZ, args.pixel, pk_grid=pk, want_eta=c is not None,
+                           eta_comp=c or "zz", vel_factor=vfac if c and c[0] == "v" else None, **common)
+        o.check()
+        if j == 0:
+            out = o
+            emit("box", (o.delta[0].cpu().numpy(), o.sigma()[0]))
+        if c is not None:
+            name = c if c[0] == "v" else f"eta_{c}"
+            emit(name, (o.eta[0].cpu().numpy(), o.sigma(1)[0]), args.nHDU if c[0] == "v" else None)
+    torch.cuda.synchronize()
+    print(f"boxes {NX}x{NY}x{NZ}: {1 + len(comps) + sum(f'Pln{i}' in grids for i in (1, 2, 3))} fields "
+          f"in {time.time() - t0:.2f} s, sigma = {out.sigma()[0]:.6f}" + (f", written to {outdir}" if write else ""))
     return out
 
 

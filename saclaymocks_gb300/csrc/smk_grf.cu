@@ -157,7 +157,7 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         return fail(SMK_EINVAL, "smk_grf_boxes: need nx, ny >= 2, nz >= 2 even, batch >= 1");
     if (!(p->dcell > 0)) return fail(SMK_EINVAL, "smk_grf_boxes: dcell must be > 0");
     if (p->want_eta && !eta) return fail(SMK_EINVAL, "smk_grf_boxes: want_eta needs an eta box");
-    if (p->eta_comp < SMK_ETA_ZZ || p->eta_comp > SMK_ETA_YZ)
+    if (p->eta_comp < SMK_ETA_ZZ || p->eta_comp > SMK_ETA_VZ)
         return fail(SMK_EINVAL, "smk_grf_boxes: unknown eta_comp");
     if (p->noise_mode != SMK_NOISE_HOST && p->noise_mode != SMK_NOISE_PHILOX)
         return fail(SMK_EINVAL, "smk_grf_boxes: unknown noise_mode");
@@ -244,6 +244,7 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         ga.sig_r = (float)sqrt(ncell);
         ga.seed = p->seed;
         ga.eta_comp = p->eta_comp;
+        ga.vfac = (float)p->vel_factor;
         // A tile writes all nx rows of its columns, so one wave of tiles touches rows spread over
         // the whole of each output box.  Past ~64 GiB for the two boxes together (2 x 40 GB at
         // 2560x2560x1536) that spread outruns the GPU's address-translation reach and the pass
@@ -290,6 +291,7 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         xa.inv_k0 = p->pk_mode == SMK_PK_ANALYTIC ? (float)(1.0 / p->k0) : 0.f;
         xa.inv_vcell = inv_vcell;
         xa.eta_comp = p->eta_comp;
+        xa.vfac = (float)p->vel_factor;
         if ((rc = run_xpass(vx, xa, st))) return rc;
         if ((rc = mark(3))) return rc;
     }

@@ -178,7 +178,8 @@ struct XArgs {
     double amp_host;
     double kfac;           // 2 * pi / dcell (2 k_Nyquist)
     float inv_k0, inv_vcell;
-    int eta_comp;          // SMK_ETA_*: eta_ij = k_i k_j / k^2 delta_k
+    int eta_comp;          // SMK_ETA_*: eta_ij = k_i k_j / k^2 delta_k, or a velocity component
+    float vfac;            // velocity: H0 * dD/dz(0)
 };
 
 // k_i k_j of the eta component (SMK_ETA_*), float32 product as numpy forms kx*ky
@@ -191,6 +192,21 @@ __device__ __forceinline__ float eta_num(int comp, float kx, float ky, float kz)
         case SMK_ETA_YZ: return __fmul_rn(ky, kz);
         default: return __fmul_rn(kz, kz);
     }
+}
+
+// The second output of the x pass from delta_k: eta_ij = k_i k_j / k^2 delta_k (components 0..5)
+// or velocity v_i = -i k_i / k^2 * vfac * delta_k (SMK_ETA_VX/VY/VZ); kk1 = k^2 with k^2(0) = 1.
+// EXACT: correctly rounded quotient (the host-noise path, compared with the reference's arrays).
+template <bool EXACT>
+__device__ __forceinline__ float2 eta_apply(int comp, float2 d, float kx, float ky, float kz, float kk1,
+                                            float vfac) {
+    if (comp >= SMK_ETA_VX) {
+        const float ki = comp == SMK_ETA_VX ? kx : (comp == SMK_ETA_VY ? ky : kz);
+        const float f = (EXACT ? __fdiv_rn(ki, kk1) : __fdividef(ki, kk1)) * vfac;
+        return make_float2(d.y * f, -d.x * f);
+    }
+    const float num = eta_num(comp, kx, ky, kz);
+    return cscale(d, EXACT ? __fdiv_rn(num, kk1) : __fdividef(num, kk1));
 }
 
 __device__ __forceinline__ float kaxis(int i, int n, double kfac, bool full) {
@@ -257,7 +273,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpass_kernel(const XArgs a) {
             s[idx] = d;
             if (pb && w < cols) {
                 const float kk1 = (kk == 0.0f) ? 1.0f : kk;  // k^2[0,0,0] = 1 (bin/make_boxes.py:306)
-                pb[e * estride + w] = cscale(d, __fdiv_rn(eta_num(a.eta_comp, kxv, ky, kz), kk1));
+                pb[e * estride + w] = eta_apply<true>(a.eta_comp, d, kxv, ky, kz, kk1, a.vfac);
             }
         }
         __syncthreads();
@@ -300,6 +316,7 @@ struct XGenArgs {
     float sig_c, sig_r;    // sqrt(N/2), sqrt(N)
     uint64_t seed;
     int eta_comp;
+    float vfac;
     int fields;            // XGEN_BOTH: W/2 delta + W/2 eta lines per tile; XGEN_DELTA / XGEN_ETA:
                            // W lines of one field (two launches; see xgen_split)
 };
@@ -395,7 +412,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
                     d = cscale(X, sc);
                     if (!ONE || a.fields == XGEN_ETA) {
                         const float kk1 = (kk == 0.0f) ? 1.0f : kk;
-                        et = cscale(d, __fdividef(eta_num(a.eta_comp, kxv, ky, kz_), kk1));
+                        et = eta_apply<false>(a.eta_comp, d, kxv, ky, kz_, kk1, a.vfac);
                     }
                 }
                 if (!ONE) {

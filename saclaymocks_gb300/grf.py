@@ -90,7 +90,8 @@ def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: flo
                seed: int = 0, *, noise: torch.Tensor | None = None, k0: float = 0.02,
                amp: float | None = None, pk_grid: torch.Tensor | None = None,
                want_eta: bool = True, batch: int = 1, out=None, workspace: GrfWorkspace | None = None,
-               stream=None, pass_events=None, eta_comp: str = "zz") -> GrfBoxes:
+               stream=None, pass_events=None, eta_comp: str = "zz",
+               vel_factor: float | None = None) -> GrfBoxes:
     """Draw delta (and eta_zz) boxes on the current CUDA device.
 
     noise:   None -> Philox white noise drawn on the GPU from ``seed`` (box b: seed + b);
@@ -103,7 +104,9 @@ def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: flo
     pass_events: optional list of 6 recorded torch.cuda.Event, marked before the first HBM
              pass and after each of the five (per-pass timing).
     eta_comp: which eta_ij = irfftn(k_i k_j / k^2 delta_k) the eta box holds ("zz", "xx",
-             "yy", "xy", "xz", "yz"; bin/make_boxes.py:315-391).
+             "yy", "xy", "xz", "yz"; bin/make_boxes.py:315-391), or a velocity
+             v_i = irfftn(-i k_i / k^2 * vel_factor * delta_k) ("vx", "vy", "vz";
+             bin/make_boxes.py:393-431, vel_factor = H0 * dD/dz(z=0)).
     """
     ny = nx if ny is None else ny
     nz = nx if nz is None else nz
@@ -116,6 +119,10 @@ def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: flo
     p.want_eta = 1 if want_eta else 0
     p.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
     p.eta_comp = _lib.SMK_ETA[eta_comp]
+    if eta_comp in ("vx", "vy", "vz"):
+        if vel_factor is None:
+            raise ValueError("velocity boxes need vel_factor = H0 * dD/dz(z=0)")
+        p.vel_factor = float(vel_factor)
     keep = []
     if noise is not None:
         if noise.dtype != torch.float32 or not noise.is_cuda or not noise.is_contiguous():

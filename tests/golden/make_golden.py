@@ -63,7 +63,13 @@ def gen_grf(NX, NY, NZ, seed, tag):
     ref_shims.FITS_CAPTURE.clear()
     tmp = tempfile.mkdtemp()
     pname = f"P{NX}.fits" if NX == NY == NZ else f"P{NX}-{NY}-{NZ}.fits"
-    ref_shims.FITS_SERVE[pname] = {"P0": P0, "Pln1": P0, "Pln2": P0, "Pln3": P0, 0: P0}
+    # distinct grids for the three lognormal boxes (any float32 grid: the step is a multiply)
+    kx = np.fft.fftfreq(NX).reshape(-1, 1, 1)
+    ky = np.fft.fftfreq(NY).reshape(-1, 1)
+    kz = np.fft.rfftfreq(NZ)
+    kq = np.sqrt(kx * kx + ky * ky + kz * kz)
+    pln = [np.float32(P0 * f) for f in (0.5, 1.0 + 2.0 * kq, np.exp(-4.0 * kq))]
+    ref_shims.FITS_SERVE[pname] = {"P0": P0, "Pln1": pln[0], "Pln2": pln[1], "Pln3": pln[2], 0: P0}
     mb = ref_shims.load_script("make_boxes")
     argv = sys.argv
     sys.argv = ["make_boxes.py", "-NX", str(NX), "-NY", str(NY), "-NZ", str(NZ),
@@ -83,6 +89,15 @@ def gen_grf(NX, NY, NZ, seed, tag):
                boxk_scaled=np.load(os.path.join(tmp, "boxk.npy")))
     for f in ("eta_xx", "eta_yy", "eta_zz", "eta_xy", "eta_xz", "eta_yz"):
         out[f] = stack(f)
+    # nHDU = 1 outputs: lognormal boxes (bin/make_boxes.py:241-275) and velocities (:393-431)
+    for f in ("boxln_1", "boxln_2", "boxln_3", "vx", "vy", "vz"):
+        out[f] = cap[f"{f}-0.fits"]["hdus"][0]["data"]
+    for i, g in enumerate(pln):
+        out[f"Pln{i + 1}"] = g
+    from saclaymocks_gb300 import fits as _f
+    dg = _f.read(os.path.join(ref_shims.REF, "etc", "dgrowth.fits"), 1)
+    out["dgrowth0"] = np.float64(dg["dD/dz"][0])
+    out["H0"] = np.float64(100.0)       # py/SaclayMocks/constant.py:36
     np.savez_compressed(os.path.join(HERE, f"grf_{tag}.npz"), **out)
     print("grf", tag, out["delta"].shape, "sigma", out["sigma"])
     return out

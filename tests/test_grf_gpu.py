@@ -250,3 +250,31 @@ def test_xgen_split_launches_equal_one_launch(G):
     delta_only = G.make_boxes(nx, ny, nz, 2.19, seed=21, batch=2, want_eta=False)
     torch.cuda.synchronize()
     assert torch.equal(delta_only.delta, one.delta)
+
+
+@pytest.mark.parametrize("tag", ["cube16", "rect"])
+def test_lognormal_and_velocity_boxes_match_reference_golden(G, golden, tag):
+    """boxln_1..3 (SMK_PK_GRID with the Pln grids, delta box only) and vx, vy, vz
+    (SMK_ETA_VX/VY/VZ, vel_factor = H0 dD/dz(0)) against the reference's main()."""
+    f = golden(f"grf_{tag}.npz")
+    NX, NY, NZ = int(f["NX"]), int(f["NY"]), int(f["NZ"])
+    dx, k0 = float(f["DX"]), float(f["k0"])
+    noise = torch.from_numpy(ograf.draw_noise(NX, NY, NZ, int(f["seed"]))).cuda()
+    for i in (1, 2, 3):
+        out = G.make_boxes(NX, NY, NZ, dx, noise=noise, pk_grid=torch.from_numpy(f[f"Pln{i}"]).cuda(),
+                           want_eta=False)
+        torch.cuda.synchronize()
+        _check(out.delta[0].cpu().numpy(), f[f"boxln_{i}"], f"boxln_{i}")
+    vf = float(f["H0"]) * float(f["dgrowth0"])
+    for c in ("vx", "vy", "vz"):
+        out = G.make_boxes(NX, NY, NZ, dx, noise=noise, k0=k0, eta_comp=c, vel_factor=vf)
+        torch.cuda.synchronize()
+        _check(out.delta[0].cpu().numpy(), f["delta"], f"delta with {c}")
+        _check(out.eta[0].cpu().numpy(), f[c], c)
+    # the same components in GPU-noise mode against the FP64 oracle on the drawn modes
+    nk = ophilox.kspace_noise(NX, NY, NZ, 77)
+    o64 = ograf.grf_from_modes(nk, NZ, dx, k0, eta=(), precision="f64", velocity=(float(f["H0"]), float(f["dgrowth0"])))
+    for c in ("vx", "vy", "vz"):
+        out = G.make_boxes(NX, NY, NZ, dx, seed=77, k0=k0, eta_comp=c, vel_factor=vf)
+        torch.cuda.synchronize()
+        _check(out.eta[0].cpu().numpy(), o64[c], f"philox {c}")

@@ -25,6 +25,23 @@ def test_grf_bit_exact_vs_make_boxes(golden, tag):
     assert np.sqrt((d ** 2).mean() / (o64["delta"] ** 2).mean()) < 2e-7
 
 
+@pytest.mark.parametrize("tag", ["cube16", "rect"])
+def test_lognormal_and_velocity_boxes_bit_exact(golden, tag):
+    """boxln_1..3 (raw modes x Pln grids) and vx, vy, vz (-i k_i/k^2 H0 dD/dz(0) x P0-scaled
+    modes) of the reference's main() (bin/make_boxes.py:241-275, 393-431)."""
+    f = golden(f"grf_{tag}.npz")
+    NX, NY, NZ = int(f["NX"]), int(f["NY"]), int(f["NZ"])
+    dx, k0 = float(f["DX"]), float(f["k0"])
+    noise = grf.draw_noise(NX, NY, NZ, int(f["seed"]))
+    nk = np.fft.rfftn(noise.astype(np.float64))
+    for i in (1, 2, 3):
+        out = grf.grf_from_modes(nk, NZ, dx, k0, eta=(), P0=f[f"Pln{i}"])
+        assert np.array_equal(out["delta"], f[f"boxln_{i}"]), i
+    out = grf.grf_from_modes(nk, NZ, dx, k0, eta=(), velocity=(float(f["H0"]), float(f["dgrowth0"])))
+    for c in grf.VELOCITY_COMPONENTS:
+        assert np.array_equal(out[c], f[c]), c
+
+
 def test_grf_scaled_k_box_matches_checkpoint(golden):
     """boxk.npy after the P0 multiply (bin/make_boxes.py:289-291)."""
     f = golden("grf_cube16.npz")
