@@ -335,6 +335,23 @@ def fit_leg(args, runner, out, table, cfg):
            "fd_s_per_grad": t_fd, "grad_speedup": t_fd / t_adj,
            "grad_rel_diff_median": float(np.median(rel)), "grad_rel_diff_max": float(rel.max()),
            "adam_steps": steps, "adjoint_fit_s": sa, "loss_start": la[0], "loss_end": la[-1]}
+    # P1D-missing tuning loop (fit_az.Fitter.iterate) on the same skewers: time per iteration
+    from saclaymocks_gb300 import tune_p1d
+    kmiss = np.arange(0.0, 20.0, 0.01)
+    pm = 0.05 * np.exp(-(kmiss / 2.0) ** 2)
+    kb = np.logspace(np.log10(0.05), np.log10(15.0), 33)
+    k_c = 0.5 * (kb[1:] + kb[:-1])
+    tuner = tune_p1d.P1DMissTuner(prob.delta, prob.eta, None, table.npix, 0.1, 1.58, 0.6, kmiss, pm,
+                                  np.concatenate([[0.0], k_c, [20.0]]), 0.1 * np.exp(-np.concatenate([[0.0], k_c, [20.0]]) / 3),
+                                  kb, ss_nz=2048, seed=3)
+    tuner.compute_p1d()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tuner.run(3)
+    torch.cuda.synchronize()
+    res["p1dmiss_tuning"] = {"iterations": tuner.niter, "s_per_iteration": (time.perf_counter() - t0) / max(tuner.niter, 1),
+                             "max_abs_ratio_minus_1": [round(x, 4) for x in tuner.history]}
+    del tuner
     if steps * t_fd < 150:
         tf, lf, sf, _ = fit.adam_fit(prob, th0, mz, pk, steps=steps, lr=0.02, grad="fd", h=1e-2, points=4,
                                      eps_rel=1e-2)

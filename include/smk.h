@@ -277,9 +277,11 @@ typedef struct {
 /* Host: pairs of equal-length skewers for the fit kernels (order_out: 2n + 16 ints). */
 int smk_fit_schedule(int64_t n, const int32_t* npix_host, int32_t* order_out, int64_t* n_slots_out);
 /* Length (doubles) of the accumulator array: [nzb] sum F per z bin, [1] sum F,
- * [nkb] sum |X|^2 dx/N per k bin, [nzb][3] A, [nzb][3] B, [1] S. */
+ * [nkb] sum P per k bin (P = |X|^2 dx/N of one skewer mode), [nzb][3] A, [nzb][3] B, [1] S,
+ * [nkb] sum P^2 per k bin (for the rms / sqrt(n) errors of util.MakeProfileHisto). */
 int smk_fit_acc_len(int32_t nzb, int32_t nkb);
-/* Forward: zeroes acc, fills sum F per z bin, sum F, P1D power sums per k bin.
+/* Forward: zeroes acc, fills sum F per z bin, sum F, P1D power sums and squared-power sums
+ * per k bin.
  * theta: device [nzb][3] (a, b, c).  Workspace: 256 bytes. */
 int smk_fit_forward(const SmkFitProblem* fp, const float* theta, double* acc, void* workspace,
                     size_t workspace_bytes, void* stream);

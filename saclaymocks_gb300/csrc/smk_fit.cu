@@ -52,7 +52,8 @@ __host__ __device__ inline int acc_psum(int nzb) { return nzb + 1; }            
 __host__ __device__ inline int acc_A(int nzb, int nkb) { return nzb + 1 + nkb; }  // [nzb][3]
 __host__ __device__ inline int acc_B(int nzb, int nkb) { return 2 * nzb + 1 + nkb + 2 * nzb; }  // [nzb][3]
 __host__ __device__ inline int acc_S(int nzb, int nkb) { return 7 * nzb + 1 + nkb; }  // [1]
-__host__ __device__ inline int acc_len(int nzb, int nkb) { return 7 * nzb + 2 + nkb; }
+__host__ __device__ inline int acc_psq(int nzb, int nkb) { return 7 * nzb + 2 + nkb; }  // [nkb]
+__host__ __device__ inline int acc_len(int nzb, int nkb) { return 7 * nzb + 2 + 2 * nkb; }
 
 __device__ __forceinline__ float flux_of(const FitArgs& a, int64_t o, const float* th, float* tau1, float* g) {
     const int j = a.zbin[o];
@@ -228,11 +229,12 @@ __global__ void __launch_bounds__(FIT_T) fit_p1d_kernel(const FitArgs a) {
     float2* s2 = smem + FFT_MAX_N;
     float2* tw = smem + 2 * FFT_MAX_N;
     __shared__ double psum[FIT_MAX_BINS];
+    __shared__ double psq[FIT_MAX_BINS];
     __shared__ double edges[FIT_MAX_BINS + 1];
     __shared__ float th[3 * FIT_MAX_BINS];
     __shared__ long long item_sh;
     __shared__ PairSetup ps;
-    for (int i = threadIdx.x; i < a.nkb; i += FIT_T) psum[i] = 0.0;
+    for (int i = threadIdx.x; i < a.nkb; i += FIT_T) psum[i] = psq[i] = 0.0;
     for (int i = threadIdx.x; i <= a.nkb; i += FIT_T) edges[i] = a.kedges[i];
     for (int i = threadIdx.x; i < 3 * a.nzb; i += FIT_T) th[i] = a.theta[i];
     const float fbar_inv = (float)((double)a.n_total / a.acc[acc_ftot(a.nzb)]);
@@ -254,21 +256,26 @@ __global__ void __launch_bounds__(FIT_T) fit_p1d_kernel(const FitArgs a) {
         for (int m0 = 0; m0 <= half; m0 += FIT_T) {    // block-uniform trip count
             const int m = m0 + (int)threadIdx.x;
             int b = -1;
-            float p = 0.f;
+            float p = 0.f, q = 0.f;
             if (m <= half) {
                 b = kbin(m, N, kfac, edges, a.nkb);
                 const float2 zk = s1[m], zm = s1[m == 0 ? 0 : N - m];
                 const float x1r = 0.5f * (zk.x + zm.x), x1i = 0.5f * (zk.y - zm.y);
                 const float x2r = 0.5f * (zk.y + zm.y), x2i = -0.5f * (zk.x - zm.x);
-                p = x1r * x1r + x1i * x1i;
-                if (ps.sid[1] >= 0) p += x2r * x2r + x2i * x2i;
-                p *= norm;
+                const float p1 = (x1r * x1r + x1i * x1i) * norm;
+                const float p2 = ps.sid[1] >= 0 ? (x2r * x2r + x2i * x2i) * norm : 0.f;
+                p = p1 + p2;
+                q = p1 * p1 + p2 * p2;
             }
             warp_bin_add(psum, b, p);
+            warp_bin_add(psq, b, q);
         }
         __syncthreads();
     }
-    for (int i = threadIdx.x; i < a.nkb; i += FIT_T) atomicAdd(a.acc + acc_psum(a.nzb) + i, psum[i]);
+    for (int i = threadIdx.x; i < a.nkb; i += FIT_T) {
+        atomicAdd(a.acc + acc_psum(a.nzb) + i, psum[i]);
+        atomicAdd(a.acc + acc_psq(a.nzb, a.nkb) + i, psq[i]);
+    }
 }
 
 // ------------------------------------------------------------------ backward
@@ -499,7 +506,7 @@ int smk_fit_backward(const SmkFitProblem* fp, const float* theta, double* acc, c
     if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     const int off = acc_A(a.nzb, a.nkb);
-    if (cudaMemsetAsync(acc + off, 0, sizeof(double) * (acc_len(a.nzb, a.nkb) - off), st) != cudaSuccess ||
+    if (cudaMemsetAsync(acc + off, 0, sizeof(double) * (acc_psq(a.nzb, a.nkb) - off), st) != cudaSuccess ||
         cudaMemsetAsync(workspace, 0, 8, st) != cudaSuccess)
         return check_launch("smk_fit_backward: memset");
     const size_t smem = 3 * FFT_MAX_N * sizeof(float2);

@@ -71,11 +71,15 @@ class FitProblem:
         # fixed counts: pixels per z bin, (skewer, mode) pairs per k bin
         self.cnt_z = torch.bincount(self.zbin.long(), minlength=self.nzb).double().cpu().numpy()
         cnt_k = np.zeros(self.nkb)
+        ksum = np.zeros(self.nkb)
         for N, mult in zip(*np.unique(self.lengths, return_counts=True)):
             k = np.fft.rfftfreq(int(N)) * 2 * (np.pi / self.dx)
             b = bin_index(k, self.kedges)
             cnt_k += mult * np.bincount(b[b >= 0], minlength=self.nkb)
+            ksum += mult * np.bincount(b[b >= 0], weights=k[b >= 0], minlength=self.nkb)
         self.cnt_k = cnt_k
+        with np.errstate(invalid="ignore", divide="ignore"):
+            self.k_mean = ksum / cnt_k        # mean k of the (skewer, mode) pairs per bin
         self.fp = _lib.SmkFitProblem(
             delta=self.delta.data_ptr(), eta=self.eta.data_ptr() if self.eta is not None else None,
             G=self.G.data_ptr() if self.G is not None else None, zbin=self.zbin.data_ptr(),
@@ -101,6 +105,21 @@ class FitProblem:
             mz = acc[:nzb] / self.cnt_z
             pk = acc[nzb + 1:nzb + 1 + nkb] / self.cnt_k
         return mz, pk, acc[nzb] / self.n_total
+
+    def p1d_profile(self, theta):
+        """util.MakeProfileHisto of the mock P1D (py/SaclayMocks/util.py:46-75 applied as in
+        powerspectrum.ComputeP1D.P1D, :231-238): per non-empty k bin the mean k, the mean
+        power and rms / sqrt(n), from the GPU sums of P and P^2 (FP64)."""
+        self.reductions(theta)
+        acc = self.acc.cpu().numpy()
+        nzb, nkb = self.nzb, self.nkb
+        s1 = acc[nzb + 1:nzb + 1 + nkb]
+        s2 = acc[7 * nzb + 2 + nkb:7 * nzb + 2 + 2 * nkb]
+        ok = self.cnt_k > 0
+        n = self.cnt_k[ok]
+        m1, m2 = s1[ok] / n, s2[ok] / n
+        err = np.sqrt(np.maximum(m2 - m1 * m1, 0.0)) / np.sqrt(n)
+        return self.k_mean[ok], m1, err
 
     def loss(self, theta, target_mz, target_pk) -> float:
         mz, pk, _ = self.reductions(theta)

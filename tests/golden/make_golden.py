@@ -292,10 +292,52 @@ def gen_util():
     print("util: Fmean", fm, "sigF", np.sqrt(s2), "chi2", chi)
 
 
+def gen_iterate():
+    """One step of fit_az.Fitter.iterate (py/SaclayMocks/fit_az.py:281-332) on synthetic
+    mock / model / P1Dmiss arrays: the P1D-missing update (ratio spline, multiplicative
+    update, smoothing spline).  The I/O and regeneration steps it ends with are stubbed."""
+    import types
+
+    import scipy.interpolate as si
+    from SaclayMocks import fit_az
+    rng = np.random.RandomState(21)
+    k = np.linspace(0.12, 9.5, 40)
+    model_k = np.linspace(0.05, 12.0, 200)
+    model_p = 0.12 * np.exp(-model_k / 2.5) + 0.01
+    p1d = (0.12 * np.exp(-k / 2.2) + 0.008) * (1 + 0.05 * rng.normal(size=k.size))
+    err = 0.04 * p1d * (1 + 0.2 * rng.uniform(size=k.size))
+    kmiss = np.arange(0.0, 20.0, 0.05)
+    pmiss = 0.05 * np.exp(-(kmiss / 2.0) ** 2) + 1e-4
+    outs = {}
+    for cf, crit in ((1.0, None), (0.6, None), (1.0, 1e3)):
+        obj = types.SimpleNamespace()
+        obj.data = {"bins": None, "p1d_model_interp": si.interp1d(model_k, model_p)}
+        obj.mock = {"k": k, "p1d": p1d, "err_p1d": err, "kmiss": kmiss, "p1dmiss": pmiss,
+                    "p1dmiss_interp": si.InterpolatedUnivariateSpline(kmiss, pmiss)}
+        obj.fit = {"a": 0.1}
+        obj.convergence_factor = cf
+        obj.convergence_criterium = crit
+        obj.converged = False
+        obj.niter = 0
+        for name in ("export_p1dmiss", "gen_small_scales", "export_p1d"):
+            setattr(obj, name, lambda *a, **kw: None)
+        obj.compute_p1d = lambda *a, **kw: None
+        fit_az.Fitter.iterate(obj)
+        tag = f"cf{cf:g}" + ("_conv" if crit else "")
+        outs[tag + "_converged"] = np.bool_(obj.converged)
+        outs[tag + "_niter"] = np.int64(obj.niter)
+        outs[tag + "_p1dmiss"] = np.asarray(obj.mock["p1dmiss"], np.float64)
+        outs[tag + "_interp_on_kmiss"] = np.asarray(obj.mock["p1dmiss_interp"](kmiss), np.float64)
+    np.savez_compressed(os.path.join(HERE, "iterate.npz"), k=k, p1d=p1d, err=err, model_k=model_k,
+                        model_p=model_p, kmiss=kmiss, pmiss=pmiss, **outs)
+    print("iterate: p1dmiss[0..3]", outs["cf1_p1dmiss"][:3])
+
+
 def main():
     g = gen_grf(16, 16, 16, 0, "cube16")
     gen_grf(20, 12, 18, 5, "rect")
     gen_readspec(g)
+    gen_iterate()
     gen_merge("fitp1d", True, 7)
     gen_merge("table", False, 9)
     gen_util()
