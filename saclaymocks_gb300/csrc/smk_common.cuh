@@ -104,13 +104,15 @@ enum : uint32_t { STREAM_KMODE = 0x4Bu, STREAM_SKEWER = 0x53u };
 // u = ((x >> 8) + 1) * 2^-24 in (0, 1] for the radius and (x >> 8) * 2^-23 in [0, 2)
 // as the angle in units of pi (both exact in float32).  The angle is evaluated as
 // pi (t - 1) in [-pi, pi) with the hardware sine/cosine (absolute error < 4e-7 there) and
-// the signs flipped back; the radius uses the reciprocal square root.
+// the signs flipped back; the radius -2 ln u uses the hardware base-2 logarithm (absolute
+// error ~1e-7 near u = 1, so deviates of radius < 0.01, probability 5e-5, carry absolute
+// errors up to ~1e-5) and the reciprocal square root.
 __device__ __forceinline__ void gauss4(u32x4 r, float g[4]) {
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const float u1 = (float)((r.v[2 * h] >> 8) + 1u) * 5.9604644775390625e-08f;  // 2^-24
         const float t = (float)(r.v[2 * h + 1] >> 8) * 1.1920928955078125e-07f;       // 2^-23
-        const float x = -2.0f * logf(u1);
+        const float x = -1.3862943611198906f * __log2f(u1);                             // -2 ln 2 log2(u)
         const float rad = x > 0.0f ? x * rsqrtf(x) : 0.0f;
         float s, c;
         __sincosf(fmaf(t, 3.14159265358979f, -3.14159265358979f), &s, &c);
