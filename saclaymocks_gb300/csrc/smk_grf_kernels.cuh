@@ -124,6 +124,10 @@ struct LineArgs {
     int64_t n_outer, ostride, estride;
     int ncol;
     int prefetch;   // pull the next tile into L2 during the transform
+    // Staged source (or null: in place).  The x pass of GPU noise can leave its output in
+    // column blocks of W: block cb of outer line o holds [n][W] contiguous at
+    // src[buf] + (cb * n_outer + o) * n * W, so a tile reads one contiguous run.
+    const float2* src[2];
 };
 
 // Forward: natural -> digit-reversed order along the axis (kept in HBM); inverse: back.
@@ -146,17 +150,30 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const LineArgs a) {
         const int cb = (int)(t - o * ncolt);
         float2* base = a.base[buf] + o * a.ostride + (int64_t)cb * W;
         const int cols = min(W, a.ncol - cb * W);
-        load_cols_async<W, T>(s, base, n, a.estride, cols);
+        const float2* sb = a.src[buf] ? a.src[buf] + ((int64_t)cb * a.n_outer + o) * n * W : nullptr;
+        if (sb)
+            load_cols_async<W, T>(s, sb, n, W, cols);
+        else
+            load_cols_async<W, T>(s, base, n, a.estride, cols);
         cp_async_wait_all();
         __syncthreads();
         if (a.prefetch && tile + gridDim.x < ntiles) {
-            // the next tile of this block: one line per row segment of its W columns
+            // the next tile of this block: one line per row segment of its W columns, or
+            // its contiguous staged run
             const int64_t tn = tile + gridDim.x;
             const int bn = (int)(tn / tpb);
             const int64_t un = tn - bn * tpb;
             const int64_t on = un / ncolt;
-            const float2* nb = a.base[bn] + on * a.ostride + (un - on * ncolt) * W;
-            for (int e = threadIdx.x; e < n; e += T) prefetch_l2(nb + (int64_t)e * a.estride);
+            const int64_t cn = un - on * ncolt;
+            if (a.src[bn]) {
+                const char* p = reinterpret_cast<const char*>(a.src[bn] + (cn * a.n_outer + on) * n * W);
+                const int64_t bytes = (int64_t)n * W * 8;
+                for (int64_t off = (int64_t)threadIdx.x * 4096; off < bytes; off += (int64_t)T * 4096)
+                    prefetch_l2_bulk(p + off, (uint32_t)(bytes - off < 4096 ? bytes - off : 4096));
+            } else {
+                const float2* nb = a.base[bn] + on * a.ostride + cn * W;
+                for (int e = threadIdx.x; e < n; e += T) prefetch_l2(nb + (int64_t)e * a.estride);
+            }
         }
         fft_tile<INV, W, W, T, C::RMAX>(s, tw, a.pl);
         store_cols<W, T>(s, base, n, a.estride, cols);
@@ -319,6 +336,13 @@ struct XGenArgs {
     float vfac;
     int fields;            // XGEN_BOTH: W/2 delta + W/2 eta lines per tile; XGEN_DELTA / XGEN_ETA:
                            // W lines of one field (two launches; see xgen_split)
+    // Staged output (or null: in place in A / B): k_z column kz of x line e of outer (b, y slot)
+    // goes to S[((kz >> sh) * batch*nx + b*nx + e) * ny + yslot) << sh | (kz & (2^sh - 1))],
+    // the column-block layout the y pass reads (block width 2^sh = the y pass's W).  Tiles then
+    // run k_z-block-major so each wave of tiles writes a compact address range.
+    float2* SA;
+    float2* SB;
+    int sh;
 };
 enum { XGEN_BOTH = 0, XGEN_DELTA = 1, XGEN_ETA = 2 };
 
@@ -348,12 +372,21 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
     float amp = 0.f;
     if (a.pk_mode == SMK_PK_ANALYTIC) amp = (float)(a.amp_host > 0.0 ? a.amp_host : *a.amp_dev);
     const int64_t ncolt = ceil_div(a.nzh, WC);
-    const int64_t ntiles = (int64_t)a.batch * a.ny * ncolt;
+    const int64_t nouter = (int64_t)a.batch * a.ny;
+    const int64_t ntiles = nouter * ncolt;
     const int64_t estride = (int64_t)a.ny * a.cp;
     const int half = a.nz / 2;
+    const bool staged = a.SA != nullptr;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int64_t o = tile / ncolt;  // b*ny + y slot
-        const int cb = (int)(tile - o * ncolt);
+        int64_t o;   // b*ny + y slot
+        int cb;
+        if (staged) {
+            cb = (int)(tile / nouter);
+            o = tile - (int64_t)cb * nouter;
+        } else {
+            o = tile / ncolt;
+            cb = (int)(tile - o * ncolt);
+        }
         const int64_t b = o / a.ny;
         const int yslot = (int)(o - b * a.ny);
         const int iy = freq_of_slot(a.ply, yslot);
@@ -426,13 +459,28 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
         __syncthreads();
         fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
         const int cols = min(WC, a.nzh - cb * WC);
-        const int64_t off = b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)cb * WC;
-        for (int idx = threadIdx.x; idx < n * W; idx += T) {
-            const int e = idx / W, l = idx % W;
-            const int c = l < WC ? l : l - WC;
-            if (c < cols) {
-                float2* dst = !ONE ? (l < WC ? a.A : a.B) : (a.fields == XGEN_DELTA ? a.A : a.B);
-                if (dst) dst[off + e * estride + c] = s[idx];
+        if (staged) {
+            const int64_t nxb = (int64_t)a.batch * a.nx;
+            const int mask = (1 << a.sh) - 1;
+            for (int idx = threadIdx.x; idx < n * W; idx += T) {
+                const int e = idx / W, l = idx % W;
+                const int c = l < WC ? l : l - WC;
+                if (c < cols) {
+                    float2* dst = !ONE ? (l < WC ? a.SA : a.SB) : (a.fields == XGEN_DELTA ? a.SA : a.SB);
+                    const int kz = cb * WC + c;
+                    const int64_t line = ((int64_t)(kz >> a.sh) * nxb + b * a.nx + e) * a.ny + yslot;
+                    if (dst) dst[(line << a.sh) | (kz & mask)] = s[idx];
+                }
+            }
+        } else {
+            const int64_t off = b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)cb * WC;
+            for (int idx = threadIdx.x; idx < n * W; idx += T) {
+                const int e = idx / W, l = idx % W;
+                const int c = l < WC ? l : l - WC;
+                if (c < cols) {
+                    float2* dst = !ONE ? (l < WC ? a.A : a.B) : (a.fields == XGEN_DELTA ? a.A : a.B);
+                    if (dst) dst[off + e * estride + c] = s[idx];
+                }
             }
         }
         __syncthreads();

@@ -79,11 +79,23 @@ def alloc_boxes(nx: int, ny: int, nz: int, batch: int = 1, want_eta: bool = True
 
 
 class GrfWorkspace:
-    """Device workspace + stats buffer reused by repeated calls."""
+    """Device workspace + stats buffer reused by repeated calls.  The workspace grows on
+    demand to smk_grf_workspace_size (the k-space staging buffer of large GPU-noise calls)."""
 
     def __init__(self, batch: int, device="cuda"):
+        self.device = device
         self.ws = torch.zeros(256 // 8, dtype=torch.float64, device=device)
         self.stats = torch.zeros((batch, 2, 4), dtype=torch.float64, device=device)
+
+    def ensure(self, nbytes: int):
+        if self.ws.numel() * 8 < nbytes:
+            self.ws = torch.empty((nbytes + 7) // 8, dtype=torch.float64, device=self.ws.device)
+        return self.ws
+
+
+# Staging is switched on by default when delta + eta span more than this: below it the
+# in-place x pass is as fast and the extra box-sized workspace is not worth its memory.
+STAGING_MIN_PAIR_BYTES = 48 * 2 ** 30
 
 
 def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: float = 2.19,
@@ -91,7 +103,7 @@ def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: flo
                amp: float | None = None, pk_grid: torch.Tensor | None = None,
                want_eta: bool = True, batch: int = 1, out=None, workspace: GrfWorkspace | None = None,
                stream=None, pass_events=None, eta_comp: str = "zz",
-               vel_factor: float | None = None) -> GrfBoxes:
+               vel_factor: float | None = None, staging: bool | None = None) -> GrfBoxes:
     """Draw delta (and eta_zz) boxes on the current CUDA device.
 
     noise:   None -> Philox white noise drawn on the GPU from ``seed`` (box b: seed + b);
@@ -107,6 +119,8 @@ def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: flo
              "yy", "xy", "xz", "yz"; bin/make_boxes.py:315-391), or a velocity
              v_i = irfftn(-i k_i / k^2 * vel_factor * delta_k) ("vx", "vy", "vz";
              bin/make_boxes.py:393-431, vel_factor = H0 * dD/dz(z=0)).
+    staging: GPU noise with eta: stage the x pass's output in column blocks (workspace grows by
+             one box of complex floats); None: on when delta + eta exceed 48 GiB.
     """
     ny = nx if ny is None else ny
     nz = nx if nz is None else nz
@@ -150,6 +164,10 @@ def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: flo
         dpad, epad = out
     if workspace is None:
         workspace = GrfWorkspace(batch, device)
+    if staging is None:
+        staging = 2 * 4 * batch * nx * ny * pitch_of(nz) > STAGING_MIN_PAIR_BYTES
+    p.kspace_staging = 1 if (staging and noise is None and want_eta) else 0
+    workspace.ensure(lib.smk_grf_workspace_size(C.byref(p)))
     if pass_events is not None:
         handles = (C.c_void_p * 6)(*[int(e.cuda_event) for e in pass_events])
         keep.append(handles)
@@ -166,13 +184,14 @@ def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: flo
 
 
 def grf_launches(nx: int, ny: int, nz: int, batch: int = 1, want_eta: bool = True, gpu_noise: bool = True) -> int:
-    """Kernel launches of one smk_grf_boxes call with the default split rule (GPU noise: x pass
-    once, or twice when delta + eta span more than 64 GiB; then y inverse and z inverse; host
-    noise: z forward, y forward, x, y inverse, z inverse)."""
+    """Kernel launches of one smk_grf_boxes call as make_boxes issues it by default (GPU noise:
+    x pass, y inverse, z inverse, with the y inverse in two launches when the x pass is staged,
+    i.e. delta + eta above STAGING_MIN_PAIR_BYTES; host noise: z forward, y forward, x,
+    y inverse, z inverse)."""
     if not gpu_noise:
         return 5
     pair = 2 * 4 * batch * nx * ny * pitch_of(nz)
-    return (2 if want_eta and pair > 64 * 2 ** 30 else 1) + 2
+    return 4 if want_eta and pair > STAGING_MIN_PAIR_BYTES else 3
 
 
 def pk_normalisation(nx: int, ny: int, nz: int, dcell: float = 2.19, k0: float = 0.02) -> float:
