@@ -280,7 +280,7 @@ def test_lognormal_and_velocity_boxes_match_reference_golden(G, golden, tag):
         _check(out.eta[0].cpu().numpy(), o64[c], f"philox {c}")
 
 
-@pytest.mark.parametrize("shape", [(40, 24, 36), (30, 18, 50), (64, 20, 14)])
+@pytest.mark.parametrize("shape", [(40, 24, 36), (30, 18, 50), (64, 20, 12)])
 def test_staged_x_pass_equals_in_place(G, shape):
     """The staged column-block path (x pass into the eta box + workspace, y pass reading
     contiguous runs) gives the same boxes, bit for bit, as the in-place path."""
