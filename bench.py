@@ -96,14 +96,35 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def dist_setup():
+def dist_setup(backend="nccl"):
+    """Replicas: one process per GPU under torchrun (RANK / WORLD_SIZE from the environment),
+    each drawing its own chunk (seed + rank); no data is exchanged, only the timings."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:
         import torch.distributed as dist
-        dist.init_process_group("nccl")
+        dist.init_process_group(backend)
         return dist, rank, world
     return None, 0, 1
+
+
+def replica_seed(base_seed: int, rank: int) -> int:
+    """Seed of the chunk replica `rank` draws (Philox boxes, skewer table, small scales)."""
+    return base_seed + rank
+
+
+def max_over_ranks(values, dist, device="cuda"):
+    """Element-wise maximum of per-rank timings (the slowest replica sets the job's time)."""
+    import torch
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
+def aggregate_value(per_rank_units: float, world: int, max_seconds: float) -> float:
+    """Whole-job throughput: the units all replicas processed over the slowest replica's time."""
+    return world * per_rank_units / max_seconds
 
 
 def cpu_baseline(cfg, sample_div, workers):
@@ -175,12 +196,13 @@ def run_ours(args, cfg):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     L = np.array([cfg["nx"], cfg["ny"], cfg["nz"]]) * cfg["dcell"]
-    table = spectra.skewers_cone(cfg["n_skewers"], L, seed=cfg["seed"] + rank, npix_range=cfg["npix"])
+    seed = replica_seed(cfg["seed"], rank)
+    table = spectra.skewers_cone(cfg["n_skewers"], L, seed=seed, npix_range=cfg["npix"])
     scfg = spectra.SpectraConfig(ss_mode=_lib.SMK_SS_PHILOX, ss_nz=cfg["ss_nz"],
-                                 pmiss=spectra.pmiss_gauss(0.05, 2.0), seed=cfg["seed"] + rank,
+                                 pmiss=spectra.pmiss_gauss(0.05, 2.0), seed=seed,
                                  abc_mode=_lib.SMK_ABC_POWERLAW, a=0.1, a_zref1=3.2, a_power=4.5,
                                  b=1.58, c=0.6, z_lo=1.8, z_hi=3.6)
-    chunk = pipeline.MockChunk(cfg["nx"], cfg["ny"], cfg["nz"], cfg["dcell"], seed=cfg["seed"] + rank,
+    chunk = pipeline.MockChunk(cfg["nx"], cfg["ny"], cfg["nz"], cfg["dcell"], seed=seed,
                                cfg=scfg)
     runner = chunk._prepare(table.start, table.direction, table.npix)
     boxes, ws = chunk.boxes, chunk.ws
@@ -195,7 +217,7 @@ def run_ours(args, cfg):
     pixels = table.total_pixels
 
     def device_step(ev=None, sk_ev=None):
-        out = grf.make_boxes(nx, ny, nz, cfg["dcell"], seed=cfg["seed"] + rank, amp=chunk.amp,
+        out = grf.make_boxes(nx, ny, nz, cfg["dcell"], seed=seed, amp=chunk.amp,
                              out=boxes, workspace=ws, pass_events=ev)
         if sk_ev:
             sk_ev[0].record()
@@ -231,10 +253,7 @@ def run_ours(args, cfg):
     pass_ms = np.mean([[evs[k][i].elapsed_time(evs[k][i + 1]) for i in range(5)]
                        for k in range(args.steps)], axis=0)
     sk_ms = float(np.mean([skevs[k][0].elapsed_time(skevs[k][1]) for k in range(args.steps)]))
-    ms_t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-    if dist:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms = float(ms_t.item())
+    ms = max_over_ranks([ms], dist)[0]
 
     # e2e: through MockChunk.run with host skewer arrays, H2D + D2H inside the timed region
     chunk.run(table.start, table.direction, table.npix)
@@ -244,10 +263,7 @@ def run_ours(args, cfg):
         chunk.run(table.start, table.direction, table.npix)
     barrier()
     e2e_s = (time.perf_counter() - t0) / args.steps
-    e2e_t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-    if dist:
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_s = float(e2e_t.item())
+    e2e_s = max_over_ranks([e2e_s], dist)[0]
 
     fit_res = None
     if not args.no_fit and rank == 0:
@@ -268,7 +284,7 @@ def run_ours(args, cfg):
     achieved = pass_bytes[dom] / (pass_ms[dom] * 1e-3) / 1e9
     grf_ms = float(np.sum(pass_ms))
     step_ms = ms / args.steps
-    value = world * cells / (step_ms * 1e-3)
+    value = aggregate_value(cells, world, step_ms * 1e-3)
     res = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic (Philox noise, synthetic skewers)",
@@ -283,7 +299,7 @@ def run_ours(args, cfg):
                         "traffic": None,
                         "per_pass_frac": {n: round(b / (m * 1e-3) / 1e9 / peak, 3)
                                           for n, b, m in zip(pass_names, pass_bytes, pass_ms)}},
-           "e2e": {"value": world * cells / e2e_s, "unit": "cells/s",
+           "e2e": {"value": aggregate_value(cells, world, e2e_s), "unit": "cells/s",
                    "h2d_bytes_per_step": chunk.h2d_bytes(), "d2h_bytes_per_step": chunk.d2h_bytes(),
                    "ms_per_step": e2e_s * 1e3},
            "gpu_launches": args.steps * (grf.grf_launches(nx, ny, nz) + 1),
