@@ -314,3 +314,45 @@ def test_skewer_launch_replayed_from_a_cuda_graph_equals_eager(env, boxes):
     g.replay()
     torch.cuda.synchronize()
     assert torch.equal(flux, eager)
+
+
+def test_empty_table_and_zero_or_one_pixel_skewers(env, boxes):
+    """Edge cases: an empty skewer table is a no-op; skewers of 0 and 1 pixels mixed with long
+    ones (ragged, odd counts per FFT length) match the oracle."""
+    _lib, _, spectra = env
+    out = boxes["out"]
+    kw = dict(nx=boxes["nx"], ny=boxes["ny"], nz=boxes["nz"], pitch=out.pitch, dcell=boxes["dx"])
+    empty = spectra.SkewerTable(np.zeros((0, 3)), np.zeros((0, 3)), np.zeros(0, np.int32))
+    f = spectra.SkewerRunner(empty, spectra.SpectraConfig()).run(out.delta_pad[0], out.eta_pad[0], **kw)
+    torch.cuda.synchronize()
+    assert f.numel() == 0
+    L = np.array([boxes["nx"], boxes["ny"], boxes["nz"]]) * boxes["dx"]
+    t = spectra.skewers_cone(9, L, seed=12, npix_range=(40, 90))
+    npix = t.npix.copy()
+    npix[[1, 4]] = 0
+    npix[[2, 7]] = 1
+    t = spectra.SkewerTable(t.start, t.direction, npix, dpix=t.dpix)
+    cfg = spectra.SpectraConfig(a=0.1, b=1.6, c=0.5)
+    g = _run(env, boxes, t, cfg)
+    ref = _oracle(boxes, t, dict(kind="const", a=0.1, b=1.6, c=0.5))
+    for s in range(t.n):
+        assert len(g[0][s]) == npix[s]
+    _cmp(g, ref, np.std(boxes["d"]))
+
+
+def test_longest_skewer_of_the_fft_rule(env, boxes):
+    """The largest small-scale FFT (4096 points, skewers up to 4046 pixels under the rule
+    256*2^n >= npix + 50) against the oracle with host noise."""
+    _lib, _, spectra = env
+    L = np.array([boxes["nx"], boxes["ny"], boxes["nz"]]) * boxes["dx"]
+    t = spectra.skewers_cone(3, L, seed=13, npix_range=(4046, 4046))
+    rs = np.random.RandomState(2)
+    noise1d = [rs.normal(size=osk.nz_rule(int(n))).astype(np.float32) for n in t.npix]
+    packed = torch.from_numpy(np.concatenate(noise1d)).cuda()
+    offs = torch.from_numpy(np.concatenate([[0], np.cumsum([len(x) for x in noise1d])[:-1]]).astype(np.int64)).cuda()
+    pm = lambda k: osk.pmiss_analytic(k)  # noqa: E731
+    cfg = spectra.SpectraConfig(ss_mode=_lib.SMK_SS_HOST, ss_nz=0, pmiss=pm, a=0.1, b=1.6, c=0.5)
+    g = _run(env, boxes, t, cfg, noise=(packed, offs))
+    ref = _oracle(boxes, t, dict(kind="const", a=0.1, b=1.6, c=0.5),
+                  small=dict(pixsize=0.2, nz="rule", pmiss=pm), noise1d=[x.astype(np.float64) for x in noise1d])
+    _cmp(g, ref, np.std(boxes["d"]))
