@@ -60,11 +60,13 @@ class MockChunk:
         return self._pin_out.numel() * 4
 
     def run(self, start, direction, npix, pass_events=None) -> np.ndarray:
-        """Flux of every pixel (packed, float32, host) for the host skewer table."""
-        r = self._prepare(start, direction, npix)
+        """Flux of every pixel (packed, float32, host) for the host skewer table.  The boxes are
+        enqueued first, so the host-side schedule and pinned copies of the skewer table run
+        while the GPU draws them."""
         out = grf.make_boxes(self.nx, self.ny, self.nz, self.dcell, seed=self.seed, k0=self.k0,
                              amp=self.amp, want_eta=self.boxes[1] is not None, out=self.boxes,
                              workspace=self.ws, pass_events=pass_events)
+        r = self._prepare(start, direction, npix)
         r.run(out.delta_pad[0], out.eta_pad[0] if out.eta_pad is not None else None, nx=self.nx,
               ny=self.ny, nz=self.nz, pitch=out.pitch, dcell=self.dcell, flux=self._flux)
         self._pin_out.copy_(self._flux, non_blocking=True)
