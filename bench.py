@@ -276,12 +276,21 @@ def run_ours(args, cfg):
         return
     peak, peak_kind = hbm_peak()
     nzh = nz // 2 + 1
-    cbytes = 8.0 * nx * ny * nzh           # one half-complex box
+    modes = nx * ny * nzh
+    cbytes = 8.0 * modes                   # one half-complex box
     rbytes = 4.0 * cells                   # one real box
-    pass_names = ["zfwd_r2c(philox)", "y_fwd", "x_fused", "y_inv(x2)", "zinv_c2r(x2)"]
-    pass_bytes = [cbytes, 2 * cbytes, 3 * cbytes, 4 * cbytes, 2 * cbytes + 2 * rbytes]
+    # GPU-noise passes (the two host-noise forward passes do not run): algorithmic bytes =
+    # x: write delta_k, eta_k; y: read + write both; z: read both half spectra, write both boxes
+    pass_names = ["x_gen", "y_inv(x2)", "zinv_c2r(x2)"]
+    pass_ms = pass_ms[2:]
+    pass_bytes = [2 * cbytes, 4 * cbytes, 2 * cbytes + 2 * rbytes]
     dom = int(np.argmax(pass_ms))
     achieved = pass_bytes[dom] / (pass_ms[dom] * 1e-3) / 1e9
+    # DRAM bytes per unit from ncu captures of the same kernels on boxes with the production
+    # line lengths (profiles/grf_passes_xgen_2560x128x1536_line_zinv_128x2560x1536.md), scaled
+    # by the units of this launch: x 7.85 B per mode and field, y 16.0 and z 16.1 B per mode
+    # and field
+    traffic = [7.85 * modes * 2, 16.0 * modes * 2, 16.06 * modes * 2][dom] / 1e9
     grf_ms = float(np.sum(pass_ms))
     step_ms = ms / args.steps
     value = aggregate_value(cells, world, step_ms * 1e-3)
@@ -296,7 +305,8 @@ def run_ours(args, cfg):
            "skewer_ms": round(sk_ms, 3),
            "roofline": {"bound": "hbm", "kernel": pass_names[dom], "achieved": achieved, "peak": peak,
                         "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                        "traffic": None,
+                        "traffic": traffic, "traffic_unit": "GB per pass (ncu, scaled)",
+                        "algorithmic_bytes": pass_bytes[dom] / 1e9,
                         "per_pass_frac": {n: round(b / (m * 1e-3) / 1e9 / peak, 3)
                                           for n, b, m in zip(pass_names, pass_bytes, pass_ms)}},
            "e2e": {"value": aggregate_value(cells, world, e2e_s), "unit": "cells/s",

@@ -338,7 +338,9 @@ size_t smk_skewers_workspace_size(const SmkSkewers* sk, const SmkSpectraParams* 
 int smk_skewers_flux(const SmkSkewers* sk, const SmkSpectraParams* p, const float* delta_box,
                      const float* eta_box, float* flux, float* delta_out, float* eta_out, float* z_out,
                      void* workspace, size_t workspace_bytes, void* stream) {
-    if (!sk || !p || !flux) return fail(SMK_EINVAL, "smk_skewers_flux: null argument");
+    if (!sk || !p) return fail(SMK_EINVAL, "smk_skewers_flux: null argument");
+    if (sk->n_slots == 0 && sk->n >= 0) return SMK_OK;   // empty table: nothing to read or write
+    if (!flux) return fail(SMK_EINVAL, "smk_skewers_flux: null flux");
     if (p->interp != SMK_INTERP_PIXELS && !delta_box)
         return fail(SMK_EINVAL, "smk_skewers_flux: a box read needs the delta box");
     if (p->interp == SMK_INTERP_GAUSS343) {

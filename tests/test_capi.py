@@ -93,6 +93,9 @@ def test_argument_validation_needs_no_gpu(lib):
     sp = _lib.SmkSpectraParams()
     assert lib.smk_skewers_flux(C.byref(sk), C.byref(sp), None, None, 0x1000, None, None, None,
                                 None, 0, None) == _lib.SMK_EINVAL
+    empty = _lib.SmkSkewers(n=0, n_slots=0)            # an empty table is a no-op
+    assert lib.smk_skewers_flux(C.byref(empty), C.byref(sp), None, None, None, None, None, None,
+                                None, 0, None) == 0
     assert lib.smk_strerror(_lib.SMK_ENULLBOX).startswith(b"SMK_ENULLBOX")
 
 
