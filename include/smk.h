@@ -84,10 +84,10 @@ typedef struct {
     int32_t n_pass_events;    /* first HBM pass and after each of the five (0: none)          */
     int32_t eta_comp;     /* SMK_ETA_*: which eta_ij or velocity the eta box holds (0 = zz)  */
     double vel_factor;    /* SMK_ETA_VX/VY/VZ: H0 * dD/dz(z = 0) (km/s/(Mpc/h) per unit z)    */
-    int32_t kspace_staging; /* GPU noise + eta: 1 stages the x pass's output in column blocks   */
-                            /* (in the eta box and one box-sized part of the workspace, see    */
-                            /* smk_grf_workspace_size) so its writes stay compact and the y    */
-                            /* pass reads contiguous runs; 0: in place                          */
+    int32_t kspace_staging; /* GPU noise + eta: 1 draws every mode once into the workspace     */
+                            /* (see smk_grf_workspace_size), then runs one x inverse per field */
+                            /* from it; 0: modes drawn inside the x pass (twice when the boxes */
+                            /* exceed 64 GiB and the pass runs one field per launch)           */
 } SmkGrfParams;
 
 /* Row pitch (floats) of the padded box layout for a z extent nz. */
@@ -95,7 +95,8 @@ int64_t smk_grf_pitch(int32_t nz);
 /* Floats of one padded output box array (all batch members). */
 int64_t smk_grf_box_floats(const SmkGrfParams* p);
 /* Workspace bytes smk_grf_boxes needs: 256 (the FP64 normalisation accumulator), plus, with
- * kspace_staging on a GPU-noise call with eta, batch*nx*ny*(pitch/2) complex floats. */
+ * kspace_staging on a GPU-noise call with eta, batch*nx*ny*roundup(nz/2+1, 32) complex floats
+ * for the drawn modes. */
 size_t smk_grf_workspace_size(const SmkGrfParams* p);
 
 /*

@@ -117,10 +117,12 @@ int64_t smk_grf_box_floats(const SmkGrfParams* p) {
     return (int64_t)p->batch * p->nx * p->ny * smk_grf_pitch(p->nz);
 }
 
-// Staging buffer of the x pass (bytes), or 0 when the call runs in place.
+// Staged-mode buffer of GPU noise (bytes), or 0 when the call draws in the x pass: delta_k of
+// every mode, k_z rounded up to the widest x-pass tile (32 columns).
 static size_t staging_bytes(const SmkGrfParams* p) {
     if (!p || !p->kspace_staging || p->noise_mode != SMK_NOISE_PHILOX || !p->want_eta) return 0;
-    return (size_t)p->batch * p->nx * p->ny * (size_t)(smk_grf_pitch(p->nz) / 2) * sizeof(float2);
+    const size_t nzh = (size_t)p->nz / 2 + 1;
+    return (size_t)p->batch * p->nx * p->ny * ((nzh + 31) / 32 * 32) * sizeof(float2);
 }
 
 size_t smk_grf_workspace_size(const SmkGrfParams* p) {
@@ -221,7 +223,6 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
     ya.estride = cp;
     ya.ncol = nzh;
     ya.prefetch = g_prefetch.load();
-    ya.src[0] = ya.src[1] = nullptr;
     bool staged = false;
     const int64_t rows_per_box = (int64_t)p->nx * p->ny;
     const float inv_vcell = 1.0f / (float)(p->dcell * p->dcell * p->dcell);
@@ -256,42 +257,38 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         // the whole of each output box.  Past ~64 GiB for the two boxes together (2 x 40 GB at
         // 2560x2560x1536) that spread outruns the GPU's address-translation reach and the pass
         // slows by 1.7x; writing delta and eta in two launches keeps each wave within one box.
-        // Staged: the x pass writes column blocks of the y pass's width (delta's into the eta box,
-        // eta's into the workspace), tiles k_z-block-major, so a wave of tiles writes a compact
-        // range and one launch serves both fields; the y pass then reads each tile as one run.
-        const int wl = variant_table(PASS_LINE)[vy].w;
+        // Staged (large boxes): draw every mode once into the workspace, then one x-inverse launch
+        // per field reads them back, so no launch writes both boxes and no mode is drawn twice.
+        const int wx = variant_table(pass_x)[vx].w;
         int sh = 0;
-        while ((1 << sh) < wl) ++sh;
+        while ((1 << sh) < wx) ++sh;
         const size_t sbytes = staging_bytes(p);
-        staged = sbytes > 0 && (1 << sh) == wl && ceil_div(nzh, wl) * wl <= cp && workspace &&
-                 workspace_bytes >= 256 + sbytes;
-        ga.SA = ga.SB = nullptr;
-        ga.sh = sh;
+        staged = sbytes > 0 && (1 << sh) == wx && workspace && workspace_bytes >= 256 + sbytes;
         if (staged) {
-            ga.SA = e2;
-            ga.SB = reinterpret_cast<float2*>(reinterpret_cast<char*>(workspace) + 256);
-        }
-        const double pair_bytes = 2.0 * 4.0 * (double)p->batch * p->nx * p->ny * (double)pitch;
-        const int sm = g_xgen_split.load();
-        const bool split = !staged && p->want_eta && (sm < 0 ? pair_bytes > 64.0 * (1ull << 30) : sm == 1);
-        ga.fields = !p->want_eta ? XGEN_DELTA : (split ? XGEN_DELTA : XGEN_BOTH);
-        if ((rc = run_xgen(vx, ga, st))) return rc;
-        if (split) {
+            ga.S = reinterpret_cast<float2*>(reinterpret_cast<char*>(workspace) + 256);
+            ga.sh = sh;
+            if ((rc = run_kgen(ga, st))) return rc;
+            ga.fields = XGEN_DELTA;
+            if ((rc = run_xinv(vx, ga, st))) return rc;
             ga.fields = XGEN_ETA;
+            if ((rc = run_xinv(vx, ga, st))) return rc;
+        } else {
+            // In place: a tile writes all nx rows of its columns, so one wave of tiles touches
+            // rows spread over the whole of each output box.  Past ~64 GiB for the two boxes
+            // together (2 x 40 GB at 2560x2560x1536) that spread outruns the GPU's
+            // address-translation reach and the pass slows by 1.7x; writing delta and eta in
+            // two launches keeps each wave within one box.
+            const double pair_bytes = 2.0 * 4.0 * (double)p->batch * p->nx * p->ny * (double)pitch;
+            const int sm = g_xgen_split.load();
+            const bool split = p->want_eta && (sm < 0 ? pair_bytes > 64.0 * (1ull << 30) : sm == 1);
+            ga.fields = !p->want_eta ? XGEN_DELTA : (split ? XGEN_DELTA : XGEN_BOTH);
             if ((rc = run_xgen(vx, ga, st))) return rc;
+            if (split) {
+                ga.fields = XGEN_ETA;
+                if ((rc = run_xgen(vx, ga, st))) return rc;
+            }
         }
         if ((rc = mark(3))) return rc;
-        if (staged) {
-            // y inverse of delta (reading its blocks from the eta box) before the eta box is
-            // overwritten by the y inverse of eta (reading the workspace)
-            ya.nbuf = 1;
-            ya.base[0] = d2;
-            ya.src[0] = e2;
-            if ((rc = run_line(vy, ya, true, st))) return rc;
-            ya.base[0] = e2;
-            ya.src[0] = ga.SB;
-            if ((rc = run_line(vy, ya, true, st))) return rc;
-        }
     } else {
         // 1. r2c along z of the caller's noise
         ZFwdArgs za;
@@ -330,13 +327,8 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
     }
 
     // 4. c2c along y, inverse, on delta (and eta)
-    if (!staged) {
-        ya.nbuf = p->want_eta ? 2 : 1;
-        ya.base[0] = d2;
-        ya.base[1] = e2;
-        ya.src[0] = ya.src[1] = nullptr;
-        if ((rc = run_line(vy, ya, true, st))) return rc;
-    }
+    ya.nbuf = p->want_eta ? 2 : 1;
+    if ((rc = run_line(vy, ya, true, st))) return rc;
     if ((rc = mark(4))) return rc;
 
     // 5. c2r along z, / N, statistics

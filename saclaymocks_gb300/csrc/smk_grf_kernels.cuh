@@ -124,10 +124,6 @@ struct LineArgs {
     int64_t n_outer, ostride, estride;
     int ncol;
     int prefetch;   // pull the next tile into L2 during the transform
-    // Staged source (or null: in place).  The x pass of GPU noise can leave its output in
-    // column blocks of W: block cb of outer line o holds [n][W] contiguous at
-    // src[buf] + (cb * n_outer + o) * n * W, so a tile reads one contiguous run.
-    const float2* src[2];
 };
 
 // Forward: natural -> digit-reversed order along the axis (kept in HBM); inverse: back.
@@ -150,30 +146,17 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const LineArgs a) {
         const int cb = (int)(t - o * ncolt);
         float2* base = a.base[buf] + o * a.ostride + (int64_t)cb * W;
         const int cols = min(W, a.ncol - cb * W);
-        const float2* sb = a.src[buf] ? a.src[buf] + ((int64_t)cb * a.n_outer + o) * n * W : nullptr;
-        if (sb)
-            load_cols_async<W, T>(s, sb, n, W, cols);
-        else
-            load_cols_async<W, T>(s, base, n, a.estride, cols);
+        load_cols_async<W, T>(s, base, n, a.estride, cols);
         cp_async_wait_all();
         __syncthreads();
         if (a.prefetch && tile + gridDim.x < ntiles) {
-            // the next tile of this block: one line per row segment of its W columns, or
-            // its contiguous staged run
+            // the next tile of this block: one line per row segment of its W columns
             const int64_t tn = tile + gridDim.x;
             const int bn = (int)(tn / tpb);
             const int64_t un = tn - bn * tpb;
             const int64_t on = un / ncolt;
-            const int64_t cn = un - on * ncolt;
-            if (a.src[bn]) {
-                const char* p = reinterpret_cast<const char*>(a.src[bn] + (cn * a.n_outer + on) * n * W);
-                const int64_t bytes = (int64_t)n * W * 8;
-                for (int64_t off = (int64_t)threadIdx.x * 4096; off < bytes; off += (int64_t)T * 4096)
-                    prefetch_l2_bulk(p + off, (uint32_t)(bytes - off < 4096 ? bytes - off : 4096));
-            } else {
-                const float2* nb = a.base[bn] + on * a.ostride + cn * W;
-                for (int e = threadIdx.x; e < n; e += T) prefetch_l2(nb + (int64_t)e * a.estride);
-            }
+            const float2* nb = a.base[bn] + on * a.ostride + (un - on * ncolt) * W;
+            for (int e = threadIdx.x; e < n; e += T) prefetch_l2(nb + (int64_t)e * a.estride);
         }
         fft_tile<INV, W, W, T, C::RMAX>(s, tw, a.pl);
         store_cols<W, T>(s, base, n, a.estride, cols);
@@ -336,14 +319,80 @@ struct XGenArgs {
     float vfac;
     int fields;            // XGEN_BOTH: W/2 delta + W/2 eta lines per tile; XGEN_DELTA / XGEN_ETA:
                            // W lines of one field (two launches; see xgen_split)
-    // Staged output (or null: in place in A / B): k_z column kz of x line e of outer (b, y slot)
-    // goes to S[((kz >> sh) * batch*nx + b*nx + e) * ny + yslot) << sh | (kz & (2^sh - 1))],
-    // the column-block layout the y pass reads (block width 2^sh = the y pass's W).  Tiles then
-    // run k_z-block-major so each wave of tiles writes a compact address range.
-    float2* SA;
-    float2* SB;
+    // Staged modes (kgen_kernel writes, xinv_kernel reads): delta_k of mode (x slot e, y slot,
+    // kz) of box b at S[((((kz >> sh) * batch + b) * ny + yslot) * nx + e) << sh | (kz & (2^sh - 1))]:
+    // column blocks of width 2^sh (the x-inverse tile width), x in the x plan's slot order, so
+    // one x-inverse tile is one contiguous run of nx * 2^sh complex values.
+    float2* S;
     int sh;
 };
+
+// delta_k = X * sqrt(P/Vcell) of the modes (ix, iy, kz0) and (ix, iy, kz0 + 1) of one box
+// (GPU noise): Philox4x32-10 block (kz0/2, ix, iy, STREAM_KMODE) keyed by seed, Box-Muller,
+// Re/Im ~ N(0, N/2); on the kz = 0 and nz/2 planes the lower flat index of (ix, iy) and
+// (-ix, -iy) owns the draw and self-conjugate modes are real with variance N.  Also returns
+// k_z and k^2 per mode for the eta split; kz >= nzh gives 0.
+struct ModePair {
+    float2 d[2];
+    float kz[2], kk[2];
+};
+__device__ __forceinline__ ModePair draw_pair(const XGenArgs& a, uint64_t seed, int ixe, int iy, int iym,
+                                              float kxv, float ky, int kz0, const float* kzt, float amp) {
+    ModePair mp;
+    float g[4];
+    {
+        u32x4 ctr;
+        ctr.v[0] = (uint32_t)(kz0 >> 1);
+        ctr.v[1] = (uint32_t)ixe;
+        ctr.v[2] = (uint32_t)iy;
+        ctr.v[3] = STREAM_KMODE;
+        gauss4(philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32)), g);
+    }
+    const int half = a.nz / 2;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int kz = kz0 + h;
+        mp.d[h] = make_float2(0.f, 0.f);
+        mp.kz[h] = 0.f;
+        mp.kk[h] = 1.f;
+        if (kz < a.nzh) {
+            float2 X = make_float2(a.sig_c * g[2 * h], a.sig_c * g[2 * h + 1]);
+            if (kz == 0 || kz == half) {
+                const int ixm = ixe == 0 ? 0 : a.nx - ixe;
+                if (ixm == ixe && iym == iy) {
+                    X = make_float2(a.sig_r * g[2 * h], 0.f);
+                } else if ((int64_t)ixe * a.ny + iy > (int64_t)ixm * a.ny + iym) {
+                    // the partner (-kx, -ky) owns the draw: take its conjugate
+                    u32x4 ctr;
+                    ctr.v[0] = (uint32_t)(kz0 >> 1);
+                    ctr.v[1] = (uint32_t)ixm;
+                    ctr.v[2] = (uint32_t)iym;
+                    ctr.v[3] = STREAM_KMODE;
+                    float gm[4];
+                    gauss4(philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32)), gm);
+                    X = make_float2(a.sig_c * gm[2 * h], -a.sig_c * gm[2 * h + 1]);
+                }
+            }
+            const float kz_ = kzt[kz];
+            const float kk = __fadd_rn(__fadd_rn(__fmul_rn(kxv, kxv), __fmul_rn(ky, ky)), __fmul_rn(kz_, kz_));
+            float sc;
+            if (a.pk_mode == SMK_PK_GRID) {
+                sc = __ldg(a.grid + ((int64_t)ixe * a.ny + iy) * a.nzh + kz);
+            } else {
+                // GPU noise has no bit-level reference: approximate square roots
+                const float k = kk > 0.0f ? kk * rsqrtf(kk) : 0.0f;
+                const float kr = k * a.inv_k0;
+                const float den = fmaf(kr, kr, 1.0f);
+                const float p = __fdividef(amp * k, den * den) * a.inv_vcell;
+                sc = p > 0.0f ? p * rsqrtf(p) : 0.0f;
+            }
+            mp.d[h] = cscale(X, sc);
+            mp.kz[h] = kz_;
+            mp.kk[h] = (kk == 0.0f) ? 1.0f : kk;
+        }
+    }
+    return mp;
+}
 enum { XGEN_BOTH = 0, XGEN_DELTA = 1, XGEN_ETA = 2 };
 
 // smem: s[n*W] | tw[n] | kx[n] | ix[n] | kzt[nzh]
@@ -375,18 +424,9 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
     const int64_t nouter = (int64_t)a.batch * a.ny;
     const int64_t ntiles = nouter * ncolt;
     const int64_t estride = (int64_t)a.ny * a.cp;
-    const int half = a.nz / 2;
-    const bool staged = a.SA != nullptr;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        int64_t o;   // b*ny + y slot
-        int cb;
-        if (staged) {
-            cb = (int)(tile / nouter);
-            o = tile - (int64_t)cb * nouter;
-        } else {
-            o = tile / ncolt;
-            cb = (int)(tile - o * ncolt);
-        }
+        const int64_t o = tile / ncolt;   // b*ny + y slot
+        const int cb = (int)(tile - o * ncolt);
         const int64_t b = o / a.ny;
         const int yslot = (int)(o - b * a.ny);
         const int iy = freq_of_slot(a.ply, yslot);
@@ -396,93 +436,134 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
         for (int idx = threadIdx.x; idx < n * NP; idx += T) {
             const int e = idx / NP, pr = idx % NP;
             const int c0 = 2 * pr, kz0 = cb * WC + c0;
-            const int ixe = ix[e];
-            float g[4];
-            {
-                u32x4 ctr;
-                ctr.v[0] = (uint32_t)(kz0 >> 1);
-                ctr.v[1] = (uint32_t)ixe;
-                ctr.v[2] = (uint32_t)iy;
-                ctr.v[3] = STREAM_KMODE;
-                gauss4(philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32)), g);
-            }
             const float kxv = kx[e];
+            const ModePair mp = draw_pair(a, seed, ix[e], iy, iym, kxv, ky, kz0, kzt, amp);
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const int kz = kz0 + h;
-                float2 d = make_float2(0.f, 0.f), et = make_float2(0.f, 0.f);
-                if (kz < a.nzh) {
-                    float2 X = make_float2(a.sig_c * g[2 * h], a.sig_c * g[2 * h + 1]);
-                    if (kz == 0 || kz == half) {
-                        const int ixm = ixe == 0 ? 0 : a.nx - ixe;
-                        if (ixm == ixe && iym == iy) {
-                            X = make_float2(a.sig_r * g[2 * h], 0.f);
-                        } else if ((int64_t)ixe * a.ny + iy > (int64_t)ixm * a.ny + iym) {
-                            // the partner (-kx, -ky) owns the draw: take its conjugate
-                            u32x4 ctr;
-                            ctr.v[0] = (uint32_t)(kz0 >> 1);
-                            ctr.v[1] = (uint32_t)ixm;
-                            ctr.v[2] = (uint32_t)iym;
-                            ctr.v[3] = STREAM_KMODE;
-                            float gm[4];
-                            gauss4(philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32)), gm);
-                            X = make_float2(a.sig_c * gm[2 * h], -a.sig_c * gm[2 * h + 1]);
-                        }
-                    }
-                    const float kz_ = kzt[kz];
-                    const float kk = __fadd_rn(__fadd_rn(__fmul_rn(kxv, kxv), __fmul_rn(ky, ky)), __fmul_rn(kz_, kz_));
-                    float sc;
-                    if (a.pk_mode == SMK_PK_GRID) {
-                        sc = __ldg(a.grid + ((int64_t)ixe * a.ny + iy) * a.nzh + kz);
-                    } else {
-                        // GPU noise has no bit-level reference: approximate square roots
-                        const float k = kk > 0.0f ? kk * rsqrtf(kk) : 0.0f;
-                        const float kr = k * a.inv_k0;
-                        const float den = fmaf(kr, kr, 1.0f);
-                        const float p = __fdividef(amp * k, den * den) * a.inv_vcell;
-                        sc = p > 0.0f ? p * rsqrtf(p) : 0.0f;
-                    }
-                    d = cscale(X, sc);
-                    if (!ONE || a.fields == XGEN_ETA) {
-                        const float kk1 = (kk == 0.0f) ? 1.0f : kk;
-                        et = eta_apply<false>(a.eta_comp, d, kxv, ky, kz_, kk1, a.vfac);
-                    }
-                }
+                float2 et = make_float2(0.f, 0.f);
+                if (!ONE || a.fields == XGEN_ETA) et = eta_apply<false>(a.eta_comp, mp.d[h], kxv, ky, mp.kz[h], mp.kk[h], a.vfac);
                 if (!ONE) {
-                    s[e * W + c0 + h] = d;
+                    s[e * W + c0 + h] = mp.d[h];
                     s[e * W + WC + c0 + h] = et;
                 } else {
-                    s[e * W + c0 + h] = a.fields == XGEN_DELTA ? d : et;
+                    s[e * W + c0 + h] = a.fields == XGEN_DELTA ? mp.d[h] : et;
                 }
             }
         }
         __syncthreads();
         fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
         const int cols = min(WC, a.nzh - cb * WC);
-        if (staged) {
-            const int64_t nxb = (int64_t)a.batch * a.nx;
-            const int mask = (1 << a.sh) - 1;
-            for (int idx = threadIdx.x; idx < n * W; idx += T) {
-                const int e = idx / W, l = idx % W;
-                const int c = l < WC ? l : l - WC;
-                if (c < cols) {
-                    float2* dst = !ONE ? (l < WC ? a.SA : a.SB) : (a.fields == XGEN_DELTA ? a.SA : a.SB);
-                    const int kz = cb * WC + c;
-                    const int64_t line = ((int64_t)(kz >> a.sh) * nxb + b * a.nx + e) * a.ny + yslot;
-                    if (dst) dst[(line << a.sh) | (kz & mask)] = s[idx];
-                }
-            }
-        } else {
-            const int64_t off = b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)cb * WC;
-            for (int idx = threadIdx.x; idx < n * W; idx += T) {
-                const int e = idx / W, l = idx % W;
-                const int c = l < WC ? l : l - WC;
-                if (c < cols) {
-                    float2* dst = !ONE ? (l < WC ? a.A : a.B) : (a.fields == XGEN_DELTA ? a.A : a.B);
-                    if (dst) dst[off + e * estride + c] = s[idx];
-                }
+        const int64_t off = b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)cb * WC;
+        for (int idx = threadIdx.x; idx < n * W; idx += T) {
+            const int e = idx / W, l = idx % W;
+            const int c = l < WC ? l : l - WC;
+            if (c < cols) {
+                float2* dst = !ONE ? (l < WC ? a.A : a.B) : (a.fields == XGEN_DELTA ? a.A : a.B);
+                if (dst) dst[off + e * estride + c] = s[idx];
             }
         }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ staged GPU noise
+// Large boxes: the modes are drawn once into the staged buffer (kgen_kernel, a streaming
+// write in address order), then each field's x inverse reads them back (xinv_kernel, one
+// launch per field, tiles k_z-block-major so a wave reads one compact block and writes rows of
+// one box only).  The x pass then touches at most one output box per launch without drawing
+// every mode twice.
+template <int T>
+__global__ void __launch_bounds__(T) kgen_kernel(const XGenArgs a) {
+    extern __shared__ float2 smem[];
+    float* kx = reinterpret_cast<float*>(smem);          // [nx] k_x of each x slot
+    int* ix = reinterpret_cast<int*>(kx + a.nx);          // [nx] frequency of each x slot
+    float* kyt = reinterpret_cast<float*>(ix + a.nx);     // [ny] k_y of each y slot
+    int* iyt = reinterpret_cast<int*>(kyt + a.ny);        // [ny] frequency of each y slot
+    float* kzt = reinterpret_cast<float*>(iyt + a.ny);    // [nzh]
+    for (int e = threadIdx.x; e < a.nx; e += T) {
+        const int f = freq_of_slot(a.pl, e);
+        ix[e] = f;
+        kx[e] = kaxis(f, a.nx, a.kfac, true);
+    }
+    for (int e = threadIdx.x; e < a.ny; e += T) {
+        const int f = freq_of_slot(a.ply, e);
+        iyt[e] = f;
+        kyt[e] = kaxis(f, a.ny, a.kfac, true);
+    }
+    for (int z = threadIdx.x; z < a.nzh; z += T) kzt[z] = kaxis(z, a.nz, a.kfac, false);
+    __syncthreads();
+    float amp = 0.f;
+    if (a.pk_mode == SMK_PK_ANALYTIC) amp = (float)(a.amp_host > 0.0 ? a.amp_host : *a.amp_dev);
+    const int wt = 1 << a.sh, npair = wt / 2;
+    const int64_t nkb = ceil_div(a.nzh, wt);
+    const int64_t items = nkb * a.batch * a.ny * (int64_t)a.nx * npair;   // k_z pairs in staged-address order
+    for (int64_t it = (int64_t)blockIdx.x * T + threadIdx.x; it < items; it += (int64_t)gridDim.x * T) {
+        const int pr = (int)(it % npair);
+        const int64_t line = it / npair;                  // (((kb * batch + b) * ny + yslot) * nx + e)
+        const int e = (int)(line % a.nx);
+        const int64_t r = line / a.nx;
+        const int yslot = (int)(r % a.ny);
+        const int64_t r2 = r / a.ny;
+        const int b = (int)(r2 % a.batch);
+        const int kb = (int)(r2 / a.batch);
+        const int kz0 = kb * wt + 2 * pr;
+        if (kz0 >= a.nzh) continue;
+        const int iy = iyt[yslot];
+        const ModePair mp = draw_pair(a, a.seed + (uint64_t)b, ix[e], iy, iy == 0 ? 0 : a.ny - iy, kx[e],
+                                      kyt[yslot], kz0, kzt, amp);
+        float4 v = make_float4(mp.d[0].x, mp.d[0].y, mp.d[1].x, mp.d[1].y);
+        *reinterpret_cast<float4*>(a.S + ((line << a.sh) | (2 * pr))) = v;
+    }
+}
+
+// x inverse of one field from the staged modes (fields = XGEN_DELTA or XGEN_ETA): the tile of
+// W = 2^sh k_z columns of (b, y slot) is one contiguous run of the staged buffer.
+// smem: s[n*W] | tw[n] | kx[n] | kzt[nzh]
+template <class C>
+__global__ void __launch_bounds__(C::T, C::MINB) xinv_kernel(const XGenArgs a) {
+    constexpr int W = C::W, T = C::T;
+    extern __shared__ float2 smem[];
+    const int n = a.pl.n;  // == nx
+    float2* s = smem;
+    float2* tw = s + n * W;
+    float* kx = reinterpret_cast<float*>(tw + n);
+    float* kzt = kx + n;
+    fill_twiddles<T>(tw, n);
+    for (int e = threadIdx.x; e < n; e += T) kx[e] = kaxis(freq_of_slot(a.pl, e), n, a.kfac, true);
+    for (int z = threadIdx.x; z < a.nzh; z += T) kzt[z] = kaxis(z, a.nz, a.kfac, false);
+    __syncthreads();
+    const bool eta = a.fields == XGEN_ETA;
+    float2* dst_box = eta ? a.B : a.A;
+    const int64_t nouter = (int64_t)a.batch * a.ny;
+    const int64_t nkb = ceil_div(a.nzh, W);
+    const int64_t ntiles = nouter * nkb;
+    const int64_t estride = (int64_t)a.ny * a.cp;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int kb = (int)(tile / nouter);
+        const int64_t o = tile - (int64_t)kb * nouter;    // b*ny + y slot
+        const int64_t b = o / a.ny;
+        const int yslot = (int)(o - b * a.ny);
+        const int cols = min(W, a.nzh - kb * W);
+        // the tile's staged run: n lines of W columns, contiguous
+        const float2* src = a.S + (((int64_t)kb * nouter + o) * n << a.sh);
+        load_cols_async<W, T>(s, src, n, W, cols);
+        cp_async_wait_all();
+        __syncthreads();
+        if (eta) {
+            const float ky = kaxis(freq_of_slot(a.ply, yslot), a.ny, a.kfac, true);
+            for (int idx = threadIdx.x; idx < n * W; idx += T) {
+                const int e = idx / W, w = idx % W;
+                if (w < cols) {
+                    const float kxv = kx[e], kz_ = kzt[kb * W + w];
+                    const float kk = __fadd_rn(__fadd_rn(__fmul_rn(kxv, kxv), __fmul_rn(ky, ky)), __fmul_rn(kz_, kz_));
+                    s[idx] = eta_apply<false>(a.eta_comp, s[idx], kxv, ky, kz_, kk == 0.0f ? 1.0f : kk, a.vfac);
+                }
+            }
+            __syncthreads();
+        }
+        fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
+        store_cols<W, T>(s, dst_box + b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)kb * W, n,
+                         estride, cols);
         __syncthreads();
     }
 }
@@ -741,6 +822,19 @@ static int launch_xgen(const XGenArgs& a, cudaStream_t st) {
     return check_launch("xgen_kernel");
 }
 
+template <class C>
+static int launch_xinv(const XGenArgs& a, cudaStream_t st) {
+    if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xinv_kernel");
+    if ((1 << a.sh) != C::W) return fail(SMK_EINVAL, "xinv_kernel: staged block width differs from the tile's");
+    const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 4 +
+                        (size_t)a.nzh * 4 + 16;
+    const int64_t ntiles = (int64_t)a.batch * a.ny * ceil_div(a.nzh, C::W);
+    int grid = 0, rc;
+    if ((rc = persistent_grid(xinv_kernel<C>, C::T, smem, ntiles, &grid))) return rc;
+    xinv_kernel<C><<<grid, C::T, smem, st>>>(a);
+    return check_launch("xinv_kernel");
+}
+
 // ------------------------------------------------------------------ tile variants
 struct TileVariant {
     int w, t, nmax;  // columns (line pairs for z passes, lines for xgen) per tile, threads, max length
@@ -775,5 +869,9 @@ int run_zinv(int v, const ZInvArgs& a, int64_t rows_per_box, cudaStream_t st);
 int run_line(int v, const LineArgs& a, bool inv, cudaStream_t st);
 int run_xpass(int v, const XArgs& a, cudaStream_t st);
 int run_xgen(int v, const XGenArgs& a, cudaStream_t st);
+// Staged GPU noise: draw into a.S (block width 2^a.sh), then the x inverse of a.fields from it
+// (tile variant v of the x pass; its W must be 2^a.sh).
+int run_kgen(const XGenArgs& a, cudaStream_t st);
+int run_xinv(int v, const XGenArgs& a, cudaStream_t st);
 
 }  // namespace smk

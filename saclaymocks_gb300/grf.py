@@ -80,7 +80,7 @@ def alloc_boxes(nx: int, ny: int, nz: int, batch: int = 1, want_eta: bool = True
 
 class GrfWorkspace:
     """Device workspace + stats buffer reused by repeated calls.  The workspace grows on
-    demand to smk_grf_workspace_size (the k-space staging buffer of large GPU-noise calls)."""
+    demand to smk_grf_workspace_size (the staged modes of GPU-noise calls with staging)."""
 
     def __init__(self, batch: int, device="cuda"):
         self.device = device
@@ -119,9 +119,8 @@ def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: flo
              "yy", "xy", "xz", "yz"; bin/make_boxes.py:315-391), or a velocity
              v_i = irfftn(-i k_i / k^2 * vel_factor * delta_k) ("vx", "vy", "vz";
              bin/make_boxes.py:393-431, vel_factor = H0 * dD/dz(z=0)).
-    staging: GPU noise with eta: stage the x pass's output in column blocks (workspace grows by
-             one box of complex floats).  Off by default: on GB300 at 2560^2 x 1536 it measured
-             99.3 ms for the x pass against 95.7 ms for the in-place two-launch form.
+    staging: GPU noise with eta: draw every mode once into the workspace (it grows by about
+             one box of complex floats), then one x inverse per field reads them back.
     """
     ny = nx if ny is None else ny
     nz = nx if nz is None else nz
