@@ -142,9 +142,13 @@ int smk_tune_get(int32_t pass, int32_t n);
  *     delta + eta boxes span more than 64 GiB, where one launch's spread of rows outruns
  *     address translation);
  *   SMK_TUNE_PREFETCH: the y and z passes pull their next tile into L2 while transforming the
- *     current one (1, default) or not (0). */
+ *     current one (1, default) or not (0);
+ *   SMK_TUNE_XGEN_CLUSTER: GPU-noise x pass with eta on clusters of four CTAs, each mode drawn
+ *     once and both fields written in one launch with row segments twice the one-CTA tile's
+ *     width (1), never (0), or by the built-in rule (-1, default). */
 #define SMK_TUNE_XGEN_SPLIT 0
 #define SMK_TUNE_PREFETCH 1
+#define SMK_TUNE_XGEN_CLUSTER 2
 int smk_tune_flag(int32_t flag, int32_t value, int32_t* previous);
 
 /* ---------------------------------------------------------------- skewers (make_spectra +

@@ -4,8 +4,8 @@ the kernels' GPU-noise modes against the oracle on identical white noise.
 Philox4x32-10 is the counter-based generator of Salmon, Moraes, Dror & Shaw, "Parallel
 random numbers: as easy as 1, 2, 3" (SC'11).  The counter/key layout and the uniform ->
 Gaussian mapping follow saclaymocks_gb300/csrc/smk_common.cuh: block (q, row, tag) keyed
-by the 64-bit seed gives four uint32 x0..x3; u = ((x >> 8) + 1) 2^-24 in (0,1],
-t = (x >> 8) 2^-23 in [0,2); (g0, g1) = sqrt(-2 ln u(x0)) (cos, sin)(pi t(x1)), same for
+by the 64-bit seed gives four uint32 x0..x3; with m = x >> 9 (23 bits), u = 1 - m 2^-23 in
+(0,1], t = m 2^-22 in [0,2); (g0, g1) = sqrt(-2 ln u(x0)) (cos, sin)(pi t(x1)), same for
 (x2, x3).  TEST INFRASTRUCTURE ONLY (float64 arithmetic; the GPU computes in float32).
 """
 from __future__ import annotations
@@ -36,8 +36,8 @@ def philox4x32_10(c0, c1, c2, c3, seed: int):
 def gauss4(x):
     out = []
     for h in range(2):
-        u1 = ((x[2 * h] >> np.uint64(8)) + np.uint64(1)).astype(np.float64) * 2.0 ** -24
-        t = (x[2 * h + 1] >> np.uint64(8)).astype(np.float64) * 2.0 ** -23
+        u1 = 1.0 - (x[2 * h] >> np.uint64(9)).astype(np.float64) * 2.0 ** -23
+        t = (x[2 * h + 1] >> np.uint64(9)).astype(np.float64) * 2.0 ** -22
         rad = np.sqrt(-2.0 * np.log(u1))
         out += [rad * np.cos(np.pi * t), rad * np.sin(np.pi * t)]
     return out

@@ -142,7 +142,7 @@ def load(path: str | None = None):
     return lib
 
 
-SMK_TUNE_XGEN_SPLIT, SMK_TUNE_PREFETCH = 0, 1
+SMK_TUNE_XGEN_SPLIT, SMK_TUNE_PREFETCH, SMK_TUNE_XGEN_CLUSTER = 0, 1, 2
 
 
 def tune_flag(flag: int, value: int) -> int:
@@ -155,6 +155,12 @@ def tune_flag(flag: int, value: int) -> int:
 def xgen_split(mode: int) -> int:
     """x-pass launch mode (-1 by footprint, 0 one launch, 1 two launches); returns the previous."""
     return tune_flag(SMK_TUNE_XGEN_SPLIT, mode)
+
+
+def xgen_cluster(mode: int) -> int:
+    """x pass on four-CTA clusters (-1 built-in rule, 0 never, 1 whenever eta is drawn);
+    returns the previous value."""
+    return tune_flag(SMK_TUNE_XGEN_CLUSTER, mode)
 
 
 def check(status: int, what: str = ""):

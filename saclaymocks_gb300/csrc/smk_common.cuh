@@ -100,22 +100,23 @@ __host__ __device__ __forceinline__ u32x4 philox4x32_10(u32x4 ctr, uint32_t k0, 
 // counter spaces.
 enum : uint32_t { STREAM_KMODE = 0x4Bu, STREAM_SKEWER = 0x53u };
 
-// Four N(0,1) deviates from one Philox block: Box-Muller on (u0,u1) and (u2,u3) with
-// u = ((x >> 8) + 1) * 2^-24 in (0, 1] for the radius and (x >> 8) * 2^-23 in [0, 2)
-// as the angle in units of pi (both exact in float32).  The angle is evaluated as
-// pi (t - 1) in [-pi, pi) with the hardware sine/cosine (absolute error < 4e-7 there) and
-// the signs flipped back; the radius -2 ln u uses the hardware base-2 logarithm (absolute
-// error ~1e-7 near u = 1, so deviates of radius < 0.01, probability 5e-5, carry absolute
-// errors up to ~1e-5) and the reciprocal square root.
+// Four N(0,1) deviates from one Philox block: Box-Muller on (x0,x1) and (x2,x3).  The top
+// 23 bits m of each word become floats by exponent insertion (no integer conversion):
+// v = 1 + m 2^-23 in [1, 2), exact; u = 2 - v = 1 - m 2^-23 in (0, 1] for the radius and
+// pi (2v - 3) in [-pi, pi) for the angle, i.e. pi (t - 1) with t = m 2^-22 in [0, 2).  The
+// angle uses the hardware sine/cosine (absolute error < 4e-7 on [-pi, pi)) with the signs
+// flipped back; the radius -2 ln u the hardware base-2 logarithm (absolute error ~1e-7 near
+// u = 1, so deviates of radius < 0.01, probability 5e-5, carry absolute errors up to ~1e-5)
+// and the reciprocal square root.
 __device__ __forceinline__ void gauss4(u32x4 r, float g[4]) {
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-        const float u1 = (float)((r.v[2 * h] >> 8) + 1u) * 5.9604644775390625e-08f;  // 2^-24
-        const float t = (float)(r.v[2 * h + 1] >> 8) * 1.1920928955078125e-07f;       // 2^-23
+        const float u1 = 2.0f - __uint_as_float(0x3F800000u | (r.v[2 * h] >> 9));
+        const float v = __uint_as_float(0x3F800000u | (r.v[2 * h + 1] >> 9));
         const float x = -1.3862943611198906f * __log2f(u1);                             // -2 ln 2 log2(u)
         const float rad = x > 0.0f ? x * rsqrtf(x) : 0.0f;
         float s, c;
-        __sincosf(fmaf(t, 3.14159265358979f, -3.14159265358979f), &s, &c);
+        __sincosf(fmaf(v, 6.28318530717958648f, -9.42477796076937972f), &s, &c);
         g[2 * h] = -rad * c;
         g[2 * h + 1] = -rad * s;
     }

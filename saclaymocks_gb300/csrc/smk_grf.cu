@@ -65,6 +65,7 @@ static struct ChoiceInit {
 
 static std::atomic<int> g_xgen_split{-1};  // -1: by footprint, 0: never, 1: always
 static std::atomic<int> g_prefetch{1};     // L2 prefetch of the next tile in the y and z passes
+static std::atomic<int> g_xgen_cluster{-1}; // -1: by default rule, 0: never, 1: when eta is drawn
 
 static int length_class(int n) { return n <= 512 ? 0 : n <= 1024 ? 1 : n <= 2560 ? 2 : 3; }
 
@@ -279,9 +280,10 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
             // address-translation reach and the pass slows by 1.7x; writing delta and eta in
             // two launches keeps each wave within one box.
             const double pair_bytes = 2.0 * 4.0 * (double)p->batch * p->nx * p->ny * (double)pitch;
-            const int sm = g_xgen_split.load();
-            const bool split = p->want_eta && (sm < 0 ? pair_bytes > 64.0 * (1ull << 30) : sm == 1);
-            ga.fields = !p->want_eta ? XGEN_DELTA : (split ? XGEN_DELTA : XGEN_BOTH);
+            const int sm = g_xgen_split.load(), cm = g_xgen_cluster.load();
+            const bool cluster = p->want_eta && cm == 1;
+            const bool split = !cluster && p->want_eta && (sm < 0 ? pair_bytes > 64.0 * (1ull << 30) : sm == 1);
+            ga.fields = !p->want_eta ? XGEN_DELTA : (cluster ? XGEN_CLUSTER : (split ? XGEN_DELTA : XGEN_BOTH));
             if ((rc = run_xgen(vx, ga, st))) return rc;
             if (split) {
                 ga.fields = XGEN_ETA;
@@ -351,6 +353,9 @@ int smk_tune_flag(int32_t flag, int32_t value, int32_t* previous) {
     if (flag == SMK_TUNE_XGEN_SPLIT) {
         if (value < -1 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: XGEN_SPLIT must be -1, 0 or 1");
         old = g_xgen_split.exchange(value);
+    } else if (flag == SMK_TUNE_XGEN_CLUSTER) {
+        if (value < -1 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: XGEN_CLUSTER must be -1, 0 or 1");
+        old = g_xgen_cluster.exchange(value);
     } else if (flag == SMK_TUNE_PREFETCH) {
         if (value < 0 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: PREFETCH must be 0 or 1");
         old = g_prefetch.exchange(value);

@@ -16,9 +16,13 @@
 #include <algorithm>
 #include <atomic>
 
+#include <cooperative_groups.h>
+
 #include "smk_fft.cuh"
 
 namespace smk {
+
+namespace cg = cooperative_groups;
 
 // W lines (or row pairs) per tile, T threads, largest FFT radix R in registers, at least B
 // resident blocks per SM requested from the register allocator.
@@ -327,17 +331,51 @@ struct XGenArgs {
     int sh;
 };
 
-// delta_k = X * sqrt(P/Vcell) of the modes (ix, iy, kz0) and (ix, iy, kz0 + 1) of one box
-// (GPU noise): Philox4x32-10 block (kz0/2, ix, iy, STREAM_KMODE) keyed by seed, Box-Muller,
-// Re/Im ~ N(0, N/2); on the kz = 0 and nz/2 planes the lower flat index of (ix, iy) and
-// (-ix, -iy) owns the draw and self-conjugate modes are real with variance N.  Also returns
-// k_z and k^2 per mode for the eta split; kz >= nzh gives 0.
+// GPU-noise mode arithmetic (no bit-level reference: the FP64 oracle restates the drawn modes
+// and the boxes are compared within the FP32 tolerance).  k^2 is formed as numpy does it
+// (kx*kx + ky*ky + kz*kz, no contraction); r = 1/k from the hardware reciprocal square root;
+// 1/k^2 = r*r (1 at k = 0, where the reference sets k^2[0,0,0] = 1).
+__device__ __forceinline__ float mode_k2(float kxv, float ky, float kz) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(kxv, kxv), __fmul_rn(ky, ky)), __fmul_rn(kz, kz));
+}
+__device__ __forceinline__ float mode_inv_k2(float kk) {
+    const float r = rsqrtf(kk);
+    return kk > 0.0f ? r * r : 1.0f;
+}
+
+// Second output of the GPU-noise x pass from delta_k and 1/k^2: eta_ij = k_i k_j / k^2 delta_k,
+// or velocity v_i = -i k_i / k^2 * vfac * delta_k (SMK_ETA_VX/VY/VZ).
+__device__ __forceinline__ float2 eta_from_inv_k2(int comp, float2 d, float kx, float ky, float kz, float ikk,
+                                                  float vfac) {
+    if (comp >= SMK_ETA_VX) {
+        const float ki = comp == SMK_ETA_VX ? kx : (comp == SMK_ETA_VY ? ky : kz);
+        const float f = ki * ikk * vfac;
+        return make_float2(d.y * f, -d.x * f);
+    }
+    return cscale(d, eta_num(comp, kx, ky, kz) * ikk);
+}
+
+// Per-launch constant of the analytic P(k) scale: sqrt(N/2) * sqrt(A / Vcell), so that
+// sqrt(N/2) * sqrt(P(k)/Vcell) = scale_c / sqrt((1 + k^2/k0^2)^2 / k) for P = A k/(1+(k/k0)^2)^2.
+__device__ __forceinline__ float pk_scale_c(const XGenArgs& a) {
+    if (a.pk_mode != SMK_PK_ANALYTIC) return a.sig_c;
+    const float amp = (float)(a.amp_host > 0.0 ? a.amp_host : *a.amp_dev);
+    return a.sig_c * sqrtf(amp * a.inv_vcell);
+}
+
+// delta_k of the modes (ix, iy, kz0) and (ix, iy, kz0 + 1) of one box (GPU noise):
+// Philox4x32-10 block (kz0/2, ix, iy, STREAM_KMODE) keyed by seed, Box-Muller, Re/Im ~ N(0, N/2),
+// times sqrt(P/Vcell).  CHECK (tiles holding the kz = 0 or nz/2 plane, or columns past nzh):
+// on the kz = 0 and nz/2 planes the lower flat index of (ix, iy) and (-ix, -iy) owns the draw
+// and self-conjugate modes are real with variance N; kz >= nzh gives 0.  Also returns k_z and
+// 1/k^2 per mode for the eta split.
 struct ModePair {
     float2 d[2];
-    float kz[2], kk[2];
+    float kz[2], ikk[2];
 };
+template <bool CHECK>
 __device__ __forceinline__ ModePair draw_pair(const XGenArgs& a, uint64_t seed, int ixe, int iy, int iym,
-                                              float kxv, float ky, int kz0, const float* kzt, float amp) {
+                                              float kxv, float ky, int kz0, const float* kzt, float scale_c) {
     ModePair mp;
     float g[4];
     {
@@ -348,19 +386,22 @@ __device__ __forceinline__ ModePair draw_pair(const XGenArgs& a, uint64_t seed, 
         ctr.v[3] = STREAM_KMODE;
         gauss4(philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32)), g);
     }
-    const int half = a.nz / 2;
+    const float inv_k0sq = a.inv_k0 * a.inv_k0;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const int kz = kz0 + h;
-        mp.d[h] = make_float2(0.f, 0.f);
-        mp.kz[h] = 0.f;
-        mp.kk[h] = 1.f;
-        if (kz < a.nzh) {
-            float2 X = make_float2(a.sig_c * g[2 * h], a.sig_c * g[2 * h + 1]);
-            if (kz == 0 || kz == half) {
+        float2 X = make_float2(g[2 * h], g[2 * h + 1]);
+        float sc = scale_c;
+        if (CHECK) {
+            mp.d[h] = make_float2(0.f, 0.f);
+            mp.kz[h] = 0.f;
+            mp.ikk[h] = 1.f;
+            if (kz >= a.nzh) continue;
+            if (kz == 0 || kz == a.nz / 2) {
                 const int ixm = ixe == 0 ? 0 : a.nx - ixe;
                 if (ixm == ixe && iym == iy) {
-                    X = make_float2(a.sig_r * g[2 * h], 0.f);
+                    X = make_float2(g[2 * h], 0.f);
+                    sc *= a.sig_r / a.sig_c;
                 } else if ((int64_t)ixe * a.ny + iy > (int64_t)ixm * a.ny + iym) {
                     // the partner (-kx, -ky) owns the draw: take its conjugate
                     u32x4 ctr;
@@ -370,30 +411,32 @@ __device__ __forceinline__ ModePair draw_pair(const XGenArgs& a, uint64_t seed, 
                     ctr.v[3] = STREAM_KMODE;
                     float gm[4];
                     gauss4(philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32)), gm);
-                    X = make_float2(a.sig_c * gm[2 * h], -a.sig_c * gm[2 * h + 1]);
+                    X = make_float2(gm[2 * h], -gm[2 * h + 1]);
                 }
             }
-            const float kz_ = kzt[kz];
-            const float kk = __fadd_rn(__fadd_rn(__fmul_rn(kxv, kxv), __fmul_rn(ky, ky)), __fmul_rn(kz_, kz_));
-            float sc;
-            if (a.pk_mode == SMK_PK_GRID) {
-                sc = __ldg(a.grid + ((int64_t)ixe * a.ny + iy) * a.nzh + kz);
-            } else {
-                // GPU noise has no bit-level reference: approximate square roots
-                const float k = kk > 0.0f ? kk * rsqrtf(kk) : 0.0f;
-                const float kr = k * a.inv_k0;
-                const float den = fmaf(kr, kr, 1.0f);
-                const float p = __fdividef(amp * k, den * den) * a.inv_vcell;
-                sc = p > 0.0f ? p * rsqrtf(p) : 0.0f;
-            }
-            mp.d[h] = cscale(X, sc);
-            mp.kz[h] = kz_;
-            mp.kk[h] = (kk == 0.0f) ? 1.0f : kk;
         }
+        const float kz_ = kzt[kz];
+        const float kk = mode_k2(kxv, ky, kz_);
+        const float r = rsqrtf(kk);   // 1/k (+inf at k = 0)
+        if (a.pk_mode == SMK_PK_GRID) {
+            sc *= __ldg(a.grid + ((int64_t)ixe * a.ny + iy) * a.nzh + kz);
+        } else {
+            // sqrt(k)/den = 1/sqrt(den^2/k): one reciprocal square root (0 at k = 0)
+            const float den = fmaf(kk, inv_k0sq, 1.0f);
+            sc *= rsqrtf(den * den * r);
+        }
+        mp.d[h] = cscale(X, sc);
+        mp.kz[h] = kz_;
+        mp.ikk[h] = kk > 0.0f ? r * r : 1.0f;
     }
     return mp;
 }
-enum { XGEN_BOTH = 0, XGEN_DELTA = 1, XGEN_ETA = 2 };
+enum { XGEN_BOTH = 0, XGEN_DELTA = 1, XGEN_ETA = 2, XGEN_CLUSTER = 3 };
+
+// True when the k_z columns [c0, c0 + w) include the kz = 0 or nz/2 plane or run past nzh.
+__device__ __forceinline__ bool tile_needs_check(const XGenArgs& a, int c0, int w) {
+    return c0 == 0 || (c0 <= a.nz / 2 && a.nz / 2 < c0 + w) || c0 + w > a.nzh;
+}
 
 // smem: s[n*W] | tw[n] | kx[n] | ix[n] | kzt[nzh]
 // ONE: one field per launch (a.fields = XGEN_DELTA or XGEN_ETA, W columns per tile), else
@@ -418,8 +461,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
     }
     for (int z = threadIdx.x; z < a.nzh; z += T) kzt[z] = kaxis(z, a.nz, a.kfac, false);
     __syncthreads();
-    float amp = 0.f;
-    if (a.pk_mode == SMK_PK_ANALYTIC) amp = (float)(a.amp_host > 0.0 ? a.amp_host : *a.amp_dev);
+    const float scale_c = pk_scale_c(a);
     const int64_t ncolt = ceil_div(a.nzh, WC);
     const int64_t nouter = (int64_t)a.batch * a.ny;
     const int64_t ntiles = nouter * ncolt;
@@ -433,23 +475,29 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
         const int iym = iy == 0 ? 0 : a.ny - iy;
         const float ky = kaxis(iy, a.ny, a.kfac, true);
         const uint64_t seed = a.seed + (uint64_t)b;
-        for (int idx = threadIdx.x; idx < n * NP; idx += T) {
-            const int e = idx / NP, pr = idx % NP;
-            const int c0 = 2 * pr, kz0 = cb * WC + c0;
-            const float kxv = kx[e];
-            const ModePair mp = draw_pair(a, seed, ix[e], iy, iym, kxv, ky, kz0, kzt, amp);
+        auto draw = [&](auto chk) {
+            for (int idx = threadIdx.x; idx < n * NP; idx += T) {
+                const int e = idx / NP, pr = idx % NP;
+                const int c0 = 2 * pr, kz0 = cb * WC + c0;
+                const float kxv = kx[e];
+                const ModePair mp = draw_pair<decltype(chk)::value>(a, seed, ix[e], iy, iym, kxv, ky, kz0, kzt, scale_c);
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                float2 et = make_float2(0.f, 0.f);
-                if (!ONE || a.fields == XGEN_ETA) et = eta_apply<false>(a.eta_comp, mp.d[h], kxv, ky, mp.kz[h], mp.kk[h], a.vfac);
-                if (!ONE) {
-                    s[e * W + c0 + h] = mp.d[h];
-                    s[e * W + WC + c0 + h] = et;
-                } else {
-                    s[e * W + c0 + h] = a.fields == XGEN_DELTA ? mp.d[h] : et;
+                for (int h = 0; h < 2; ++h) {
+                    float2 et = make_float2(0.f, 0.f);
+                    if (!ONE || a.fields == XGEN_ETA) et = eta_from_inv_k2(a.eta_comp, mp.d[h], kxv, ky, mp.kz[h], mp.ikk[h], a.vfac);
+                    if (!ONE) {
+                        s[e * W + c0 + h] = mp.d[h];
+                        s[e * W + WC + c0 + h] = et;
+                    } else {
+                        s[e * W + c0 + h] = a.fields == XGEN_DELTA ? mp.d[h] : et;
+                    }
                 }
             }
-        }
+        };
+        if (tile_needs_check(a, cb * WC, WC))
+            draw(std::true_type{});
+        else
+            draw(std::false_type{});
         __syncthreads();
         fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
         const int cols = min(WC, a.nzh - cb * WC);
@@ -463,6 +511,112 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
             }
         }
         __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ clustered GPU-noise x pass
+// Both fields in one launch with every mode drawn once, on clusters of four CTAs.  A tile is
+// 2W k_z columns of one (box, y slot); CTA rank r = h + 2f holds the W columns of half h for
+// field f (0 delta, 1 eta) in its shared memory.  Each mode is drawn once, by CTA (h, f) for
+// the x slots of half f, which stores delta_k into CTA (h, 0) and eta_k into CTA (h, 1)
+// (distributed shared memory); every CTA then takes the x inverse of its W lines; CTA (h, f)
+// finally writes field f for the x slots of half h, all 2W columns, so each output row
+// segment is 2W * 8 bytes (128 B for W = 8) rather than the W * 8 of a one-CTA tile.
+// smem: s[n*W] | tw[n] | kx[n] | ix[n] | kzt[nzh]  (same offsets in every CTA of the cluster)
+template <class C>
+__global__ void __launch_bounds__(C::T, C::MINB) xgc_kernel(const XGenArgs a) {
+    constexpr int W = C::W, T = C::T;
+    constexpr int NP = W / 2;  // mode pairs per row of one CTA's columns
+    static_assert(W % 2 == 0, "xgc tiles hold column pairs");
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const int h = rank & 1, f = rank >> 1;
+    extern __shared__ float2 smem[];
+    const int n = a.pl.n;  // == nx
+    float2* s = smem;
+    float2* tw = s + n * W;
+    float* kx = reinterpret_cast<float*>(tw + n);
+    int* ix = reinterpret_cast<int*>(kx + n);
+    float* kzt = reinterpret_cast<float*>(ix + n);
+    fill_twiddles<T>(tw, n);
+    for (int e = threadIdx.x; e < n; e += T) {
+        const int fr = freq_of_slot(a.pl, e);
+        ix[e] = fr;
+        kx[e] = kaxis(fr, n, a.kfac, true);
+    }
+    for (int z = threadIdx.x; z < a.nzh; z += T) kzt[z] = kaxis(z, a.nz, a.kfac, false);
+    // every CTA of the cluster has started (and filled its tables) before any remote access
+    cl.sync();
+    // the partners' tiles (this CTA's own through its local shared address)
+    float2* s_delta = f == 0 ? s : cl.map_shared_rank(s, h);       // (h, delta): draw target
+    float2* s_eta = f == 1 ? s : cl.map_shared_rank(s, h | 2);     // (h, eta): draw target
+    const float2* s_lo = h == 0 ? s : cl.map_shared_rank(s, f << 1);       // (0, f): columns 0..W-1
+    const float2* s_hi = h == 1 ? s : cl.map_shared_rank(s, 1 | (f << 1)); // (1, f): columns W..2W-1
+    const float scale_c = pk_scale_c(a);
+    const int nh = n / 2;
+    const int ea0 = f ? nh : 0, ea1 = f ? n : nh;  // x slots this CTA draws
+    const int ec0 = h ? nh : 0, ec1 = h ? n : nh;  // x slots this CTA writes
+    const int64_t ncolt = ceil_div(a.nzh, 2 * W);
+    const int64_t ntiles = (int64_t)a.batch * a.ny * ncolt;
+    const int64_t estride = (int64_t)a.ny * a.cp;
+    const int64_t ncl = gridDim.x / 4;
+    for (int64_t tile = blockIdx.x / 4; tile < ntiles; tile += ncl) {
+        const int64_t o = tile / ncolt;  // b*ny + y slot
+        const int cb = (int)(tile - o * ncolt);
+        const int64_t b = o / a.ny;
+        const int yslot = (int)(o - b * a.ny);
+        const int iy = freq_of_slot(a.ply, yslot);
+        const int iym = iy == 0 ? 0 : a.ny - iy;
+        const float ky = kaxis(iy, a.ny, a.kfac, true);
+        const uint64_t seed = a.seed + (uint64_t)b;
+        const int col0 = cb * 2 * W + h * W;
+        auto draw = [&](auto chk) {
+            for (int idx = threadIdx.x; idx < (ea1 - ea0) * NP; idx += T) {
+                const int e = ea0 + idx / NP, pr = idx % NP;
+                const float kxv = kx[e];
+                const ModePair mp = draw_pair<decltype(chk)::value>(a, seed, ix[e], iy, iym, kxv, ky, col0 + 2 * pr, kzt, scale_c);
+                const float2 e0 = eta_from_inv_k2(a.eta_comp, mp.d[0], kxv, ky, mp.kz[0], mp.ikk[0], a.vfac);
+                const float2 e1 = eta_from_inv_k2(a.eta_comp, mp.d[1], kxv, ky, mp.kz[1], mp.ikk[1], a.vfac);
+                *reinterpret_cast<float4*>(s_delta + e * W + 2 * pr) = make_float4(mp.d[0].x, mp.d[0].y, mp.d[1].x, mp.d[1].y);
+                *reinterpret_cast<float4*>(s_eta + e * W + 2 * pr) = make_float4(e0.x, e0.y, e1.x, e1.y);
+            }
+        };
+        if (tile_needs_check(a, col0, W))
+            draw(std::true_type{});
+        else
+            draw(std::false_type{});
+        cl.sync();
+        fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
+        cl.sync();
+        const int cols = min(2 * W, a.nzh - cb * 2 * W);
+        float2* dst = (f ? a.B : a.A) + b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)cb * 2 * W;
+        // U independent (partly remote) shared loads in flight per thread before the stores
+        constexpr int U = 4;
+        const int items = (ec1 - ec0) * W;
+        for (int base = threadIdx.x; base < items; base += U * T) {
+            float4 v[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int idx = base + u * T;
+                if (idx < items) {
+                    const int e = ec0 + idx / W, c = 2 * (idx % W);  // columns c, c + 1 of 2W
+                    v[u] = *reinterpret_cast<const float4*>((c < W ? s_lo : s_hi) + e * W + (c & (W - 1)));
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int idx = base + u * T;
+                if (idx < items) {
+                    const int e = ec0 + idx / W, c = 2 * (idx % W);
+                    float2* d = dst + e * estride + c;
+                    if (c + 1 < cols)
+                        *reinterpret_cast<float4*>(d) = v[u];
+                    else if (c < cols)
+                        *d = make_float2(v[u].x, v[u].y);
+                }
+            }
+        }
+        cl.sync();
     }
 }
 
@@ -492,8 +646,7 @@ __global__ void __launch_bounds__(T) kgen_kernel(const XGenArgs a) {
     }
     for (int z = threadIdx.x; z < a.nzh; z += T) kzt[z] = kaxis(z, a.nz, a.kfac, false);
     __syncthreads();
-    float amp = 0.f;
-    if (a.pk_mode == SMK_PK_ANALYTIC) amp = (float)(a.amp_host > 0.0 ? a.amp_host : *a.amp_dev);
+    const float scale_c = pk_scale_c(a);
     const int wt = 1 << a.sh, npair = wt / 2;
     const int64_t nkb = ceil_div(a.nzh, wt);
     const int64_t items = nkb * a.batch * a.ny * (int64_t)a.nx * npair;   // k_z pairs in staged-address order
@@ -509,8 +662,8 @@ __global__ void __launch_bounds__(T) kgen_kernel(const XGenArgs a) {
         const int kz0 = kb * wt + 2 * pr;
         if (kz0 >= a.nzh) continue;
         const int iy = iyt[yslot];
-        const ModePair mp = draw_pair(a, a.seed + (uint64_t)b, ix[e], iy, iy == 0 ? 0 : a.ny - iy, kx[e],
-                                      kyt[yslot], kz0, kzt, amp);
+        const ModePair mp = draw_pair<true>(a, a.seed + (uint64_t)b, ix[e], iy, iy == 0 ? 0 : a.ny - iy, kx[e],
+                                            kyt[yslot], kz0, kzt, scale_c);
         float4 v = make_float4(mp.d[0].x, mp.d[0].y, mp.d[1].x, mp.d[1].y);
         *reinterpret_cast<float4*>(a.S + ((line << a.sh) | (2 * pr))) = v;
     }
@@ -555,8 +708,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xinv_kernel(const XGenArgs a) {
                 const int e = idx / W, w = idx % W;
                 if (w < cols) {
                     const float kxv = kx[e], kz_ = kzt[kb * W + w];
-                    const float kk = __fadd_rn(__fadd_rn(__fmul_rn(kxv, kxv), __fmul_rn(ky, ky)), __fmul_rn(kz_, kz_));
-                    s[idx] = eta_apply<false>(a.eta_comp, s[idx], kxv, ky, kz_, kk == 0.0f ? 1.0f : kk, a.vfac);
+                    s[idx] = eta_from_inv_k2(a.eta_comp, s[idx], kxv, ky, kz_, mode_inv_k2(mode_k2(kxv, ky, kz_)), a.vfac);
                 }
             }
             __syncthreads();
@@ -805,7 +957,11 @@ static int launch_xpass(const XArgs& a, cudaStream_t st) {
 }
 
 template <class C>
+static int launch_xgc(const XGenArgs& a, cudaStream_t st);
+
+template <class C>
 static int launch_xgen(const XGenArgs& a, cudaStream_t st) {
+    if (a.fields == XGEN_CLUSTER) return launch_xgc<C>(a, st);
     if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xgen_kernel");
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 +
                         (size_t)a.nzh * 4 + 16;
@@ -820,6 +976,36 @@ static int launch_xgen(const XGenArgs& a, cudaStream_t st) {
         xgen_kernel<C, false><<<grid, C::T, smem, st>>>(a);
     }
     return check_launch("xgen_kernel");
+}
+
+// Clusters of four CTAs (xgc_kernel), as many as can be resident, at most one per tile.
+template <class C>
+static int launch_xgc(const XGenArgs& a, cudaStream_t st) {
+    if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xgc_kernel");
+    const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 +
+                        (size_t)a.nzh * 4 + 16;
+    const int64_t ntiles = (int64_t)a.batch * a.ny * ceil_div(a.nzh, 2 * C::W);
+    if (cudaFuncSetAttribute(xgc_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return check_launch("cudaFuncSetAttribute(xgc)");
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 4;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(C::T, 1, 1);
+    cfg.gridDim = dim3(4 * sm_count(), 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, xgc_kernel<C>, &cfg) != cudaSuccess)
+        return check_launch("cudaOccupancyMaxActiveClusters(xgc)");
+    if (nclusters < 1) return fail(SMK_ENOTSUPP, "xgc_kernel: no cluster of 4 fits (smem %zu B)", smem);
+    cfg.gridDim = dim3((unsigned)(4 * std::min<int64_t>(nclusters, ntiles)), 1, 1);
+    if (cudaLaunchKernelEx(&cfg, xgc_kernel<C>, a) != cudaSuccess) return check_launch("xgc_kernel");
+    return check_launch("xgc_kernel");
 }
 
 template <class C>

@@ -37,6 +37,56 @@ def _check(gpu, ref, tag):
     assert ma <= MAX_ABS_SIGMA, f"{tag}: max abs / sigma {ma:.3e}"
 
 
+@pytest.mark.parametrize("shape", [(40, 24, 36), (45, 18, 50), (64, 20, 12), (30, 6, 160)])
+def test_xgen_cluster_equals_split_launches(G, shape):
+    """The four-CTA cluster form of the GPU-noise x pass (each mode drawn once, both fields in
+    one launch) gives the same boxes, bit for bit, as two one-field launches; also for odd nx,
+    k_z extents that end inside a tile, batches and a velocity component."""
+    from saclaymocks_gb300 import _lib
+    nx, ny, nz = shape
+    ps, pc = _lib.xgen_split(1), _lib.xgen_cluster(0)
+    try:
+        ref = G.make_boxes(nx, ny, nz, 2.19, seed=23, batch=2)
+        refv = G.make_boxes(nx, ny, nz, 2.19, seed=24, eta_comp="vy", vel_factor=100.0)
+        _lib.xgen_cluster(1)
+        got = G.make_boxes(nx, ny, nz, 2.19, seed=23, batch=2)
+        gotv = G.make_boxes(nx, ny, nz, 2.19, seed=24, eta_comp="vy", vel_factor=100.0)
+        torch.cuda.synchronize()
+    finally:
+        _lib.xgen_split(ps)
+        _lib.xgen_cluster(pc)
+    assert torch.equal(got.delta, ref.delta)
+    assert torch.equal(got.eta, ref.eta)
+    assert torch.equal(gotv.eta, refv.eta)
+    np.testing.assert_array_equal(got.sigma(), ref.sigma())
+
+
+def test_xgen_cluster_every_variant_is_exact(G):
+    """Every x-pass tile variant run in the cluster form matches the FP64 oracle."""
+    import ctypes as C
+    from saclaymocks_gb300 import _lib, tune
+    lib = _lib.load()
+    pid = _lib.SMK_PASS_XGEN
+    pc = _lib.xgen_cluster(1)
+    try:
+        for v, w, t in tune.variants(pid, 2):
+            nm = C.c_int32()
+            lib.smk_tune_info(pid, v, None, None, C.byref(nm))
+            nx, ny, nz = CLASS_LEN[nm.value], 4, 72
+            _lib.check(lib.smk_tune_set(pid, nx, v))
+            try:
+                out = G.make_boxes(nx, ny, nz, 2.19, seed=19)
+                torch.cuda.synchronize()
+            finally:
+                lib.smk_tune_set(pid, nx, -1)
+            nk = ophilox.kspace_noise(nx, ny, nz, 19)
+            o64 = ograf.grf_from_modes(nk, nz, 2.19, 0.02, eta=("zz",), precision="f64")
+            _check(out.delta[0].cpu().numpy(), o64["delta"], f"xgc variant {v} (W={w}, T={t})")
+            _check(out.eta[0].cpu().numpy(), o64["eta_zz"], f"xgc variant {v} eta")
+    finally:
+        _lib.xgen_cluster(pc)
+
+
 @pytest.mark.parametrize("tag", ["cube16", "rect"])
 def test_grf_matches_reference_golden(G, golden, tag):
     f = golden(f"grf_{tag}.npz")
