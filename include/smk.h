@@ -107,7 +107,8 @@ size_t smk_grf_workspace_size(const SmkGrfParams* p);
  * zeroed by the call) receives for box b and field f (0 = delta, 1 = eta_zz):
  * stats[8b+4f+0] = sum, [8b+4f+1] = sum of squares, [8b+4f+2] = count of non-finite
  * cells, [8b+4f+3] = 0 (FP64); the caller derives sigma and the null check
- * (smk_grf_check does it on the host from one 4-double record).
+ * (smk_grf_check does it on the host from one 4-double record).  delta, eta and the workspace
+ * must be 16-byte aligned (the passes move 16-byte vectors); SMK_EINVAL otherwise.
  */
 int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats,
                   void* workspace, size_t workspace_bytes, void* stream);

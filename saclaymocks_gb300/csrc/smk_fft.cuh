@@ -33,6 +33,11 @@ struct FftPlan {
     int m[FFT_MAX_STAGES];        // L_s / R_s: stride between the inputs of a butterfly
     int tstep[FFT_MAX_STAGES];    // n / L_s: twiddle-table step
     uint32_t magic[FFT_MAX_STAGES];  // floor(2^32/m) + 1: x / m == umulhi(x, magic) for x < 2^16
+    // Per-stage twiddle tables (warp engine): stage s with m > 1 keeps W_L^(r q), L = R m, for
+    // q < m, 1 <= r < R at twoff[s] + q (R - 1) + r - 1, so lanes with different q read
+    // different banks; twn = total entries (< n + n/8).
+    int twoff[FFT_MAX_STAGES];
+    int twn;
 };
 
 // Host: radix plan of n.  rmax >= 16: 16s first; a single factor 2 left over becomes a
@@ -340,6 +345,17 @@ __device__ __forceinline__ void fft_tile(float2* __restrict__ s, const float2* _
         for (int st = 0; st < pl.nst; ++st) fft_stage_any<false, W, SN, T, RMAX>(s, tw, pl, st);
     } else {
         for (int st = pl.nst - 1; st >= 0; --st) fft_stage_any<true, W, SN, T, RMAX>(s, tw, pl, st);
+    }
+}
+
+// Per-stage twiddle tables of the plan (FftPlan::twoff), filled by the block (no barrier).
+__device__ __forceinline__ void fill_stage_twiddles(float2* stw, const FftPlan& pl) {
+    for (int i = threadIdx.x; i < pl.twn; i += blockDim.x) {
+        int st = 0;
+        while (st + 1 < pl.nst && pl.twoff[st + 1] <= i) ++st;
+        const int loc = i - pl.twoff[st];
+        const int q = loc / (pl.r[st] - 1), r = loc - q * (pl.r[st] - 1) + 1;
+        stw[i] = twiddle(r * q * pl.tstep[st], pl.n);
     }
 }
 

@@ -50,6 +50,7 @@ int sm_count() {
 // ------------------------------------------------------------------ tile-variant tables
 #define X(W, T, N, R, B) {W, T, N, R, B},
 static const TileVariant kZVar[] = {SMK_Z_VARIANTS(X)};
+static const TileVariant kZInvVar[] = {SMK_ZINV_VARIANTS(X)};
 static const TileVariant kLineVar[] = {SMK_LINE_VARIANTS(X)};
 static const TileVariant kXVar[] = {SMK_X_VARIANTS(X)};
 static const TileVariant kXGenVar[] = {SMK_XGEN_VARIANTS(X)};
@@ -71,8 +72,8 @@ static int length_class(int n) { return n <= 512 ? 0 : n <= 1024 ? 1 : n <= 2560
 
 const TileVariant* variant_table(int pass) {
     switch (pass) {
-        case PASS_ZFWD:
-        case PASS_ZINV: return kZVar;
+        case PASS_ZFWD: return kZVar;
+        case PASS_ZINV: return kZInvVar;
         case PASS_LINE: return kLineVar;
         case PASS_XPASS: return kXVar;
         case PASS_XGEN: return kXGenVar;
@@ -82,8 +83,8 @@ const TileVariant* variant_table(int pass) {
 
 int variant_count(int pass) {
     switch (pass) {
-        case PASS_ZFWD:
-        case PASS_ZINV: return (int)(sizeof(kZVar) / sizeof(kZVar[0]));
+        case PASS_ZFWD: return (int)(sizeof(kZVar) / sizeof(kZVar[0]));
+        case PASS_ZINV: return (int)(sizeof(kZInvVar) / sizeof(kZInvVar[0]));
         case PASS_LINE: return (int)(sizeof(kLineVar) / sizeof(kLineVar[0]));
         case PASS_XPASS: return (int)(sizeof(kXVar) / sizeof(kXVar[0]));
         case PASS_XGEN: return (int)(sizeof(kXGenVar) / sizeof(kXGenVar[0]));
@@ -165,6 +166,8 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         return fail(SMK_EINVAL, "smk_grf_boxes: need nx, ny >= 2, nz >= 2 even, batch >= 1");
     if (!(p->dcell > 0)) return fail(SMK_EINVAL, "smk_grf_boxes: dcell must be > 0");
     if (p->want_eta && !eta) return fail(SMK_EINVAL, "smk_grf_boxes: want_eta needs an eta box");
+    if (((uintptr_t)delta & 15) || (p->want_eta && ((uintptr_t)eta & 15)) || ((uintptr_t)workspace & 15))
+        return fail(SMK_EINVAL, "smk_grf_boxes: delta, eta and workspace must be 16-byte aligned");
     if (p->eta_comp < SMK_ETA_ZZ || p->eta_comp > SMK_ETA_VZ)
         return fail(SMK_EINVAL, "smk_grf_boxes: unknown eta_comp");
     if (p->noise_mode != SMK_NOISE_HOST && p->noise_mode != SMK_NOISE_PHILOX)

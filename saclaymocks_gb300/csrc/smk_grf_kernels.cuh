@@ -884,6 +884,246 @@ __global__ void __launch_bounds__(C::T, C::MINB) zinv_kernel(const ZInvArgs a) {
     }
 }
 
+// ------------------------------------------------------------------ z inverse, one warp per row pair
+// The same c2r + 1/N + statistics as zinv_kernel, but every warp transforms its own row pair in
+// a private region of shared memory and synchronises only with __syncwarp: the warps of an SM
+// run out of phase, so one warp's loads, another's transform and a third's stores overlap.
+// Slot p of a warp's line sits at p + (p >> 5) (one pad per 32 slots), which spreads the
+// digit-reversed scatter of the half spectrum (slot strides of n/16) over the banks.
+__host__ __device__ __forceinline__ int zpad(int p) { return p + (p >> 5); }
+
+// One stage of a warp's line (slots padded by zpad) with the plan's per-stage twiddles.
+// LAST (the final stage of the inverse, m = n / R, natural-order outputs e = q + r m): the
+// outputs go to out(e, v) instead of back to shared memory.
+template <int R, bool INV, bool LAST, class Out>
+__device__ __forceinline__ void warp_fft_stage(float2* __restrict__ s, const float2* __restrict__ stw,
+                                               const FftPlan& pl, const int st, const int lane, Out&& out) {
+    const int m = pl.m[st];
+    const int nb = pl.n / R;
+    const float2* tws = stw + pl.twoff[st];
+    for (int j = lane; j < nb; j += 32) {
+        const int blk = div_m(pl, st, j);
+        const int q = j - blk * m;
+        const int p0 = blk * R * m + q;
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = s[zpad(p0 + r * m)];
+        const float2* t = tws + q * (R - 1) - 1;
+        if (INV) {
+            if (q != 0) {
+#pragma unroll
+                for (int r = 1; r < R; ++r) v[r] = cmulc(v[r], t[r]);
+            }
+            Dft<R, true>::run(v);
+        } else {
+            Dft<R, false>::run(v);
+            if (q != 0) {
+#pragma unroll
+                for (int r = 1; r < R; ++r) v[r] = cmul(v[r], t[r]);
+            }
+        }
+        if constexpr (LAST) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) out(p0 + r * m, v[r]);
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) s[zpad(p0 + r * m)] = v[r];
+        }
+    }
+    __syncwarp();
+}
+
+// Inverse transform of a warp's line (digit-reversed slots in, natural order out): every stage
+// but the last in place, the last one's outputs handed to out(e, value).
+template <int RMAX, class Out>
+__device__ __forceinline__ void warp_ifft_out(float2* s, const float2* stw, const FftPlan& pl, const int lane,
+                                              Out&& out) {
+    auto none = [](int, float2) {};
+    for (int st = pl.nst - 1; st >= 0; --st) {
+        const bool last = st == 0;
+#define SMK_WSTAGE(RR)                                                              \
+    if (last)                                                                       \
+        warp_fft_stage<RR, true, true>(s, stw, pl, st, lane, out);                  \
+    else                                                                            \
+        warp_fft_stage<RR, true, false>(s, stw, pl, st, lane, none);
+        switch (pl.r[st]) {
+            case 32:
+                if constexpr (RMAX >= 32) { SMK_WSTAGE(32) }
+                break;
+            case 16:
+                if constexpr (RMAX >= 16) { SMK_WSTAGE(16) }
+                break;
+            case 10:
+                if constexpr (RMAX >= 16) { SMK_WSTAGE(10) }
+                break;
+            case 6:
+                if constexpr (RMAX >= 16) { SMK_WSTAGE(6) }
+                break;
+            case 8: SMK_WSTAGE(8) break;
+            case 4: SMK_WSTAGE(4) break;
+            case 2: SMK_WSTAGE(2) break;
+            case 3: SMK_WSTAGE(3) break;
+            default: SMK_WSTAGE(5) break;
+        }
+#undef SMK_WSTAGE
+    }
+}
+
+// The output positions e that warp_ifft_out hands to a lane (its final-stage butterflies).
+template <class F>
+__device__ __forceinline__ void warp_out_positions(const FftPlan& pl, const int lane, F&& f) {
+    const int R = pl.r[0], m = pl.m[0];
+    for (int j = lane; j < m; j += 32)
+        for (int r = 0; r < R; ++r) f(j + r * m);
+}
+
+// Warp-level sums of three doubles; lane 0 adds them to dst[0..2].
+__device__ __forceinline__ void warp_flush_stats(double s1, double s2, double bad, double* dst) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        s1 += __shfl_down_sync(0xffffffffu, s1, off);
+        s2 += __shfl_down_sync(0xffffffffu, s2, off);
+        bad += __shfl_down_sync(0xffffffffu, bad, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(dst, s1);
+        atomicAdd(dst + 1, s2);
+        atomicAdd(dst + 2, bad);
+    }
+}
+
+// Shared memory of zinvw_kernel for `warps` warps: stw[twn] | sof[n] | per-warp lines.
+__host__ __device__ inline size_t zinvw_line_slots(int n) { return (size_t)zpad(n - 1) + 1; }
+inline size_t zinvw_smem(const FftPlan& pl, int warps) {
+    return (size_t)pl.twn * sizeof(float2) + (size_t)(pl.n + (pl.n & 1)) * sizeof(int) +
+           (size_t)warps * zinvw_line_slots(pl.n) * sizeof(float2);
+}
+
+// smem: stw[twn] | sof[n] | line[warp][zinvw_line_slots(n)]
+template <class C>
+__global__ void __launch_bounds__(C::T, C::MINB) zinvw_kernel(const ZInvArgs a) {
+    extern __shared__ float2 smem[];
+    const int n = a.pl.n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    float2* stw = smem;
+    int* sof = reinterpret_cast<int*>(stw + a.pl.twn);
+    float2* sw = reinterpret_cast<float2*>(sof + n + (n & 1)) + (size_t)warp * zinvw_line_slots(n);
+    fill_stage_twiddles(stw, a.pl);
+    for (int m = threadIdx.x; m < n; m += blockDim.x) sof[m] = zpad(slot_of_freq(a.pl, m));
+    __syncthreads();
+    const int nh = n / 2 + 1, half = n / 2;
+    const int64_t rpb = a.zt.rows_per_box;
+    const int64_t ppb = (rpb + 1) / 2;                  // row pairs per box
+    const int64_t per_buf = ppb * a.batch;
+    const int64_t npairs = per_buf * a.nbuf;
+    const int64_t cp = a.pitch / 2;
+    const int64_t gw = (int64_t)blockIdx.x * nwarp + warp, nw = (int64_t)gridDim.x * nwarp;
+    double acc1 = 0.0, acc2 = 0.0, accb = 0.0;
+    int64_t cur = -1;
+    for (int64_t pi = gw; pi < npairs; pi += nw) {
+        const int buf = (int)(pi / per_buf);
+        const int64_t t = pi - buf * per_buf;
+        const int64_t b = t / ppb;
+        const int64_t lrow = 2 * (t - b * ppb);         // first row of the pair inside box b
+        const bool two = lrow + 1 < rpb;
+        const int64_t row0 = b * rpb + lrow;
+        const int64_t key = (int64_t)buf * a.batch + b;
+        if (a.stats && key != cur) {
+            if (cur >= 0) warp_flush_stats(acc1, acc2, accb, a.stats + 8 * (cur % a.batch) + 4 * (cur / a.batch));
+            acc1 = acc2 = accb = 0.0;
+            cur = key;
+        }
+        const float2* in1 = reinterpret_cast<const float2*>(a.buf[buf]) + row0 * cp;
+        const float2* in2 = in1 + cp;
+        if (a.prefetch && lane < 2 && pi + nw < npairs) {
+            // the next pair of this warp: one bulk L2 prefetch per row
+            const int64_t tn = pi + nw;
+            const int bn = (int)(tn / per_buf);
+            const int64_t un = tn - bn * per_buf;
+            const int64_t bbn = un / ppb;
+            const int64_t rn = bbn * rpb + 2 * (un - bbn * ppb) + lane;
+            if (rn < (bbn + 1) * rpb) prefetch_l2_bulk(a.buf[bn] + rn * a.pitch, (uint32_t)(a.pitch * 4));
+        }
+        // Z_k = X1_k + i X2_k (k <= n/2), Z_{n-k} = X1_k* + i X2_k*; DC and Nyquist real parts.
+        // Frequencies are loaded in 16-byte pairs (2k, 2k+1), U pairs per row in flight.
+        auto put = [&](int k, float2 x1, float2 x2) {
+            if (k == 0 || k == half) {
+                sw[sof[k]] = make_float2(x1.x, x2.x);
+            } else {
+                sw[sof[k]] = make_float2(x1.x - x2.y, x1.y + x2.x);
+                sw[sof[n - k]] = make_float2(x1.x + x2.y, x2.x - x1.y);
+            }
+        };
+        constexpr int U = 8;
+        const int nkp = nh >> 1;
+        const float4* in1q = reinterpret_cast<const float4*>(in1);
+        const float4* in2q = reinterpret_cast<const float4*>(in2);
+        for (int kp0 = lane; kp0 < nkp; kp0 += 32 * U) {
+            float4 x1[U], x2[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int kp = kp0 + 32 * u;
+                x1[u] = x2[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (kp < nkp) {
+                    x1[u] = __ldcs(in1q + kp);
+                    if (two) x2[u] = __ldcs(in2q + kp);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int kp = kp0 + 32 * u;
+                if (kp >= nkp) break;
+                put(2 * kp, make_float2(x1[u].x, x1[u].y), make_float2(x2[u].x, x2[u].y));
+                put(2 * kp + 1, make_float2(x1[u].z, x1[u].w), make_float2(x2[u].z, x2[u].w));
+            }
+        }
+        if ((nh & 1) && lane == 0) {
+            const int k = nh - 1;
+            put(k, __ldcs(in1 + k), two ? __ldcs(in2 + k) : make_float2(0.f, 0.f));
+        }
+        __syncwarp();
+        // the last stage writes z_e = x1_e + i x2_e, x 1/N, straight from registers
+        float* o1 = a.buf[buf] + row0 * a.pitch;
+        float* o2 = o1 + a.pitch;
+        float p1 = 0.f, p2 = 0.f;
+        const float sc = a.scale;
+        warp_ifft_out<C::RMAX>(sw, stw, a.pl, lane, [&](int e, float2 z) {
+            const float v0 = z.x * sc;
+            __stcs(o1 + e, v0);
+            p1 += v0;
+            p2 = fmaf(v0, v0, p2);
+            if (two) {
+                const float v1 = z.y * sc;
+                __stcs(o2 + e, v1);
+                p1 += v1;
+                p2 = fmaf(v1, v1, p2);
+            }
+        });
+        if (!(fabsf(p2) < INFINITY)) {
+            // a non-finite value in this lane's share: recount it exactly (finite values only)
+            // from the outputs this lane wrote (rows of this pair, read back from global)
+            p1 = p2 = 0.f;
+            float pb = 0.f;
+            warp_out_positions(a.pl, lane, [&](int e) {
+                const float v[2] = {o1[e], two ? o2[e] : 0.0f};
+                for (int r = 0; r < (two ? 2 : 1); ++r) {
+                    if (isfinite(v[r])) {
+                        p1 += v[r];
+                        p2 = fmaf(v[r], v[r], p2);
+                    } else {
+                        pb += 1.f;
+                    }
+                }
+            });
+            accb += pb;
+        }
+        acc1 += p1;
+        acc2 += p2;
+        __syncwarp();
+    }
+    if (a.stats && cur >= 0) warp_flush_stats(acc1, acc2, accb, a.stats + 8 * (cur % a.batch) + 4 * (cur / a.batch));
+}
+
 // ------------------------------------------------------------------ launch helpers
 int sm_count();
 
@@ -917,8 +1157,37 @@ static int launch_zfwd(ZFwdArgs a, int64_t rows_per_box, cudaStream_t st) {
     return check_launch("zfwd_kernel");
 }
 
+// One warp per row pair (variants with W = 0): as many warps per block as fit in shared
+// memory, up to C::T / 32.
+template <class C>
+static int launch_zinvw(ZInvArgs a, int64_t rows_per_box, cudaStream_t st) {
+    if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "zinvw_kernel");
+    a.zt.rows_per_box = rows_per_box;
+    a.zt.tiles_per_box = 0;
+    int dev = 0, smem_max = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    int warps = C::T / 32;
+    while (warps > 1 && zinvw_smem(a.pl, warps) > (size_t)smem_max) --warps;
+    const size_t smem = zinvw_smem(a.pl, warps);
+    if (smem > (size_t)smem_max) return fail(SMK_ENOTSUPP, "zinvw_kernel: line of %d does not fit", a.pl.n);
+    if (cudaFuncSetAttribute(zinvw_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return check_launch("cudaFuncSetAttribute(zinvw)");
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zinvw_kernel<C>, 32 * warps, smem) != cudaSuccess)
+        return check_launch("cudaOccupancyMaxActiveBlocksPerMultiprocessor(zinvw)");
+    if (per_sm < 1) return fail(SMK_ENOTSUPP, "zinvw_kernel does not fit on an SM (smem %zu B)", smem);
+    const int64_t npairs = (rows_per_box + 1) / 2 * a.batch * a.nbuf;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(npairs, warps), (int64_t)per_sm * sm_count()));
+    zinvw_kernel<C><<<grid, 32 * warps, smem, st>>>(a);
+    return check_launch("zinvw_kernel");
+}
+
 template <class C>
 static int launch_zinv(ZInvArgs a, int64_t rows_per_box, cudaStream_t st) {
+    if constexpr (C::W == 0) {
+        return launch_zinvw<C>(a, rows_per_box, st);
+    } else {
     if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "zinv_kernel");
     a.zt.init(rows_per_box, C::W);
     const size_t smem = zpass_smem<C>(a.pl.n);
@@ -927,6 +1196,7 @@ static int launch_zinv(ZInvArgs a, int64_t rows_per_box, cudaStream_t st) {
     if ((rc = persistent_grid(zinv_kernel<C>, C::T, smem, ntiles, &grid))) return rc;
     zinv_kernel<C><<<grid, C::T, smem, st>>>(a);
     return check_launch("zinv_kernel");
+    }
 }
 
 template <class C>
@@ -1032,6 +1302,9 @@ struct TileVariant {
     X(8, 256, 2560, 32, 1) X(2, 128, 2560, 16, 4) X(4, 128, 2560, 16, 2) X(4, 256, 2560, 16, 2) \
     X(2, 256, 4096, 16, 2) X(8, 256, 2560, 16, 1) X(1, 64, 2560, 16, 6) X(2, 64, 2560, 16, 6) \
     X(1, 128, 2560, 16, 4) X(2, 128, 2560, 32, 2)
+// z inverse: the z-pass variants, then one-warp-per-row-pair variants (W = 0; T = most threads)
+#define SMK_ZINV_VARIANTS(X) SMK_Z_VARIANTS(X) X(0, 512, 2560, 16, 1) X(0, 512, 1024, 16, 1) \
+    X(0, 256, 1024, 16, 2) X(0, 512, 4096, 16, 1) X(0, 256, 2560, 32, 1)
 // y pass (line): W = columns per tile
 #define SMK_LINE_VARIANTS(X) X(16, 256, 512, 32, 1) X(32, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(16, 1024, 1024, 8, 1) \
     X(8, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1) X(4, 1024, 4096, 8, 1) X(8, 256, 2560, 32, 1) \

@@ -61,14 +61,18 @@ bool make_plan(int n, FftPlan* p, int rmax) {
     if (nr > FFT_MAX_STAGES) return false;
     p->n = n;
     p->nst = nr;
-    int L = n;
+    int L = n, tw = 0;
     for (int s = 0; s < nr; ++s) {
         p->r[s] = rad[s];
         p->m[s] = L / rad[s];
         p->tstep[s] = n / L;
         p->magic[s] = p->m[s] == 1 ? 0u : (uint32_t)((1ull << 32) / (uint64_t)p->m[s] + 1ull);
+        p->twoff[s] = tw;
+        if (p->m[s] > 1) tw += p->m[s] * (rad[s] - 1);
         L = p->m[s];
     }
+    for (int s = nr; s < FFT_MAX_STAGES; ++s) p->twoff[s] = tw;
+    p->twn = tw;
     return true;
 }
 

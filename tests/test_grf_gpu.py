@@ -165,6 +165,22 @@ def test_grf_philox_mode_matches_oracle_modes(G, shape):
         _check(out.eta[b].cpu().numpy(), o64["eta_zz"], f"philox eta {b}")
 
 
+def test_grf_rejects_misaligned_boxes(G):
+    """Boxes not on a 16-byte boundary are refused on the host (SMK_EINVAL), before any launch."""
+    import ctypes as C
+    from saclaymocks_gb300 import _lib
+    nx, ny, nz = 8, 6, 10
+    p = _lib.SmkGrfParams()
+    p.nx, p.ny, p.nz, p.batch, p.dcell = nx, ny, nz, 1, 2.19
+    p.noise_mode, p.pk_mode, p.k0, p.amp, p.seed, p.want_eta = _lib.SMK_NOISE_PHILOX, _lib.SMK_PK_ANALYTIC, 0.02, 1.0, 1, 1
+    buf = torch.zeros(2 * nx * ny * _lib.load().smk_grf_pitch(nz) + 16, device="cuda")
+    base = buf.data_ptr()
+    rc = _lib.load().smk_grf_boxes(C.byref(p), base + 8, base + 4096, None, None, 0, None)
+    assert rc == _lib.SMK_EINVAL
+    rc = _lib.load().smk_grf_boxes(C.byref(p), base, base + 4100, None, None, 0, None)
+    assert rc == _lib.SMK_EINVAL
+
+
 def test_kspace_noise_is_hermitian_on_the_real_planes():
     nk = ophilox.kspace_noise(6, 5, 8, 3)
     for p in (0, 4):
