@@ -281,8 +281,8 @@ template <int R, bool INV, int W, int SN, int T>
 __device__ __forceinline__ void fft_stage(float2* __restrict__ s, const float2* __restrict__ tw,
                                           const FftPlan& pl, const int st) {
     const int m = pl.m[st];
-    const int tstep = pl.tstep[st];
     const int nb = (pl.n / R) * W;
+    const float2* tws = tw + pl.twoff[st] - 1;
 #pragma unroll(T >= 1024 ? 1 : 2)
     for (int bf = threadIdx.x; bf < nb; bf += T) {
         const int j = bf / W, w = bf % W;
@@ -292,17 +292,18 @@ __device__ __forceinline__ void fft_stage(float2* __restrict__ s, const float2* 
         float2 v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) v[r] = p[r * m * SN];
+        const float2* t = tws + q * (R - 1);   // t[r] = W_L^(r q), 1 <= r < R
         if (INV) {
             if (q != 0) {
 #pragma unroll
-                for (int r = 1; r < R; ++r) v[r] = cmulc(v[r], tw[r * q * tstep]);
+                for (int r = 1; r < R; ++r) v[r] = cmulc(v[r], t[r]);
             }
             Dft<R, true>::run(v);
         } else {
             Dft<R, false>::run(v);
             if (q != 0) {
 #pragma unroll
-                for (int r = 1; r < R; ++r) v[r] = cmul(v[r], tw[r * q * tstep]);
+                for (int r = 1; r < R; ++r) v[r] = cmul(v[r], t[r]);
             }
         }
 #pragma unroll
@@ -335,7 +336,8 @@ __device__ __forceinline__ void fft_stage_any(float2* s, const float2* tw, const
 }
 
 // Full transform of the W lines of the tile: forward natural -> digit-reversed, inverse
-// digit-reversed -> natural (unnormalised).  The caller synchronises after filling s; on
+// digit-reversed -> natural (unnormalised).  tw holds the plan's per-stage twiddle tables
+// (fill_stage_twiddles).  The caller synchronises after filling s; on
 // return the block is synchronised.  The plan's radices must be <= RMAX (plan_fits; the
 // launchers check it), larger radices are not compiled into the kernel.
 template <bool INV, int W, int SN, int T, int RMAX = fft_max_radix(T)>
@@ -348,7 +350,8 @@ __device__ __forceinline__ void fft_tile(float2* __restrict__ s, const float2* _
     }
 }
 
-// Per-stage twiddle tables of the plan (FftPlan::twoff), filled by the block (no barrier).
+// Per-stage twiddle tables of the plan (FftPlan::twoff; fewer than n entries), filled by the
+// block (no barrier).
 __device__ __forceinline__ void fill_stage_twiddles(float2* stw, const FftPlan& pl) {
     for (int i = threadIdx.x; i < pl.twn; i += blockDim.x) {
         int st = 0;
@@ -359,10 +362,5 @@ __device__ __forceinline__ void fill_stage_twiddles(float2* stw, const FftPlan& 
     }
 }
 
-// Twiddle table tw[m] = exp(-2 pi i m / n), m < n, filled by the block (no barrier).
-template <int T>
-__device__ __forceinline__ void fill_twiddles(float2* tw, int n) {
-    for (int m = threadIdx.x; m < n; m += T) tw[m] = twiddle(m, n);
-}
 
 }  // namespace smk

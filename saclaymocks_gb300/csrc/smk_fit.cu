@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(FIT_T) fit_p1d_kernel(const FitArgs a) {
         int slot;
         const int M = bluestein_m(N, &slot);
         if (M != curM) {
-            fill_twiddles<FIT_T>(tw, M);
+            fill_stage_twiddles(tw, a.plans[slot]);
             curM = M;
         }
         load_pair(a, th, fbar_inv, ps, s1);
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(FIT_T) fit_adjoint_kernel(const FitArgs a) {
         int slot;
         const int M = bluestein_m(N, &slot);
         if (M != curM) {
-            fill_twiddles<FIT_T>(tw, M);
+            fill_stage_twiddles(tw, a.plans[slot]);
             curM = M;
         }
         load_pair(a, th, fbar_inv, ps, s1);

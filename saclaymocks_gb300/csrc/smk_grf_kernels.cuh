@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) zfwd_kernel(const ZFwdArgs a) {
     float2* tw = s + n * SN;
     int* sof = reinterpret_cast<int*>(tw + n);
     float* sf = reinterpret_cast<float*>(s);
-    fill_twiddles<T>(tw, n);
+    fill_stage_twiddles(tw, a.pl);
     for (int k = threadIdx.x; k < n; k += T) sof[k] = slot_of_freq(a.pl, k);
     const int nh = n / 2 + 1;
     const int64_t ntiles = a.zt.tiles_per_box * a.batch;
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const LineArgs a) {
     const int n = a.pl.n;
     float2* s = smem;
     float2* tw = s + n * W;
-    fill_twiddles<T>(tw, n);
+    fill_stage_twiddles(tw, a.pl);
     const int64_t ncolt = ceil_div(a.ncol, W);
     const int64_t tpb = a.n_outer * ncolt;
     const int64_t ntiles = tpb * a.nbuf;
@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpass_kernel(const XArgs a) {
     float* kx = reinterpret_cast<float*>(tw + n);
     int* ix = reinterpret_cast<int*>(kx + n);
     float* kt = reinterpret_cast<float*>(ix + n);
-    fill_twiddles<T>(tw, n);
+    fill_stage_twiddles(tw, a.pl);
     for (int e = threadIdx.x; e < n; e += T) {
         const int f = freq_of_slot(a.pl, e);
         ix[e] = f;
@@ -453,7 +453,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
     float* kx = reinterpret_cast<float*>(tw + n);
     int* ix = reinterpret_cast<int*>(kx + n);
     float* kzt = reinterpret_cast<float*>(ix + n);
-    fill_twiddles<T>(tw, n);
+    fill_stage_twiddles(tw, a.pl);
     for (int e = threadIdx.x; e < n; e += T) {
         const int f = freq_of_slot(a.pl, e);
         ix[e] = f;
@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgc_kernel(const XGenArgs a) {
     float* kx = reinterpret_cast<float*>(tw + n);
     int* ix = reinterpret_cast<int*>(kx + n);
     float* kzt = reinterpret_cast<float*>(ix + n);
-    fill_twiddles<T>(tw, n);
+    fill_stage_twiddles(tw, a.pl);
     for (int e = threadIdx.x; e < n; e += T) {
         const int fr = freq_of_slot(a.pl, e);
         ix[e] = fr;
@@ -681,7 +681,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xinv_kernel(const XGenArgs a) {
     float2* tw = s + n * W;
     float* kx = reinterpret_cast<float*>(tw + n);
     float* kzt = kx + n;
-    fill_twiddles<T>(tw, n);
+    fill_stage_twiddles(tw, a.pl);
     for (int e = threadIdx.x; e < n; e += T) kx[e] = kaxis(freq_of_slot(a.pl, e), n, a.kfac, true);
     for (int z = threadIdx.x; z < a.nzh; z += T) kzt[z] = kaxis(z, a.nz, a.kfac, false);
     __syncthreads();
@@ -774,7 +774,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) zinv_kernel(const ZInvArgs a) {
     int* sof = reinterpret_cast<int*>(tw + n);
     double* red = reinterpret_cast<double*>(sof + n + (n & 1));
     float* sf = reinterpret_cast<float*>(s);
-    fill_twiddles<T>(tw, n);
+    fill_stage_twiddles(tw, a.pl);
     for (int k = threadIdx.x; k < n; k += T) sof[k] = slot_of_freq(a.pl, k);
     __syncthreads();
     const int nh = n / 2 + 1, half = n / 2;

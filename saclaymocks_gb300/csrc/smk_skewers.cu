@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(SK_T, 2) skewer_kernel(const SkArgs a) {
             const int cls = ss_class(nzz);
             const FftPlan& pl = a.plans[cls];
             if (nzz != cur_nz) {
-                fill_twiddles<SK_T>(tw, nzz);
+                fill_stage_twiddles(tw, pl);
                 for (int k = threadIdx.x; k < nzz; k += SK_T) sof[k] = slot_of_freq(pl, k);
                 cur_nz = nzz;
                 __syncthreads();
