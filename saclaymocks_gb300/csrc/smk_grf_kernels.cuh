@@ -616,7 +616,11 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgc_kernel(const XGenArgs a) {
                 }
             }
         }
-        cl.sync();
+        // The partners' shared loads above have returned (their values feed the stores), so the
+        // next tile may overwrite the tiles once every thread arrives; a relaxed arrival keeps
+        // the global stores in flight instead of draining them at the barrier.
+        asm volatile("barrier.cluster.arrive.relaxed.aligned;\n" ::: "memory");
+        asm volatile("barrier.cluster.wait.aligned;\n" ::: "memory");
     }
 }
 
