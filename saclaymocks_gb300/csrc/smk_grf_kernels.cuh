@@ -476,6 +476,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
         const float ky = kaxis(iy, a.ny, a.kfac, true);
         const uint64_t seed = a.seed + (uint64_t)b;
         auto draw = [&](auto chk) {
+#pragma unroll 2
             for (int idx = threadIdx.x; idx < n * NP; idx += T) {
                 const int e = idx / NP, pr = idx % NP;
                 const int c0 = 2 * pr, kz0 = cb * WC + c0;
