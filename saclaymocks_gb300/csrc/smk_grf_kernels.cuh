@@ -1050,41 +1050,31 @@ __global__ void __launch_bounds__(C::T, C::MINB) zinvw_kernel(const ZInvArgs a) 
             if (rn < (bbn + 1) * rpb) prefetch_l2_bulk(a.buf[bn] + rn * a.pitch, (uint32_t)(a.pitch * 4));
         }
         // Z_k = X1_k + i X2_k (k <= n/2), Z_{n-k} = X1_k* + i X2_k*; DC and Nyquist real parts.
-        // Frequencies are loaded in 16-byte pairs (2k, 2k+1), U pairs per row in flight.
-        auto put = [&](int k, float2 x1, float2 x2) {
-            if (k == 0 || k == half) {
-                sw[sof[k]] = make_float2(x1.x, x2.x);
-            } else {
-                sw[sof[k]] = make_float2(x1.x - x2.y, x1.y + x2.x);
-                sw[sof[n - k]] = make_float2(x1.x + x2.y, x2.x - x1.y);
-            }
-        };
-        constexpr int U = 8;
-        const int nkp = nh >> 1;
-        const float4* in1q = reinterpret_cast<const float4*>(in1);
-        const float4* in2q = reinterpret_cast<const float4*>(in2);
-        for (int kp0 = lane; kp0 < nkp; kp0 += 32 * U) {
-            float4 x1[U], x2[U];
+        // Lanes take consecutive k (the scatter to slot_of_freq(k) then spreads over the banks),
+        // U loads per row in flight.
+        constexpr int U = 12;
+        for (int k0 = lane; k0 < nh; k0 += 32 * U) {
+            float2 x1[U], x2[U];
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                const int kp = kp0 + 32 * u;
-                x1[u] = x2[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (kp < nkp) {
-                    x1[u] = __ldcs(in1q + kp);
-                    if (two) x2[u] = __ldcs(in2q + kp);
+                const int k = k0 + 32 * u;
+                x1[u] = x2[u] = make_float2(0.f, 0.f);
+                if (k < nh) {
+                    x1[u] = __ldcs(in1 + k);
+                    if (two) x2[u] = __ldcs(in2 + k);
                 }
             }
 #pragma unroll
             for (int u = 0; u < U; ++u) {
-                const int kp = kp0 + 32 * u;
-                if (kp >= nkp) break;
-                put(2 * kp, make_float2(x1[u].x, x1[u].y), make_float2(x2[u].x, x2[u].y));
-                put(2 * kp + 1, make_float2(x1[u].z, x1[u].w), make_float2(x2[u].z, x2[u].w));
+                const int k = k0 + 32 * u;
+                if (k >= nh) break;
+                if (k == 0 || k == half) {
+                    sw[sof[k]] = make_float2(x1[u].x, x2[u].x);
+                } else {
+                    sw[sof[k]] = make_float2(x1[u].x - x2[u].y, x1[u].y + x2[u].x);
+                    sw[sof[n - k]] = make_float2(x1[u].x + x2[u].y, x2[u].x - x1[u].y);
+                }
             }
-        }
-        if ((nh & 1) && lane == 0) {
-            const int k = nh - 1;
-            put(k, __ldcs(in1 + k), two ? __ldcs(in2 + k) : make_float2(0.f, 0.f));
         }
         __syncwarp();
         // the last stage writes z_e = x1_e + i x2_e, x 1/N, straight from registers
