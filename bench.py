@@ -287,10 +287,10 @@ def run_ours(args, cfg):
     dom = int(np.argmax(pass_ms))
     achieved = pass_bytes[dom] / (pass_ms[dom] * 1e-3) / 1e9
     # DRAM bytes per unit from ncu captures of the same kernels on boxes with the production
-    # line lengths (profiles/grf_passes_xgen_2560x128x1536_line_zinv_128x2560x1536.md), scaled
-    # by the units of this launch: x 7.85 B per mode and field, y 16.0 and z 16.1 B per mode
+    # line lengths (profiles/grf_passes_xgen_2560x128x1536_line_zinvw_128x2560x1536.md), scaled
+    # by the units of this launch: x 7.81 B per mode and field, y 16.0 and z 16.1 B per mode
     # and field
-    traffic = [7.85 * modes * 2, 16.0 * modes * 2, 16.06 * modes * 2][dom] / 1e9
+    traffic = [7.81 * modes * 2, 16.0 * modes * 2, 16.14 * modes * 2][dom] / 1e9
     grf_ms = float(np.sum(pass_ms))
     step_ms = ms / args.steps
     value = aggregate_value(cells, world, step_ms * 1e-3)
