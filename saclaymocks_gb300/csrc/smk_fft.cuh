@@ -44,7 +44,8 @@ struct FftPlan {
 // radix-32 stage (rmax >= 32), else joins a 5 (radix 10) or a 3 (radix 6), else stays a 2;
 // rmax 8: 8s, then 4s / 2.  3s and 5s follow.
 // Returns false unless 2 <= n <= FFT_MAX_N and n = 2^a 3^b 5^c.
-bool make_plan(int n, FftPlan* p, int rmax = 16);
+// mid: a three-stage plan (R, R, x) becomes (R, x, R) (the warp z pass's conflict-free order).
+bool make_plan(int n, FftPlan* p, int rmax = 16, bool mid = false);
 
 // Largest radix a kernel of T threads per block runs in registers without spilling (the
 // register budget per thread is 65536 / T): radix 32 for <= 256 threads, 16 for 512, 8 above.

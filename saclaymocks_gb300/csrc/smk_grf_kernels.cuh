@@ -893,14 +893,19 @@ __global__ void __launch_bounds__(C::T, C::MINB) zinv_kernel(const ZInvArgs a) {
 // The same c2r + 1/N + statistics as zinv_kernel, but every warp transforms its own row pair in
 // a private region of shared memory and synchronises only with __syncwarp: the warps of an SM
 // run out of phase, so one warp's loads, another's transform and a third's stores overlap.
-// Slot p of a warp's line sits at p + (p >> 5) (one pad per 32 slots), which spreads the
-// digit-reversed scatter of the half spectrum (slot strides of n/16) over the banks.
-__host__ __device__ __forceinline__ int zpad(int p) { return p + (p >> 5); }
+// Slot p of a warp's line sits at zslot<SWZ>(p).  SWZ = 1: p ^ ((p >> 4) & 15), an XOR swizzle
+// inside blocks of 16 slots that, with the odd radix in the middle of the plan ((16, 6, 16) for
+// 1536, (16, 10, 16) for 2560), makes every stage's accesses conflict-free and spreads the
+// digit-reversed scatter of the half spectrum over the banks.  SWZ = 0: p + (p >> 5), one pad
+// per 32 slots (power-of-two lengths >= 2048, whose scatter the swizzle does not spread).
+template <int SWZ>
+__host__ __device__ __forceinline__ int zslot(int p) { return SWZ ? (p ^ ((p >> 4) & 15)) : p + (p >> 5); }
+__host__ __device__ __forceinline__ int zpad(int p) { return zslot<0>(p); }
 
 // One stage of a warp's line (slots padded by zpad) with the plan's per-stage twiddles.
 // LAST (the final stage of the inverse, m = n / R, natural-order outputs e = q + r m): the
 // outputs go to out(e, v) instead of back to shared memory.
-template <int R, bool INV, bool LAST, class Out>
+template <int R, bool INV, bool LAST, int SWZ, class Out>
 __device__ __forceinline__ void warp_fft_stage(float2* __restrict__ s, const float2* __restrict__ stw,
                                                const FftPlan& pl, const int st, const int lane, Out&& out) {
     const int m = pl.m[st];
@@ -912,7 +917,7 @@ __device__ __forceinline__ void warp_fft_stage(float2* __restrict__ s, const flo
         const int p0 = blk * R * m + q;
         float2 v[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = s[zpad(p0 + r * m)];
+        for (int r = 0; r < R; ++r) v[r] = s[zslot<SWZ>(p0 + r * m)];
         const float2* t = tws + q * (R - 1) - 1;
         if (INV) {
             if (q != 0) {
@@ -932,7 +937,7 @@ __device__ __forceinline__ void warp_fft_stage(float2* __restrict__ s, const flo
             for (int r = 0; r < R; ++r) out(p0 + r * m, v[r]);
         } else {
 #pragma unroll
-            for (int r = 0; r < R; ++r) s[zpad(p0 + r * m)] = v[r];
+            for (int r = 0; r < R; ++r) s[zslot<SWZ>(p0 + r * m)] = v[r];
         }
     }
     __syncwarp();
@@ -940,7 +945,7 @@ __device__ __forceinline__ void warp_fft_stage(float2* __restrict__ s, const flo
 
 // Inverse transform of a warp's line (digit-reversed slots in, natural order out): every stage
 // but the last in place, the last one's outputs handed to out(e, value).
-template <int RMAX, class Out>
+template <int RMAX, int SWZ, class Out>
 __device__ __forceinline__ void warp_ifft_out(float2* s, const float2* stw, const FftPlan& pl, const int lane,
                                               Out&& out) {
     auto none = [](int, float2) {};
@@ -948,9 +953,9 @@ __device__ __forceinline__ void warp_ifft_out(float2* s, const float2* stw, cons
         const bool last = st == 0;
 #define SMK_WSTAGE(RR)                                                              \
     if (last)                                                                       \
-        warp_fft_stage<RR, true, true>(s, stw, pl, st, lane, out);                  \
+        warp_fft_stage<RR, true, true, SWZ>(s, stw, pl, st, lane, out);             \
     else                                                                            \
-        warp_fft_stage<RR, true, false>(s, stw, pl, st, lane, none);
+        warp_fft_stage<RR, true, false, SWZ>(s, stw, pl, st, lane, none);
         switch (pl.r[st]) {
             case 32:
                 if constexpr (RMAX >= 32) { SMK_WSTAGE(32) }
@@ -998,23 +1003,25 @@ __device__ __forceinline__ void warp_flush_stats(double s1, double s2, double ba
 }
 
 // Shared memory of zinvw_kernel for `warps` warps: stw[twn] | sof[n] | per-warp lines.
-__host__ __device__ inline size_t zinvw_line_slots(int n) { return (size_t)zpad(n - 1) + 1; }
-inline size_t zinvw_smem(const FftPlan& pl, int warps) {
+__host__ __device__ inline size_t zinvw_line_slots(int n, int swz) {
+    return swz ? (size_t)(n + 15) / 16 * 16 : (size_t)zpad(n - 1) + 1;
+}
+inline size_t zinvw_smem(const FftPlan& pl, int warps, int swz) {
     return (size_t)pl.twn * sizeof(float2) + (size_t)(pl.n + (pl.n & 1)) * sizeof(int) +
-           (size_t)warps * zinvw_line_slots(pl.n) * sizeof(float2);
+           (size_t)warps * zinvw_line_slots(pl.n, swz) * sizeof(float2);
 }
 
-// smem: stw[twn] | sof[n] | line[warp][zinvw_line_slots(n)]
-template <class C>
+// smem: stw[twn] | sof[n] | line[warp][zinvw_line_slots(n, SWZ)]
+template <class C, int SWZ>
 __global__ void __launch_bounds__(C::T, C::MINB) zinvw_kernel(const ZInvArgs a) {
     extern __shared__ float2 smem[];
     const int n = a.pl.n;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     float2* stw = smem;
     int* sof = reinterpret_cast<int*>(stw + a.pl.twn);
-    float2* sw = reinterpret_cast<float2*>(sof + n + (n & 1)) + (size_t)warp * zinvw_line_slots(n);
+    float2* sw = reinterpret_cast<float2*>(sof + n + (n & 1)) + (size_t)warp * zinvw_line_slots(n, SWZ);
     fill_stage_twiddles(stw, a.pl);
-    for (int m = threadIdx.x; m < n; m += blockDim.x) sof[m] = zpad(slot_of_freq(a.pl, m));
+    for (int m = threadIdx.x; m < n; m += blockDim.x) sof[m] = zslot<SWZ>(slot_of_freq(a.pl, m));
     __syncthreads();
     const int nh = n / 2 + 1, half = n / 2;
     const int64_t rpb = a.zt.rows_per_box;
@@ -1082,7 +1089,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) zinvw_kernel(const ZInvArgs a) 
         float* o2 = o1 + a.pitch;
         float p1 = 0.f, p2 = 0.f;
         const float sc = a.scale;
-        warp_ifft_out<C::RMAX>(sw, stw, a.pl, lane, [&](int e, float2 z) {
+        warp_ifft_out<C::RMAX, SWZ>(sw, stw, a.pl, lane, [&](int e, float2 z) {
             const float v0 = z.x * sc;
             __stcs(o1 + e, v0);
             p1 += v0;
@@ -1159,22 +1166,27 @@ static int launch_zinvw(ZInvArgs a, int64_t rows_per_box, cudaStream_t st) {
     if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "zinvw_kernel");
     a.zt.rows_per_box = rows_per_box;
     a.zt.tiles_per_box = 0;
+    // layout: XOR swizzle with the odd radix mid-plan, except power-of-two lengths >= 2048
+    const int n = a.pl.n;
+    const int swz = ((n & (n - 1)) != 0 || n < 2048) ? 1 : 0;
+    if (swz && !make_plan(n, &a.pl, C::RMAX, true)) return fail(SMK_ENOTSUPP, "zinvw_kernel: no plan for %d", n);
     int dev = 0, smem_max = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     int warps = C::T / 32;
-    while (warps > 1 && zinvw_smem(a.pl, warps) > (size_t)smem_max) --warps;
-    const size_t smem = zinvw_smem(a.pl, warps);
-    if (smem > (size_t)smem_max) return fail(SMK_ENOTSUPP, "zinvw_kernel: line of %d does not fit", a.pl.n);
-    if (cudaFuncSetAttribute(zinvw_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    while (warps > 1 && zinvw_smem(a.pl, warps, swz) > (size_t)smem_max) --warps;
+    const size_t smem = zinvw_smem(a.pl, warps, swz);
+    if (smem > (size_t)smem_max) return fail(SMK_ENOTSUPP, "zinvw_kernel: line of %d does not fit", n);
+    auto kern = swz ? zinvw_kernel<C, 1> : zinvw_kernel<C, 0>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return check_launch("cudaFuncSetAttribute(zinvw)");
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zinvw_kernel<C>, 32 * warps, smem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * warps, smem) != cudaSuccess)
         return check_launch("cudaOccupancyMaxActiveBlocksPerMultiprocessor(zinvw)");
     if (per_sm < 1) return fail(SMK_ENOTSUPP, "zinvw_kernel does not fit on an SM (smem %zu B)", smem);
     const int64_t npairs = (rows_per_box + 1) / 2 * a.batch * a.nbuf;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(npairs, warps), (int64_t)per_sm * sm_count()));
-    zinvw_kernel<C><<<grid, 32 * warps, smem, st>>>(a);
+    kern<<<grid, 32 * warps, smem, st>>>(a);
     return check_launch("zinvw_kernel");
 }
 

@@ -27,7 +27,7 @@ int check_launch(const char* what) {
     return SMK_OK;
 }
 
-bool make_plan(int n, FftPlan* p, int rmax) {
+bool make_plan(int n, FftPlan* p, int rmax, bool mid) {
     if (n < 2 || n > FFT_MAX_N) return false;
     int m = n, p2 = 0, p3 = 0, p5 = 0;
     while (m % 2 == 0) { m /= 2; ++p2; }
@@ -59,6 +59,10 @@ bool make_plan(int n, FftPlan* p, int rmax) {
     for (int i = 0; i < p3; ++i) rad[nr++] = 3;
     for (int i = 0; i < p5; ++i) rad[nr++] = 5;
     if (nr > FFT_MAX_STAGES) return false;
+    if (mid && nr == 3 && rad[0] == rad[1] && rad[2] != rad[0]) {
+        rad[2] = rad[1];   // (R, R, x) -> (R, x, R)
+        rad[1] = (n / rad[0]) / rad[0];
+    }
     p->n = n;
     p->nst = nr;
     int L = n, tw = 0;
