@@ -632,45 +632,46 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgc_kernel(const XGenArgs a) {
 // one box only).  The x pass then touches at most one output box per launch without drawing
 // every mode twice.
 template <int T>
-__global__ void __launch_bounds__(T) kgen_kernel(const XGenArgs a) {
+__global__ void __launch_bounds__(T, 3) kgen_kernel(const XGenArgs a) {
     extern __shared__ float2 smem[];
     float* kx = reinterpret_cast<float*>(smem);          // [nx] k_x of each x slot
     int* ix = reinterpret_cast<int*>(kx + a.nx);          // [nx] frequency of each x slot
-    float* kyt = reinterpret_cast<float*>(ix + a.nx);     // [ny] k_y of each y slot
-    int* iyt = reinterpret_cast<int*>(kyt + a.ny);        // [ny] frequency of each y slot
-    float* kzt = reinterpret_cast<float*>(iyt + a.ny);    // [nzh]
+    float* kzt = reinterpret_cast<float*>(ix + a.nx);     // [nzh]
     for (int e = threadIdx.x; e < a.nx; e += T) {
         const int f = freq_of_slot(a.pl, e);
         ix[e] = f;
         kx[e] = kaxis(f, a.nx, a.kfac, true);
     }
-    for (int e = threadIdx.x; e < a.ny; e += T) {
-        const int f = freq_of_slot(a.ply, e);
-        iyt[e] = f;
-        kyt[e] = kaxis(f, a.ny, a.kfac, true);
-    }
     for (int z = threadIdx.x; z < a.nzh; z += T) kzt[z] = kaxis(z, a.nz, a.kfac, false);
     __syncthreads();
     const float scale_c = pk_scale_c(a);
-    const int wt = 1 << a.sh, npair = wt / 2;
-    const int64_t nkb = ceil_div(a.nzh, wt);
-    const int64_t items = nkb * a.batch * a.ny * (int64_t)a.nx * npair;   // k_z pairs in staged-address order
-    for (int64_t it = (int64_t)blockIdx.x * T + threadIdx.x; it < items; it += (int64_t)gridDim.x * T) {
-        const int pr = (int)(it % npair);
-        const int64_t line = it / npair;                  // (((kb * batch + b) * ny + yslot) * nx + e)
-        const int e = (int)(line % a.nx);
-        const int64_t r = line / a.nx;
-        const int yslot = (int)(r % a.ny);
-        const int64_t r2 = r / a.ny;
+    const int wt = 1 << a.sh, psh = a.sh - 1, pmask = (wt >> 1) - 1;
+    const int nkb = (int)ceil_div(a.nzh, wt);
+    // a line = the nx x-slots of one (k_z block, box, y slot): one contiguous staged run
+    const int64_t nlines = (int64_t)nkb * a.batch * a.ny;
+    const int per_line = a.nx << psh;                     // mode pairs of a line
+    for (int64_t line = blockIdx.x; line < nlines; line += gridDim.x) {
+        const int yslot = (int)(line % a.ny);
+        const int64_t r2 = line / a.ny;
         const int b = (int)(r2 % a.batch);
         const int kb = (int)(r2 / a.batch);
-        const int kz0 = kb * wt + 2 * pr;
-        if (kz0 >= a.nzh) continue;
-        const int iy = iyt[yslot];
-        const ModePair mp = draw_pair<true>(a, a.seed + (uint64_t)b, ix[e], iy, iy == 0 ? 0 : a.ny - iy, kx[e],
-                                            kyt[yslot], kz0, kzt, scale_c);
-        float4 v = make_float4(mp.d[0].x, mp.d[0].y, mp.d[1].x, mp.d[1].y);
-        *reinterpret_cast<float4*>(a.S + ((line << a.sh) | (2 * pr))) = v;
+        const int iy = freq_of_slot(a.ply, yslot);
+        const int iym = iy == 0 ? 0 : a.ny - iy;
+        const float ky = kaxis(iy, a.ny, a.kfac, true);
+        const uint64_t seed = a.seed + (uint64_t)b;
+        float4* dst = reinterpret_cast<float4*>(a.S + ((line * a.nx) << a.sh));
+        auto draw = [&](auto chk) {
+            for (int it = threadIdx.x; it < per_line; it += T) {
+                const int e = it >> psh, pr = it & pmask;
+                const ModePair mp = draw_pair<decltype(chk)::value>(a, seed, ix[e], iy, iym, kx[e], ky,
+                                                                     kb * wt + 2 * pr, kzt, scale_c);
+                __stcs(dst + it, make_float4(mp.d[0].x, mp.d[0].y, mp.d[1].x, mp.d[1].y));
+            }
+        };
+        if (tile_needs_check(a, kb * wt, wt))
+            draw(std::true_type{});
+        else
+            draw(std::false_type{});
     }
 }
 
@@ -707,6 +708,13 @@ __global__ void __launch_bounds__(C::T, C::MINB) xinv_kernel(const XGenArgs a) {
         load_cols_async<W, T>(s, src, n, W, cols);
         cp_async_wait_all();
         __syncthreads();
+        if (threadIdx.x == 0 && tile + gridDim.x < ntiles) {
+            // the next tile's run (tiles are consecutive runs): one bulk L2 prefetch
+            const int64_t tn = tile + gridDim.x;
+            const int kbn = (int)(tn / nouter);
+            prefetch_l2_bulk(a.S + (((int64_t)kbn * nouter + (tn - (int64_t)kbn * nouter)) * n << a.sh),
+                             (uint32_t)((size_t)n * W * sizeof(float2)));
+        }
         if (eta) {
             const float ky = kaxis(freq_of_slot(a.ply, yslot), a.ny, a.kfac, true);
             for (int idx = threadIdx.x; idx < n * W; idx += T) {

@@ -32,11 +32,12 @@ int run_xinv(int v, const XGenArgs& a, cudaStream_t st) {
 
 int run_kgen(const XGenArgs& a, cudaStream_t st) {
     constexpr int T = 256;
-    const size_t smem = (size_t)(a.nx + a.ny) * 8 + (size_t)a.nzh * 4 + 16;
+    if (a.sh < 1) return fail(SMK_EINVAL, "kgen: staged blocks of at least 2 columns");
+    const size_t smem = (size_t)a.nx * 8 + (size_t)a.nzh * 4 + 16;
     const int64_t wt = (int64_t)1 << a.sh;
-    const int64_t items = ceil_div(a.nzh, wt) * a.batch * a.ny * (int64_t)a.nx * (wt / 2);
+    const int64_t lines = ceil_div(a.nzh, wt) * a.batch * a.ny;
     int grid = 0, rc;
-    if ((rc = persistent_grid(kgen_kernel<T>, T, smem, ceil_div(items, T), &grid))) return rc;
+    if ((rc = persistent_grid(kgen_kernel<T>, T, smem, lines, &grid))) return rc;
     kgen_kernel<T><<<grid, T, smem, st>>>(a);
     return check_launch("kgen_kernel");
 }
