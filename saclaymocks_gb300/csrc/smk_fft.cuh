@@ -278,9 +278,15 @@ template <bool INV> struct Dft<16, INV> : DftComposite<16, INV> {};
 template <bool INV> struct Dft<32, INV> : DftComposite<32, INV> {};
 
 // ------------------------------------------------------------------ one in-place stage
-template <int R, bool INV, int W, int SN, int T>
+// OUT = false: results back to shared memory, then a block barrier.  OUT = true (the last
+// stage of an inverse, st = 0, natural-order outputs e = q + r m of line w): results go to
+// out(e, w, value) and there is no barrier (the caller synchronises before reusing s).
+struct NoOut {
+    __device__ __forceinline__ void operator()(int, int, float2) const {}
+};
+template <int R, bool INV, int W, int SN, int T, bool OUT = false, class Out = NoOut>
 __device__ __forceinline__ void fft_stage(float2* __restrict__ s, const float2* __restrict__ tw,
-                                          const FftPlan& pl, const int st) {
+                                          const FftPlan& pl, const int st, Out&& out = Out{}) {
     const int m = pl.m[st];
     const int nb = (pl.n / R) * W;
     const float2* tws = tw + pl.twoff[st] - 1;
@@ -307,32 +313,38 @@ __device__ __forceinline__ void fft_stage(float2* __restrict__ s, const float2* 
                 for (int r = 1; r < R; ++r) v[r] = cmul(v[r], t[r]);
             }
         }
+        if constexpr (OUT) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) p[r * m * SN] = v[r];
+            for (int r = 0; r < R; ++r) out(q + r * m, w, v[r]);
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) p[r * m * SN] = v[r];
+        }
     }
-    __syncthreads();
+    if constexpr (!OUT) __syncthreads();
 }
 
-template <bool INV, int W, int SN, int T, int RMAX>
-__device__ __forceinline__ void fft_stage_any(float2* s, const float2* tw, const FftPlan& pl, int st) {
+template <bool INV, int W, int SN, int T, int RMAX, bool OUT = false, class Out = NoOut>
+__device__ __forceinline__ void fft_stage_any(float2* s, const float2* tw, const FftPlan& pl, int st,
+                                              Out&& out = Out{}) {
     switch (pl.r[st]) {
         case 32:
-            if constexpr (RMAX >= 32) fft_stage<32, INV, W, SN, T>(s, tw, pl, st);
+            if constexpr (RMAX >= 32) fft_stage<32, INV, W, SN, T, OUT>(s, tw, pl, st, out);
             break;
         case 16:
-            if constexpr (RMAX >= 16) fft_stage<16, INV, W, SN, T>(s, tw, pl, st);
+            if constexpr (RMAX >= 16) fft_stage<16, INV, W, SN, T, OUT>(s, tw, pl, st, out);
             break;
         case 10:
-            if constexpr (RMAX >= 16) fft_stage<10, INV, W, SN, T>(s, tw, pl, st);
+            if constexpr (RMAX >= 16) fft_stage<10, INV, W, SN, T, OUT>(s, tw, pl, st, out);
             break;
         case 6:
-            if constexpr (RMAX >= 16) fft_stage<6, INV, W, SN, T>(s, tw, pl, st);
+            if constexpr (RMAX >= 16) fft_stage<6, INV, W, SN, T, OUT>(s, tw, pl, st, out);
             break;
-        case 8: fft_stage<8, INV, W, SN, T>(s, tw, pl, st); break;
-        case 4: fft_stage<4, INV, W, SN, T>(s, tw, pl, st); break;
-        case 2: fft_stage<2, INV, W, SN, T>(s, tw, pl, st); break;
-        case 3: fft_stage<3, INV, W, SN, T>(s, tw, pl, st); break;
-        default: fft_stage<5, INV, W, SN, T>(s, tw, pl, st); break;
+        case 8: fft_stage<8, INV, W, SN, T, OUT>(s, tw, pl, st, out); break;
+        case 4: fft_stage<4, INV, W, SN, T, OUT>(s, tw, pl, st, out); break;
+        case 2: fft_stage<2, INV, W, SN, T, OUT>(s, tw, pl, st, out); break;
+        case 3: fft_stage<3, INV, W, SN, T, OUT>(s, tw, pl, st, out); break;
+        default: fft_stage<5, INV, W, SN, T, OUT>(s, tw, pl, st, out); break;
     }
 }
 
@@ -349,6 +361,16 @@ __device__ __forceinline__ void fft_tile(float2* __restrict__ s, const float2* _
     } else {
         for (int st = pl.nst - 1; st >= 0; --st) fft_stage_any<true, W, SN, T, RMAX>(s, tw, pl, st);
     }
+}
+
+// Inverse of the W lines with the last stage's natural-order results handed to out(e, w, v)
+// (element e of line w) instead of written back: every stage but the last ends with a block
+// barrier; the caller synchronises before it reuses s.
+template <int W, int SN, int T, int RMAX, class Out>
+__device__ __forceinline__ void ifft_tile_out(float2* __restrict__ s, const float2* __restrict__ tw,
+                                              const FftPlan& pl, Out&& out) {
+    for (int st = pl.nst - 1; st >= 1; --st) fft_stage_any<true, W, SN, T, RMAX>(s, tw, pl, st);
+    fft_stage_any<true, W, SN, T, RMAX, true>(s, tw, pl, 0, out);
 }
 
 // Per-stage twiddle tables of the plan (FftPlan::twoff; fewer than n entries), filled by the

@@ -162,8 +162,16 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const LineArgs a) {
             const float2* nb = a.base[bn] + on * a.ostride + (un - on * ncolt) * W;
             for (int e = threadIdx.x; e < n; e += T) prefetch_l2(nb + (int64_t)e * a.estride);
         }
-        fft_tile<INV, W, W, T, C::RMAX>(s, tw, a.pl);
-        store_cols<W, T>(s, base, n, a.estride, cols);
+        if constexpr (INV) {
+            // the last stage stores straight from registers
+            const int64_t es = a.estride;
+            ifft_tile_out<W, W, T, C::RMAX>(s, tw, a.pl, [&](int e, int w, float2 v) {
+                if (w < cols) base[e * es + w] = v;
+            });
+        } else {
+            fft_tile<INV, W, W, T, C::RMAX>(s, tw, a.pl);
+            store_cols<W, T>(s, base, n, a.estride, cols);
+        }
         __syncthreads();
     }
 }
@@ -500,15 +508,23 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
         else
             draw(std::false_type{});
         __syncthreads();
-        fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
         const int cols = min(WC, a.nzh - cb * WC);
         const int64_t off = b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)cb * WC;
-        for (int idx = threadIdx.x; idx < n * W; idx += T) {
-            const int e = idx / W, l = idx % W;
-            const int c = l < WC ? l : l - WC;
-            if (c < cols) {
-                float2* dst = !ONE ? (l < WC ? a.A : a.B) : (a.fields == XGEN_DELTA ? a.A : a.B);
-                if (dst) dst[off + e * estride + c] = s[idx];
+        if constexpr (ONE) {
+            // the last stage stores straight from registers
+            float2* dst = (a.fields == XGEN_DELTA ? a.A : a.B) + off;
+            ifft_tile_out<W, W, T, C::RMAX>(s, tw, a.pl, [&](int e, int w, float2 v) {
+                if (w < cols) dst[e * estride + w] = v;
+            });
+        } else {
+            fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
+            for (int idx = threadIdx.x; idx < n * W; idx += T) {
+                const int e = idx / W, l = idx % W;
+                const int c = l < WC ? l : l - WC;
+                if (c < cols) {
+                    float2* dst = l < WC ? a.A : a.B;
+                    if (dst) dst[off + e * estride + c] = s[idx];
+                }
             }
         }
         __syncthreads();
@@ -726,9 +742,10 @@ __global__ void __launch_bounds__(C::T, C::MINB) xinv_kernel(const XGenArgs a) {
             }
             __syncthreads();
         }
-        fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
-        store_cols<W, T>(s, dst_box + b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)kb * W, n,
-                         estride, cols);
+        float2* dst = dst_box + b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)kb * W;
+        ifft_tile_out<W, W, T, C::RMAX>(s, tw, a.pl, [&](int e, int w, float2 v) {
+            if (w < cols) dst[e * estride + w] = v;
+        });
         __syncthreads();
     }
 }
