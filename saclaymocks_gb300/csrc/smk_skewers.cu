@@ -57,6 +57,7 @@ struct SkArgs {
     float* eta_out;
     float* z_out;
     unsigned long long* counter;
+    int ss_nmax;              // longest small-scale FFT of the launch (shared-memory sizing)
 };
 
 __device__ __forceinline__ int ss_class(int nzz) {
@@ -92,11 +93,15 @@ struct SkewerGeo {
 // axis; value = sum(w rho) / sum(w), with periodic wrap.
 constexpr int GR = 3;
 
-__global__ void __launch_bounds__(SK_T, 2) skewer_kernel(const SkArgs a) {
+// GAUSS: the Gaussian 7^3 read (more registers, two blocks per SM); otherwise trilinear or
+// per-pixel inputs (three blocks per SM).  smem holds the small-scale FFT of the longest line
+// the launch needs (a.ss_nmax points: line, twiddles, slots).
+template <bool GAUSS>
+__global__ void __launch_bounds__(SK_T, GAUSS ? 2 : 3) skewer_kernel(const SkArgs a) {
     extern __shared__ float2 smem[];
-    float2* s = smem;                                          // FFT_MAX_N
-    float2* tw = smem + FFT_MAX_N;                             // FFT_MAX_N
-    int* sof = reinterpret_cast<int*>(smem + 2 * FFT_MAX_N);   // slot of each frequency
+    float2* s = smem;                                          // ss_nmax
+    float2* tw = smem + a.ss_nmax;                             // ss_nmax
+    int* sof = reinterpret_cast<int*>(smem + 2 * a.ss_nmax);   // slot of each frequency
     __shared__ long long item_sh;
     __shared__ SkewerGeo geo[2];
     __shared__ int sk_id[2], sk_np[2];
@@ -128,11 +133,25 @@ __global__ void __launch_bounds__(SK_T, 2) skewer_kernel(const SkArgs a) {
         __syncthreads();
         const int np0 = sk_np[0], np1 = sk_np[1];
         float inv_nz = 0.f;
+        // a pair whose small-scale field does not fit the launch's FFT length (a table built
+        // without smk_skewer_schedule's checks) gets NaN flux instead of a read past the line
+        bool too_long = false;
         if (a.ss_mode != SMK_SS_NONE) {
+            const int npmax = max(np0, np1);
             int nzz = a.ss_nz;
             if (nzz <= 0) {
                 nzz = 256;
-                while (nzz < np0 + 50) nzz *= 2;
+                while (nzz < npmax + 50 && nzz < a.ss_nmax) nzz *= 2;
+                too_long = nzz < npmax + 50;
+            } else {
+                too_long = npmax > nzz;
+            }
+        }
+        if (a.ss_mode != SMK_SS_NONE && !too_long) {
+            int nzz = a.ss_nz;
+            if (nzz <= 0) {
+                nzz = 256;
+                while (nzz < max(np0, np1) + 50) nzz *= 2;
             }
             const int cls = ss_class(nzz);
             const FftPlan& pl = a.plans[cls];
@@ -201,7 +220,7 @@ __global__ void __launch_bounds__(SK_T, 2) skewer_kernel(const SkArgs a) {
                 dl = __ldg(a.pix_delta + o);
                 et = a.pix_eta ? __ldg(a.pix_eta + o) : 0.f;
                 z = __ldg(a.pix_z + o);
-            } else if (a.interp == SMK_INTERP_GAUSS343) {
+            } else if (GAUSS) {
                 const SkewerGeo& g = geo[t];
                 int ci[3];
                 float ew[3][2 * GR + 1];
@@ -297,7 +316,7 @@ __global__ void __launch_bounds__(SK_T, 2) skewer_kernel(const SkArgs a) {
                 z = a.z_lo + (a.z_hi - a.z_lo) * (xc / nxf);
             }
             float ds = 0.f;
-            if (a.ss_mode != SMK_SS_NONE) ds = (t ? s[i].y : s[i].x) * inv_nz;
+            if (a.ss_mode != SMK_SS_NONE) ds = too_long ? __int_as_float(0x7fc00000) : (t ? s[i].y : s[i].x) * inv_nz;
             float pa = a.a, pb = a.b, pc = a.c;
             if (a.abc_mode == SMK_ABC_POWERLAW) {
                 pa = a.a * powf((1.0f + z) / a.a_zref1, a.a_power);
@@ -427,16 +446,20 @@ int smk_skewers_flux(const SmkSkewers* sk, const SmkSpectraParams* p, const floa
     cudaStream_t st = (cudaStream_t)stream;
     if (cudaMemsetAsync(a.counter, 0, sizeof(unsigned long long), st) != cudaSuccess)
         return check_launch("cudaMemsetAsync(counter)");
-    const size_t smem = 2 * FFT_MAX_N * sizeof(float2) + FFT_MAX_N * sizeof(int);
-    if (cudaFuncSetAttribute(skewer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    // small-scale lines: fixed ss_nz, or (ss_nz = 0) per skewer up to FFT_MAX_N
+    a.ss_nmax = p->ss_mode == SMK_SS_NONE ? 0 : (p->ss_nz > 0 ? p->ss_nz : FFT_MAX_N);
+    const size_t smem = 2 * (size_t)a.ss_nmax * sizeof(float2) + (size_t)a.ss_nmax * sizeof(int) + 16;
+    const bool gauss = p->interp == SMK_INTERP_GAUSS343;
+    auto kern = gauss ? skewer_kernel<true> : skewer_kernel<false>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return check_launch("cudaFuncSetAttribute(skewer_kernel)");
     int per_sm = 0, dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, skewer_kernel, SK_T, smem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, SK_T, smem) != cudaSuccess)
         return check_launch("occupancy(skewer_kernel)");
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(a.n_items, (int64_t)std::max(per_sm, 1) * nsm));
-    skewer_kernel<<<grid, SK_T, smem, st>>>(a);
+    kern<<<grid, SK_T, smem, st>>>(a);
     return check_launch("skewer_kernel");
 }
 
