@@ -97,7 +97,7 @@ constexpr int GR = 3;
 // per-pixel inputs (three blocks per SM).  smem holds the small-scale FFT of the longest line
 // the launch needs (a.ss_nmax points: line, twiddles, slots).
 template <bool GAUSS>
-__global__ void __launch_bounds__(SK_T, GAUSS ? 2 : 3) skewer_kernel(const SkArgs a) {
+__global__ void __launch_bounds__(SK_T, GAUSS ? 2 : 4) skewer_kernel(const SkArgs a) {
     extern __shared__ float2 smem[];
     float2* s = smem;                                          // ss_nmax
     float2* tw = smem + a.ss_nmax;                             // ss_nmax
