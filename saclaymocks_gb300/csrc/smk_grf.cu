@@ -7,7 +7,12 @@ namespace smk {
 
 // ------------------------------------------------------------------ P(k) normalisation
 __global__ void pk_norm_kernel(int nx, int ny, int nz, double kfac, float inv_k0, double* acc) {
+    // k_z of every column once per block (the per-mode arithmetic stays in float32: FP64 is a
+    // small fraction of the FP32 rate on this GPU)
+    extern __shared__ float kzt[];
     const int nzh = nz / 2 + 1;
+    for (int z = threadIdx.x; z < nzh; z += blockDim.x) kzt[z] = kaxis(z, nz, kfac, false);
+    __syncthreads();
     const int nchunk = (nzh + 63) / 64;
     const int64_t items = (int64_t)nx * ny * nchunk;
     double tsum = 0.0;
@@ -21,7 +26,7 @@ __global__ void pk_norm_kernel(int nx, int ny, int nz, double kfac, float inv_k0
         float part = 0.f;
         const int z1 = min(nzh, 64 * ch + 64);
         for (int z = 64 * ch; z < z1; ++z) {
-            const float kz = kaxis(z, nz, kfac, false);
+            const float kz = kzt[z];
             const float k = __fsqrt_rn(__fadd_rn(kxy, __fmul_rn(kz, kz)));
             const float kr = k * inv_k0;
             const float den = fmaf(kr, kr, 1.0f);
@@ -141,7 +146,8 @@ int smk_pk_normalisation(int32_t nx, int32_t ny, int32_t nz, double dcell, doubl
     const double kfac = 2.0 * (3.14159265358979323846 / dcell);
     const int64_t items = (int64_t)nx * ny * ((nz / 2 + 1 + 63) / 64);
     const int grid = (int)std::min<int64_t>(ceil_div(items, 256), 8LL * sm_count());
-    pk_norm_kernel<<<grid, 256, 0, st>>>(nx, ny, nz, kfac, (float)(1.0 / k0), amp_dev);
+    pk_norm_kernel<<<grid, 256, (size_t)(nz / 2 + 1) * sizeof(float), st>>>(nx, ny, nz, kfac, (float)(1.0 / k0),
+                                                                          amp_dev);
     int rc = check_launch("pk_norm_kernel");
     if (rc) return rc;
     const double vcell = (double)(float)(dcell * dcell * dcell);
