@@ -700,8 +700,9 @@ def main():
                     help="--grf-shape: draw the modes once into the workspace, one x inverse per field")
     ap.add_argument("--xgen-split", type=int, default=None, choices=[-1, 0, 1],
                     help="--grf-shape: x pass as one launch (0), two one-field launches (1), by footprint (-1)")
-    ap.add_argument("--xgen-cluster", type=int, default=None, choices=[-1, 0, 1],
-                    help="GPU-noise x pass on four-CTA clusters: built-in rule (-1), never (0), always (1)")
+    ap.add_argument("--xgen-cluster", type=int, default=None, choices=[-1, 0, 1, 2],
+                    help="GPU-noise x pass: built-in rule (-1), one-CTA tiles (0), four-CTA clusters "
+                         "drawing once (1), CTA pairs writing 128-byte segments (2)")
     ap.add_argument("--precision", default=None, const="1536,100000,1024", nargs="?",
                     help="only the FP32-vs-FP64 precision report: N,skewers,pixels (default 1536^3, 1e5 x 1024)")
     ap.add_argument("--variants", default=None,

@@ -144,9 +144,10 @@ int smk_tune_get(int32_t pass, int32_t n);
  *     address translation);
  *   SMK_TUNE_PREFETCH: the y and z passes pull their next tile into L2 while transforming the
  *     current one (1, default) or not (0);
- *   SMK_TUNE_XGEN_CLUSTER: GPU-noise x pass with eta on clusters of four CTAs, each mode drawn
- *     once and both fields written in one launch with row segments twice the one-CTA tile's
- *     width (1), never (0), or by the built-in rule (-1, default). */
+ *   SMK_TUNE_XGEN_CLUSTER: GPU-noise x pass on one-CTA tiles (0; the built-in rule, -1, picks
+ *     it), on clusters of four CTAs drawing each mode once and writing both fields in one launch
+ *     (1), or on CTA pairs writing one field per launch with row segments twice the one-CTA
+ *     tile's width (2).  All forms give identical boxes. */
 #define SMK_TUNE_XGEN_SPLIT 0
 #define SMK_TUNE_PREFETCH 1
 #define SMK_TUNE_XGEN_CLUSTER 2

@@ -158,7 +158,8 @@ def xgen_split(mode: int) -> int:
 
 
 def xgen_cluster(mode: int) -> int:
-    """x pass on four-CTA clusters (-1 built-in rule, 0 never, 1 whenever eta is drawn);
+    """x-pass form: -1 built-in rule, 0 one-CTA tiles, 1 four-CTA clusters (each mode drawn
+    once, both fields per launch), 2 CTA pairs (128-byte row segments, one field per launch);
     returns the previous value."""
     return tune_flag(SMK_TUNE_XGEN_CLUSTER, mode)
 

@@ -71,7 +71,8 @@ static struct ChoiceInit {
 
 static std::atomic<int> g_xgen_split{-1};  // -1: by footprint, 0: never, 1: always
 static std::atomic<int> g_prefetch{1};     // L2 prefetch of the next tile in the y and z passes
-static std::atomic<int> g_xgen_cluster{-1}; // -1: by default rule, 0: never, 1: when eta is drawn
+static std::atomic<int> g_xgen_cluster{-1}; // -1: built-in rule (one-CTA tiles), 0: one-CTA tiles,
+                                            // 1: four-CTA clusters (with eta), 2: CTA pairs
 
 static int length_class(int n) { return n <= 512 ? 0 : n <= 1024 ? 1 : n <= 2560 ? 2 : 3; }
 
@@ -239,7 +240,7 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
     if (gpu_noise) {
         // Fourier modes drawn in the x pass: no forward z / y passes
         if ((rc = mark(1)) || (rc = mark(2))) return rc;
-        XGenArgs ga;
+        XGenArgs ga = {};
         ga.pl = plx;
         ga.ply = ply;
         ga.A = d2;
@@ -291,6 +292,7 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
             const double pair_bytes = 2.0 * 4.0 * (double)p->batch * p->nx * p->ny * (double)pitch;
             const int sm = g_xgen_split.load(), cm = g_xgen_cluster.load();
             const bool cluster = p->want_eta && cm == 1;
+            ga.pair = cm == 2 ? 1 : 0;
             const bool split = !cluster && p->want_eta && (sm < 0 ? pair_bytes > 64.0 * (1ull << 30) : sm == 1);
             ga.fields = !p->want_eta ? XGEN_DELTA : (cluster ? XGEN_CLUSTER : (split ? XGEN_DELTA : XGEN_BOTH));
             if ((rc = run_xgen(vx, ga, st))) return rc;
@@ -363,7 +365,7 @@ int smk_tune_flag(int32_t flag, int32_t value, int32_t* previous) {
         if (value < -1 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: XGEN_SPLIT must be -1, 0 or 1");
         old = g_xgen_split.exchange(value);
     } else if (flag == SMK_TUNE_XGEN_CLUSTER) {
-        if (value < -1 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: XGEN_CLUSTER must be -1, 0 or 1");
+        if (value < -1 || value > 2) return fail(SMK_EINVAL, "smk_tune_flag: XGEN_CLUSTER must be -1, 0, 1 or 2");
         old = g_xgen_cluster.exchange(value);
     } else if (flag == SMK_TUNE_PREFETCH) {
         if (value < 0 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: PREFETCH must be 0 or 1");

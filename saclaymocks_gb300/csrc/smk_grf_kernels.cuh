@@ -337,6 +337,7 @@ struct XGenArgs {
     // one x-inverse tile is one contiguous run of nx * 2^sh complex values.
     float2* S;
     int sh;
+    int pair;              // one-field launches on CTA pairs (xgp_kernel): 128-byte row segments
 };
 
 // GPU-noise mode arithmetic (no bit-level reference: the FP64 oracle restates the drawn modes
@@ -528,6 +529,114 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
             }
         }
         __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ GPU-noise x pass on CTA pairs
+// One field per launch (fields = XGEN_DELTA or XGEN_ETA) on clusters of two CTAs.  A tile is 2W
+// k_z columns of one (box, y slot); CTA h draws the modes of its W columns for every x slot and
+// takes their x inverse in its own shared memory, then writes the x slots of half h for all
+// 2W columns (W read from the partner through distributed shared memory), so every output row
+// segment is 2W * 8 bytes (128 B for W = 8) where a one-CTA tile writes W * 8.  Each mode is
+// drawn once per launch, as in xgen_kernel.
+// smem: s[n*W] | tw[n] | kx[n] | ix[n] | kzt[nzh]  (same offsets in both CTAs)
+template <class C>
+__global__ void __launch_bounds__(C::T, C::MINB) xgp_kernel(const XGenArgs a) {
+    constexpr int W = C::W, T = C::T;
+    constexpr int NP = W / 2;
+    static_assert(W % 2 == 0, "xgp tiles hold column pairs");
+    cg::cluster_group cl = cg::this_cluster();
+    const int h = (int)cl.block_rank();
+    extern __shared__ float2 smem[];
+    const int n = a.pl.n;  // == nx
+    float2* s = smem;
+    float2* tw = s + n * W;
+    float* kx = reinterpret_cast<float*>(tw + n);
+    int* ix = reinterpret_cast<int*>(kx + n);
+    float* kzt = reinterpret_cast<float*>(ix + n);
+    fill_stage_twiddles(tw, a.pl);
+    for (int e = threadIdx.x; e < n; e += T) {
+        const int fr = freq_of_slot(a.pl, e);
+        ix[e] = fr;
+        kx[e] = kaxis(fr, n, a.kfac, true);
+    }
+    for (int z = threadIdx.x; z < a.nzh; z += T) kzt[z] = kaxis(z, a.nz, a.kfac, false);
+    cl.sync();   // both CTAs started (and filled their tables) before any remote access
+    const float2* s_lo = h == 0 ? s : cl.map_shared_rank(s, 0);   // columns 0..W-1 of the tile
+    const float2* s_hi = h == 1 ? s : cl.map_shared_rank(s, 1);   // columns W..2W-1
+    const float scale_c = pk_scale_c(a);
+    const bool eta = a.fields == XGEN_ETA;
+    float2* box = eta ? a.B : a.A;
+    const int nh = n / 2;
+    const int ec0 = h ? nh : 0, ec1 = h ? n : nh;   // x slots this CTA writes
+    const int64_t ncolt = ceil_div(a.nzh, 2 * W);
+    const int64_t ntiles = (int64_t)a.batch * a.ny * ncolt;
+    const int64_t estride = (int64_t)a.ny * a.cp;
+    const int64_t ncl = gridDim.x / 2;
+    for (int64_t tile = blockIdx.x / 2; tile < ntiles; tile += ncl) {
+        const int64_t o = tile / ncolt;  // b*ny + y slot
+        const int cb = (int)(tile - o * ncolt);
+        const int64_t b = o / a.ny;
+        const int yslot = (int)(o - b * a.ny);
+        const int iy = freq_of_slot(a.ply, yslot);
+        const int iym = iy == 0 ? 0 : a.ny - iy;
+        const float ky = kaxis(iy, a.ny, a.kfac, true);
+        const uint64_t seed = a.seed + (uint64_t)b;
+        const int col0 = cb * 2 * W + h * W;
+        auto draw = [&](auto chk) {
+#pragma unroll 2
+            for (int idx = threadIdx.x; idx < n * NP; idx += T) {
+                const int e = idx / NP, pr = idx % NP;
+                const float kxv = kx[e];
+                const ModePair mp = draw_pair<decltype(chk)::value>(a, seed, ix[e], iy, iym, kxv, ky, col0 + 2 * pr,
+                                                                     kzt, scale_c);
+                float2 v0 = mp.d[0], v1 = mp.d[1];
+                if (eta) {
+                    v0 = eta_from_inv_k2(a.eta_comp, v0, kxv, ky, mp.kz[0], mp.ikk[0], a.vfac);
+                    v1 = eta_from_inv_k2(a.eta_comp, v1, kxv, ky, mp.kz[1], mp.ikk[1], a.vfac);
+                }
+                *reinterpret_cast<float4*>(s + e * W + 2 * pr) = make_float4(v0.x, v0.y, v1.x, v1.y);
+            }
+        };
+        if (tile_needs_check(a, col0, W))
+            draw(std::true_type{});
+        else
+            draw(std::false_type{});
+        __syncthreads();
+        fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
+        cl.sync();   // the partner's transform is complete
+        const int cols = min(2 * W, a.nzh - cb * 2 * W);
+        float2* dst = box + b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)cb * 2 * W;
+        constexpr int U = 4;
+        const int items = (ec1 - ec0) * W;   // column pairs of the half
+        for (int base = threadIdx.x; base < items; base += U * T) {
+            float4 v[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int idx = base + u * T;
+                if (idx < items) {
+                    const int e = ec0 + idx / W, c = 2 * (idx % W);
+                    v[u] = *reinterpret_cast<const float4*>((c < W ? s_lo : s_hi) + e * W + (c & (W - 1)));
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int idx = base + u * T;
+                if (idx < items) {
+                    const int e = ec0 + idx / W, c = 2 * (idx % W);
+                    float2* d = dst + e * estride + c;
+                    if (c + 1 < cols)
+                        *reinterpret_cast<float4*>(d) = v[u];
+                    else if (c < cols)
+                        *d = make_float2(v[u].x, v[u].y);
+                }
+            }
+        }
+        // the partner's shared loads above have returned (their values feed the stores): the
+        // next tile may overwrite the tiles once both CTAs arrive; relaxed, so the stores stay
+        // in flight
+        asm volatile("barrier.cluster.arrive.relaxed.aligned;\n" ::: "memory");
+        asm volatile("barrier.cluster.wait.aligned;\n" ::: "memory");
     }
 }
 
@@ -1260,10 +1369,13 @@ static int launch_xpass(const XArgs& a, cudaStream_t st) {
 
 template <class C>
 static int launch_xgc(const XGenArgs& a, cudaStream_t st);
+template <class C>
+static int launch_xgp(const XGenArgs& a, cudaStream_t st);
 
 template <class C>
 static int launch_xgen(const XGenArgs& a, cudaStream_t st) {
     if (a.fields == XGEN_CLUSTER) return launch_xgc<C>(a, st);
+    if (a.pair && a.fields != XGEN_BOTH) return launch_xgp<C>(a, st);
     if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xgen_kernel");
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 +
                         (size_t)a.nzh * 4 + 16;
@@ -1308,6 +1420,36 @@ static int launch_xgc(const XGenArgs& a, cudaStream_t st) {
     cfg.gridDim = dim3((unsigned)(4 * std::min<int64_t>(nclusters, ntiles)), 1, 1);
     if (cudaLaunchKernelEx(&cfg, xgc_kernel<C>, a) != cudaSuccess) return check_launch("xgc_kernel");
     return check_launch("xgc_kernel");
+}
+
+// Clusters of two CTAs (xgp_kernel), as many as can be resident, at most one per tile.
+template <class C>
+static int launch_xgp(const XGenArgs& a, cudaStream_t st) {
+    if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xgp_kernel");
+    const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 +
+                        (size_t)a.nzh * 4 + 16;
+    const int64_t ntiles = (int64_t)a.batch * a.ny * ceil_div(a.nzh, 2 * C::W);
+    if (cudaFuncSetAttribute(xgp_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return check_launch("cudaFuncSetAttribute(xgp)");
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(C::T, 1, 1);
+    cfg.gridDim = dim3(2 * sm_count(), 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, xgp_kernel<C>, &cfg) != cudaSuccess)
+        return check_launch("cudaOccupancyMaxActiveClusters(xgp)");
+    if (nclusters < 1) return fail(SMK_ENOTSUPP, "xgp_kernel: no cluster of 2 fits (smem %zu B)", smem);
+    cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(nclusters, ntiles)), 1, 1);
+    if (cudaLaunchKernelEx(&cfg, xgp_kernel<C>, a) != cudaSuccess) return check_launch("xgp_kernel");
+    return check_launch("xgp_kernel");
 }
 
 template <class C>
