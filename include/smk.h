@@ -151,6 +151,7 @@ int smk_tune_get(int32_t pass, int32_t n);
 #define SMK_TUNE_XGEN_SPLIT 0
 #define SMK_TUNE_PREFETCH 1
 #define SMK_TUNE_XGEN_CLUSTER 2
+#define SMK_TUNE_TMA 3  /* y pass tiles loaded by TMA tensor copies (1, default) or cp.async (0) */
 int smk_tune_flag(int32_t flag, int32_t value, int32_t* previous);
 
 /* ---------------------------------------------------------------- skewers (make_spectra +

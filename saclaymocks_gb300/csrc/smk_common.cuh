@@ -2,6 +2,7 @@
 // Philox4x32-10 counter-based random numbers, twiddle factors.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -16,6 +17,12 @@ int fail(int code, const char* fmt, ...);
 int check_launch(const char* what);
 
 inline int64_t div_up(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Host: tiled TMA map over an array of 8-byte elements (complex float) with dims (d0, d1, d2),
+// element strides s1 (dim 1) and s2 (dim 2), boxes of b0 x b1 x 1, zero fill outside; false if
+// the driver cannot encode it (the caller then loads without TMA).
+bool encode_map_3d_8b(CUtensorMap* m, const void* base, uint64_t d0, uint64_t d1, uint64_t d2, uint64_t s1,
+                      uint64_t s2, uint32_t b0, uint32_t b1);
 
 // ------------------------------------------------------------------ complex helpers
 __host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
@@ -60,6 +67,42 @@ __device__ __forceinline__ void cp_async(void* smem_dst, const void* gmem_src, i
                      "r"(src_bytes));
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// ------------------------------------------------------------------ TMA tensor loads + mbarrier
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+// Makes barrier initialisation visible to the asynchronous (TMA) proxy.
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+// One arrival that also expects `bytes` of transactions (the TMA copies of this phase).
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+// Waits for the phase of the given parity to complete, for at most ~`limit` clock cycles;
+// false on time-out (the caller flags its results instead of waiting on).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, long long limit) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > limit) return false;
+    return true;
+}
+// Orders this thread's earlier generic-proxy shared-memory accesses before later TMA writes.
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+// Tiled 3D TMA load of one box at (x, y, z) into shared memory, completing on `bar`.
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n"
+        ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
 
 // Hints that pull the next tile's bytes into L2 while the current tile is transformed: one
 // cache line, or a 16-byte-aligned run of bytes (a multiple of 16) with the bulk form.

@@ -71,6 +71,7 @@ static struct ChoiceInit {
 
 static std::atomic<int> g_xgen_split{-1};  // -1: by footprint, 0: never, 1: always
 static std::atomic<int> g_prefetch{1};     // L2 prefetch of the next tile in the y and z passes
+static std::atomic<int> g_tma{1};          // TMA tensor loads of the y pass's tiles
 static std::atomic<int> g_xgen_cluster{-1}; // -1: built-in rule (one-CTA tiles), 0: one-CTA tiles,
                                             // 1: four-CTA clusters (with eta), 2: CTA pairs
 
@@ -224,7 +225,7 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
     if ((rc = mark(0))) return rc;
     float2* d2 = reinterpret_cast<float2*>(delta);
     float2* e2 = reinterpret_cast<float2*>(eta);
-    LineArgs ya;
+    LineArgs ya = {};
     ya.pl = ply;
     ya.base[0] = d2;
     ya.base[1] = e2;
@@ -234,6 +235,26 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
     ya.estride = cp;
     ya.ncol = nzh;
     ya.prefetch = g_prefetch.load();
+    ya.tma = 0;
+    if (g_tma.load()) {
+        // tile boxes: the variant's W columns x the largest divisor of ny up to 256 rows
+        const int wl = variant_table(PASS_LINE)[vy].w;
+        int rows = 1;
+        for (int d = std::min(p->ny, 256); d >= 1; --d)
+            if (p->ny % d == 0) {
+                rows = d;
+                break;
+            }
+        ya.box_rows = rows;
+        // every box lands on a 128-byte boundary of the tile
+        ya.tma = ((size_t)rows * wl * sizeof(float2)) % 128 == 0 &&
+                 encode_map_3d_8b(&ya.tmap[0], delta, (uint64_t)nzh, (uint64_t)p->ny, (uint64_t)ya.n_outer,
+                                  (uint64_t)cp, (uint64_t)ya.ostride, (uint32_t)wl, (uint32_t)rows) &&
+                         (!p->want_eta || encode_map_3d_8b(&ya.tmap[1], eta, (uint64_t)nzh, (uint64_t)p->ny,
+                                                           (uint64_t)ya.n_outer, (uint64_t)cp, (uint64_t)ya.ostride,
+                                                           (uint32_t)wl, (uint32_t)rows))
+                     ? 1 : 0;
+    }
     bool staged = false;
     const int64_t rows_per_box = (int64_t)p->nx * p->ny;
     const float inv_vcell = 1.0f / (float)(p->dcell * p->dcell * p->dcell);
@@ -367,6 +388,9 @@ int smk_tune_flag(int32_t flag, int32_t value, int32_t* previous) {
     } else if (flag == SMK_TUNE_XGEN_CLUSTER) {
         if (value < -1 || value > 2) return fail(SMK_EINVAL, "smk_tune_flag: XGEN_CLUSTER must be -1, 0, 1 or 2");
         old = g_xgen_cluster.exchange(value);
+    } else if (flag == SMK_TUNE_TMA) {
+        if (value < 0 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: TMA must be 0 or 1");
+        old = g_tma.exchange(value);
     } else if (flag == SMK_TUNE_PREFETCH) {
         if (value < 0 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: PREFETCH must be 0 or 1");
         old = g_prefetch.exchange(value);

@@ -128,18 +128,33 @@ struct LineArgs {
     int64_t n_outer, ostride, estride;
     int ncol;
     int prefetch;   // pull the next tile into L2 during the transform
+    // TMA tile loads (tma = 1): one 3D tensor map per buffer over (column, element, outer) of
+    // 8-byte complex values, boxes of W columns x box_rows elements (box_rows divides n)
+    int tma, box_rows;
+    CUtensorMap tmap[2];
 };
 
 // Forward: natural -> digit-reversed order along the axis (kept in HBM); inverse: back.
 // smem: s[n*W] | tw[n]
 template <class C, bool INV>
-__global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const LineArgs a) {
+__global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_constant__ LineArgs a) {
     constexpr int W = C::W, T = C::T;
-    extern __shared__ float2 smem[];
+    extern __shared__ __align__(128) float2 smem[];
+    __shared__ __align__(8) uint64_t bar;   // TMA completion of the current tile
+    __shared__ int timed_out;
     const int n = a.pl.n;
     float2* s = smem;
     float2* tw = s + n * W;
     fill_stage_twiddles(tw, a.pl);
+    if (threadIdx.x == 0) {
+        timed_out = 0;
+        if (a.tma) {
+            mbar_init(&bar, 1);
+            mbar_fence_init();
+        }
+    }
+    __syncthreads();
+    unsigned parity = 0;
     const int64_t ncolt = ceil_div(a.ncol, W);
     const int64_t tpb = a.n_outer * ncolt;
     const int64_t ntiles = tpb * a.nbuf;
@@ -150,9 +165,29 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const LineArgs a) {
         const int cb = (int)(t - o * ncolt);
         float2* base = a.base[buf] + o * a.ostride + (int64_t)cb * W;
         const int cols = min(W, a.ncol - cb * W);
-        load_cols_async<W, T>(s, base, n, a.estride, cols);
-        cp_async_wait_all();
-        __syncthreads();
+        if (a.tma) {
+            // n / box_rows tensor boxes of W columns (columns past ncol read as zeros)
+            if (threadIdx.x == 0) {
+                mbar_arrive_expect_tx(&bar, (unsigned)(n * W * sizeof(float2)));
+                for (int e0 = 0; e0 < n; e0 += a.box_rows) tma_load_3d(s + e0 * W, &a.tmap[buf], &bar, cb * W, e0, (int)o);
+            }
+            // bounded wait (~1 s at 2 GHz): on time-out the tile is poisoned with NaN, which the
+            // z pass counts as non-finite cells (SMK_ENULLBOX from smk_grf_check), and the
+            // block stops after a last bounded wait for its copies
+            if (!mbar_wait_bounded(&bar, parity, 2000000000LL)) timed_out = 1;
+            parity ^= 1u;
+            __syncthreads();
+            if (timed_out) {
+                if (threadIdx.x == 0) mbar_wait_bounded(&bar, parity ^ 1u, 2000000000LL);
+                __syncthreads();
+                for (int i = threadIdx.x; i < n * W; i += T) s[i] = make_float2(__int_as_float(0x7fc00000), 0.f);
+                __syncthreads();
+            }
+        } else {
+            load_cols_async<W, T>(s, base, n, a.estride, cols);
+            cp_async_wait_all();
+            __syncthreads();
+        }
         if (a.prefetch && tile + gridDim.x < ntiles) {
             // the next tile of this block: one line per row segment of its W columns
             const int64_t tn = tile + gridDim.x;
@@ -172,7 +207,9 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const LineArgs a) {
             fft_tile<INV, W, W, T, C::RMAX>(s, tw, a.pl);
             store_cols<W, T>(s, base, n, a.estride, cols);
         }
+        if (a.tma) fence_proxy_async_smem();   // this tile's shared accesses before the next TMA writes
         __syncthreads();
+        if (timed_out) break;
     }
 }
 

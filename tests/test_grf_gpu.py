@@ -87,6 +87,29 @@ def test_xgen_pairs_equal_one_cta_launches(G, shape):
     assert torch.equal(gotv.eta, refv.eta)
 
 
+@pytest.mark.parametrize("shape", [(24, 2560, 40), (6, 1536, 96), (10, 600, 72), (8, 45, 24)])
+def test_y_pass_tma_loads_equal_cp_async(G, shape):
+    """The y pass loading its tiles with TMA tensor copies gives the same boxes, bit for bit, as
+    the cp.async loads (GPU noise and host noise; y lengths with 256-, 200- and 45-row boxes)."""
+    from saclaymocks_gb300 import _lib
+    nx, ny, nz = shape
+    noise = torch.from_numpy(np.random.RandomState(4).normal(size=(nx, ny, nz)).astype(np.float32)).cuda()
+    prev = _lib.tune_flag(_lib.SMK_TUNE_TMA, 0)
+    try:
+        ref = G.make_boxes(nx, ny, nz, 2.19, seed=41, batch=2)
+        refh = G.make_boxes(nx, ny, nz, 2.19, noise=noise)
+        _lib.tune_flag(_lib.SMK_TUNE_TMA, 1)
+        got = G.make_boxes(nx, ny, nz, 2.19, seed=41, batch=2)
+        goth = G.make_boxes(nx, ny, nz, 2.19, noise=noise)
+        torch.cuda.synchronize()
+    finally:
+        _lib.tune_flag(_lib.SMK_TUNE_TMA, prev)
+    assert torch.equal(got.delta, ref.delta)
+    assert torch.equal(got.eta, ref.eta)
+    assert torch.equal(goth.delta, refh.delta)
+    assert torch.equal(goth.eta, refh.eta)
+
+
 def test_xgen_pairs_every_variant_is_exact(G):
     """Every x-pass tile variant run on CTA pairs matches the FP64 oracle."""
     import ctypes as C
