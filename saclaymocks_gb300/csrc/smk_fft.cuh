@@ -281,12 +281,18 @@ template <bool INV> struct Dft<32, INV> : DftComposite<32, INV> {};
 // OUT = false: results back to shared memory, then a block barrier.  OUT = true (the last
 // stage of an inverse, st = 0, natural-order outputs e = q + r m of line w): results go to
 // out(e, w, value) and there is no barrier (the caller synchronises before reusing s).
+// PRE: each loaded value v of element e, line w becomes pre(e, w, v) first (a pointwise factor
+// folded into the first stage an inverse executes).
 struct NoOut {
     __device__ __forceinline__ void operator()(int, int, float2) const {}
 };
-template <int R, bool INV, int W, int SN, int T, bool OUT = false, class Out = NoOut>
+struct NoPre {
+    __device__ __forceinline__ float2 operator()(int, int, float2 v) const { return v; }
+};
+template <int R, bool INV, int W, int SN, int T, bool OUT = false, bool PRE = false, class Out = NoOut,
+          class Pre = NoPre>
 __device__ __forceinline__ void fft_stage(float2* __restrict__ s, const float2* __restrict__ tw,
-                                          const FftPlan& pl, const int st, Out&& out = Out{}) {
+                                          const FftPlan& pl, const int st, Out&& out = Out{}, Pre&& pre = Pre{}) {
     const int m = pl.m[st];
     const int nb = (pl.n / R) * W;
     const float2* tws = tw + pl.twoff[st] - 1;
@@ -299,6 +305,11 @@ __device__ __forceinline__ void fft_stage(float2* __restrict__ s, const float2* 
         float2 v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) v[r] = p[r * m * SN];
+        if constexpr (PRE) {
+            const int e0 = blk * R * m + q;
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[r] = pre(e0 + r * m, w, v[r]);
+        }
         const float2* t = tws + q * (R - 1);   // t[r] = W_L^(r q), 1 <= r < R
         if (INV) {
             if (q != 0) {
@@ -324,27 +335,28 @@ __device__ __forceinline__ void fft_stage(float2* __restrict__ s, const float2* 
     if constexpr (!OUT) __syncthreads();
 }
 
-template <bool INV, int W, int SN, int T, int RMAX, bool OUT = false, class Out = NoOut>
+template <bool INV, int W, int SN, int T, int RMAX, bool OUT = false, bool PRE = false, class Out = NoOut,
+          class Pre = NoPre>
 __device__ __forceinline__ void fft_stage_any(float2* s, const float2* tw, const FftPlan& pl, int st,
-                                              Out&& out = Out{}) {
+                                              Out&& out = Out{}, Pre&& pre = Pre{}) {
     switch (pl.r[st]) {
         case 32:
-            if constexpr (RMAX >= 32) fft_stage<32, INV, W, SN, T, OUT>(s, tw, pl, st, out);
+            if constexpr (RMAX >= 32) fft_stage<32, INV, W, SN, T, OUT, PRE>(s, tw, pl, st, out, pre);
             break;
         case 16:
-            if constexpr (RMAX >= 16) fft_stage<16, INV, W, SN, T, OUT>(s, tw, pl, st, out);
+            if constexpr (RMAX >= 16) fft_stage<16, INV, W, SN, T, OUT, PRE>(s, tw, pl, st, out, pre);
             break;
         case 10:
-            if constexpr (RMAX >= 16) fft_stage<10, INV, W, SN, T, OUT>(s, tw, pl, st, out);
+            if constexpr (RMAX >= 16) fft_stage<10, INV, W, SN, T, OUT, PRE>(s, tw, pl, st, out, pre);
             break;
         case 6:
-            if constexpr (RMAX >= 16) fft_stage<6, INV, W, SN, T, OUT>(s, tw, pl, st, out);
+            if constexpr (RMAX >= 16) fft_stage<6, INV, W, SN, T, OUT, PRE>(s, tw, pl, st, out, pre);
             break;
-        case 8: fft_stage<8, INV, W, SN, T, OUT>(s, tw, pl, st, out); break;
-        case 4: fft_stage<4, INV, W, SN, T, OUT>(s, tw, pl, st, out); break;
-        case 2: fft_stage<2, INV, W, SN, T, OUT>(s, tw, pl, st, out); break;
-        case 3: fft_stage<3, INV, W, SN, T, OUT>(s, tw, pl, st, out); break;
-        default: fft_stage<5, INV, W, SN, T, OUT>(s, tw, pl, st, out); break;
+        case 8: fft_stage<8, INV, W, SN, T, OUT, PRE>(s, tw, pl, st, out, pre); break;
+        case 4: fft_stage<4, INV, W, SN, T, OUT, PRE>(s, tw, pl, st, out, pre); break;
+        case 2: fft_stage<2, INV, W, SN, T, OUT, PRE>(s, tw, pl, st, out, pre); break;
+        case 3: fft_stage<3, INV, W, SN, T, OUT, PRE>(s, tw, pl, st, out, pre); break;
+        default: fft_stage<5, INV, W, SN, T, OUT, PRE>(s, tw, pl, st, out, pre); break;
     }
 }
 
@@ -370,6 +382,19 @@ template <int W, int SN, int T, int RMAX, class Out>
 __device__ __forceinline__ void ifft_tile_out(float2* __restrict__ s, const float2* __restrict__ tw,
                                               const FftPlan& pl, Out&& out) {
     for (int st = pl.nst - 1; st >= 1; --st) fft_stage_any<true, W, SN, T, RMAX>(s, tw, pl, st);
+    fft_stage_any<true, W, SN, T, RMAX, true>(s, tw, pl, 0, out);
+}
+
+// The same with pre(e, w, v) applied to every input value as the first stage loads it.
+template <int W, int SN, int T, int RMAX, class Pre, class Out>
+__device__ __forceinline__ void ifft_tile_pre_out(float2* __restrict__ s, const float2* __restrict__ tw,
+                                                  const FftPlan& pl, Pre&& pre, Out&& out) {
+    if (pl.nst == 1) {
+        fft_stage_any<true, W, SN, T, RMAX, true, true>(s, tw, pl, 0, out, pre);
+        return;
+    }
+    fft_stage_any<true, W, SN, T, RMAX, false, true>(s, tw, pl, pl.nst - 1, NoOut{}, pre);
+    for (int st = pl.nst - 2; st >= 1; --st) fft_stage_any<true, W, SN, T, RMAX>(s, tw, pl, st);
     fft_stage_any<true, W, SN, T, RMAX, true>(s, tw, pl, 0, out);
 }
 

@@ -859,6 +859,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xinv_kernel(const XGenArgs a) {
     const int64_t nkb = ceil_div(a.nzh, W);
     const int64_t ntiles = nouter * nkb;
     const int64_t estride = (int64_t)a.ny * a.cp;
+    const unsigned run_bytes = (unsigned)((size_t)n * W * sizeof(float2));
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int kb = (int)(tile / nouter);
         const int64_t o = tile - (int64_t)kb * nouter;    // b*ny + y slot
@@ -867,31 +868,33 @@ __global__ void __launch_bounds__(C::T, C::MINB) xinv_kernel(const XGenArgs a) {
         const int cols = min(W, a.nzh - kb * W);
         // the tile's staged run: n lines of W columns, contiguous
         const float2* src = a.S + (((int64_t)kb * nouter + o) * n << a.sh);
-        load_cols_async<W, T>(s, src, n, W, cols);
+        load_cols_async<W, T>(s, src, n, W, W);
         cp_async_wait_all();
         __syncthreads();
         if (threadIdx.x == 0 && tile + gridDim.x < ntiles) {
             // the next tile's run (tiles are consecutive runs): one bulk L2 prefetch
             const int64_t tn = tile + gridDim.x;
             const int kbn = (int)(tn / nouter);
-            prefetch_l2_bulk(a.S + (((int64_t)kbn * nouter + (tn - (int64_t)kbn * nouter)) * n << a.sh),
-                             (uint32_t)((size_t)n * W * sizeof(float2)));
-        }
-        if (eta) {
-            const float ky = kaxis(freq_of_slot(a.ply, yslot), a.ny, a.kfac, true);
-            for (int idx = threadIdx.x; idx < n * W; idx += T) {
-                const int e = idx / W, w = idx % W;
-                if (w < cols) {
-                    const float kxv = kx[e], kz_ = kzt[kb * W + w];
-                    s[idx] = eta_from_inv_k2(a.eta_comp, s[idx], kxv, ky, kz_, mode_inv_k2(mode_k2(kxv, ky, kz_)), a.vfac);
-                }
-            }
-            __syncthreads();
+            prefetch_l2_bulk(a.S + (((int64_t)kbn * nouter + (tn - (int64_t)kbn * nouter)) * n << a.sh), run_bytes);
         }
         float2* dst = dst_box + b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)kb * W;
-        ifft_tile_out<W, W, T, C::RMAX>(s, tw, a.pl, [&](int e, int w, float2 v) {
+        auto out = [&](int e, int w, float2 v) {
             if (w < cols) dst[e * estride + w] = v;
-        });
+        };
+        if (eta) {
+            // eta_k = (k_i k_j / k^2) delta_k applied as the first stage loads each value
+            const float ky = kaxis(freq_of_slot(a.ply, yslot), a.ny, a.kfac, true);
+            const int zc = kb * W;
+            ifft_tile_pre_out<W, W, T, C::RMAX>(
+                s, tw, a.pl,
+                [&](int e, int w, float2 v) {
+                    const float kxv = kx[e], kz_ = kzt[min(zc + w, a.nzh - 1)];
+                    return eta_from_inv_k2(a.eta_comp, v, kxv, ky, kz_, mode_inv_k2(mode_k2(kxv, ky, kz_)), a.vfac);
+                },
+                out);
+        } else {
+            ifft_tile_out<W, W, T, C::RMAX>(s, tw, a.pl, out);
+        }
         __syncthreads();
     }
 }
