@@ -142,7 +142,7 @@ def load(path: str | None = None):
     return lib
 
 
-SMK_TUNE_XGEN_SPLIT, SMK_TUNE_PREFETCH, SMK_TUNE_XGEN_CLUSTER, SMK_TUNE_TMA = 0, 1, 2, 3
+SMK_TUNE_XGEN_SPLIT, SMK_TUNE_PREFETCH, SMK_TUNE_XGEN_CLUSTER, SMK_TUNE_TMA, SMK_TUNE_TMA_WAIT_TEST = 0, 1, 2, 3, 4
 
 
 def tune_flag(flag: int, value: int) -> int:

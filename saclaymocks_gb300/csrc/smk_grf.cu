@@ -72,6 +72,7 @@ static struct ChoiceInit {
 static std::atomic<int> g_xgen_split{-1};  // -1: by footprint, 0: never, 1: always
 static std::atomic<int> g_prefetch{1};     // L2 prefetch of the next tile in the y and z passes
 static std::atomic<int> g_tma{1};          // TMA tensor loads of the y pass's tiles
+static std::atomic<int> g_tma_wait_test{0};  // y-pass TMA waits made to run out (failure test)
 static std::atomic<int> g_xgen_cluster{-1}; // -1: built-in rule (one-CTA tiles), 0: one-CTA tiles,
                                             // 1: four-CTA clusters (with eta), 2: CTA pairs
 
@@ -236,6 +237,9 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
     ya.ncol = nzh;
     ya.prefetch = g_prefetch.load();
     ya.tma = 0;
+    const bool wait_test = g_tma_wait_test.load() != 0;
+    ya.tma_extra_tx = wait_test ? 16 : 0;
+    ya.tma_wait_limit = wait_test ? 20000000LL : 2000000000LL;   // ~10 ms / ~1 s at 2 GHz
     if (g_tma.load()) {
         // tile boxes: the variant's W columns x the largest divisor of ny up to 256 rows
         const int wl = variant_table(PASS_LINE)[vy].w;
@@ -388,6 +392,9 @@ int smk_tune_flag(int32_t flag, int32_t value, int32_t* previous) {
     } else if (flag == SMK_TUNE_XGEN_CLUSTER) {
         if (value < -1 || value > 2) return fail(SMK_EINVAL, "smk_tune_flag: XGEN_CLUSTER must be -1, 0, 1 or 2");
         old = g_xgen_cluster.exchange(value);
+    } else if (flag == SMK_TUNE_TMA_WAIT_TEST) {
+        if (value < 0 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: TMA_WAIT_TEST must be 0 or 1");
+        old = g_tma_wait_test.exchange(value);
     } else if (flag == SMK_TUNE_TMA) {
         if (value < 0 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: TMA must be 0 or 1");
         old = g_tma.exchange(value);

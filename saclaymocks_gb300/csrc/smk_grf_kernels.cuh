@@ -131,6 +131,10 @@ struct LineArgs {
     // TMA tile loads (tma = 1): one 3D tensor map per buffer over (column, element, outer) of
     // 8-byte complex values, boxes of W columns x box_rows elements (box_rows divides n)
     int tma, box_rows;
+    // wait test (SMK_TUNE_TMA_WAIT_TEST): extra bytes the barrier expects beyond the copies, so
+    // the phase never completes, and the wait limit in clock cycles
+    int tma_extra_tx;
+    long long tma_wait_limit;
     CUtensorMap tmap[2];
 };
 
@@ -168,17 +172,17 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
         if (a.tma) {
             // n / box_rows tensor boxes of W columns (columns past ncol read as zeros)
             if (threadIdx.x == 0) {
-                mbar_arrive_expect_tx(&bar, (unsigned)(n * W * sizeof(float2)));
+                mbar_arrive_expect_tx(&bar, (unsigned)(n * W * sizeof(float2)) + (unsigned)a.tma_extra_tx);
                 for (int e0 = 0; e0 < n; e0 += a.box_rows) tma_load_3d(s + e0 * W, &a.tmap[buf], &bar, cb * W, e0, (int)o);
             }
             // bounded wait (~1 s at 2 GHz): on time-out the tile is poisoned with NaN, which the
             // z pass counts as non-finite cells (SMK_ENULLBOX from smk_grf_check), and the
             // block stops after a last bounded wait for its copies
-            if (!mbar_wait_bounded(&bar, parity, 2000000000LL)) timed_out = 1;
+            if (!mbar_wait_bounded(&bar, parity, a.tma_wait_limit)) timed_out = 1;
             parity ^= 1u;
             __syncthreads();
             if (timed_out) {
-                if (threadIdx.x == 0) mbar_wait_bounded(&bar, parity ^ 1u, 2000000000LL);
+                if (threadIdx.x == 0) mbar_wait_bounded(&bar, parity ^ 1u, a.tma_wait_limit);
                 __syncthreads();
                 for (int i = threadIdx.x; i < n * W; i += T) s[i] = make_float2(__int_as_float(0x7fc00000), 0.f);
                 __syncthreads();

@@ -110,6 +110,32 @@ def test_y_pass_tma_loads_equal_cp_async(G, shape):
     assert torch.equal(goth.eta, refh.eta)
 
 
+def test_y_pass_tma_wait_running_out_is_reported(G):
+    """A y-pass TMA wait that runs out (the barrier made to expect more bytes than its copies
+    bring) ends within its limit, leaves NaN that the box check reports as SMK_ENULLBOX, and
+    the next call on the same context is correct again."""
+    from saclaymocks_gb300 import _lib
+    from saclaymocks_gb300._lib import SmkError
+    nx, ny, nz = 8, 512, 16
+    good = G.make_boxes(nx, ny, nz, 2.19, seed=7)
+    torch.cuda.synchronize()
+    prev = _lib.tune_flag(_lib.SMK_TUNE_TMA, 1)
+    _lib.tune_flag(_lib.SMK_TUNE_TMA_WAIT_TEST, 1)
+    try:
+        bad = G.make_boxes(nx, ny, nz, 2.19, seed=7)
+        torch.cuda.synchronize()
+    finally:
+        _lib.tune_flag(_lib.SMK_TUNE_TMA_WAIT_TEST, 0)
+        _lib.tune_flag(_lib.SMK_TUNE_TMA, prev)
+    with pytest.raises(SmkError) as e:
+        bad.check()
+    assert e.value.status == _lib.SMK_ENULLBOX
+    again = G.make_boxes(nx, ny, nz, 2.19, seed=7)
+    torch.cuda.synchronize()
+    again.check()
+    assert torch.equal(again.delta, good.delta)
+
+
 def test_xgen_pairs_every_variant_is_exact(G):
     """Every x-pass tile variant run on CTA pairs matches the FP64 oracle."""
     import ctypes as C
