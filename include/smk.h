@@ -151,7 +151,8 @@ int smk_tune_get(int32_t pass, int32_t n);
 #define SMK_TUNE_XGEN_SPLIT 0
 #define SMK_TUNE_PREFETCH 1
 #define SMK_TUNE_XGEN_CLUSTER 2
-#define SMK_TUNE_TMA 3  /* y pass tiles loaded by TMA tensor copies (1, default) or cp.async (0) */
+#define SMK_TUNE_TMA 3  /* y pass tiles loaded by TMA tensor copies (1, default), loaded and */
+                        /* stored by TMA tensor copies (2), or loaded by cp.async (0)         */
 /* Failure test of the y pass's bounded TMA waits (0 by default): 1 makes every tile's barrier
  * expect 16 bytes more than its copies deliver, with a ~10 ms limit, so each wait runs out; the
  * pass then writes NaN and smk_grf_check reports SMK_ENULLBOX.  Nothing faults or hangs. */

@@ -104,6 +104,19 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
         : "memory");
 }
 
+// Tiled 3D TMA store of one box from shared memory at (x, y, z) (elements outside the map's
+// dims are not written), in the thread's current bulk group.
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, const void* src, int x, int y, int z) {
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];\n"
+                 ::"l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(src))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
+// Waits until the shared-memory sources of this thread's bulk stores have been read.
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory"); }
+// Waits until this thread's bulk stores are complete.
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
+
 // Hints that pull the next tile's bytes into L2 while the current tile is transformed: one
 // cache line, or a 16-byte-aligned run of bytes (a multiple of 16) with the bulk form.
 __device__ __forceinline__ void prefetch_l2(const void* p) {

@@ -257,7 +257,7 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
                          (!p->want_eta || encode_map_3d_8b(&ya.tmap[1], eta, (uint64_t)nzh, (uint64_t)p->ny,
                                                            (uint64_t)ya.n_outer, (uint64_t)cp, (uint64_t)ya.ostride,
                                                            (uint32_t)wl, (uint32_t)rows))
-                     ? 1 : 0;
+                     ? g_tma.load() : 0;
     }
     bool staged = false;
     const int64_t rows_per_box = (int64_t)p->nx * p->ny;
@@ -396,7 +396,7 @@ int smk_tune_flag(int32_t flag, int32_t value, int32_t* previous) {
         if (value < 0 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: TMA_WAIT_TEST must be 0 or 1");
         old = g_tma_wait_test.exchange(value);
     } else if (flag == SMK_TUNE_TMA) {
-        if (value < 0 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: TMA must be 0 or 1");
+        if (value < 0 || value > 2) return fail(SMK_EINVAL, "smk_tune_flag: TMA must be 0, 1 or 2");
         old = g_tma.exchange(value);
     } else if (flag == SMK_TUNE_PREFETCH) {
         if (value < 0 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: PREFETCH must be 0 or 1");

@@ -172,6 +172,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
         if (a.tma) {
             // n / box_rows tensor boxes of W columns (columns past ncol read as zeros)
             if (threadIdx.x == 0) {
+                if (a.tma == 2) bulk_wait_read_all();   // the previous tile's stores have read s
                 mbar_arrive_expect_tx(&bar, (unsigned)(n * W * sizeof(float2)) + (unsigned)a.tma_extra_tx);
                 for (int e0 = 0; e0 < n; e0 += a.box_rows) tma_load_3d(s + e0 * W, &a.tmap[buf], &bar, cb * W, e0, (int)o);
             }
@@ -201,7 +202,17 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
             const float2* nb = a.base[bn] + on * a.ostride + (un - on * ncolt) * W;
             for (int e = threadIdx.x; e < n; e += T) prefetch_l2(nb + (int64_t)e * a.estride);
         }
-        if constexpr (INV) {
+        if (INV && a.tma == 2) {
+            // transform in shared memory, then TMA tensor stores of the tile (columns past ncol
+            // are not written); the next load waits until these stores have read s
+            fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
+            fence_proxy_async_smem();
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (int e0 = 0; e0 < n; e0 += a.box_rows) tma_store_3d(&a.tmap[buf], s + e0 * W, cb * W, e0, (int)o);
+                bulk_commit();
+            }
+        } else if constexpr (INV) {
             // the last stage stores straight from registers
             const int64_t es = a.estride;
             ifft_tile_out<W, W, T, C::RMAX>(s, tw, a.pl, [&](int e, int w, float2 v) {
@@ -215,6 +226,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
         __syncthreads();
         if (timed_out) break;
     }
+    if (a.tma == 2 && threadIdx.x == 0) bulk_wait_all();
 }
 
 // ------------------------------------------------------------------ fused x pass

@@ -98,16 +98,17 @@ def test_y_pass_tma_loads_equal_cp_async(G, shape):
     try:
         ref = G.make_boxes(nx, ny, nz, 2.19, seed=41, batch=2)
         refh = G.make_boxes(nx, ny, nz, 2.19, noise=noise)
-        _lib.tune_flag(_lib.SMK_TUNE_TMA, 1)
-        got = G.make_boxes(nx, ny, nz, 2.19, seed=41, batch=2)
-        goth = G.make_boxes(nx, ny, nz, 2.19, noise=noise)
-        torch.cuda.synchronize()
+        for mode in (1, 2):   # TMA loads; TMA loads and TMA tensor stores
+            _lib.tune_flag(_lib.SMK_TUNE_TMA, mode)
+            got = G.make_boxes(nx, ny, nz, 2.19, seed=41, batch=2)
+            goth = G.make_boxes(nx, ny, nz, 2.19, noise=noise)
+            torch.cuda.synchronize()
+            assert torch.equal(got.delta, ref.delta)
+            assert torch.equal(got.eta, ref.eta)
+            assert torch.equal(goth.delta, refh.delta)
+            assert torch.equal(goth.eta, refh.eta)
     finally:
         _lib.tune_flag(_lib.SMK_TUNE_TMA, prev)
-    assert torch.equal(got.delta, ref.delta)
-    assert torch.equal(got.eta, ref.eta)
-    assert torch.equal(goth.delta, refh.delta)
-    assert torch.equal(goth.eta, refh.eta)
 
 
 def test_y_pass_tma_wait_running_out_is_reported(G):
