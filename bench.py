@@ -299,6 +299,18 @@ def run_ours(args, cfg):
     traffic = [7.81 * modes * 2, 16.0 * modes * 2, 16.14 * modes * 2][dom] / 1e9
     grf_ms = float(np.sum(pass_ms))
     step_ms = ms / args.steps
+    # The x pass is instruction-bound, so its issue-slot roofline is reported beside the HBM one:
+    # warp instructions per mode and field from the same ncu capture (1.311e9 for 2560x128x769
+    # modes, one field), scaled by the modes of this launch; peak = SMs x 4 schedulers x the
+    # median SM clock sampled during the timed region
+    clk_sum = clk.summary()
+    sm_hz = float(clk_sum.get("sm_mhz") or 2070.0) * 1e6
+    nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+    x_winst = 1.311e9 / (2560 * 128 * 769) * modes * 2
+    issue = {"kernel": "x_gen", "warp_instructions": x_winst,
+             "achieved_per_s": x_winst / (pass_ms[0] * 1e-3), "peak_per_s": nsm * 4 * sm_hz,
+             "frac": x_winst / (pass_ms[0] * 1e-3) / (nsm * 4 * sm_hz),
+             "basis": "ncu smsp__inst_executed.sum per mode and field, scaled; peak SMs x 4 x SM clock"}
     value = aggregate_value(cells, world, step_ms * 1e-3)
     res = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
@@ -314,13 +326,14 @@ def run_ours(args, cfg):
                         "traffic": traffic, "traffic_unit": "GB per pass (ncu, scaled)",
                         "algorithmic_bytes": pass_bytes[dom] / 1e9,
                         "per_pass_frac": {n: round(b / (m * 1e-3) / 1e9 / peak, 3)
-                                          for n, b, m in zip(pass_names, pass_bytes, pass_ms)}},
+                                          for n, b, m in zip(pass_names, pass_bytes, pass_ms)},
+                        "issue": issue},
            "e2e": {"value": aggregate_value(cells, world, e2e_s), "unit": "cells/s",
                    "h2d_bytes_per_step": chunk.h2d_bytes(), "d2h_bytes_per_step": chunk.d2h_bytes(),
                    "ms_per_step": e2e_s * 1e3},
            "gpu_launches": args.steps * (grf.grf_launches(nx, ny, nz) + 1),
            "tile_variants": tuned,
-           "clocks": clk.summary(),
+           "clocks": clk_sum,
            "fit": fit_res,
            "batching": batch_res}
     if not args.no_cpu:
