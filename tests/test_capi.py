@@ -117,3 +117,18 @@ def test_tune_flags(lib):
     assert _lib.tune_flag(_lib.SMK_TUNE_PREFETCH, 0) == 1
     assert _lib.tune_flag(_lib.SMK_TUNE_PREFETCH, 1) == 0
     assert lib.smk_tune_flag(_lib.SMK_TUNE_PREFETCH, 2, None) == _lib.SMK_EINVAL
+
+
+def test_x_pass_form_and_tma_flags(lib):
+    """The x-pass form (one-CTA tiles, four-CTA clusters, CTA pairs), the y pass's TMA mode and
+    the TMA wait test switch are host-only settings with checked ranges."""
+    for flag, good, bad in ((_lib.SMK_TUNE_XGEN_CLUSTER, (-1, 0, 1, 2), (3, -2)),
+                            (_lib.SMK_TUNE_TMA, (0, 1, 2), (3, -1)),
+                            (_lib.SMK_TUNE_TMA_WAIT_TEST, (0, 1), (2, -1))):
+        first = _lib.tune_flag(flag, good[0])
+        for v in good[1:]:
+            _lib.tune_flag(flag, v)
+        assert _lib.tune_flag(flag, first) == good[-1]
+        for v in bad:
+            assert lib.smk_tune_flag(flag, v, None) == _lib.SMK_EINVAL
+    assert _lib.tune_flag(_lib.SMK_TUNE_TMA_WAIT_TEST, 0) == 0
