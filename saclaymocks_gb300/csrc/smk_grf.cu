@@ -105,6 +105,11 @@ int variant_for(int pass, int n) {
     const int cnt = variant_count(pass);
     const int c = g_choice[pass][length_class(n)].load();
     if (c >= 0 && c < cnt && t[c].nmax >= n) return c;
+    // built-in choice: the z inverse prefers the one-warp-per-row-pair engine (W = 0), every
+    // pass otherwise the first variant whose line length covers n
+    if (pass == PASS_ZINV)
+        for (int i = 0; i < cnt; ++i)
+            if (t[i].w == 0 && t[i].nmax >= n) return i;
     for (int i = 0; i < cnt; ++i)
         if (t[i].nmax >= n) return i;
     return cnt - 1;
