@@ -126,7 +126,9 @@ int smk_pk_normalisation(int32_t nx, int32_t ny, int32_t nz, double dcell, doubl
 /* Tile variants of the HBM passes (autotuner hooks; no counterpart in the reference).  Each
  * pass has a table of variants (tile width W and threads per block T, valid up to a line
  * length); smk_tune_set picks the variant used for the lengths of n's class (<=512, <=1024,
- * <=2560, <=4096; v = -1 restores the built-in choice).  Process-wide setting. */
+ * <=2560, <=4096; v = -1 restores the built-in choice).  Process-wide setting.  The built-in
+ * choice is the first variant whose length covers n; for SMK_PASS_ZINV the first such variant
+ * with W = 0 (one warp per row pair, as many warps per block as fit, up to T/32). */
 #define SMK_PASS_ZFWD 0  /* r2c along z (host noise)                              */
 #define SMK_PASS_LINE 1  /* c2c along y                                            */
 #define SMK_PASS_XPASS 2 /* x pass of host noise                                   */
