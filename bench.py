@@ -680,20 +680,19 @@ def run_grf_only(args, shape):
         from saclaymocks_gb300 import tune
         tuned = tune.tune_grf(nx, ny, nz, out=boxes, workspace=ws, use_cache=False)
     for _ in range(args.warmup):
-        grf.make_boxes(nx, ny, nz, seed=1, amp=amp, out=boxes, workspace=ws, want_eta=want_eta,
-                       staging=args.staging)
+        grf.make_boxes(nx, ny, nz, seed=1, amp=amp, out=boxes, workspace=ws, want_eta=want_eta)
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(args.steps)]
     for e in [x for row in evs for x in row]:
         e.record()
     torch.cuda.synchronize()
     for k in range(args.steps):
         out = grf.make_boxes(nx, ny, nz, seed=1, amp=amp, out=boxes, workspace=ws, pass_events=evs[k],
-                             want_eta=want_eta, staging=args.staging)
+                             want_eta=want_eta)
     torch.cuda.synchronize()
     out.check()
     pass_ms = np.mean([[evs[k][i].elapsed_time(evs[k][i + 1]) for i in range(5)]
                        for k in range(args.steps)], axis=0)
-    print(json.dumps({"grf_shape": shape, "staging": args.staging, "pass_ms": [round(float(x), 4) for x in pass_ms], "tuned": tuned,
+    print(json.dumps({"grf_shape": shape, "pass_ms": [round(float(x), 4) for x in pass_ms], "tuned": tuned,
                       "grf_cells_per_s": nx * ny * nz / (pass_ms.sum() * 1e-3)}))
 
 
@@ -709,13 +708,8 @@ def main():
     ap.add_argument("--no-batching", action="store_true", help="skip the batched / graph-replay leg")
     ap.add_argument("--no-eta", action="store_true", help="--grf-shape: delta box only")
     ap.add_argument("--no-prefetch", action="store_true", help="--grf-shape: no L2 prefetch of the next tile")
-    ap.add_argument("--staging", action="store_true",
-                    help="--grf-shape: draw the modes once into the workspace, one x inverse per field")
     ap.add_argument("--xgen-split", type=int, default=None, choices=[-1, 0, 1],
                     help="--grf-shape: x pass as one launch (0), two one-field launches (1), by footprint (-1)")
-    ap.add_argument("--xgen-cluster", type=int, default=None, choices=[-1, 0, 1, 2],
-                    help="GPU-noise x pass: built-in rule (-1), one-CTA tiles (0), four-CTA clusters "
-                         "drawing once (1), CTA pairs writing 128-byte segments (2)")
     ap.add_argument("--precision", default=None, const="1536,100000,1024", nargs="?",
                     help="only the FP32-vs-FP64 precision report: N,skewers,pixels (default 1536^3, 1e5 x 1024)")
     ap.add_argument("--variants", default=None,
@@ -725,9 +719,6 @@ def main():
     ap.add_argument("--grf-shape", default=None,
                     help="NX,NY,NZ: time only the GRF boxes of this shape (profiling case)")
     args = ap.parse_args()
-    if args.xgen_cluster is not None:
-        from saclaymocks_gb300 import _lib
-        _lib.xgen_cluster(args.xgen_cluster)
     cfg = SMALL if args.small else PRODUCTION
     if args.grf_shape:
         run_grf_only(args, [int(x) for x in args.grf_shape.split(",")])

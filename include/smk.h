@@ -84,19 +84,13 @@ typedef struct {
     int32_t n_pass_events;    /* first HBM pass and after each of the five (0: none)          */
     int32_t eta_comp;     /* SMK_ETA_*: which eta_ij or velocity the eta box holds (0 = zz)  */
     double vel_factor;    /* SMK_ETA_VX/VY/VZ: H0 * dD/dz(z = 0) (km/s/(Mpc/h) per unit z)    */
-    int32_t kspace_staging; /* GPU noise + eta: 1 draws every mode once into the workspace     */
-                            /* (see smk_grf_workspace_size), then runs one x inverse per field */
-                            /* from it; 0: modes drawn inside the x pass (twice when the boxes */
-                            /* exceed 64 GiB and the pass runs one field per launch)           */
 } SmkGrfParams;
 
 /* Row pitch (floats) of the padded box layout for a z extent nz. */
 int64_t smk_grf_pitch(int32_t nz);
 /* Floats of one padded output box array (all batch members). */
 int64_t smk_grf_box_floats(const SmkGrfParams* p);
-/* Workspace bytes smk_grf_boxes needs: 256 (the FP64 normalisation accumulator), plus, with
- * kspace_staging on a GPU-noise call with eta, batch*nx*ny*roundup(nz/2+1, 32) complex floats
- * for the drawn modes. */
+/* Workspace bytes smk_grf_boxes needs: 256 (the FP64 normalisation accumulator). */
 size_t smk_grf_workspace_size(const SmkGrfParams* p);
 
 /*
@@ -145,14 +139,9 @@ int smk_tune_get(int32_t pass, int32_t n);
  *     delta + eta boxes span more than 64 GiB, where one launch's spread of rows outruns
  *     address translation);
  *   SMK_TUNE_PREFETCH: the y and z passes pull their next tile into L2 while transforming the
- *     current one (1, default) or not (0);
- *   SMK_TUNE_XGEN_CLUSTER: GPU-noise x pass on one-CTA tiles (0; the built-in rule, -1, picks
- *     it), on clusters of four CTAs drawing each mode once and writing both fields in one launch
- *     (1), or on CTA pairs writing one field per launch with row segments twice the one-CTA
- *     tile's width (2).  All forms give identical boxes. */
+ *     current one (1, default) or not (0). */
 #define SMK_TUNE_XGEN_SPLIT 0
 #define SMK_TUNE_PREFETCH 1
-#define SMK_TUNE_XGEN_CLUSTER 2
 #define SMK_TUNE_TMA 3  /* y pass tiles loaded by TMA tensor copies (1, default), loaded and */
                         /* stored by TMA tensor copies (2), or loaded by cp.async (0)         */
 /* Failure test of the y pass's bounded TMA waits (0 by default): 1 makes every tile's barrier
@@ -193,6 +182,9 @@ typedef struct {
     const float* pix_delta;/* SMK_INTERP_PIXELS: packed delta_l per pixel                */
     const float* pix_eta;  /* SMK_INTERP_PIXELS: packed eta_par per pixel (NULL: no RSD)  */
     const float* pix_z;    /* SMK_INTERP_PIXELS: packed redshift per pixel               */
+    const int32_t* forest; /* [n][2] Lya-forest pixel range [f0, f1) of each skewer, or     */
+                           /* NULL (every pixel).  A skewer with an empty range gets no     */
+                           /* small-scale field (bin/merge_spectra.py:305-306, 327-330)      */
 } SmkSkewers;
 
 typedef struct {
@@ -221,7 +213,18 @@ typedef struct {
     float z_lo, z_hi;      /* redshift mapped linearly along x: z = z_lo + (z_hi-z_lo) x/Lx */
     int32_t growth_mode;   /* SMK_G_ONE / SMK_G_MERGE                                     */
     float growth24;        /* fgrowth(2.4) for SMK_G_MERGE                                */
+    /* redshift-dependent P1Dmiss (util.InterpP1Dmissing, py/SaclayMocks/util.py:448-474, as
+     * bin/merge_spectra.py:116-118, 305-325 use it without --fit-p1d): with ss_nztab > 0,
+     * ss_scale holds ss_nztab table sets of SMK_SS_SET_FLOATS floats (set j: the five nz
+     * classes above for redshift ss_ztab[j]); each skewer takes the set whose redshift is
+     * nearest to zeff = mean redshift of its forest pixels, and, with ss_zsigma, its delta_s
+     * is multiplied pixel by pixel by sigma_s(z)/sigma_s(zeff) (linear in z on ss_ztab,
+     * clamped at the ends).  ss_nztab = 0: one set (the layout above).                       */
+    int32_t ss_nztab;
+    const float* ss_ztab;   /* [ss_nztab] ascending redshifts (device)                     */
+    const float* ss_zsigma; /* [ss_nztab] sigma_s at ss_ztab (device), or NULL            */
 } SmkSpectraParams;
+#define SMK_SS_SET_FLOATS 3973 /* sum over nz = 256<<j, j = 0..4, of nz/2+1 */
 
 /* Host: build the work schedule of smk_skewers_flux from the host copy of npix.  Skewers
  * are grouped by small-scale FFT length, longest first, in pairs of equal length (one

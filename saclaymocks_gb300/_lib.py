@@ -24,6 +24,7 @@ SMK_INTERP_TRILINEAR, SMK_INTERP_PIXELS, SMK_INTERP_GAUSS343 = 0, 1, 2
 SMK_SS_NONE, SMK_SS_HOST, SMK_SS_PHILOX = 0, 1, 2
 SMK_ABC_CONST, SMK_ABC_POWERLAW, SMK_ABC_TABLE = 0, 1, 2
 SMK_G_ONE, SMK_G_MERGE = 0, 1
+SMK_SS_SET_FLOATS = 3973
 SMK_ETA = {"zz": 0, "xx": 1, "yy": 2, "xy": 3, "xz": 4, "yz": 5, "vx": 6, "vy": 7, "vz": 8}
 SMK_PASS_ZFWD, SMK_PASS_LINE, SMK_PASS_XPASS, SMK_PASS_XGEN, SMK_PASS_ZINV = 0, 1, 2, 3, 4
 
@@ -42,14 +43,15 @@ class SmkGrfParams(C.Structure):
                 ("amp", C.c_double), ("pk_grid", C.c_void_p), ("noise_mode", C.c_int32),
                 ("noise", C.c_void_p), ("seed", C.c_uint64), ("want_eta", C.c_int32),
                 ("pass_events", C.c_void_p), ("n_pass_events", C.c_int32), ("eta_comp", C.c_int32),
-                ("vel_factor", C.c_double), ("kspace_staging", C.c_int32)]
+                ("vel_factor", C.c_double)]
 
 
 class SmkSkewers(C.Structure):
     _fields_ = [("n", C.c_int64), ("start", C.c_void_p), ("dir", C.c_void_p),
                 ("npix", C.c_void_p), ("offset", C.c_void_p), ("dpix", C.c_double),
                 ("order", C.c_void_p), ("n_slots", C.c_int64),
-                ("pix_delta", C.c_void_p), ("pix_eta", C.c_void_p), ("pix_z", C.c_void_p)]
+                ("pix_delta", C.c_void_p), ("pix_eta", C.c_void_p), ("pix_z", C.c_void_p),
+                ("forest", C.c_void_p)]
 
 
 class SmkSpectraParams(C.Structure):
@@ -61,7 +63,8 @@ class SmkSpectraParams(C.Structure):
                 ("a_zref1", C.c_float), ("a_power", C.c_float), ("abc_tab", C.c_void_p),
                 ("n_tab", C.c_int32), ("z_tab0", C.c_float), ("dz_tab", C.c_float),
                 ("z_lo", C.c_float), ("z_hi", C.c_float), ("growth_mode", C.c_int32),
-                ("growth24", C.c_float)]
+                ("growth24", C.c_float), ("ss_nztab", C.c_int32), ("ss_ztab", C.c_void_p),
+                ("ss_zsigma", C.c_void_p)]
 
 
 class SmkFitProblem(C.Structure):
@@ -142,7 +145,7 @@ def load(path: str | None = None):
     return lib
 
 
-SMK_TUNE_XGEN_SPLIT, SMK_TUNE_PREFETCH, SMK_TUNE_XGEN_CLUSTER, SMK_TUNE_TMA, SMK_TUNE_TMA_WAIT_TEST = 0, 1, 2, 3, 4
+SMK_TUNE_XGEN_SPLIT, SMK_TUNE_PREFETCH, SMK_TUNE_TMA, SMK_TUNE_TMA_WAIT_TEST = 0, 1, 3, 4
 
 
 def tune_flag(flag: int, value: int) -> int:
@@ -155,13 +158,6 @@ def tune_flag(flag: int, value: int) -> int:
 def xgen_split(mode: int) -> int:
     """x-pass launch mode (-1 by footprint, 0 one launch, 1 two launches); returns the previous."""
     return tune_flag(SMK_TUNE_XGEN_SPLIT, mode)
-
-
-def xgen_cluster(mode: int) -> int:
-    """x-pass form: -1 built-in rule, 0 one-CTA tiles, 1 four-CTA clusters (each mode drawn
-    once, both fields per launch), 2 CTA pairs (128-byte row segments, one field per launch);
-    returns the previous value."""
-    return tune_flag(SMK_TUNE_XGEN_CLUSTER, mode)
 
 
 def check(status: int, what: str = ""):

@@ -73,8 +73,6 @@ static std::atomic<int> g_xgen_split{-1};  // -1: by footprint, 0: never, 1: alw
 static std::atomic<int> g_prefetch{1};     // L2 prefetch of the next tile in the y and z passes
 static std::atomic<int> g_tma{1};          // TMA tensor loads of the y pass's tiles
 static std::atomic<int> g_tma_wait_test{0};  // y-pass TMA waits made to run out (failure test)
-static std::atomic<int> g_xgen_cluster{-1}; // -1: built-in rule (one-CTA tiles), 0: one-CTA tiles,
-                                            // 1: four-CTA clusters (with eta), 2: CTA pairs
 
 static int length_class(int n) { return n <= 512 ? 0 : n <= 1024 ? 1 : n <= 2560 ? 2 : 3; }
 
@@ -132,16 +130,9 @@ int64_t smk_grf_box_floats(const SmkGrfParams* p) {
     return (int64_t)p->batch * p->nx * p->ny * smk_grf_pitch(p->nz);
 }
 
-// Staged-mode buffer of GPU noise (bytes), or 0 when the call draws in the x pass: delta_k of
-// every mode, k_z rounded up to the widest x-pass tile (32 columns).
-static size_t staging_bytes(const SmkGrfParams* p) {
-    if (!p || !p->kspace_staging || p->noise_mode != SMK_NOISE_PHILOX || !p->want_eta) return 0;
-    const size_t nzh = (size_t)p->nz / 2 + 1;
-    return (size_t)p->batch * p->nx * p->ny * ((nzh + 31) / 32 * 32) * sizeof(float2);
-}
-
 size_t smk_grf_workspace_size(const SmkGrfParams* p) {
-    return 256 + staging_bytes(p);  // [0] FP64 mode sum, [1] amplitude A; then the staging buffer
+    (void)p;
+    return 256;  // [0] FP64 mode sum, [1] amplitude A
 }
 
 int smk_pk_normalisation(int32_t nx, int32_t ny, int32_t nz, double dcell, double k0, double* amp_dev,
@@ -264,7 +255,6 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
                                                            (uint32_t)wl, (uint32_t)rows))
                      ? g_tma.load() : 0;
     }
-    bool staged = false;
     const int64_t rows_per_box = (int64_t)p->nx * p->ny;
     const float inv_vcell = 1.0f / (float)(p->dcell * p->dcell * p->dcell);
     if (gpu_noise) {
@@ -298,38 +288,14 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         // the whole of each output box.  Past ~64 GiB for the two boxes together (2 x 40 GB at
         // 2560x2560x1536) that spread outruns the GPU's address-translation reach and the pass
         // slows by 1.7x; writing delta and eta in two launches keeps each wave within one box.
-        // Staged (large boxes): draw every mode once into the workspace, then one x-inverse launch
-        // per field reads them back, so no launch writes both boxes and no mode is drawn twice.
-        const int wx = variant_table(pass_x)[vx].w;
-        int sh = 0;
-        while ((1 << sh) < wx) ++sh;
-        const size_t sbytes = staging_bytes(p);
-        staged = sbytes > 0 && (1 << sh) == wx && workspace && workspace_bytes >= 256 + sbytes;
-        if (staged) {
-            ga.S = reinterpret_cast<float2*>(reinterpret_cast<char*>(workspace) + 256);
-            ga.sh = sh;
-            if ((rc = run_kgen(ga, st))) return rc;
-            ga.fields = XGEN_DELTA;
-            if ((rc = run_xinv(vx, ga, st))) return rc;
+        const double pair_bytes = 2.0 * 4.0 * (double)p->batch * p->nx * p->ny * (double)pitch;
+        const int sm = g_xgen_split.load();
+        const bool split = p->want_eta && (sm < 0 ? pair_bytes > 64.0 * (1ull << 30) : sm == 1);
+        ga.fields = !p->want_eta ? XGEN_DELTA : (split ? XGEN_DELTA : XGEN_BOTH);
+        if ((rc = run_xgen(vx, ga, st))) return rc;
+        if (split) {
             ga.fields = XGEN_ETA;
-            if ((rc = run_xinv(vx, ga, st))) return rc;
-        } else {
-            // In place: a tile writes all nx rows of its columns, so one wave of tiles touches
-            // rows spread over the whole of each output box.  Past ~64 GiB for the two boxes
-            // together (2 x 40 GB at 2560x2560x1536) that spread outruns the GPU's
-            // address-translation reach and the pass slows by 1.7x; writing delta and eta in
-            // two launches keeps each wave within one box.
-            const double pair_bytes = 2.0 * 4.0 * (double)p->batch * p->nx * p->ny * (double)pitch;
-            const int sm = g_xgen_split.load(), cm = g_xgen_cluster.load();
-            const bool cluster = p->want_eta && cm == 1;
-            ga.pair = cm == 2 ? 1 : 0;
-            const bool split = !cluster && p->want_eta && (sm < 0 ? pair_bytes > 64.0 * (1ull << 30) : sm == 1);
-            ga.fields = !p->want_eta ? XGEN_DELTA : (cluster ? XGEN_CLUSTER : (split ? XGEN_DELTA : XGEN_BOTH));
             if ((rc = run_xgen(vx, ga, st))) return rc;
-            if (split) {
-                ga.fields = XGEN_ETA;
-                if ((rc = run_xgen(vx, ga, st))) return rc;
-            }
         }
         if ((rc = mark(3))) return rc;
     } else {
@@ -394,9 +360,6 @@ int smk_tune_flag(int32_t flag, int32_t value, int32_t* previous) {
     if (flag == SMK_TUNE_XGEN_SPLIT) {
         if (value < -1 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: XGEN_SPLIT must be -1, 0 or 1");
         old = g_xgen_split.exchange(value);
-    } else if (flag == SMK_TUNE_XGEN_CLUSTER) {
-        if (value < -1 || value > 2) return fail(SMK_EINVAL, "smk_tune_flag: XGEN_CLUSTER must be -1, 0, 1 or 2");
-        old = g_xgen_cluster.exchange(value);
     } else if (flag == SMK_TUNE_TMA_WAIT_TEST) {
         if (value < 0 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: TMA_WAIT_TEST must be 0 or 1");
         old = g_tma_wait_test.exchange(value);

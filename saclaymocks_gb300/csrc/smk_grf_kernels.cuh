@@ -384,13 +384,6 @@ struct XGenArgs {
     float vfac;
     int fields;            // XGEN_BOTH: W/2 delta + W/2 eta lines per tile; XGEN_DELTA / XGEN_ETA:
                            // W lines of one field (two launches; see xgen_split)
-    // Staged modes (kgen_kernel writes, xinv_kernel reads): delta_k of mode (x slot e, y slot,
-    // kz) of box b at S[((((kz >> sh) * batch + b) * ny + yslot) * nx + e) << sh | (kz & (2^sh - 1))]:
-    // column blocks of width 2^sh (the x-inverse tile width), x in the x plan's slot order, so
-    // one x-inverse tile is one contiguous run of nx * 2^sh complex values.
-    float2* S;
-    int sh;
-    int pair;              // one-field launches on CTA pairs (xgp_kernel): 128-byte row segments
 };
 
 // GPU-noise mode arithmetic (no bit-level reference: the FP64 oracle restates the drawn modes
@@ -493,7 +486,7 @@ __device__ __forceinline__ ModePair draw_pair(const XGenArgs& a, uint64_t seed, 
     }
     return mp;
 }
-enum { XGEN_BOTH = 0, XGEN_DELTA = 1, XGEN_ETA = 2, XGEN_CLUSTER = 3 };
+enum { XGEN_BOTH = 0, XGEN_DELTA = 1, XGEN_ETA = 2 };
 
 // True when the k_z columns [c0, c0 + w) include the kz = 0 or nz/2 plane or run past nzh.
 __device__ __forceinline__ bool tile_needs_check(const XGenArgs& a, int c0, int w) {
@@ -585,336 +578,6 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
     }
 }
 
-// ------------------------------------------------------------------ GPU-noise x pass on CTA pairs
-// One field per launch (fields = XGEN_DELTA or XGEN_ETA) on clusters of two CTAs.  A tile is 2W
-// k_z columns of one (box, y slot); CTA h draws the modes of its W columns for every x slot and
-// takes their x inverse in its own shared memory, then writes the x slots of half h for all
-// 2W columns (W read from the partner through distributed shared memory), so every output row
-// segment is 2W * 8 bytes (128 B for W = 8) where a one-CTA tile writes W * 8.  Each mode is
-// drawn once per launch, as in xgen_kernel.
-// smem: s[n*W] | tw[n] | kx[n] | ix[n] | kzt[nzh]  (same offsets in both CTAs)
-template <class C>
-__global__ void __launch_bounds__(C::T, C::MINB) xgp_kernel(const XGenArgs a) {
-    constexpr int W = C::W, T = C::T;
-    constexpr int NP = W / 2;
-    static_assert(W % 2 == 0, "xgp tiles hold column pairs");
-    cg::cluster_group cl = cg::this_cluster();
-    const int h = (int)cl.block_rank();
-    extern __shared__ float2 smem[];
-    const int n = a.pl.n;  // == nx
-    float2* s = smem;
-    float2* tw = s + n * W;
-    float* kx = reinterpret_cast<float*>(tw + n);
-    int* ix = reinterpret_cast<int*>(kx + n);
-    float* kzt = reinterpret_cast<float*>(ix + n);
-    fill_stage_twiddles(tw, a.pl);
-    for (int e = threadIdx.x; e < n; e += T) {
-        const int fr = freq_of_slot(a.pl, e);
-        ix[e] = fr;
-        kx[e] = kaxis(fr, n, a.kfac, true);
-    }
-    for (int z = threadIdx.x; z < a.nzh; z += T) kzt[z] = kaxis(z, a.nz, a.kfac, false);
-    cl.sync();   // both CTAs started (and filled their tables) before any remote access
-    const float2* s_lo = h == 0 ? s : cl.map_shared_rank(s, 0);   // columns 0..W-1 of the tile
-    const float2* s_hi = h == 1 ? s : cl.map_shared_rank(s, 1);   // columns W..2W-1
-    const float scale_c = pk_scale_c(a);
-    const bool eta = a.fields == XGEN_ETA;
-    float2* box = eta ? a.B : a.A;
-    const int nh = n / 2;
-    const int ec0 = h ? nh : 0, ec1 = h ? n : nh;   // x slots this CTA writes
-    const int64_t ncolt = ceil_div(a.nzh, 2 * W);
-    const int64_t ntiles = (int64_t)a.batch * a.ny * ncolt;
-    const int64_t estride = (int64_t)a.ny * a.cp;
-    const int64_t ncl = gridDim.x / 2;
-    for (int64_t tile = blockIdx.x / 2; tile < ntiles; tile += ncl) {
-        const int64_t o = tile / ncolt;  // b*ny + y slot
-        const int cb = (int)(tile - o * ncolt);
-        const int64_t b = o / a.ny;
-        const int yslot = (int)(o - b * a.ny);
-        const int iy = freq_of_slot(a.ply, yslot);
-        const int iym = iy == 0 ? 0 : a.ny - iy;
-        const float ky = kaxis(iy, a.ny, a.kfac, true);
-        const uint64_t seed = a.seed + (uint64_t)b;
-        const int col0 = cb * 2 * W + h * W;
-        auto draw = [&](auto chk) {
-#pragma unroll 2
-            for (int idx = threadIdx.x; idx < n * NP; idx += T) {
-                const int e = idx / NP, pr = idx % NP;
-                const float kxv = kx[e];
-                const ModePair mp = draw_pair<decltype(chk)::value>(a, seed, ix[e], iy, iym, kxv, ky, col0 + 2 * pr,
-                                                                     kzt, scale_c);
-                float2 v0 = mp.d[0], v1 = mp.d[1];
-                if (eta) {
-                    v0 = eta_from_inv_k2(a.eta_comp, v0, kxv, ky, mp.kz[0], mp.ikk[0], a.vfac);
-                    v1 = eta_from_inv_k2(a.eta_comp, v1, kxv, ky, mp.kz[1], mp.ikk[1], a.vfac);
-                }
-                *reinterpret_cast<float4*>(s + e * W + 2 * pr) = make_float4(v0.x, v0.y, v1.x, v1.y);
-            }
-        };
-        if (tile_needs_check(a, col0, W))
-            draw(std::true_type{});
-        else
-            draw(std::false_type{});
-        __syncthreads();
-        fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
-        cl.sync();   // the partner's transform is complete
-        const int cols = min(2 * W, a.nzh - cb * 2 * W);
-        float2* dst = box + b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)cb * 2 * W;
-        constexpr int U = 4;
-        const int items = (ec1 - ec0) * W;   // column pairs of the half
-        for (int base = threadIdx.x; base < items; base += U * T) {
-            float4 v[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int idx = base + u * T;
-                if (idx < items) {
-                    const int e = ec0 + idx / W, c = 2 * (idx % W);
-                    v[u] = *reinterpret_cast<const float4*>((c < W ? s_lo : s_hi) + e * W + (c & (W - 1)));
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int idx = base + u * T;
-                if (idx < items) {
-                    const int e = ec0 + idx / W, c = 2 * (idx % W);
-                    float2* d = dst + e * estride + c;
-                    if (c + 1 < cols)
-                        *reinterpret_cast<float4*>(d) = v[u];
-                    else if (c < cols)
-                        *d = make_float2(v[u].x, v[u].y);
-                }
-            }
-        }
-        // the partner's shared loads above have returned (their values feed the stores): the
-        // next tile may overwrite the tiles once both CTAs arrive; relaxed, so the stores stay
-        // in flight
-        asm volatile("barrier.cluster.arrive.relaxed.aligned;\n" ::: "memory");
-        asm volatile("barrier.cluster.wait.aligned;\n" ::: "memory");
-    }
-}
-
-// ------------------------------------------------------------------ clustered GPU-noise x pass
-// Both fields in one launch with every mode drawn once, on clusters of four CTAs.  A tile is
-// 2W k_z columns of one (box, y slot); CTA rank r = h + 2f holds the W columns of half h for
-// field f (0 delta, 1 eta) in its shared memory.  Each mode is drawn once, by CTA (h, f) for
-// the x slots of half f, which stores delta_k into CTA (h, 0) and eta_k into CTA (h, 1)
-// (distributed shared memory); every CTA then takes the x inverse of its W lines; CTA (h, f)
-// finally writes field f for the x slots of half h, all 2W columns, so each output row
-// segment is 2W * 8 bytes (128 B for W = 8) rather than the W * 8 of a one-CTA tile.
-// smem: s[n*W] | tw[n] | kx[n] | ix[n] | kzt[nzh]  (same offsets in every CTA of the cluster)
-template <class C>
-__global__ void __launch_bounds__(C::T, C::MINB) xgc_kernel(const XGenArgs a) {
-    constexpr int W = C::W, T = C::T;
-    constexpr int NP = W / 2;  // mode pairs per row of one CTA's columns
-    static_assert(W % 2 == 0, "xgc tiles hold column pairs");
-    cg::cluster_group cl = cg::this_cluster();
-    const int rank = (int)cl.block_rank();
-    const int h = rank & 1, f = rank >> 1;
-    extern __shared__ float2 smem[];
-    const int n = a.pl.n;  // == nx
-    float2* s = smem;
-    float2* tw = s + n * W;
-    float* kx = reinterpret_cast<float*>(tw + n);
-    int* ix = reinterpret_cast<int*>(kx + n);
-    float* kzt = reinterpret_cast<float*>(ix + n);
-    fill_stage_twiddles(tw, a.pl);
-    for (int e = threadIdx.x; e < n; e += T) {
-        const int fr = freq_of_slot(a.pl, e);
-        ix[e] = fr;
-        kx[e] = kaxis(fr, n, a.kfac, true);
-    }
-    for (int z = threadIdx.x; z < a.nzh; z += T) kzt[z] = kaxis(z, a.nz, a.kfac, false);
-    // every CTA of the cluster has started (and filled its tables) before any remote access
-    cl.sync();
-    // the partners' tiles (this CTA's own through its local shared address)
-    float2* s_delta = f == 0 ? s : cl.map_shared_rank(s, h);       // (h, delta): draw target
-    float2* s_eta = f == 1 ? s : cl.map_shared_rank(s, h | 2);     // (h, eta): draw target
-    const float2* s_lo = h == 0 ? s : cl.map_shared_rank(s, f << 1);       // (0, f): columns 0..W-1
-    const float2* s_hi = h == 1 ? s : cl.map_shared_rank(s, 1 | (f << 1)); // (1, f): columns W..2W-1
-    const float scale_c = pk_scale_c(a);
-    const int nh = n / 2;
-    const int ea0 = f ? nh : 0, ea1 = f ? n : nh;  // x slots this CTA draws
-    const int ec0 = h ? nh : 0, ec1 = h ? n : nh;  // x slots this CTA writes
-    const int64_t ncolt = ceil_div(a.nzh, 2 * W);
-    const int64_t ntiles = (int64_t)a.batch * a.ny * ncolt;
-    const int64_t estride = (int64_t)a.ny * a.cp;
-    const int64_t ncl = gridDim.x / 4;
-    for (int64_t tile = blockIdx.x / 4; tile < ntiles; tile += ncl) {
-        const int64_t o = tile / ncolt;  // b*ny + y slot
-        const int cb = (int)(tile - o * ncolt);
-        const int64_t b = o / a.ny;
-        const int yslot = (int)(o - b * a.ny);
-        const int iy = freq_of_slot(a.ply, yslot);
-        const int iym = iy == 0 ? 0 : a.ny - iy;
-        const float ky = kaxis(iy, a.ny, a.kfac, true);
-        const uint64_t seed = a.seed + (uint64_t)b;
-        const int col0 = cb * 2 * W + h * W;
-        auto draw = [&](auto chk) {
-            for (int idx = threadIdx.x; idx < (ea1 - ea0) * NP; idx += T) {
-                const int e = ea0 + idx / NP, pr = idx % NP;
-                const float kxv = kx[e];
-                const ModePair mp = draw_pair<decltype(chk)::value>(a, seed, ix[e], iy, iym, kxv, ky, col0 + 2 * pr, kzt, scale_c);
-                const float2 e0 = eta_from_inv_k2(a.eta_comp, mp.d[0], kxv, ky, mp.kz[0], mp.ikk[0], a.vfac);
-                const float2 e1 = eta_from_inv_k2(a.eta_comp, mp.d[1], kxv, ky, mp.kz[1], mp.ikk[1], a.vfac);
-                *reinterpret_cast<float4*>(s_delta + e * W + 2 * pr) = make_float4(mp.d[0].x, mp.d[0].y, mp.d[1].x, mp.d[1].y);
-                *reinterpret_cast<float4*>(s_eta + e * W + 2 * pr) = make_float4(e0.x, e0.y, e1.x, e1.y);
-            }
-        };
-        if (tile_needs_check(a, col0, W))
-            draw(std::true_type{});
-        else
-            draw(std::false_type{});
-        cl.sync();
-        fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
-        cl.sync();
-        const int cols = min(2 * W, a.nzh - cb * 2 * W);
-        float2* dst = (f ? a.B : a.A) + b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)cb * 2 * W;
-        // U independent (partly remote) shared loads in flight per thread before the stores
-        constexpr int U = 4;
-        const int items = (ec1 - ec0) * W;
-        for (int base = threadIdx.x; base < items; base += U * T) {
-            float4 v[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int idx = base + u * T;
-                if (idx < items) {
-                    const int e = ec0 + idx / W, c = 2 * (idx % W);  // columns c, c + 1 of 2W
-                    v[u] = *reinterpret_cast<const float4*>((c < W ? s_lo : s_hi) + e * W + (c & (W - 1)));
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int idx = base + u * T;
-                if (idx < items) {
-                    const int e = ec0 + idx / W, c = 2 * (idx % W);
-                    float2* d = dst + e * estride + c;
-                    if (c + 1 < cols)
-                        *reinterpret_cast<float4*>(d) = v[u];
-                    else if (c < cols)
-                        *d = make_float2(v[u].x, v[u].y);
-                }
-            }
-        }
-        // The partners' shared loads above have returned (their values feed the stores), so the
-        // next tile may overwrite the tiles once every thread arrives; a relaxed arrival keeps
-        // the global stores in flight instead of draining them at the barrier.
-        asm volatile("barrier.cluster.arrive.relaxed.aligned;\n" ::: "memory");
-        asm volatile("barrier.cluster.wait.aligned;\n" ::: "memory");
-    }
-}
-
-// ------------------------------------------------------------------ staged GPU noise
-// Large boxes: the modes are drawn once into the staged buffer (kgen_kernel, a streaming
-// write in address order), then each field's x inverse reads them back (xinv_kernel, one
-// launch per field, tiles k_z-block-major so a wave reads one compact block and writes rows of
-// one box only).  The x pass then touches at most one output box per launch without drawing
-// every mode twice.
-template <int T>
-__global__ void __launch_bounds__(T, 3) kgen_kernel(const XGenArgs a) {
-    extern __shared__ float2 smem[];
-    float* kx = reinterpret_cast<float*>(smem);          // [nx] k_x of each x slot
-    int* ix = reinterpret_cast<int*>(kx + a.nx);          // [nx] frequency of each x slot
-    float* kzt = reinterpret_cast<float*>(ix + a.nx);     // [nzh]
-    for (int e = threadIdx.x; e < a.nx; e += T) {
-        const int f = freq_of_slot(a.pl, e);
-        ix[e] = f;
-        kx[e] = kaxis(f, a.nx, a.kfac, true);
-    }
-    for (int z = threadIdx.x; z < a.nzh; z += T) kzt[z] = kaxis(z, a.nz, a.kfac, false);
-    __syncthreads();
-    const float scale_c = pk_scale_c(a);
-    const int wt = 1 << a.sh, psh = a.sh - 1, pmask = (wt >> 1) - 1;
-    const int nkb = (int)ceil_div(a.nzh, wt);
-    // a line = the nx x-slots of one (k_z block, box, y slot): one contiguous staged run
-    const int64_t nlines = (int64_t)nkb * a.batch * a.ny;
-    const int per_line = a.nx << psh;                     // mode pairs of a line
-    for (int64_t line = blockIdx.x; line < nlines; line += gridDim.x) {
-        const int yslot = (int)(line % a.ny);
-        const int64_t r2 = line / a.ny;
-        const int b = (int)(r2 % a.batch);
-        const int kb = (int)(r2 / a.batch);
-        const int iy = freq_of_slot(a.ply, yslot);
-        const int iym = iy == 0 ? 0 : a.ny - iy;
-        const float ky = kaxis(iy, a.ny, a.kfac, true);
-        const uint64_t seed = a.seed + (uint64_t)b;
-        float4* dst = reinterpret_cast<float4*>(a.S + ((line * a.nx) << a.sh));
-        auto draw = [&](auto chk) {
-            for (int it = threadIdx.x; it < per_line; it += T) {
-                const int e = it >> psh, pr = it & pmask;
-                const ModePair mp = draw_pair<decltype(chk)::value>(a, seed, ix[e], iy, iym, kx[e], ky,
-                                                                     kb * wt + 2 * pr, kzt, scale_c);
-                __stcs(dst + it, make_float4(mp.d[0].x, mp.d[0].y, mp.d[1].x, mp.d[1].y));
-            }
-        };
-        if (tile_needs_check(a, kb * wt, wt))
-            draw(std::true_type{});
-        else
-            draw(std::false_type{});
-    }
-}
-
-// x inverse of one field from the staged modes (fields = XGEN_DELTA or XGEN_ETA): the tile of
-// W = 2^sh k_z columns of (b, y slot) is one contiguous run of the staged buffer.
-// smem: s[n*W] | tw[n] | kx[n] | kzt[nzh]
-template <class C>
-__global__ void __launch_bounds__(C::T, C::MINB) xinv_kernel(const XGenArgs a) {
-    constexpr int W = C::W, T = C::T;
-    extern __shared__ float2 smem[];
-    const int n = a.pl.n;  // == nx
-    float2* s = smem;
-    float2* tw = s + n * W;
-    float* kx = reinterpret_cast<float*>(tw + n);
-    float* kzt = kx + n;
-    fill_stage_twiddles(tw, a.pl);
-    for (int e = threadIdx.x; e < n; e += T) kx[e] = kaxis(freq_of_slot(a.pl, e), n, a.kfac, true);
-    for (int z = threadIdx.x; z < a.nzh; z += T) kzt[z] = kaxis(z, a.nz, a.kfac, false);
-    __syncthreads();
-    const bool eta = a.fields == XGEN_ETA;
-    float2* dst_box = eta ? a.B : a.A;
-    const int64_t nouter = (int64_t)a.batch * a.ny;
-    const int64_t nkb = ceil_div(a.nzh, W);
-    const int64_t ntiles = nouter * nkb;
-    const int64_t estride = (int64_t)a.ny * a.cp;
-    const unsigned run_bytes = (unsigned)((size_t)n * W * sizeof(float2));
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int kb = (int)(tile / nouter);
-        const int64_t o = tile - (int64_t)kb * nouter;    // b*ny + y slot
-        const int64_t b = o / a.ny;
-        const int yslot = (int)(o - b * a.ny);
-        const int cols = min(W, a.nzh - kb * W);
-        // the tile's staged run: n lines of W columns, contiguous
-        const float2* src = a.S + (((int64_t)kb * nouter + o) * n << a.sh);
-        load_cols_async<W, T>(s, src, n, W, W);
-        cp_async_wait_all();
-        __syncthreads();
-        if (threadIdx.x == 0 && tile + gridDim.x < ntiles) {
-            // the next tile's run (tiles are consecutive runs): one bulk L2 prefetch
-            const int64_t tn = tile + gridDim.x;
-            const int kbn = (int)(tn / nouter);
-            prefetch_l2_bulk(a.S + (((int64_t)kbn * nouter + (tn - (int64_t)kbn * nouter)) * n << a.sh), run_bytes);
-        }
-        float2* dst = dst_box + b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)kb * W;
-        auto out = [&](int e, int w, float2 v) {
-            if (w < cols) dst[e * estride + w] = v;
-        };
-        if (eta) {
-            // eta_k = (k_i k_j / k^2) delta_k applied as the first stage loads each value
-            const float ky = kaxis(freq_of_slot(a.ply, yslot), a.ny, a.kfac, true);
-            const int zc = kb * W;
-            ifft_tile_pre_out<W, W, T, C::RMAX>(
-                s, tw, a.pl,
-                [&](int e, int w, float2 v) {
-                    const float kxv = kx[e], kz_ = kzt[min(zc + w, a.nzh - 1)];
-                    return eta_from_inv_k2(a.eta_comp, v, kxv, ky, kz_, mode_inv_k2(mode_k2(kxv, ky, kz_)), a.vfac);
-                },
-                out);
-        } else {
-            ifft_tile_out<W, W, T, C::RMAX>(s, tw, a.pl, out);
-        }
-        __syncthreads();
-    }
-}
-
 // ------------------------------------------------------------------ z inverse (c2r) + stats
 struct ZInvArgs {
     FftPlan pl;
@@ -928,159 +591,8 @@ struct ZInvArgs {
     int prefetch;   // pull the next tile into L2 during the transform
 };
 
-template <int T>
-__device__ __forceinline__ void flush_stats(double s1, double s2, double bad, double* red, double* dst) {
-    // block sum of three doubles, then one atomic per quantity
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        s1 += __shfl_down_sync(0xffffffffu, s1, off);
-        s2 += __shfl_down_sync(0xffffffffu, s2, off);
-        bad += __shfl_down_sync(0xffffffffu, bad, off);
-    }
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) {
-        red[3 * wid] = s1;
-        red[3 * wid + 1] = s2;
-        red[3 * wid + 2] = bad;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t1 = 0, t2 = 0, t3 = 0;
-        for (int i = 0; i < T / 32; ++i) {
-            t1 += red[3 * i];
-            t2 += red[3 * i + 1];
-            t3 += red[3 * i + 2];
-        }
-        atomicAdd(dst, t1);
-        atomicAdd(dst + 1, t2);
-        atomicAdd(dst + 2, t3);
-    }
-    __syncthreads();
-}
-
-// smem: s[n*SN] | tw[n] | sof[n] | red[3*T/32] (doubles)
-template <class C>
-__global__ void __launch_bounds__(C::T, C::MINB) zinv_kernel(const ZInvArgs a) {
-    constexpr int W = C::W, SN = W + 1, T = C::T;
-    extern __shared__ float2 smem[];
-    const int n = a.pl.n;
-    float2* s = smem;
-    float2* tw = s + n * SN;
-    int* sof = reinterpret_cast<int*>(tw + n);
-    double* red = reinterpret_cast<double*>(sof + n + (n & 1));
-    float* sf = reinterpret_cast<float*>(s);
-    fill_stage_twiddles(tw, a.pl);
-    for (int k = threadIdx.x; k < n; k += T) sof[k] = slot_of_freq(a.pl, k);
-    __syncthreads();
-    const int nh = n / 2 + 1, half = n / 2;
-    const int64_t tpbuf = a.zt.tiles_per_box * a.batch;
-    const int64_t ntiles = tpbuf * a.nbuf;
-    const int64_t cp = a.pitch / 2;
-    double acc1 = 0.0, acc2 = 0.0, accb = 0.0;
-    int64_t cur = -1;
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int buf = (int)(tile / tpbuf);
-        const int64_t t = tile - buf * tpbuf;
-        const int64_t b = t / a.zt.tiles_per_box;
-        const int64_t lrow0 = (t - b * a.zt.tiles_per_box) * (2 * W);
-        const int64_t grow0 = b * a.zt.rows_per_box + lrow0;
-        const int rows_here = (int)min((int64_t)(2 * W), a.zt.rows_per_box - lrow0);
-        const int64_t key = (int64_t)buf * a.batch + b;
-        if (a.stats && key != cur) {
-            if (cur >= 0) {
-                const int64_t cb = cur % a.batch, cf = cur / a.batch;
-                flush_stats<T>(acc1, acc2, accb, red, a.stats + 8 * cb + 4 * cf);
-            }
-            acc1 = acc2 = accb = 0.0;
-            cur = key;
-        }
-        const float2* in2 = reinterpret_cast<const float2*>(a.buf[buf]) + grow0 * cp;
-        // Row pair w holds the half spectra X1 (even row) and X2 (odd row); the complex line
-        // Z_k = X1_k + i X2_k (k <= n/2), Z_{n-k} = X1_k* + i X2_k* goes to the slot of each
-        // frequency (DC and Nyquist: real parts, re from X1, im from X2).  The pair index is
-        // the fast index of the thread mapping: a warp reads W rows x (32/W) consecutive k
-        // (whole 32-byte sectors) and writes W-contiguous slots.  Four items per thread are
-        // loaded before any is used.
-        constexpr int U = 4;
-        const int items = W * nh;
-        for (int base = threadIdx.x; base < items; base += U * T) {
-            float2 x1[U], x2[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int idx = base + u * T;
-                const int w = idx % W, k = idx / W;
-                x1[u] = x2[u] = make_float2(0.f, 0.f);
-                if (idx < items) {
-                    if (2 * w < rows_here) x1[u] = __ldcs(in2 + (int64_t)(2 * w) * cp + k);
-                    if (2 * w + 1 < rows_here) x2[u] = __ldcs(in2 + (int64_t)(2 * w + 1) * cp + k);
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int idx = base + u * T;
-                if (idx >= items) break;
-                const int w = idx % W, k = idx / W;
-                if (k == 0 || k == half) {
-                    s[sof[k] * SN + w] = make_float2(x1[u].x, x2[u].x);
-                } else {
-                    s[sof[k] * SN + w] = make_float2(x1[u].x - x2[u].y, x1[u].y + x2[u].x);
-                    s[sof[n - k] * SN + w] = make_float2(x1[u].x + x2[u].y, x2[u].x - x1[u].y);
-                }
-            }
-        }
-        __syncthreads();
-        if (a.prefetch && tile + gridDim.x < ntiles && threadIdx.x < 2 * W) {
-            // the next tile of this block: its rows, one bulk prefetch per row
-            const int64_t tn = tile + gridDim.x;
-            const int bufn = (int)(tn / tpbuf);
-            const int64_t un = tn - bufn * tpbuf;
-            const int64_t bn = un / a.zt.tiles_per_box;
-            const int64_t lrn = (un - bn * a.zt.tiles_per_box) * (2 * W) + threadIdx.x;
-            if (lrn < a.zt.rows_per_box)
-                prefetch_l2_bulk(a.buf[bufn] + (bn * a.zt.rows_per_box + lrn) * a.pitch, (uint32_t)(a.pitch * 4));
-        }
-        fft_tile<true, W, SN, T, C::RMAX>(s, tw, a.pl);
-        // z_e = x1_e + i x2_e: one 8-byte shared read gives both rows' values
-        float p1 = 0.f, p2 = 0.f, pb = 0.f;
-        float* out = a.buf[buf] + grow0 * a.pitch;
-        for (int w = 0; 2 * w < rows_here; ++w) {
-            float* r0 = out + (int64_t)(2 * w) * a.pitch;
-            float* r1 = r0 + a.pitch;
-            const bool two = 2 * w + 1 < rows_here;
-            for (int e = threadIdx.x; e < n; e += T) {
-                const float2 z = s[e * SN + w];
-                const float v0 = z.x * a.scale, v1 = z.y * a.scale;
-                r0[e] = v0;
-                if (isfinite(v0)) {
-                    p1 += v0;
-                    p2 = fmaf(v0, v0, p2);
-                } else {
-                    pb += 1.f;
-                }
-                if (two) {
-                    r1[e] = v1;
-                    if (isfinite(v1)) {
-                        p1 += v1;
-                        p2 = fmaf(v1, v1, p2);
-                    } else {
-                        pb += 1.f;
-                    }
-                }
-            }
-        }
-        acc1 += p1;
-        acc2 += p2;
-        accb += pb;
-        __syncthreads();
-    }
-    if (a.stats && cur >= 0) {
-        const int64_t cb = cur % a.batch, cf = cur / a.batch;
-        flush_stats<T>(acc1, acc2, accb, red, a.stats + 8 * cb + 4 * cf);
-    }
-}
-
 // ------------------------------------------------------------------ z inverse, one warp per row pair
-// The same c2r + 1/N + statistics as zinv_kernel, but every warp transforms its own row pair in
+// c2r of row pairs + 1/N + FP64 statistics: every warp transforms its own row pair in
 // a private region of shared memory and synchronises only with __syncwarp: the warps of an SM
 // run out of phase, so one warp's loads, another's transform and a third's stores overlap.
 // Slot p of a warp's line sits at zslot<SWZ>(p).  SWZ = 1: p ^ ((p >> 4) & 15), an XOR swizzle
@@ -1382,18 +894,7 @@ static int launch_zinvw(ZInvArgs a, int64_t rows_per_box, cudaStream_t st) {
 
 template <class C>
 static int launch_zinv(ZInvArgs a, int64_t rows_per_box, cudaStream_t st) {
-    if constexpr (C::W == 0) {
-        return launch_zinvw<C>(a, rows_per_box, st);
-    } else {
-    if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "zinv_kernel");
-    a.zt.init(rows_per_box, C::W);
-    const size_t smem = zpass_smem<C>(a.pl.n);
-    const int64_t ntiles = a.zt.tiles_per_box * a.batch * a.nbuf;
-    int grid = 0, rc;
-    if ((rc = persistent_grid(zinv_kernel<C>, C::T, smem, ntiles, &grid))) return rc;
-    zinv_kernel<C><<<grid, C::T, smem, st>>>(a);
-    return check_launch("zinv_kernel");
-    }
+    return launch_zinvw<C>(a, rows_per_box, st);
 }
 
 template <class C>
@@ -1424,14 +925,7 @@ static int launch_xpass(const XArgs& a, cudaStream_t st) {
 }
 
 template <class C>
-static int launch_xgc(const XGenArgs& a, cudaStream_t st);
-template <class C>
-static int launch_xgp(const XGenArgs& a, cudaStream_t st);
-
-template <class C>
 static int launch_xgen(const XGenArgs& a, cudaStream_t st) {
-    if (a.fields == XGEN_CLUSTER) return launch_xgc<C>(a, st);
-    if (a.pair && a.fields != XGEN_BOTH) return launch_xgp<C>(a, st);
     if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xgen_kernel");
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 +
                         (size_t)a.nzh * 4 + 16;
@@ -1448,103 +942,25 @@ static int launch_xgen(const XGenArgs& a, cudaStream_t st) {
     return check_launch("xgen_kernel");
 }
 
-// Clusters of four CTAs (xgc_kernel), as many as can be resident, at most one per tile.
-template <class C>
-static int launch_xgc(const XGenArgs& a, cudaStream_t st) {
-    if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xgc_kernel");
-    const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 +
-                        (size_t)a.nzh * 4 + 16;
-    const int64_t ntiles = (int64_t)a.batch * a.ny * ceil_div(a.nzh, 2 * C::W);
-    if (cudaFuncSetAttribute(xgc_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return check_launch("cudaFuncSetAttribute(xgc)");
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 4;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.blockDim = dim3(C::T, 1, 1);
-    cfg.gridDim = dim3(4 * sm_count(), 1, 1);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    int nclusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&nclusters, xgc_kernel<C>, &cfg) != cudaSuccess)
-        return check_launch("cudaOccupancyMaxActiveClusters(xgc)");
-    if (nclusters < 1) return fail(SMK_ENOTSUPP, "xgc_kernel: no cluster of 4 fits (smem %zu B)", smem);
-    cfg.gridDim = dim3((unsigned)(4 * std::min<int64_t>(nclusters, ntiles)), 1, 1);
-    if (cudaLaunchKernelEx(&cfg, xgc_kernel<C>, a) != cudaSuccess) return check_launch("xgc_kernel");
-    return check_launch("xgc_kernel");
-}
-
-// Clusters of two CTAs (xgp_kernel), as many as can be resident, at most one per tile.
-template <class C>
-static int launch_xgp(const XGenArgs& a, cudaStream_t st) {
-    if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xgp_kernel");
-    const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 +
-                        (size_t)a.nzh * 4 + 16;
-    const int64_t ntiles = (int64_t)a.batch * a.ny * ceil_div(a.nzh, 2 * C::W);
-    if (cudaFuncSetAttribute(xgp_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return check_launch("cudaFuncSetAttribute(xgp)");
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 2;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.blockDim = dim3(C::T, 1, 1);
-    cfg.gridDim = dim3(2 * sm_count(), 1, 1);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    int nclusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&nclusters, xgp_kernel<C>, &cfg) != cudaSuccess)
-        return check_launch("cudaOccupancyMaxActiveClusters(xgp)");
-    if (nclusters < 1) return fail(SMK_ENOTSUPP, "xgp_kernel: no cluster of 2 fits (smem %zu B)", smem);
-    cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(nclusters, ntiles)), 1, 1);
-    if (cudaLaunchKernelEx(&cfg, xgp_kernel<C>, a) != cudaSuccess) return check_launch("xgp_kernel");
-    return check_launch("xgp_kernel");
-}
-
-template <class C>
-static int launch_xinv(const XGenArgs& a, cudaStream_t st) {
-    if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xinv_kernel");
-    if ((1 << a.sh) != C::W) return fail(SMK_EINVAL, "xinv_kernel: staged block width differs from the tile's");
-    const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 4 +
-                        (size_t)a.nzh * 4 + 16;
-    const int64_t ntiles = (int64_t)a.batch * a.ny * ceil_div(a.nzh, C::W);
-    int grid = 0, rc;
-    if ((rc = persistent_grid(xinv_kernel<C>, C::T, smem, ntiles, &grid))) return rc;
-    xinv_kernel<C><<<grid, C::T, smem, st>>>(a);
-    return check_launch("xinv_kernel");
-}
-
 // ------------------------------------------------------------------ tile variants
 struct TileVariant {
     int w, t, nmax;  // columns (line pairs for z passes, lines for xgen) per tile, threads, max length
     int rmax, minb;  // largest FFT radix, requested resident blocks per SM
 };
-// z passes (zfwd, zinv): W = row pairs per tile
-#define SMK_Z_VARIANTS(X) X(16, 256, 512, 32, 1) X(8, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 1024, 16, 1) \
-    X(8, 512, 2560, 16, 1) X(4, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) X(4, 256, 2560, 32, 1) X(4, 512, 4096, 16, 1) X(2, 512, 4096, 16, 1) \
-    X(8, 256, 2560, 32, 1) X(2, 128, 2560, 16, 4) X(4, 128, 2560, 16, 2) X(4, 256, 2560, 16, 2) \
-    X(2, 256, 4096, 16, 2) X(8, 256, 2560, 16, 1) X(1, 64, 2560, 16, 6) X(2, 64, 2560, 16, 6) \
-    X(1, 128, 2560, 16, 4) X(2, 128, 2560, 32, 2)
-// z inverse: the z-pass variants, then one-warp-per-row-pair variants (W = 0; T = most threads)
-#define SMK_ZINV_VARIANTS(X) SMK_Z_VARIANTS(X) X(0, 512, 2560, 16, 1) X(0, 512, 1024, 16, 1) \
-    X(0, 256, 1024, 16, 2) X(0, 512, 4096, 16, 1) X(0, 256, 2560, 32, 1)
+// r2c along z of host noise (zfwd): W = row pairs per tile
+#define SMK_Z_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(4, 512, 2560, 16, 1) \
+    X(2, 128, 2560, 16, 4) X(4, 512, 4096, 16, 1)
+// z inverse: one warp per row pair (W = 0; as many warps per block as fit, up to T / 32)
+#define SMK_ZINV_VARIANTS(X) X(0, 512, 2560, 16, 1) X(0, 512, 1024, 16, 1) X(0, 256, 1024, 16, 2) \
+    X(0, 512, 4096, 16, 1) X(0, 256, 2560, 32, 1)
 // y pass (line): W = columns per tile
-#define SMK_LINE_VARIANTS(X) X(16, 256, 512, 32, 1) X(32, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(16, 1024, 1024, 8, 1) \
-    X(8, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1) X(4, 1024, 4096, 8, 1) X(8, 256, 2560, 32, 1) \
-    X(4, 128, 2560, 16, 2) X(4, 256, 2560, 16, 2) X(8, 256, 2560, 16, 1)
+#define SMK_LINE_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) \
+    X(4, 512, 4096, 16, 1) X(8, 256, 2560, 16, 1)
 // x pass of host noise: W = columns per tile
 #define SMK_X_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(4, 512, 4096, 16, 1)
-// x pass of GPU noise: W = lines per tile (W/2 delta columns + W/2 eta columns)
-#define SMK_XGEN_VARIANTS(X) X(32, 256, 512, 32, 1) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(16, 1024, 1024, 8, 1) \
-    X(8, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1) X(4, 1024, 4096, 8, 1) X(8, 256, 2560, 32, 1) \
-    X(8, 256, 2560, 16, 1)
+// x pass of GPU noise: W = lines per tile (one field per launch: W columns; both fields: W/2 + W/2)
+#define SMK_XGEN_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) \
+    X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1)
 
 enum { PASS_ZFWD = 0, PASS_LINE = 1, PASS_XPASS = 2, PASS_XGEN = 3, PASS_ZINV = 4, NPASS = 5 };
 
@@ -1558,9 +974,5 @@ int run_zinv(int v, const ZInvArgs& a, int64_t rows_per_box, cudaStream_t st);
 int run_line(int v, const LineArgs& a, bool inv, cudaStream_t st);
 int run_xpass(int v, const XArgs& a, cudaStream_t st);
 int run_xgen(int v, const XGenArgs& a, cudaStream_t st);
-// Staged GPU noise: draw into a.S (block width 2^a.sh), then the x inverse of a.fields from it
-// (tile variant v of the x pass; its W must be 2^a.sh).
-int run_kgen(const XGenArgs& a, cudaStream_t st);
-int run_xinv(int v, const XGenArgs& a, cudaStream_t st);
 
 }  // namespace smk

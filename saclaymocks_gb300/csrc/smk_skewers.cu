@@ -43,6 +43,10 @@ struct SkArgs {
     const float* ss_noise;
     const int64_t* ss_noise_offset;
     uint64_t seed;
+    const int32_t* forest;    // [n][2] forest pixel range [f0, f1) of each skewer, or null (all)
+    int ss_nztab;             // 0: one table set; > 0: one set per redshift ss_ztab[j]
+    const float* ss_ztab;     // [ss_nztab] ascending redshifts of the table sets
+    const float* ss_zsigma;   // [ss_nztab] sigma_s at ss_ztab, or null: no sigma_s(z)/sigma_s(zeff)
     FftPlan plans[SK_NCLASS];
     int abc_mode;
     float a, b, c, a_zref1, a_power;
@@ -87,6 +91,31 @@ struct SkewerGeo {
     long long i0u[3]; // i0 before wrapping (unwrapped line of sight, for the eta projection)
 };
 
+// Floats of one small-scale table set: sqrt(P1Dmiss/pix) for nz = 256 << j, j = 0..4.
+constexpr int SK_SS_SET = 129 + 257 + 513 + 1025 + 2049;
+
+// Redshift of pixel i of a skewer read from the boxes: z_lo..z_hi mapped linearly on the
+// wrapped x coordinate x/dcell (the trilinear read's rule).
+__device__ __forceinline__ float pixel_z_box(const SkArgs& a, const SkewerGeo& g, int i) {
+    const long long q = g.f0[0] + (long long)i * g.step[0];
+    const float fr = (float)(unsigned)(q & 0xffffffffLL) * 2.3283064365386963e-10f;
+    float xc = (float)wrap((int64_t)g.i0[0] + (q >> 32), a.nx) + fr + 0.5f;
+    if (xc >= (float)a.nx) xc -= (float)a.nx;
+    return a.z_lo + (a.z_hi - a.z_lo) * (xc / (float)a.nx);
+}
+
+// sigma_s(z) by linear interpolation on (ss_ztab, ss_zsigma), clamped to the table's ends.
+__device__ __forceinline__ float zsigma_at(const SkArgs& a, float z) {
+    const int n = a.ss_nztab;
+    if (n == 1 || z <= a.ss_ztab[0]) return a.ss_zsigma[0];
+    if (z >= a.ss_ztab[n - 1]) return a.ss_zsigma[n - 1];
+    int j = 0;
+    while (j < n - 2 && z > a.ss_ztab[j + 1]) ++j;
+    const float z0 = a.ss_ztab[j], z1 = a.ss_ztab[j + 1];
+    const float t = (z - z0) / (z1 - z0);
+    return fmaf(t, a.ss_zsigma[j + 1] - a.ss_zsigma[j], a.ss_zsigma[j]);
+}
+
 // Gaussian-weighted read of the (2*GR+1)^3 cells around the pixel (ReadSpec of
 // bin/make_spectra.py:39-68, 104-129): for the cell holding p (index floor(p/dcell)), weights
 // exp(-|r_cell - p|^2 / (2 dcell^2)) = prod_d exp(-(c_d + 0.5 - f_d)^2 / 2), one 1D factor per
@@ -106,6 +135,9 @@ __global__ void __launch_bounds__(SK_T, GAUSS ? 2 : 4) skewer_kernel(const SkArg
     __shared__ SkewerGeo geo[2];
     __shared__ int sk_id[2], sk_np[2];
     __shared__ int64_t sk_off[2];
+    __shared__ int sk_f0[2], sk_f1[2], sk_set[2];
+    __shared__ float sk_sig_eff[2];
+    __shared__ double zsum_sh[2][SK_T / 32];
     int cur_nz = 0;
     const int dims[3] = {a.nx, a.ny, a.nz};
     for (;;) {
@@ -129,9 +161,56 @@ __global__ void __launch_bounds__(SK_T, GAUSS ? 2 : 4) skewer_kernel(const SkArg
                     geo[t].step[d] = __double2ll_rn(a.dpix * (double)a.dir[3 * sid + d] / a.dcell * 4294967296.0);
                 }
             }
+            // forest pixels (bin/merge_spectra.py:305-306): no range given means all pixels
+            int f0 = 0, f1 = sk_np[t];
+            if (sid >= 0 && a.forest) {
+                f0 = max(0, a.forest[2 * sid]);
+                f1 = min(sk_np[t], a.forest[2 * sid + 1]);
+            }
+            sk_f0[t] = f0;
+            sk_f1[t] = max(f0, f1);
+            sk_set[t] = 0;
+            sk_sig_eff[t] = 1.f;
         }
         __syncthreads();
         const int np0 = sk_np[0], np1 = sk_np[1];
+        // redshift tables: zeff = mean z over the forest pixels (bin/merge_spectra.py:315), the
+        // table set of the nearest redshift (util.InterpP1Dmissing, util.py:467-474) and
+        // sigma_s(zeff) for the sigma_s(z)/sigma_s(zeff) rescale (:324-325)
+        if (a.ss_mode != SMK_SS_NONE && a.ss_nztab > 0) {
+#pragma unroll
+            for (int t = 0; t < 2; ++t) {
+                double zs = 0.0;
+                for (int i = sk_f0[t] + threadIdx.x; i < sk_f1[t]; i += SK_T)
+                    zs += a.interp == SMK_INTERP_PIXELS ? (double)__ldg(a.pix_z + sk_off[t] + i)
+                                                        : (double)pixel_z_box(a, geo[t], i);
+#pragma unroll
+                for (int m = 16; m; m >>= 1) zs += __shfl_xor_sync(0xffffffffu, zs, m);
+                if ((threadIdx.x & 31) == 0) zsum_sh[t][threadIdx.x >> 5] = zs;
+            }
+            __syncthreads();
+            if (threadIdx.x < 2) {
+                const int t = threadIdx.x;
+                const int cnt = sk_f1[t] - sk_f0[t];
+                if (cnt > 0) {
+                    double zs = 0.0;
+                    for (int w = 0; w < SK_T / 32; ++w) zs += zsum_sh[t][w];
+                    const float zeff = (float)(zs / cnt);
+                    int best = 0;
+                    float bd = fabsf(a.ss_ztab[0] - zeff);
+                    for (int j = 1; j < a.ss_nztab; ++j) {
+                        const float d = fabsf(a.ss_ztab[j] - zeff);
+                        if (d < bd) { bd = d; best = j; }
+                    }
+                    sk_set[t] = best;
+                    if (a.ss_zsigma) sk_sig_eff[t] = zsigma_at(a, zeff);
+                }
+            }
+            __syncthreads();
+        }
+        // skewers without forest pixels get no small-scale field (bin/merge_spectra.py:327-330)
+        const bool live0 = sk_id[0] >= 0 && sk_f1[0] > sk_f0[0];
+        const bool live1 = sk_id[1] >= 0 && sk_f1[1] > sk_f0[1];
         float inv_nz = 0.f;
         // a pair whose small-scale field does not fit the launch's FFT length (a table built
         // without smk_skewer_schedule's checks) gets NaN flux instead of a read past the line
@@ -161,18 +240,35 @@ __global__ void __launch_bounds__(SK_T, GAUSS ? 2 : 4) skewer_kernel(const SkArg
                 cur_nz = nzz;
                 __syncthreads();
             }
-            const float* S = a.ss_scale + ss_table_offset(cls);
+            const float* S = a.ss_scale + (int64_t)sk_set[0] * SK_SS_SET + ss_table_offset(cls);
+            const float* S1 = a.ss_scale + (int64_t)sk_set[1] * SK_SS_SET + ss_table_offset(cls);
+            const bool one_set = S1 == S;
             const int half = nzz / 2;
             if (a.ss_mode == SMK_SS_HOST) {
-                const float* n0 = a.ss_noise + a.ss_noise_offset[sk_id[0]];
-                const float* n1 = sk_id[1] >= 0 ? a.ss_noise + a.ss_noise_offset[sk_id[1]] : nullptr;
+                const float* n0 = live0 ? a.ss_noise + a.ss_noise_offset[sk_id[0]] : nullptr;
+                const float* n1 = live1 ? a.ss_noise + a.ss_noise_offset[sk_id[1]] : nullptr;
                 for (int e = threadIdx.x; e < nzz; e += SK_T)
-                    s[e] = make_float2(__ldg(n0 + e), n1 ? __ldg(n1 + e) : 0.f);
+                    s[e] = make_float2(n0 ? __ldg(n0 + e) : 0.f, n1 ? __ldg(n1 + e) : 0.f);
                 __syncthreads();
                 fft_tile<false, 1, 1, SK_T, 16>(s, tw, pl);
-                for (int e = threadIdx.x; e < nzz; e += SK_T) {
-                    const int f = freq_of_slot(pl, e);
-                    s[e] = cscale(s[e], __ldg(S + (f <= half ? f : nzz - f)));
+                if (one_set) {
+                    for (int e = threadIdx.x; e < nzz; e += SK_T) {
+                        const int f = freq_of_slot(pl, e);
+                        s[e] = cscale(s[e], __ldg(S + (f <= half ? f : nzz - f)));
+                    }
+                } else {
+                    // Y_k = A_k + i B_k holds both spectra; with Z_k = S0_k A_k + i S1_k B_k:
+                    // Z_k = P Y_k + M conj(Y_{nz-k}), P = (S0 + S1)/2, M = (S0 - S1)/2
+                    for (int k = threadIdx.x; k <= half; k += SK_T) {
+                        const int e = sof[k], em = sof[k == 0 ? 0 : nzz - k];
+                        const float s0 = __ldg(S + k), s1 = __ldg(S1 + k);
+                        const float P = 0.5f * (s0 + s1), M = 0.5f * (s0 - s1);
+                        const float2 y = s[e], ym = s[em];
+                        const float2 z = make_float2(P * y.x + M * ym.x, P * y.y - M * ym.y);
+                        const float2 zm = make_float2(P * ym.x + M * y.x, P * ym.y - M * y.y);
+                        s[e] = z;   // slots e and em belong to this thread alone
+                        if (em != e) s[em] = zm;
+                    }
                 }
                 __syncthreads();
             } else {
@@ -183,7 +279,7 @@ __global__ void __launch_bounds__(SK_T, GAUSS ? 2 : 4) skewer_kernel(const SkArg
                     float g[2][4];
 #pragma unroll
                     for (int t = 0; t < 2; ++t) {
-                        if (sk_id[t] >= 0)
+                        if (t == 0 ? live0 : live1)
                             philox_gauss4(a.seed, (uint64_t)sk_id[t], (uint32_t)j, STREAM_SKEWER, g[t]);
                         else
                             g[t][0] = g[t][1] = g[t][2] = g[t][3] = 0.f;
@@ -193,13 +289,26 @@ __global__ void __launch_bounds__(SK_T, GAUSS ? 2 : 4) skewer_kernel(const SkArg
                         const int k = 2 * j + h;
                         if (k > half) break;
                         const float sk = __ldg(S + k);
-                        if (k == 0 || k == half) {
-                            s[sof[k]] = make_float2(sk * r1 * g[0][2 * h], sk * r1 * g[1][2 * h]);
+                        if (one_set) {
+                            if (k == 0 || k == half) {
+                                s[sof[k]] = make_float2(sk * r1 * g[0][2 * h], sk * r1 * g[1][2 * h]);
+                            } else {
+                                const float ar = rh * g[0][2 * h], ai = rh * g[0][2 * h + 1];
+                                const float br = rh * g[1][2 * h], bi = rh * g[1][2 * h + 1];
+                                s[sof[k]] = make_float2(sk * (ar - bi), sk * (ai + br));
+                                s[sof[nzz - k]] = make_float2(sk * (ar + bi), sk * (br - ai));
+                            }
                         } else {
-                            const float ar = rh * g[0][2 * h], ai = rh * g[0][2 * h + 1];
-                            const float br = rh * g[1][2 * h], bi = rh * g[1][2 * h + 1];
-                            s[sof[k]] = make_float2(sk * (ar - bi), sk * (ai + br));
-                            s[sof[nzz - k]] = make_float2(sk * (ar + bi), sk * (br - ai));
+                            // each skewer's modes scaled by its own table set
+                            const float sk1 = __ldg(S1 + k);
+                            if (k == 0 || k == half) {
+                                s[sof[k]] = make_float2(sk * r1 * g[0][2 * h], sk1 * r1 * g[1][2 * h]);
+                            } else {
+                                const float ar = sk * rh * g[0][2 * h], ai = sk * rh * g[0][2 * h + 1];
+                                const float br = sk1 * rh * g[1][2 * h], bi = sk1 * rh * g[1][2 * h + 1];
+                                s[sof[k]] = make_float2(ar - bi, ai + br);
+                                s[sof[nzz - k]] = make_float2(ar + bi, br - ai);
+                            }
                         }
                     }
                 }
@@ -316,7 +425,10 @@ __global__ void __launch_bounds__(SK_T, GAUSS ? 2 : 4) skewer_kernel(const SkArg
                 z = a.z_lo + (a.z_hi - a.z_lo) * (xc / nxf);
             }
             float ds = 0.f;
-            if (a.ss_mode != SMK_SS_NONE) ds = too_long ? __int_as_float(0x7fc00000) : (t ? s[i].y : s[i].x) * inv_nz;
+            if (a.ss_mode != SMK_SS_NONE && (t ? live1 : live0)) {
+                ds = too_long ? __int_as_float(0x7fc00000) : (t ? s[i].y : s[i].x) * inv_nz;
+                if (a.ss_zsigma && a.ss_nztab > 0) ds *= zsigma_at(a, z) / sk_sig_eff[t];
+            }
             float pa = a.a, pb = a.b, pc = a.c;
             if (a.abc_mode == SMK_ABC_POWERLAW) {
                 pa = a.a * powf((1.0f + z) / a.a_zref1, a.a_power);
@@ -386,6 +498,8 @@ int smk_skewers_flux(const SmkSkewers* sk, const SmkSpectraParams* p, const floa
             return fail(SMK_EINVAL, "smk_skewers_flux: ss_nz must be 0 or a power of two in 256..4096");
         if (p->ss_mode == SMK_SS_HOST && (!p->ss_noise || !p->ss_noise_offset))
             return fail(SMK_EINVAL, "smk_skewers_flux: SMK_SS_HOST needs ss_noise and offsets");
+        if (p->ss_nztab < 0 || (p->ss_nztab > 0 && !p->ss_ztab))
+            return fail(SMK_EINVAL, "smk_skewers_flux: ss_nztab > 0 needs the ss_ztab redshifts");
     }
     if (p->abc_mode == SMK_ABC_TABLE && (!p->abc_tab || p->n_tab < 2 || !(p->dz_tab > 0)))
         return fail(SMK_EINVAL, "smk_skewers_flux: bad a,b,c table");
@@ -423,6 +537,10 @@ int smk_skewers_flux(const SmkSkewers* sk, const SmkSpectraParams* p, const floa
     a.ss_noise = p->ss_noise;
     a.ss_noise_offset = p->ss_noise_offset;
     a.seed = p->seed;
+    a.forest = sk->forest;
+    a.ss_nztab = p->ss_mode != SMK_SS_NONE ? p->ss_nztab : 0;
+    a.ss_ztab = p->ss_ztab;
+    a.ss_zsigma = p->ss_zsigma;
     for (int j = 0; j < SK_NCLASS; ++j) make_plan(256 << j, &a.plans[j], 16);
     a.abc_mode = p->abc_mode;
     a.a = p->a;

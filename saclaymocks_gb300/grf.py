@@ -79,8 +79,8 @@ def alloc_boxes(nx: int, ny: int, nz: int, batch: int = 1, want_eta: bool = True
 
 
 class GrfWorkspace:
-    """Device workspace + stats buffer reused by repeated calls.  The workspace grows on
-    demand to smk_grf_workspace_size (the staged modes of GPU-noise calls with staging)."""
+    """Device workspace + stats buffer reused by repeated calls (the workspace grows on
+    demand to smk_grf_workspace_size)."""
 
     def __init__(self, batch: int, device="cuda"):
         self.device = device
@@ -103,7 +103,7 @@ def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: flo
                amp: float | None = None, pk_grid: torch.Tensor | None = None,
                want_eta: bool = True, batch: int = 1, out=None, workspace: GrfWorkspace | None = None,
                stream=None, pass_events=None, eta_comp: str = "zz",
-               vel_factor: float | None = None, staging: bool = False) -> GrfBoxes:
+               vel_factor: float | None = None) -> GrfBoxes:
     """Draw delta (and eta_zz) boxes on the current CUDA device.
 
     noise:   None -> Philox white noise drawn on the GPU from ``seed`` (box b: seed + b);
@@ -119,8 +119,6 @@ def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: flo
              "yy", "xy", "xz", "yz"; bin/make_boxes.py:315-391), or a velocity
              v_i = irfftn(-i k_i / k^2 * vel_factor * delta_k) ("vx", "vy", "vz";
              bin/make_boxes.py:393-431, vel_factor = H0 * dD/dz(z=0)).
-    staging: GPU noise with eta: draw every mode once into the workspace (it grows by about
-             one box of complex floats), then one x inverse per field reads them back.
     """
     ny = nx if ny is None else ny
     nz = nx if nz is None else nz
@@ -164,7 +162,6 @@ def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: flo
         dpad, epad = out
     if workspace is None:
         workspace = GrfWorkspace(batch, device)
-    p.kspace_staging = 1 if (staging and noise is None and want_eta) else 0
     workspace.ensure(lib.smk_grf_workspace_size(C.byref(p)))
     if pass_events is not None:
         handles = (C.c_void_p * 6)(*[int(e.cuda_event) for e in pass_events])

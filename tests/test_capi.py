@@ -119,11 +119,10 @@ def test_tune_flags(lib):
     assert lib.smk_tune_flag(_lib.SMK_TUNE_PREFETCH, 2, None) == _lib.SMK_EINVAL
 
 
-def test_x_pass_form_and_tma_flags(lib):
-    """The x-pass form (one-CTA tiles, four-CTA clusters, CTA pairs), the y pass's TMA mode and
-    the TMA wait test switch are host-only settings with checked ranges."""
-    for flag, good, bad in ((_lib.SMK_TUNE_XGEN_CLUSTER, (-1, 0, 1, 2), (3, -2)),
-                            (_lib.SMK_TUNE_TMA, (0, 1, 2), (3, -1)),
+def test_tma_flags(lib):
+    """The y pass's TMA mode and the TMA wait test switch are host-only settings with checked
+    ranges."""
+    for flag, good, bad in ((_lib.SMK_TUNE_TMA, (0, 1, 2), (3, -1)),
                             (_lib.SMK_TUNE_TMA_WAIT_TEST, (0, 1), (2, -1))):
         first = _lib.tune_flag(flag, good[0])
         for v in good[1:]:
@@ -135,18 +134,14 @@ def test_x_pass_form_and_tma_flags(lib):
 
 
 def test_grf_workspace_size_and_alignment_need_no_gpu(lib):
-    """The workspace query (the staged-mode buffer is one complex box with k_z rounded up to
-    32 columns) and the 16-byte alignment rule of the boxes are host-side: a misaligned delta,
-    eta or workspace is refused with SMK_EINVAL before any CUDA call."""
+    """The workspace query (256 bytes: the FP64 normalisation accumulator) and the 16-byte
+    alignment rule of the boxes are host-side: a misaligned delta, eta or workspace is refused
+    with SMK_EINVAL before any CUDA call."""
     p = _lib.SmkGrfParams()
     p.nx, p.ny, p.nz, p.batch, p.dcell = 10, 6, 40, 2, 2.19
     p.noise_mode, p.pk_mode, p.k0, p.amp, p.want_eta = _lib.SMK_NOISE_PHILOX, _lib.SMK_PK_ANALYTIC, 0.02, 1.0, 1
     lib.smk_grf_workspace_size.restype = C.c_size_t
     assert lib.smk_grf_workspace_size(C.byref(p)) == 256
-    p.kspace_staging = 1
-    nzh = 40 // 2 + 1
-    assert lib.smk_grf_workspace_size(C.byref(p)) == 256 + 2 * 10 * 6 * ((nzh + 31) // 32 * 32) * 8
-    p.kspace_staging = 0
     base = 1 << 20   # never dereferenced: the call returns before touching memory
     for d, e, w in ((base + 8, base + 4096, None), (base, base + 4100, None), (base, base + 4096, base + 4)):
         assert lib.smk_grf_boxes(C.byref(p), d, e, None, w, 0, None) == _lib.SMK_EINVAL

@@ -38,53 +38,26 @@ def _check(gpu, ref, tag):
 
 
 @pytest.mark.parametrize("shape", [(40, 24, 36), (45, 18, 50), (64, 20, 12), (30, 6, 160)])
-def test_xgen_cluster_equals_split_launches(G, shape):
-    """The four-CTA cluster form of the GPU-noise x pass (each mode drawn once, both fields in
-    one launch) gives the same boxes, bit for bit, as two one-field launches; also for odd nx,
-    k_z extents that end inside a tile, batches and a velocity component."""
+def test_xgen_one_launch_equals_split_launches(G, shape):
+    """The GPU-noise x pass writing delta and eta in one launch (each mode drawn once) gives
+    the same boxes, bit for bit, as two one-field launches; also for odd nx, k_z extents that
+    end inside a tile, batches and a velocity component."""
     from saclaymocks_gb300 import _lib
     nx, ny, nz = shape
-    ps, pc = _lib.xgen_split(1), _lib.xgen_cluster(0)
+    ps = _lib.xgen_split(1)
     try:
         ref = G.make_boxes(nx, ny, nz, 2.19, seed=23, batch=2)
         refv = G.make_boxes(nx, ny, nz, 2.19, seed=24, eta_comp="vy", vel_factor=100.0)
-        _lib.xgen_cluster(1)
+        _lib.xgen_split(0)
         got = G.make_boxes(nx, ny, nz, 2.19, seed=23, batch=2)
         gotv = G.make_boxes(nx, ny, nz, 2.19, seed=24, eta_comp="vy", vel_factor=100.0)
         torch.cuda.synchronize()
     finally:
         _lib.xgen_split(ps)
-        _lib.xgen_cluster(pc)
     assert torch.equal(got.delta, ref.delta)
     assert torch.equal(got.eta, ref.eta)
     assert torch.equal(gotv.eta, refv.eta)
     np.testing.assert_array_equal(got.sigma(), ref.sigma())
-
-
-@pytest.mark.parametrize("shape", [(40, 24, 36), (45, 18, 50), (64, 20, 12), (30, 6, 160)])
-def test_xgen_pairs_equal_one_cta_launches(G, shape):
-    """The x pass on CTA pairs (each CTA draws and transforms its columns, the pair writes
-    128-byte row segments) gives the same boxes, bit for bit, as one-CTA tiles: both fields,
-    delta alone, odd nx, k_z extents ending inside a tile, a batch and a velocity component."""
-    from saclaymocks_gb300 import _lib
-    nx, ny, nz = shape
-    ps, pc = _lib.xgen_split(1), _lib.xgen_cluster(0)
-    try:
-        ref = G.make_boxes(nx, ny, nz, 2.19, seed=29, batch=2)
-        refd = G.make_boxes(nx, ny, nz, 2.19, seed=30, want_eta=False)
-        refv = G.make_boxes(nx, ny, nz, 2.19, seed=31, eta_comp="vx", vel_factor=80.0)
-        _lib.xgen_cluster(2)
-        got = G.make_boxes(nx, ny, nz, 2.19, seed=29, batch=2)
-        gotd = G.make_boxes(nx, ny, nz, 2.19, seed=30, want_eta=False)
-        gotv = G.make_boxes(nx, ny, nz, 2.19, seed=31, eta_comp="vx", vel_factor=80.0)
-        torch.cuda.synchronize()
-    finally:
-        _lib.xgen_split(ps)
-        _lib.xgen_cluster(pc)
-    assert torch.equal(got.delta, ref.delta)
-    assert torch.equal(got.eta, ref.eta)
-    assert torch.equal(gotd.delta, refd.delta)
-    assert torch.equal(gotv.eta, refv.eta)
 
 
 @pytest.mark.parametrize("shape", [(24, 2560, 40), (6, 1536, 96), (10, 600, 72), (8, 45, 24)])
@@ -135,58 +108,6 @@ def test_y_pass_tma_wait_running_out_is_reported(G):
     torch.cuda.synchronize()
     again.check()
     assert torch.equal(again.delta, good.delta)
-
-
-def test_xgen_pairs_every_variant_is_exact(G):
-    """Every x-pass tile variant run on CTA pairs matches the FP64 oracle."""
-    import ctypes as C
-    from saclaymocks_gb300 import _lib, tune
-    lib = _lib.load()
-    pid = _lib.SMK_PASS_XGEN
-    pc = _lib.xgen_cluster(2)
-    try:
-        for v, w, t in tune.variants(pid, 2):
-            nm = C.c_int32()
-            lib.smk_tune_info(pid, v, None, None, C.byref(nm))
-            nx, ny, nz = CLASS_LEN[nm.value], 4, 72
-            _lib.check(lib.smk_tune_set(pid, nx, v))
-            try:
-                out = G.make_boxes(nx, ny, nz, 2.19, seed=21)
-                torch.cuda.synchronize()
-            finally:
-                lib.smk_tune_set(pid, nx, -1)
-            nk = ophilox.kspace_noise(nx, ny, nz, 21)
-            o64 = ograf.grf_from_modes(nk, nz, 2.19, 0.02, eta=("zz",), precision="f64")
-            _check(out.delta[0].cpu().numpy(), o64["delta"], f"xgp variant {v} (W={w}, T={t})")
-            _check(out.eta[0].cpu().numpy(), o64["eta_zz"], f"xgp variant {v} eta")
-    finally:
-        _lib.xgen_cluster(pc)
-
-
-def test_xgen_cluster_every_variant_is_exact(G):
-    """Every x-pass tile variant run in the cluster form matches the FP64 oracle."""
-    import ctypes as C
-    from saclaymocks_gb300 import _lib, tune
-    lib = _lib.load()
-    pid = _lib.SMK_PASS_XGEN
-    pc = _lib.xgen_cluster(1)
-    try:
-        for v, w, t in tune.variants(pid, 2):
-            nm = C.c_int32()
-            lib.smk_tune_info(pid, v, None, None, C.byref(nm))
-            nx, ny, nz = CLASS_LEN[nm.value], 4, 72
-            _lib.check(lib.smk_tune_set(pid, nx, v))
-            try:
-                out = G.make_boxes(nx, ny, nz, 2.19, seed=19)
-                torch.cuda.synchronize()
-            finally:
-                lib.smk_tune_set(pid, nx, -1)
-            nk = ophilox.kspace_noise(nx, ny, nz, 19)
-            o64 = ograf.grf_from_modes(nk, nz, 2.19, 0.02, eta=("zz",), precision="f64")
-            _check(out.delta[0].cpu().numpy(), o64["delta"], f"xgc variant {v} (W={w}, T={t})")
-            _check(out.eta[0].cpu().numpy(), o64["eta_zz"], f"xgc variant {v} eta")
-    finally:
-        _lib.xgen_cluster(pc)
 
 
 @pytest.mark.parametrize("tag", ["cube16", "rect"])
@@ -446,16 +367,3 @@ def test_lognormal_and_velocity_boxes_match_reference_golden(G, golden, tag):
         out = G.make_boxes(NX, NY, NZ, dx, seed=77, k0=k0, eta_comp=c, vel_factor=vf)
         torch.cuda.synchronize()
         _check(out.eta[0].cpu().numpy(), o64[c], f"philox {c}")
-
-
-@pytest.mark.parametrize("shape", [(40, 24, 36), (30, 18, 50), (64, 20, 12)])
-def test_staged_x_pass_equals_in_place(G, shape):
-    """The staged column-block path (x pass into the eta box + workspace, y pass reading
-    contiguous runs) gives the same boxes, bit for bit, as the in-place path."""
-    nx, ny, nz = shape
-    a = G.make_boxes(nx, ny, nz, 2.19, seed=31, batch=2, staging=False)
-    b = G.make_boxes(nx, ny, nz, 2.19, seed=31, batch=2, staging=True)
-    torch.cuda.synchronize()
-    assert torch.equal(a.delta, b.delta)
-    assert torch.equal(a.eta, b.eta)
-    np.testing.assert_array_equal(a.sigma(), b.sigma())
