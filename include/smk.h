@@ -156,7 +156,8 @@ int smk_tune_flag(int32_t flag, int32_t value, int32_t* previous);
 #define SMK_INTERP_PIXELS 1    /* no box read: delta_l, eta_par, z given per pixel      */
                                /* (the merge_spectra input, bin/merge_spectra.py:282-300) */
 #define SMK_INTERP_GAUSS343 2  /* the reference's read: Gaussian weights over the 7^3   */
-                               /* cells around the pixel, eta_par = r_i r_j eta_ij / r^2  */
+                               /* cells around the pixel ((2 dmax + 1)^3 with gauss_dmax), */
+                               /* eta_par = r_i r_j eta_ij / r^2                          */
                                /* from six eta boxes (bin/make_spectra.py:39-139)         */
 
 #define SMK_SS_NONE 0     /* no small-scale field                                      */
@@ -172,8 +173,8 @@ int smk_tune_flag(int32_t flag, int32_t value, int32_t* previous);
 
 typedef struct {
     int64_t n;             /* number of skewers                                         */
-    const float* start;    /* [n][3] first pixel, box-corner frame, Mpc/h                */
-    const float* dir;      /* [n][3] unit direction                                      */
+    const float* start;    /* [n][3] first pixel, box-corner frame, Mpc/h (or start64)   */
+    const float* dir;      /* [n][3] unit direction (or dir64)                           */
     const int32_t* npix;   /* [n] pixels                                                 */
     const int64_t* offset; /* [n] index of the skewer's first pixel in the packed outputs */
     double dpix;           /* pixel spacing along the skewer, Mpc/h                      */
@@ -185,6 +186,8 @@ typedef struct {
     const int32_t* forest; /* [n][2] Lya-forest pixel range [f0, f1) of each skewer, or     */
                            /* NULL (every pixel).  A skewer with an empty range gets no     */
                            /* small-scale field (bin/merge_spectra.py:305-306, 327-330)      */
+    const double* start64; /* optional [n][3] FP64 start points; when given, start is unused */
+    const double* dir64;   /* optional [n][3] FP64 unit directions; when given, dir is unused */
 } SmkSkewers;
 
 typedef struct {
@@ -223,6 +226,8 @@ typedef struct {
     int32_t ss_nztab;
     const float* ss_ztab;   /* [ss_nztab] ascending redshifts (device)                     */
     const float* ss_zsigma; /* [ss_nztab] sigma_s at ss_ztab (device), or NULL            */
+    int32_t gauss_dmax;     /* GAUSS343: half-width of the Gaussian read in cells, 1..4 (the */
+                            /* reference's -dmax); 0 means 3 (the 7^3 read)                 */
 } SmkSpectraParams;
 #define SMK_SS_SET_FLOATS 3973 /* sum over nz = 256<<j, j = 0..4, of nz/2+1 */
 

@@ -193,3 +193,56 @@ def skewer_flux(delta_box, eta_box, skewers: dict, dcell: float, *, dpix: float,
         out["z"].append(z)
         out["delta_s"].append(ds)
     return out
+
+
+def merge_spectra_loop(spectra: list, rs: np.random.RandomState, *, pixsize: float = 0.2,
+                       pmiss_fit=None, ptab: dict | None = None, abc=(0.1, 1.6, 0.5),
+                       rsd: bool = True, addnoise: bool = True, lylimit: float = 0.0):
+    """The per-spectrum loop of bin/merge_spectra.py (:303-339) in float64.
+
+    spectra: list of dicts (wav, delta_l, eta_par, z, zq) in the loop's order, wavelengths
+    ascending.  rs: the RandomState the loop draws from (np.random.seed(seed + i), :75-79).
+    pmiss_fit: callable P1Dmiss(k) of the --fit-p1d branch (no clip, no sigma rescale); else
+    ptab = dict(z, k, pk, sigma) of the default branch (util.InterpP1Dmissing, util.py:448-474:
+    nearest-z table, linear in k; negative values clipped, :319; delta_s rescaled by
+    sigma(z)/sigma(zeff), :324-325).  abc: a, b, c scalars or callables of z.
+    A spectrum without forest pixels (lylimit < lambda/(1+zq) < lya) draws nothing and gets
+    delta_s = 0 (:327-330).  Returns (flux list, delta_s list).
+    """
+    fl, dsl = [], []
+    for sp in spectra:
+        wav = np.asarray(sp["wav"], np.float64)
+        z = np.asarray(sp["z"])
+        n = len(wav)
+        dl = np.asarray(sp["delta_l"], np.float64)
+        ds = np.zeros(n)
+        if addnoise:
+            wav_rf = wav / (1 + sp["zq"])
+            mmm = np.where((wav_rf < LYA) & (wav_rf > lylimit))[0]
+            if len(mmm) > 0:
+                nz = nz_rule(n)
+                noise = rs.normal(size=nz)
+                k = np.fft.rfftfreq(nz) * 2 * (np.pi / pixsize)
+                zeff = z[mmm].mean()
+                if pmiss_fit is not None:
+                    pm = np.asarray(pmiss_fit(k), np.float64)
+                else:
+                    iz = np.argsort(np.abs(np.asarray(ptab["z"]) - zeff))[0]
+                    pm = np.interp(k, ptab["k"], ptab["pk"][iz])
+                    pm[pm < 0] = 0
+                ds = np.fft.irfft(np.fft.rfft(noise) * np.sqrt(pm / pixsize), n=nz)[:n]
+                if pmiss_fit is None and ptab.get("sigma") is not None:
+                    ds = ds * np.interp(z, ptab["z"], ptab["sigma"]) / np.interp(zeff, ptab["z"], ptab["sigma"])
+        a, b, c = (p(z) if callable(p) else p for p in abc)
+        G = growth_merge(np.asarray(z, np.float64))
+        eta = np.asarray(sp["eta_par"], np.float64) if rsd else 0.0
+        fl.append(fgpa(dl + ds, eta, G, a, b, c))
+        dsl.append(ds)
+    return fl, dsl
+
+
+def merge_forest(sp: dict, lylimit: float = 0.0) -> np.ndarray:
+    """Indices of the forest pixels of a spectrum: lylimit < lambda/(1+zq) < lya
+    (bin/merge_spectra.py:305-306)."""
+    wav_rf = np.asarray(sp["wav"], np.float64) / (1 + sp["zq"])
+    return np.where((wav_rf < LYA) & (wav_rf > lylimit))[0]

@@ -51,7 +51,7 @@ class SmkSkewers(C.Structure):
                 ("npix", C.c_void_p), ("offset", C.c_void_p), ("dpix", C.c_double),
                 ("order", C.c_void_p), ("n_slots", C.c_int64),
                 ("pix_delta", C.c_void_p), ("pix_eta", C.c_void_p), ("pix_z", C.c_void_p),
-                ("forest", C.c_void_p)]
+                ("forest", C.c_void_p), ("start64", C.c_void_p), ("dir64", C.c_void_p)]
 
 
 class SmkSpectraParams(C.Structure):
@@ -64,7 +64,7 @@ class SmkSpectraParams(C.Structure):
                 ("n_tab", C.c_int32), ("z_tab0", C.c_float), ("dz_tab", C.c_float),
                 ("z_lo", C.c_float), ("z_hi", C.c_float), ("growth_mode", C.c_int32),
                 ("growth24", C.c_float), ("ss_nztab", C.c_int32), ("ss_ztab", C.c_void_p),
-                ("ss_zsigma", C.c_void_p)]
+                ("ss_zsigma", C.c_void_p), ("gauss_dmax", C.c_int32)]
 
 
 class SmkFitProblem(C.Structure):

@@ -10,8 +10,8 @@ True, eta_{xx,yy,zz,xy,xz,yz}-{i}.fits (one x plane per file) and v{x,y,z}-{i}.f
 files, velocity factor H0 * dD/dz(z=0) from the growth-rate table of -dgrowthfile or
 $SACLAYMOCKS_BASE/etc/dgrowth.fits).  Without a P-grid file the analytic spectrum
 A k/(1+(k/k0)^2)^2 with E[var delta] = 1 is used (no lognormal boxes).  -ncpu is accepted and
-ignored.  Extra flags: --noise numpy|gpu (numpy: the reference's MT19937 plane-order draws,
-bit-identical input; gpu: Fourier modes drawn on the GPU), -k0, --eta-only-zz (write only the
+ignored.  Extra flags: --noise numpy|gpu (numpy, the default: the reference's MT19937
+plane-order draws, bit-identical input; gpu: Fourier modes drawn on the GPU), -k0, --eta-only-zz (write only the
 eta_zz box the trilinear skewer read uses), --no-write.
 """
 from __future__ import annotations
@@ -48,7 +48,7 @@ def parser():
     p.add_argument("-dgrowthfile", default=None)
     p.add_argument("-outDir", default=".")
     p.add_argument("-k0", type=float, default=0.02)
-    p.add_argument("--noise", choices=["numpy", "gpu"], default="gpu")
+    p.add_argument("--noise", choices=["numpy", "gpu"], default="numpy")
     p.add_argument("--eta-only-zz", action="store_true")
     p.add_argument("--no-write", action="store_true")
     return p

@@ -22,6 +22,8 @@ constexpr int SK_NCLASS = 5;  // small-scale FFT lengths 256 << j
 struct SkArgs {
     const float* start;
     const float* dir;
+    const double* start64;    // optional FP64 start / direction (override start / dir)
+    const double* dir64;
     const int32_t* npix;
     const int64_t* offset;
     double dpix;
@@ -116,17 +118,16 @@ __device__ __forceinline__ float zsigma_at(const SkArgs& a, float z) {
     return fmaf(t, a.ss_zsigma[j + 1] - a.ss_zsigma[j], a.ss_zsigma[j]);
 }
 
-// Gaussian-weighted read of the (2*GR+1)^3 cells around the pixel (ReadSpec of
+// Gaussian-weighted read of the (2*GR+1)^3 cells around the pixel, GR = dmax (ReadSpec of
 // bin/make_spectra.py:39-68, 104-129): for the cell holding p (index floor(p/dcell)), weights
 // exp(-|r_cell - p|^2 / (2 dcell^2)) = prod_d exp(-(c_d + 0.5 - f_d)^2 / 2), one 1D factor per
 // axis; value = sum(w rho) / sum(w), with periodic wrap.
-constexpr int GR = 3;
-
-// GAUSS: the Gaussian 7^3 read (more registers, two blocks per SM); otherwise trilinear or
-// per-pixel inputs (three blocks per SM).  smem holds the small-scale FFT of the longest line
+// GR > 0: the Gaussian (2 GR + 1)^3 read (more registers, two blocks per SM); GR = 0: trilinear
+// or per-pixel inputs (four blocks per SM).  smem holds the small-scale FFT of the longest line
 // the launch needs (a.ss_nmax points: line, twiddles, slots).
-template <bool GAUSS>
-__global__ void __launch_bounds__(SK_T, GAUSS ? 2 : 4) skewer_kernel(const SkArgs a) {
+template <int GR>
+__global__ void __launch_bounds__(SK_T, GR ? 2 : 4) skewer_kernel(const SkArgs a) {
+    constexpr bool GAUSS = GR > 0;
     extern __shared__ float2 smem[];
     float2* s = smem;                                          // ss_nmax
     float2* tw = smem + a.ss_nmax;                             // ss_nmax
@@ -153,12 +154,14 @@ __global__ void __launch_bounds__(SK_T, GAUSS ? 2 : 4) skewer_kernel(const SkArg
             sk_off[t] = sid >= 0 ? a.offset[sid] : 0;
             if (sid >= 0 && a.interp != SMK_INTERP_PIXELS) {
                 for (int d = 0; d < 3; ++d) {
-                    const double u0 = (double)a.start[3 * sid + d] / a.dcell - 0.5;
+                    const double st0 = a.start64 ? a.start64[3 * sid + d] : (double)a.start[3 * sid + d];
+                    const double dr = a.dir64 ? a.dir64[3 * sid + d] : (double)a.dir[3 * sid + d];
+                    const double u0 = st0 / a.dcell - 0.5;
                     const double fl = floor(u0);
                     geo[t].i0[d] = wrap((int64_t)fl, dims[d]);
                     geo[t].i0u[d] = (long long)fl;
                     geo[t].f0[d] = __double2ll_rn((u0 - fl) * 4294967296.0);
-                    geo[t].step[d] = __double2ll_rn(a.dpix * (double)a.dir[3 * sid + d] / a.dcell * 4294967296.0);
+                    geo[t].step[d] = __double2ll_rn(a.dpix * dr / a.dcell * 4294967296.0);
                 }
             }
             // forest pixels (bin/merge_spectra.py:305-306): no range given means all pixels
@@ -332,7 +335,7 @@ __global__ void __launch_bounds__(SK_T, GAUSS ? 2 : 4) skewer_kernel(const SkArg
             } else if (GAUSS) {
                 const SkewerGeo& g = geo[t];
                 int ci[3];
-                float ew[3][2 * GR + 1];
+                float ew[3][2 * GR + 1 + !GAUSS];
                 double rpos[3];
                 float fux = 0.f;
 #pragma unroll
@@ -356,7 +359,7 @@ __global__ void __launch_bounds__(SK_T, GAUSS ? 2 : 4) skewer_kernel(const SkArg
                     sy += ew[1][c];
                     sz += ew[2][c];
                 }
-                int izs[2 * GR + 1];
+                int izs[2 * GR + 1 + !GAUSS];
 #pragma unroll
                 for (int c = 0; c < 2 * GR + 1; ++c) izs[c] = wrap((int64_t)ci[2] + c - GR, dims[2]);
                 const bool rsd = a.eta6[0] != nullptr;
@@ -477,6 +480,8 @@ int smk_skewers_flux(const SmkSkewers* sk, const SmkSpectraParams* p, const floa
     if (p->interp == SMK_INTERP_GAUSS343) {
         const int nset = !!p->eta6[0] + !!p->eta6[1] + !!p->eta6[2] + !!p->eta6[3] + !!p->eta6[4] + !!p->eta6[5];
         if (nset != 0 && nset != 6) return fail(SMK_EINVAL, "smk_skewers_flux: give all six eta_ij boxes or none");
+        if (p->gauss_dmax < 0 || p->gauss_dmax > 4)
+            return fail(SMK_EINVAL, "smk_skewers_flux: gauss_dmax must be 0 (= 3) or 1..4");
     }
     if (p->interp == SMK_INTERP_PIXELS && (!sk->pix_delta || !sk->pix_z))
         return fail(SMK_EINVAL, "smk_skewers_flux: SMK_INTERP_PIXELS needs pix_delta and pix_z");
@@ -484,7 +489,8 @@ int smk_skewers_flux(const SmkSkewers* sk, const SmkSpectraParams* p, const floa
     if (sk->n_slots == 0) return SMK_OK;
     if (!sk->npix || !sk->offset || !sk->order) return fail(SMK_EINVAL, "smk_skewers_flux: null skewer table array");
     if (p->interp == SMK_INTERP_TRILINEAR || p->interp == SMK_INTERP_GAUSS343) {
-        if (!sk->start || !sk->dir) return fail(SMK_EINVAL, "smk_skewers_flux: null start/dir");
+        if ((!sk->start && !sk->start64) || (!sk->dir && !sk->dir64))
+            return fail(SMK_EINVAL, "smk_skewers_flux: null start/dir");
         if (p->nx < 1 || p->ny < 1 || p->nz < 1 || p->pitch < p->nz || !(p->dcell > 0) || !(sk->dpix > 0))
             return fail(SMK_EINVAL, "smk_skewers_flux: bad box geometry");
     } else if (p->interp != SMK_INTERP_PIXELS) {
@@ -513,6 +519,8 @@ int smk_skewers_flux(const SmkSkewers* sk, const SmkSpectraParams* p, const floa
     SkArgs a;
     a.start = sk->start;
     a.dir = sk->dir;
+    a.start64 = sk->start64;
+    a.dir64 = sk->dir64;
     a.npix = sk->npix;
     a.offset = sk->offset;
     a.dpix = sk->dpix;
@@ -568,7 +576,9 @@ int smk_skewers_flux(const SmkSkewers* sk, const SmkSpectraParams* p, const floa
     a.ss_nmax = p->ss_mode == SMK_SS_NONE ? 0 : (p->ss_nz > 0 ? p->ss_nz : FFT_MAX_N);
     const size_t smem = 2 * (size_t)a.ss_nmax * sizeof(float2) + (size_t)a.ss_nmax * sizeof(int) + 16;
     const bool gauss = p->interp == SMK_INTERP_GAUSS343;
-    auto kern = gauss ? skewer_kernel<true> : skewer_kernel<false>;
+    const int dmax = p->gauss_dmax > 0 ? p->gauss_dmax : 3;
+    auto kern = !gauss ? skewer_kernel<0> : dmax == 1 ? skewer_kernel<1> : dmax == 2 ? skewer_kernel<2>
+              : dmax == 3 ? skewer_kernel<3> : skewer_kernel<4>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return check_launch("cudaFuncSetAttribute(skewer_kernel)");
     int per_sm = 0, dev = 0, nsm = 0;

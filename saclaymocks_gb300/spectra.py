@@ -40,6 +40,49 @@ def ss_scale_tables(pmiss, pixsize: float = 0.2) -> np.ndarray:
     return np.concatenate(out).astype(np.float32)
 
 
+class P1DMissTable:
+    """P1D_miss tabulated on a redshift grid, as util.InterpP1Dmissing reads it
+    (py/SaclayMocks/util.py:448-474: extensions ``z`` [nz], ``k`` [nk], ``pk`` [nz, nk]) plus the
+    ``sigma`` extension merge_spectra interpolates in z (bin/merge_spectra.py:118).  Each
+    skewer takes the table nearest to the mean redshift of its forest pixels, interpolated
+    linearly in k and clipped at 0, and, with sigma, its delta_s is rescaled pixel by pixel by
+    sigma(z)/sigma(zeff) (bin/merge_spectra.py:305-325)."""
+
+    def __init__(self, z, k, pk, sigma=None):
+        z = np.asarray(z, np.float64).reshape(-1)
+        order = np.argsort(z, kind="stable")
+        self.z = z[order]
+        self.k = np.asarray(k, np.float64).reshape(-1)
+        self.pk = np.asarray(pk, np.float64).reshape(len(z), -1)[order]
+        self.sigma = None if sigma is None else np.asarray(sigma, np.float64).reshape(-1)[order]
+        if self.pk.shape[1] != len(self.k):
+            raise ValueError("pk must be [len(z), len(k)]")
+
+    @classmethod
+    def from_fits(cls, path):
+        from . import fits
+        return cls(fits.read(path, "z"), fits.read(path, "k"), fits.read(path, "pk"), fits.read(path, "sigma"))
+
+    def scale_sets(self, pixsize: float = 0.2) -> np.ndarray:
+        """Table sets of smk_skewers_flux (ss_nztab of them, SMK_SS_SET_FLOATS floats each)."""
+        return np.concatenate([ss_scale_tables(lambda kk, j=j: np.interp(kk, self.k, self.pk[j]), pixsize)
+                               for j in range(len(self.z))])
+
+
+def forest_ranges(wav, zqso, lya: float = 1215.67, lylimit: float = 0.0) -> np.ndarray:
+    """[n, 2] pixel range [f0, f1) of the Lya forest of each skewer: the pixels with
+    lylimit < lambda/(1+z_qso) < lya (bin/merge_spectra.py:305-306), wavelengths ascending."""
+    out = np.zeros((len(wav), 2), np.int32)
+    for s, (w, zq) in enumerate(zip(wav, zqso)):
+        rf = np.asarray(w, np.float64) / (1.0 + float(zq))
+        idx = np.nonzero((rf < lya) & (rf > lylimit))[0]
+        if len(idx):
+            if idx[-1] - idx[0] + 1 != len(idx):
+                raise ValueError(f"skewer {s}: forest pixels are not contiguous (wavelengths unsorted?)")
+            out[s] = idx[0], idx[-1] + 1
+    return out
+
+
 def pmiss_gauss(amp: float = 0.05, kscale: float = 2.0):
     """P1D_miss(k) = amp * exp(-(k/kscale)^2) (k in h/Mpc)."""
     return lambda k: amp * np.exp(-(np.asarray(k, np.float64) / kscale) ** 2)
@@ -52,6 +95,9 @@ class SkewerTable:
     npix: np.ndarray               # [n] int32
     dpix: float = 0.2
     offset: np.ndarray = field(default=None)   # [n] int64 (filled by __post_init__)
+    forest: np.ndarray | None = None           # [n, 2] int32 forest pixel range, None: all pixels
+    start64: np.ndarray | None = None          # [n, 3] float64 start points (override start)
+    dir64: np.ndarray | None = None            # [n, 3] float64 unit directions (override direction)
 
     def __post_init__(self):
         self.start = np.ascontiguousarray(self.start, dtype=np.float32).reshape(-1, 3)
@@ -62,6 +108,17 @@ class SkewerTable:
                 if len(self.npix) else np.zeros(0, np.int64)
         if not (len(self.start) == len(self.direction) == len(self.npix) == len(self.offset)):
             raise ValueError("skewer table arrays differ in length")
+        for name in ("start64", "dir64"):
+            v = getattr(self, name)
+            if v is not None:
+                v = np.ascontiguousarray(v, dtype=np.float64).reshape(-1, 3)
+                if len(v) != len(self.npix):
+                    raise ValueError(f"{name} and skewers differ in length")
+                setattr(self, name, v)
+        if self.forest is not None:
+            self.forest = np.ascontiguousarray(self.forest, dtype=np.int32).reshape(-1, 2)
+            if len(self.forest) != len(self.npix):
+                raise ValueError("forest ranges and skewers differ in length")
 
     @property
     def n(self) -> int:
@@ -125,7 +182,8 @@ class SpectraConfig:
     """Small-scale and FGPA settings of :func:`skewer_flux` (see include/smk.h)."""
     ss_mode: int = _lib.SMK_SS_NONE
     ss_nz: int = 0                    # 0: reference rule 256*2^n >= npix+50
-    pmiss: object = None              # callable P1Dmiss(k); default 0.05 exp(-(k/2)^2)
+    pmiss: object = None              # callable P1Dmiss(k) (default 0.05 exp(-(k/2)^2)), or a
+                                      # P1DMissTable (redshift-dependent, merge_spectra's default)
     pixsize: float = 0.2
     seed: int = 0
     abc_mode: int = _lib.SMK_ABC_CONST
@@ -140,6 +198,7 @@ class SpectraConfig:
     growth: int = _lib.SMK_G_ONE
     read: str = "trilinear"           # "trilinear" or "gauss343" (the reference's 7^3 read)
     observer: tuple = (0.0, 0.0, 0.0)  # gauss343: observer in the box-corner frame (Mpc/h)
+    dmax: int = 3                     # gauss343: half-width of the read in cells (1..4)
 
 
 class SkewerRunner:
@@ -158,7 +217,18 @@ class SkewerRunner:
         self.d_order = torch.from_numpy(order).to(dv)
         self.n_slots = len(order)
         pm = cfg.pmiss if cfg.pmiss is not None else pmiss_gauss()
-        self.d_scale = torch.from_numpy(ss_scale_tables(pm, cfg.pixsize)).to(dv)
+        self.nztab, self.d_ztab, self.d_zsig = 0, None, None
+        if isinstance(pm, P1DMissTable):
+            self.d_scale = torch.from_numpy(pm.scale_sets(cfg.pixsize)).to(dv)
+            self.nztab = len(pm.z)
+            self.d_ztab = torch.from_numpy(pm.z.astype(np.float32)).to(dv)
+            if pm.sigma is not None:
+                self.d_zsig = torch.from_numpy(pm.sigma.astype(np.float32)).to(dv)
+        else:
+            self.d_scale = torch.from_numpy(ss_scale_tables(pm, cfg.pixsize)).to(dv)
+        self.d_forest = torch.from_numpy(table.forest).to(dv) if table.forest is not None else None
+        self.d_start64 = torch.from_numpy(table.start64).to(dv) if table.start64 is not None else None
+        self.d_dir64 = torch.from_numpy(table.dir64).to(dv) if table.dir64 is not None else None
         self.d_tab = None
         if cfg.abc_mode == _lib.SMK_ABC_TABLE:
             t = np.asarray(cfg.abc_table, np.float64)
@@ -178,11 +248,15 @@ class SkewerRunner:
         sk.dpix = float(self.table.dpix)
         sk.order = self.d_order.data_ptr()
         sk.n_slots = self.n_slots
+        sk.forest = self.d_forest.data_ptr() if self.d_forest is not None else None
+        sk.start64 = self.d_start64.data_ptr() if self.d_start64 is not None else None
+        sk.dir64 = self.d_dir64.data_ptr() if self.d_dir64 is not None else None
         p = _lib.SmkSpectraParams()
         p.interp = _lib.SMK_INTERP_TRILINEAR
         if cfg.read == "gauss343":
             p.interp = _lib.SMK_INTERP_GAUSS343
             p.obs[:] = [float(v) for v in cfg.observer]
+            p.gauss_dmax = int(cfg.dmax)
             if eta6 is not None:
                 if len(eta6) != 6:
                     raise ValueError("eta6: six boxes eta_xx, yy, zz, xy, xz, yz")
@@ -198,6 +272,10 @@ class SkewerRunner:
         p.ss_mode = cfg.ss_mode
         p.ss_nz = int(cfg.ss_nz)
         p.ss_scale = self.d_scale.data_ptr()
+        if self.nztab:
+            p.ss_nztab = self.nztab
+            p.ss_ztab = self.d_ztab.data_ptr()
+            p.ss_zsigma = self.d_zsig.data_ptr() if self.d_zsig is not None else None
         if cfg.ss_mode == _lib.SMK_SS_HOST:
             p.ss_noise = noise[0].data_ptr()
             p.ss_noise_offset = noise[1].data_ptr()

@@ -1,6 +1,8 @@
 """Regenerate the golden fixtures in this directory by running the REFERENCE's own code.
 
-    python tests/golden/make_golden.py        # needs the reference checkout at /root/reference
+    python tests/golden/make_golden.py --ref <checkout of igmhub/SaclayMocks> [name ...]
+    (or SACLAYMOCKS_REF=<checkout> python tests/golden/make_golden.py); names pick fixtures
+    (grf, readspec, spectra, iterate, merge, util), default all.
 
 Every fixture is produced by calling igmhub/SaclayMocks functions (or running a
 pipeline script's ``main()``) under the import shims of ``ref_shims.py``:
@@ -10,6 +12,9 @@ pipeline script's ``main()``) under the import shims of ``ref_shims.py``:
                      sqrt(P/Vcell) grid of the analytic spectrum A*k/(1+(k/k0)^2)^2;
 * ``readspec.npz``   ``ReadSpec``/``ComputeWeight``/``computeRho`` compiled out of
                      bin/make_spectra.py:39-139 (Gaussian 7^3-cell read + eta_par projection);
+* ``spectra_qso.npz`` bin/make_spectra.py ``main()`` on box files and a QSO catalogue written
+                     to disk (lines of sight :286-472, Gaussian read, METADATA/LAMBDA/DELTA_L/
+                     ETA_PAR/REDSHIFT of spectra-{i}-{hdu});
 * ``merge_*.npz``    bin/merge_spectra.py ``main()`` on a served spectra file
                      (small-scale loop :303-331 and FGPA :336-339);
 * ``util.npz``       util.fgpa :421-433, util.fgrowth :123-134, util.sigma_p1d :372-398,
@@ -29,6 +34,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
+if "--ref" in sys.argv:
+    _k = sys.argv.index("--ref")
+    os.environ["SACLAYMOCKS_REF"] = sys.argv[_k + 1]
+    del sys.argv[_k:_k + 2]
 import ref_shims  # noqa: E402
 
 ref_shims.install()
@@ -333,15 +342,91 @@ def gen_iterate():
     print("iterate: p1dmiss[0..3]", outs["cf1_p1dmiss"][:3])
 
 
-def main():
-    g = gen_grf(16, 16, 16, 0, "cube16")
-    gen_grf(20, 12, 18, 5, "rect")
-    gen_readspec(g)
-    gen_iterate()
-    gen_merge("fitp1d", True, 7)
-    gen_merge("table", False, 9)
-    gen_util()
+def gen_spectra():
+    """make_spectra main() on seeded 12 x 12 x 40 boxes of 12 Mpc/h cells (deep enough along z to
+    reach lambda > 3476 A behind the box centre at z0) and a QSO catalogue, both written to disk:
+    the lines of sight of bin/make_spectra.py:286-472 (cosmology, pixel grid, slice and forest
+    cuts) and the Gaussian read, with the redshift range set so every line stays in the box."""
+    from saclaymocks_gb300 import fits as _f
+    NX, NY, NZ, dx = 12, 12, 40, 12.0
+    rng = np.random.RandomState(23)
+    names = ["delta"] + ["eta_" + c for c in ("xx", "yy", "zz", "xy", "xz", "yz")]
+    boxes = {nm: rng.normal(0.0, 1.0 if nm == "delta" else 0.4, (NX, NY, NZ)).astype(np.float32) for nm in names}
+    tmp = tempfile.mkdtemp()
+    boxdir, outdir = os.path.join(tmp, "boxes"), os.path.join(tmp, "spec")
+    os.makedirs(boxdir)
+    os.makedirs(outdir)
+    hdr = {"DX": dx, "DY": dx, "DZ": dx, "NX": NX, "NY": NY, "NZ": NZ}
+    for nm in names:
+        prefix = "box" if nm == "delta" else nm
+        for i in range(NX):
+            _f.write_image(os.path.join(boxdir, f"{prefix}-{i}.fits"), boxes[nm][i:i + 1], hdr)
+    util = __import__("SaclayMocks.util", fromlist=["cosmo"])
+    const = __import__("SaclayMocks.constant", fromlist=["h"])
+    cos = util.cosmo(const.omega_M_0, Ok=const.omega_k_0, H0=100 * const.h)
+    R0 = const.h * cos.r_comoving(const.z0)
+    LX, LZ = dx * NX, dx * NZ
+    margin = 3 * dx + 1.0
+    zmin = max(float(cos.r_2_z((R0 - LZ / 2 + margin) / const.h)), 3480.0 / const.lya - 1)
+    zmax = float(cos.r_2_z((R0 + LZ / 2 - margin) / const.h))
+    n = 9
+    ang = 0.8 * (LX / 2 - margin) / (R0 + LZ / 2) * 180 / np.pi     # degrees: lines stay inside
+    ra = 180.0 + rng.uniform(-ang, ang, n)
+    dec = rng.uniform(-ang, ang, n)
+    zq = np.concatenate([[zmax, zmax - 1e-3], rng.uniform(zmin + 0.005, zmax, n - 4), [zmax + 0.01, zmin - 0.01]])
+    ra[3] = 180.0 + 40 * ang                                  # outside the slice cone: skipped
+    cat = {"RA": ra, "DEC": dec, "Z_QSO_NO_RSD": (zq - 1e-4).astype(np.float32),
+           "Z_QSO_RSD": zq.astype(np.float32), "THING_ID": np.arange(100, 100 + n, dtype=np.int64),
+           "HDU": np.array([0, 1, 0, 1, 0, 1, 0, 1, 0], np.int64),
+           "PLATE": np.full(n, 7, np.int64), "MJD": np.full(n, 55000, np.int32),
+           "FIBERID": np.arange(n, dtype=np.int32), "PMF": np.array([f"7-55000-{i}" for i in range(n)])}
+    qso = os.path.join(tmp, "QSO-")
+    _f.FitsWriter(qso + "0-1.fits").table(cat, {"RA0": 180.0, "DEC0": 0.0}).close()
+    ref_shims.FITS_CAPTURE.clear()
+    ms = ref_shims.load_script("make_spectra")
+    argv = sys.argv
+    sys.argv = ["make_spectra.py", "-QSOfile", qso, "-boxdir", boxdir, "-outDir", outdir, "-i", "0", "-N", "1",
+                "-zmin", repr(zmin), "-zmax", repr(zmax), "-pixel", "0.2", "-dmax", "3", "-rsd", "True"]
+    try:
+        ms.main()
+    finally:
+        sys.argv = argv
+    out = dict(zmin=zmin, zmax=zmax, dx=dx, **{f"box_{k}": v for k, v in boxes.items()},
+               **{f"cat_{k}": v for k, v in cat.items() if k != "PMF"})
+    for hdu in (0, 1):
+        rec = ref_shims.FITS_CAPTURE[f"spectra-0-{hdu}.fits.gz"]["hdus"]
+        hd = {h["extname"]: h for h in rec}
+        for k in ("LAMBDA", "DELTA_L", "ETA_PAR", "REDSHIFT"):
+            out[f"h{hdu}_{k}"] = np.asarray(hd[k]["data"])
+        meta = hd["METADATA"]["data"]
+        for k in ("THING_ID", "Z", "Z_noRSD", "RA", "DEC", "HDU"):
+            out[f"h{hdu}_{k}"] = np.asarray(meta[k])
+        hh = hd["METADATA"]["header"]
+        out[f"h{hdu}_header"] = np.array([hh["z0"], hh["pixel"], hh["Npixel"], hh["NX"], hh["dmax"],
+                                          hh["ra0"], hh["dec0"]], np.float64)
+    np.savez_compressed(os.path.join(HERE, "spectra_qso.npz"), **out)
+    print("spectra", {k: v.shape for k, v in out.items() if k.startswith("h")})
+
+
+def main(names=()):
+    want = lambda n: not names or n in names  # noqa: E731
+    if want("grf"):
+        g = gen_grf(16, 16, 16, 0, "cube16")
+        gen_grf(20, 12, 18, 5, "rect")
+    else:
+        g = dict(np.load(os.path.join(HERE, "grf_cube16.npz")))
+    if want("readspec"):
+        gen_readspec(g)
+    if want("spectra"):
+        gen_spectra()
+    if want("iterate"):
+        gen_iterate()
+    if want("merge"):
+        gen_merge("fitp1d", True, 7)
+        gen_merge("table", False, 9)
+    if want("util"):
+        gen_util()
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

@@ -25,7 +25,8 @@ import types
 
 import numpy as np
 
-REF = "/root/reference"
+# checkout of the reference (igmhub/SaclayMocks), from SACLAYMOCKS_REF or make_golden.py --ref
+REF = os.environ.get("SACLAYMOCKS_REF", "")
 REPO = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, REPO)
 
@@ -132,10 +133,13 @@ def _fitsio_read_header(path, ext=0):
 
 # ----------------------------------------------------------------------------- install
 def install():
+    if not REF or not os.path.isdir(os.path.join(REF, "py", "SaclayMocks")):
+        raise SystemExit("set SACLAYMOCKS_REF (or make_golden.py --ref) to a checkout of igmhub/SaclayMocks")
     import scipy
     for name in ("pi", "array", "exp", "ones_like", "zeros_like", "sqrt", "indices",
                  "arange", "log", "zeros", "ones", "cos", "sin", "mean", "where",
-                 "concatenate", "float32", "int32", "float64", "log10", "absolute"):
+                 "concatenate", "float32", "int32", "float64", "log10", "absolute", "power",
+                 "interp", "radians", "degrees", "arctan", "tan", "floor"):
         if not hasattr(scipy, name):
             setattr(scipy, name, getattr(np, name))
     scipy.save = lambda *a, **k: None          # only ever used for FFTW wisdom files
