@@ -151,6 +151,36 @@ def cpu_baseline(cfg, sample_div, workers):
                 sample=f"{nx}x{ny}x{nz} box (1/{f ** 3} of the cells) + {nsk} skewers")
 
 
+def skewer_sector_bytes(table, nx, ny, nz, pitch, dcell, chunk=20_000, device="cuda"):
+    """Compulsory DRAM bytes of the trilinear skewer read of one box: 32 B for every distinct
+    32-byte sector the 8 corners of the pixels touch, counted on the GPU from the geometry
+    (the kernel's cell-centred rule, periodic wrap).  Bookkeeping of the roofline only."""
+    import torch
+    nsec = (nx * ny * pitch * 4 + 31) // 32
+    mark = torch.zeros(nsec, dtype=torch.uint8, device=device)
+    st = torch.from_numpy(table.start.astype("float64")).to(device)
+    dr = torch.from_numpy(table.direction.astype("float64")).to(device)
+    npx = torch.from_numpy(table.npix.astype("int64")).to(device)
+    dims = torch.tensor([nx, ny, nz], device=device)
+    for a in range(0, table.n, chunk):
+        b = min(table.n, a + chunk)
+        n = npx[a:b]
+        sk = torch.repeat_interleave(torch.arange(b - a, device=device), n)
+        first = torch.cumsum(n, 0) - n
+        i = torch.arange(int(n.sum()), device=device) - torch.repeat_interleave(first, n)
+        p = st[a:b][sk] + (i.double() * table.dpix)[:, None] * dr[a:b][sk]
+        c0 = torch.floor(p / dcell - 0.5).long()
+        for cx in (0, 1):
+            ix = torch.remainder(c0[:, 0] + cx, dims[0])
+            for cy in (0, 1):
+                iy = torch.remainder(c0[:, 1] + cy, dims[1])
+                row = (ix * ny + iy) * pitch
+                for cz in (0, 1):
+                    iz = torch.remainder(c0[:, 2] + cz, dims[2])
+                    mark[((row + iz) * 4) // 32] = 1
+    return 32.0 * float(mark.sum().item())
+
+
 def workload_config(cfg, world):
     """The `config` of both arms' JSON lines (same workload, same keys)."""
     return {"workload": f"production chunk {cfg['nx']}x{cfg['ny']}x{cfg['nz']} delta+eta_par boxes + "
@@ -271,6 +301,26 @@ def run_ours(args, cfg):
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_s = max_over_ranks([e2e_s], dist)[0]
 
+    # host-noise mode (the reference's own noise fed in: z r2c, y forward, x, y inverse, z c2r):
+    # the same chunk with a dense device noise box, timed per pass
+    host_res = None
+    if not args.no_host_noise and rank == 0:
+        noise = torch.randn(nx * ny * nz, dtype=torch.float32, device="cuda").view(nx, ny, nz)
+        hev = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(3)]
+        for k in range(3):
+            hout = grf.make_boxes(nx, ny, nz, cfg["dcell"], noise=noise, amp=chunk.amp, out=boxes, workspace=ws,
+                                  pass_events=hev[k])
+        torch.cuda.synchronize()
+        hout.check()
+        hp = np.mean([[hev[k][i].elapsed_time(hev[k][i + 1]) for i in range(5)] for k in (1, 2)], axis=0)
+        del noise, hout
+        torch.cuda.empty_cache()
+        host_res = {"grf_ms": round(float(hp.sum()), 3),
+                    "pass_ms": dict(zip(["zfwd_r2c", "y_fwd", "x_fwd_scale_inv(x2)", "y_inv(x2)", "zinv_c2r(x2)"],
+                                        [round(float(x), 3) for x in hp])),
+                    "ms_per_step": round(float(hp.sum()) + sk_ms, 3),
+                    "noise": "dense device noise box (torch.randn), 2 timed calls after 1 warm-up"}
+
     fit_res = None
     if not args.no_fit and rank == 0:
         fit_res = fit_leg(args, runner, out, table, cfg)
@@ -311,6 +361,15 @@ def run_ours(args, cfg):
              "achieved_per_s": x_winst / (pass_ms[0] * 1e-3), "peak_per_s": nsm * 4 * sm_hz,
              "frac": x_winst / (pass_ms[0] * 1e-3) / (nsm * 4 * sm_hz),
              "basis": "ncu smsp__inst_executed.sum per mode and field, scaled; peak SMs x 4 x SM clock"}
+    # skewer stage: 4 B of flux per pixel + the distinct 32-byte sectors of delta and eta the
+    # trilinear corners touch (Philox small scales: no noise bytes)
+    sec = skewer_sector_bytes(table, nx, ny, nz, boxes[0].shape[-1], cfg["dcell"])
+    sk_bytes = 4.0 * pixels + 2.0 * sec
+    sk_roof = {"kernel": "skewer_kernel", "algorithmic_bytes": sk_bytes / 1e9,
+               "achieved": sk_bytes / (sk_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+               "frac": sk_bytes / (sk_ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
+               "box_sector_bytes": sec / 1e9, "naive_upper_bytes": 68.0 * pixels / 1e9,
+               "basis": "4 B/pixel flux + distinct 32-B sectors of delta and eta touched by the 8 corners"}
     value = aggregate_value(cells, world, step_ms * 1e-3)
     res = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
@@ -327,7 +386,8 @@ def run_ours(args, cfg):
                         "algorithmic_bytes": pass_bytes[dom] / 1e9,
                         "per_pass_frac": {n: round(b / (m * 1e-3) / 1e9 / peak, 3)
                                           for n, b, m in zip(pass_names, pass_bytes, pass_ms)},
-                        "issue": issue},
+                        "issue": issue, "skewer": sk_roof},
+           "host_noise": host_res,
            "e2e": {"value": aggregate_value(cells, world, e2e_s), "unit": "cells/s",
                    "h2d_bytes_per_step": chunk.h2d_bytes(), "d2h_bytes_per_step": chunk.d2h_bytes(),
                    "ms_per_step": e2e_s * 1e3},
@@ -715,6 +775,7 @@ def main():
     ap.add_argument("--variants", default=None,
                     help="fixed tile variants, e.g. xgen=5,line=5,zinv=4 (no autotuning)")
     ap.add_argument("--no-fit", action="store_true", help="skip the (a,b,c) fit leg")
+    ap.add_argument("--no-host-noise", action="store_true", help="skip the host-noise (5-pass) GRF leg")
     ap.add_argument("--fit-steps", type=int, default=20, help="Adam steps of the fit leg")
     ap.add_argument("--grf-shape", default=None,
                     help="NX,NY,NZ: time only the GRF boxes of this shape (profiling case)")

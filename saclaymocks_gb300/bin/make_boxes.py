@@ -115,6 +115,9 @@ def main(argv=None):
     vfac = None
     if rsd and not args.eta_only_zz:
         path = args.dgrowthfile or os.path.expandvars("$SACLAYMOCKS_BASE/etc/dgrowth.fits")
+        if not os.path.exists(path):
+            raise SystemExit(f"make_boxes: growth-rate table {path} not found (give -dgrowthfile, set "
+                             "$SACLAYMOCKS_BASE, or use -rsd False / --eta-only-zz)")
         vfac = H0 * growth_rate_at_zero(path)
     common = dict(seed=seed, noise=noise, k0=args.k0)
     write = not args.no_write

@@ -193,7 +193,10 @@ def test_boxes_spectra_merge_chain(ok, tmp_path, golden):
     g = golden("spectra_qso.npz")
     _, qso = _write_qso_inputs(tmp_path, g)
     bdir, sdir, mdir = tmp_path / "gb", tmp_path / "spec", tmp_path / "merged"
-    make_boxes.main(["-NX", "12", "-NY", "12", "-NZ", "40", "-pixel", "12", "-seed", "4", "-outDir", str(bdir)])
+    dg = tmp_path / "dgrowth.fits"
+    fits.FitsWriter(str(dg)).table({"dD/dz": np.array([-0.52, -0.5])}).close()
+    make_boxes.main(["-NX", "12", "-NY", "12", "-NZ", "40", "-pixel", "12", "-seed", "4", "-outDir", str(bdir),
+                     "-dgrowthfile", str(dg)])
     make_spectra.main(["-QSOfile", qso, "-boxdir", str(bdir), "-outDir", str(sdir), "-i", "0", "-N", "1",
                        "-zmin", repr(float(g["zmin"])), "-zmax", repr(float(g["zmax"]))])
     ptab = dict(z=np.array([1.8, 1.9, 2.0]), k=np.linspace(0, 20, 2001), sigma=np.array([0.3, 0.27, 0.25]))
