@@ -108,6 +108,41 @@ def dist_setup(backend="nccl"):
     return None, 0, 1
 
 
+def spawn_replicas(n: int, argv: list, timeout: float | None = None) -> int:
+    """`python bench.py --gpus N` without a launcher: start N copies of this script, one per
+    GPU (LOCAL_RANK = RANK = i, WORLD_SIZE = N, rendezvous on 127.0.0.1), forward rank 0's
+    output and return the first non-zero exit status (0 when all succeed)."""
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    procs = []
+    for r in range(n):
+        env = dict(os.environ, RANK=str(r), LOCAL_RANK=str(r), WORLD_SIZE=str(n), LOCAL_WORLD_SIZE=str(n),
+                   MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, os.path.abspath(__file__), *argv], env=env,
+                                      stdout=None if r == 0 else subprocess.DEVNULL))
+    rc = 0
+    for p in procs:
+        code = p.wait(timeout=timeout)
+        rc = rc or code
+    return rc
+
+
+def selftest_replicas(args):
+    """Replica bookkeeping without a GPU (gloo): every rank reports a made-up step time, rank 0
+    prints the job line (the N > 1 path's barrier / max-over-ranks / aggregate arithmetic)."""
+    dist, rank, world = dist_setup("gloo")
+    t = [0.5 + 0.25 * rank]
+    mx = max_over_ranks(t, dist, device="cpu")[0]
+    if rank == 0:
+        print(json.dumps({"n_gpus": world, "seeds": [replica_seed(1, r) for r in range(world)], "max_s": mx,
+                          "value": aggregate_value(100.0, world, mx), "parallelism": "replicas"}))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
 def replica_seed(base_seed: int, rank: int) -> int:
     """Seed of the chunk replica `rank` draws (Philox boxes, skewer table, small scales)."""
     return base_seed + rank
@@ -307,6 +342,8 @@ def run_ours(args, cfg):
     if not args.no_host_noise and rank == 0:
         noise = torch.randn(nx * ny * nz, dtype=torch.float32, device="cuda").view(nx, ny, nz)
         hev = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(3)]
+        for e in [x for row in hev for x in row]:
+            e.record()                          # materialise the raw event handles
         for k in range(3):
             hout = grf.make_boxes(nx, ny, nz, cfg["dcell"], noise=noise, amp=chunk.amp, out=boxes, workspace=ws,
                                   pass_events=hev[k])
@@ -343,7 +380,7 @@ def run_ours(args, cfg):
     dom = int(np.argmax(pass_ms))
     achieved = pass_bytes[dom] / (pass_ms[dom] * 1e-3) / 1e9
     # DRAM bytes per unit from ncu captures of the same kernels on boxes with the production
-    # line lengths (profiles/grf_passes_xgen_2560x128x1536_line_zinvw_128x2560x1536.md), scaled
+    # line lengths (2560 x 128 x 1536 for the x pass, 128 x 2560 x 1536 for y and z), scaled
     # by the units of this launch: x 7.81 B per mode and field, y 16.0 and z 16.1 B per mode
     # and field
     traffic = [7.81 * modes * 2, 16.0 * modes * 2, 16.14 * modes * 2][dom] / 1e9
@@ -429,16 +466,37 @@ def fit_leg(args, runner, out, table, cfg):
         prob.loss_grad(th0, mz, pk)
     t_adj = (time.perf_counter() - t0) / 3
     _, g_adj = prob.loss_grad(th0, mz, pk)
+    # the same adjoint with the chirp spectra transformed in the kernels (no table)
+    import copy
+    nt = copy.copy(prob)
+    nt.fp = type(prob.fp).from_buffer_copy(prob.fp)
+    nt.without_chirp_table()
+    nt.loss_grad(th0, mz, pk)
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    g_fd = prob.fd_grad(th0, mz, pk, h=1e-2, points=4)
+    for _ in range(3):
+        nt.loss_grad(th0, mz, pk)
+    t_adj_nt = (time.perf_counter() - t0) / 3
+    del nt
+    # finite-difference comparator: central differences, relative step 1e-4, 2 * 30 loss evaluations
+    t0 = time.perf_counter()
+    g_fd = prob.fd_grad(th0, mz, pk, h=1e-4, points=2)
     t_fd = time.perf_counter() - t0
     rel = np.abs(g_fd - g_adj) / np.abs(g_adj)
+    scale = float(np.abs(g_adj).max())
     steps = args.fit_steps
     ta, la, sa, _ = fit.adam_fit(prob, th0, mz, pk, steps=steps, lr=0.02, grad="adjoint", eps_rel=1e-2)
+    # algorithmic bytes of one gradient: delta + eta (4 B each) + z bin (2 B) per pixel read by the
+    # mean-flux pass, the P1D pass and twice by the adjoint pass (pair load + accumulation)
+    grad_bytes = 4 * 10.0 * prob.n_total
     res = {"params": "10 z bins x (a,b,c)", "pixels": prob.n_total, "adjoint_s_per_grad": t_adj,
-           "fd": "4-point stencil, relative step 1e-2 (120 loss evaluations per gradient)",
+           "adjoint_s_per_grad_without_chirp_table": t_adj_nt,
+           "adjoint_gbs": grad_bytes / t_adj / 1e9,
+           "adjoint_bytes_basis": "10 B/pixel (delta, eta, z bin) x 4 reads per gradient",
+           "fd": "central differences, relative step 1e-4 (60 loss evaluations per gradient)",
            "fd_s_per_grad": t_fd, "grad_speedup": t_fd / t_adj,
            "grad_rel_diff_median": float(np.median(rel)), "grad_rel_diff_max": float(rel.max()),
+           "grad_abs_diff_max_over_max": float(np.abs(g_fd - g_adj).max() / scale),
            "adam_steps": steps, "adjoint_fit_s": sa, "loss_start": la[0], "loss_end": la[-1]}
     # P1D-missing tuning loop (fit_az.Fitter.iterate) on the same skewers: time per iteration
     from saclaymocks_gb300 import tune_p1d
@@ -458,7 +516,7 @@ def fit_leg(args, runner, out, table, cfg):
                              "max_abs_ratio_minus_1": [round(x, 4) for x in tuner.history]}
     del tuner
     if steps * t_fd < 150:
-        tf, lf, sf, _ = fit.adam_fit(prob, th0, mz, pk, steps=steps, lr=0.02, grad="fd", h=1e-2, points=4,
+        tf, lf, sf, _ = fit.adam_fit(prob, th0, mz, pk, steps=steps, lr=0.02, grad="fd", h=1e-4, points=2,
                                      eps_rel=1e-2)
         res.update({"fd_fit_s": sf, "fit_speedup": sf / sa,
                     "max_rel_param_diff": float(np.max(np.abs(ta - tf) / np.abs(tf)))})
@@ -779,7 +837,14 @@ def main():
     ap.add_argument("--fit-steps", type=int, default=20, help="Adam steps of the fit leg")
     ap.add_argument("--grf-shape", default=None,
                     help="NX,NY,NZ: time only the GRF boxes of this shape (profiling case)")
+    ap.add_argument("--selftest-replicas", action="store_true", help=argparse.SUPPRESS)
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # no launcher: one replica process per GPU, rank 0 prints the job's line
+        sys.exit(spawn_replicas(args.gpus, sys.argv[1:]))
+    if args.selftest_replicas:
+        selftest_replicas(args)
+        return
     cfg = SMALL if args.small else PRODUCTION
     if args.grf_shape:
         run_grf_only(args, [int(x) for x in args.grf_shape.split(",")])

@@ -300,8 +300,23 @@ typedef struct {
     int32_t nzb, nkb;       /* redshift bins, log-k bins (1..64 each)                     */
     const double* kedges;   /* [nkb+1] k bin edges, h/Mpc (device)                        */
     double dx;              /* pixel size, Mpc/h                                          */
+    const float* chirp;     /* optional (with chirp_off): smk_fit_chirps' table of the chirp */
+                            /* spectra of the problem's lengths (one transform of the three  */
+                            /* of each Bluestein DFT saved), or NULL                        */
+    const int64_t* chirp_off; /* [2049]: offset (complex elements) of length N's spectrum in */
+                              /* chirp, or -1 (then computed in the kernel)                    */
 } SmkFitProblem;
 
+/* Cyclic convolution length of the Bluestein DFT of a length-n skewer: the smallest
+ * 2^a 3^b 5^c >= 2n - 1 (0 outside 1..2048).  No counterpart in the reference. */
+int smk_fit_bluestein_m(int32_t n);
+/* Chirp spectra of the Bluestein DFTs (they depend on the skewer lengths only, not on theta):
+ * for i < n_lengths, out[2*offsets[i] .. 2*(offsets[i] + M_i)) receives the complex FFT_M of
+ * the length-lengths[i] chirp, M_i = smk_fit_bluestein_m(lengths[i]) (device arrays, offsets
+ * in complex elements).  SmkFitProblem.chirp_off[N] = offsets[i] for N = lengths[i], -1 for
+ * lengths without an entry.  No counterpart in the reference. */
+int smk_fit_chirps(int32_t n_lengths, const int32_t* lengths, const int64_t* offsets, float* out,
+                   void* stream);
 /* Host: pairs of equal-length skewers for the fit kernels (order_out: 2n + 16 ints). */
 int smk_fit_schedule(int64_t n, const int32_t* npix_host, int32_t* order_out, int64_t* n_slots_out);
 /* Length (doubles) of the accumulator array: [nzb] sum F per z bin, [1] sum F,

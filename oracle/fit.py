@@ -116,3 +116,36 @@ class ZBinProblem:
                 grad[j, p] = (self.loss(tp, target_mz, target_pk)
                               - self.loss(tm, target_mz, target_pk)) / (2 * step)
         return grad
+
+
+def torch_loss(problem: ZBinProblem, theta, target_mz, target_pk):
+    """The same loss written with torch operations in float64, so that torch.autograd gives its
+    gradient (the reference-autograd check of the adjoint): FGPA per pixel with the
+    parameters of the pixel's z bin, <F>_j by scatter-add, dF = F/<F> - 1, |rfft|^2 dx/N per
+    skewer (skewers of one length batched), binned as MakeProfileHisto bins them."""
+    import torch
+    th = theta if isinstance(theta, torch.Tensor) else torch.as_tensor(theta, dtype=torch.float64)
+    p = problem
+    zb = torch.as_tensor(p.zbin)
+    delta, eta, G = (torch.as_tensor(x) for x in (p.delta, p.eta, p.G))
+    a, b, c = th[zb, 0], th[zb, 1], th[zb, 2]
+    F = torch.exp(-a * torch.exp(b * G * (delta + c * eta)))
+    cnt_z = torch.bincount(zb, minlength=p.nzb).double()
+    mz = torch.zeros(p.nzb, dtype=torch.float64).index_add(0, zb, F) / cnt_z
+    dF = F / F.mean() - 1
+    psum = torch.zeros(p.nkb, dtype=torch.float64)
+    cnt_k = torch.zeros(p.nkb, dtype=torch.float64)
+    for n in np.unique(p.lengths):
+        rows = np.nonzero(p.lengths == n)[0]
+        idx = torch.as_tensor((p.offsets[rows][:, None] + np.arange(n)[None, :]).ravel())
+        X = torch.fft.rfft(dF[idx].reshape(len(rows), int(n)), dim=1)
+        P = (X.real ** 2 + X.imag ** 2) * p.dx / n
+        kb = _p1d.bin_index(_p1d.p1d_k(int(n), p.dx), p.kedges)
+        m = kb >= 0
+        kbt = torch.as_tensor(kb[m])
+        psum = psum.index_add(0, kbt, P[:, torch.as_tensor(m)].sum(0))
+        cnt_k = cnt_k.index_add(0, kbt, torch.full((int(m.sum()),), float(len(rows)), dtype=torch.float64))
+    pk = psum / cnt_k
+    tm = torch.as_tensor(np.asarray(target_mz, np.float64))
+    tp = torch.as_tensor(np.asarray(target_pk, np.float64))
+    return ((mz - tm) ** 2).sum() + (((pk - tp) / tp) ** 2).sum()

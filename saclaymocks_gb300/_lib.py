@@ -71,7 +71,7 @@ class SmkFitProblem(C.Structure):
     _fields_ = [("delta", C.c_void_p), ("eta", C.c_void_p), ("G", C.c_void_p), ("zbin", C.c_void_p),
                 ("offset", C.c_void_p), ("npix", C.c_void_p), ("order", C.c_void_p),
                 ("n_slots", C.c_int64), ("n_total", C.c_int64), ("nzb", C.c_int32), ("nkb", C.c_int32),
-                ("kedges", C.c_void_p), ("dx", C.c_double)]
+                ("kedges", C.c_void_p), ("dx", C.c_double), ("chirp", C.c_void_p), ("chirp_off", C.c_void_p)]
 
 
 # (name, restype, argtypes) of every exported entry point
@@ -105,6 +105,8 @@ _SIGS = [
                                           C.c_void_p, C.c_void_p]),
     ("smk_fit_schedule", C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]),
     ("smk_fit_acc_len", C.c_int, [C.c_int32, C.c_int32]),
+    ("smk_fit_bluestein_m", C.c_int, [C.c_int32]),
+    ("smk_fit_chirps", C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("smk_fit_forward", C.c_int, [C.POINTER(SmkFitProblem), C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_size_t, C.c_void_p]),
     ("smk_fit_backward", C.c_int, [C.POINTER(SmkFitProblem), C.c_void_p, C.c_void_p, C.c_void_p,

@@ -40,12 +40,63 @@ struct FftPlan {
     int twn;
 };
 
-// Host: radix plan of n.  rmax >= 16: 16s first; a single factor 2 left over becomes a
+// Radix plan of n (host or device).  rmax >= 16: 16s first; a single factor 2 left over becomes a
 // radix-32 stage (rmax >= 32), else joins a 5 (radix 10) or a 3 (radix 6), else stays a 2;
 // rmax 8: 8s, then 4s / 2.  3s and 5s follow.
 // Returns false unless 2 <= n <= FFT_MAX_N and n = 2^a 3^b 5^c.
 // mid: a three-stage plan (R, R, x) becomes (R, x, R) (the warp z pass's conflict-free order).
-bool make_plan(int n, FftPlan* p, int rmax = 16, bool mid = false);
+__host__ __device__ inline bool make_plan(int n, FftPlan* p, int rmax = 16, bool mid = false) {
+    if (n < 2 || n > FFT_MAX_N) return false;
+    int m = n, p2 = 0, p3 = 0, p5 = 0;
+    while (m % 2 == 0) { m /= 2; ++p2; }
+    while (m % 3 == 0) { m /= 3; ++p3; }
+    while (m % 5 == 0) { m /= 5; ++p5; }
+    if (m != 1) return false;
+    // rmax >= 16: radix-16 stages (a radix-32 one when one factor 2 is left over and
+    // rmax >= 32), then 8, 4 or 2 for the rest of the power of two; rmax 8: 8s, then 4s / 2.
+    // 3s and 5s follow.
+    int rad[32], nr = 0;
+    if (rmax >= 16) {
+        while (p2 >= 4) { rad[nr++] = 16; p2 -= 4; }
+        if (p2 == 1 && nr > 0 && rmax >= 32) {
+            rad[0] = 32;
+        } else if (p2 == 1 && p5 > 0) {
+            rad[nr++] = 10;
+            --p5;
+        } else if (p2 == 1 && p3 > 0) {
+            rad[nr++] = 6;
+            --p3;
+        } else if (p2 > 0) {
+            rad[nr++] = 1 << p2;
+        }
+    } else {
+        while (p2 >= 3 && p2 - 3 != 1) { rad[nr++] = 8; p2 -= 3; }
+        while (p2 >= 2) { rad[nr++] = 4; p2 -= 2; }
+        if (p2 == 1) rad[nr++] = 2;
+    }
+    for (int i = 0; i < p3; ++i) rad[nr++] = 3;
+    for (int i = 0; i < p5; ++i) rad[nr++] = 5;
+    if (nr > FFT_MAX_STAGES) return false;
+    if (mid && nr == 3 && rad[0] == rad[1] && rad[2] != rad[0]) {
+        rad[2] = rad[1];   // (R, R, x) -> (R, x, R)
+        rad[1] = (n / rad[0]) / rad[0];
+    }
+    p->n = n;
+    p->nst = nr;
+    int L = n, tw = 0;
+    for (int s = 0; s < nr; ++s) {
+        p->r[s] = rad[s];
+        p->m[s] = L / rad[s];
+        p->tstep[s] = n / L;
+        p->magic[s] = p->m[s] == 1 ? 0u : (uint32_t)((1ull << 32) / (uint64_t)p->m[s] + 1ull);
+        p->twoff[s] = tw;
+        if (p->m[s] > 1) tw += p->m[s] * (rad[s] - 1);
+        L = p->m[s];
+    }
+    for (int s = nr; s < FFT_MAX_STAGES; ++s) p->twoff[s] = tw;
+    p->twn = tw;
+    return true;
+}
 
 // Largest radix a kernel of T threads per block runs in registers without spilling (the
 // register budget per thread is 65536 / T): radix 32 for <= 256 threads, 16 for 512, 8 above.

@@ -42,7 +42,8 @@ struct FitArgs {
     const double* gM;      // backward: dL/d<F>_j / n_j            [nzb]
     const double* gP;      // backward: dL/dP_b / count_b          [nkb]
     unsigned long long* counter;
-    FftPlan plans[2];      // M = 2048, 4096
+    const float2* chirp;   // optional: FFT_M of the forward chirp of every length N, digit-reversed
+    const int64_t* chirp_off;  // [FFT_MAX_N / 2 + 1]: offset (complex) of length N in chirp, or -1
 };
 
 // accumulator layout (doubles)
@@ -106,19 +107,37 @@ __device__ __forceinline__ float2 chirp(int n, int N) {
     return twiddle((int)r, 2 * N);
 }
 
-// smallest power of two >= 2N - 1 (N <= 2048) and its plan slot
-__device__ __forceinline__ int bluestein_m(int N, int* slot) {
-    const int M = (2 * N - 1 <= 2048) ? 2048 : 4096;
-    *slot = M == 2048 ? 0 : 1;
-    return M;
+// Smallest M = 2^a 3^b 5^c >= 2N - 1 (N <= 2048, so M <= 4096): the cyclic convolution length
+// of Bluestein's transform, a length the mixed-radix engine runs.
+__host__ __device__ inline int bluestein_m(int N) {
+    for (int M = 2 * N - 1;; ++M) {
+        int m = M;
+        while (m % 2 == 0) m /= 2;
+        while (m % 3 == 0) m /= 3;
+        while (m % 5 == 0) m /= 5;
+        if (m == 1 && M >= 2) return M;
+    }
+}
+
+// Forward chirp of length N wrapped into M slots: b_d = conj(w_d) at d and M - d, |d| < N.  It
+// is even (b_d = b_{M-d}), so its DFT is even and the inverse transform's chirp spectrum
+// FFT(conj b) is the elementwise conjugate of FFT(b).
+__device__ __forceinline__ float2 chirp_b(int n, int N, int M) {
+    const int d = n < N ? n : (n > M - N ? M - n : -1);
+    if (d < 0) return make_float2(0.f, 0.f);
+    const float2 w = chirp(d, N);
+    return make_float2(w.x, -w.y);
 }
 
 // Unnormalised length-N DFT of the complex sequence held in s1[0..N) (natural order),
 // forward (e^{-}) or inverse (e^{+}); result left in s1[0..N) in natural order.  s2 is
-// scratch of M elements; tw the twiddle table of M.  Block-synchronous.
+// scratch of M elements; tw the twiddle table of M.  Bc (may be null): FFT_M of the forward
+// chirp in the engine's digit-reversed order, which saves one of the three transforms.
+// Block-synchronous.
 template <bool INV>
-__device__ void bluestein(float2* s1, float2* s2, const float2* tw, int N, int M, const FftPlan& pl) {
-    // a_n = x_n w_n (INV: x_n conj(w_n)); b_d = conj(w_d) (INV: w_d) for |d| < N, wrapped
+__device__ void bluestein(float2* s1, float2* s2, const float2* tw, int N, int M, const FftPlan& pl,
+                          const float2* __restrict__ Bc) {
+    // a_n = x_n w_n (INV: x_n conj(w_n)); b = the chirp (INV: its conjugate)
     for (int n = threadIdx.x; n < M; n += FIT_T) {
         if (n < N) {
             const float2 w = chirp(n, N);
@@ -126,18 +145,22 @@ __device__ void bluestein(float2* s1, float2* s2, const float2* tw, int N, int M
         } else {
             s1[n] = make_float2(0.f, 0.f);
         }
-        const int d = n < N ? n : (n > M - N ? M - n : -1);
-        if (d >= 0) {
-            const float2 w = chirp(d, N);
-            s2[n] = INV ? w : make_float2(w.x, -w.y);
-        } else {
-            s2[n] = make_float2(0.f, 0.f);
+        if (!Bc) {
+            const float2 b = chirp_b(n, N, M);
+            s2[n] = INV ? make_float2(b.x, -b.y) : b;
         }
     }
     __syncthreads();
     fft_tile<false, 1, 1, FIT_T, 16>(s1, tw, pl);
-    fft_tile<false, 1, 1, FIT_T, 16>(s2, tw, pl);
-    for (int n = threadIdx.x; n < M; n += FIT_T) s1[n] = cmul(s1[n], s2[n]);  // digit-reversed, same order
+    if (Bc) {
+        for (int n = threadIdx.x; n < M; n += FIT_T) {
+            const float2 b = __ldg(Bc + n);
+            s1[n] = cmul(s1[n], INV ? make_float2(b.x, -b.y) : b);   // digit-reversed, same order
+        }
+    } else {
+        fft_tile<false, 1, 1, FIT_T, 16>(s2, tw, pl);
+        for (int n = threadIdx.x; n < M; n += FIT_T) s1[n] = cmul(s1[n], s2[n]);  // digit-reversed, same order
+    }
     __syncthreads();
     fft_tile<true, 1, 1, FIT_T, 16>(s1, tw, pl);
     const float inv_m = 1.0f / (float)M;
@@ -239,17 +262,20 @@ __global__ void __launch_bounds__(FIT_T) fit_p1d_kernel(const FitArgs a) {
     for (int i = threadIdx.x; i < 3 * a.nzb; i += FIT_T) th[i] = a.theta[i];
     const float fbar_inv = (float)((double)a.n_total / a.acc[acc_ftot(a.nzb)]);
     const double kfac = 2.0 * (3.14159265358979323846 / a.dx);
+    __shared__ FftPlan pl;
     int curM = 0;
     while (next_pair(a, &item_sh, &ps)) {
         const int N = ps.N;
-        int slot;
-        const int M = bluestein_m(N, &slot);
+        const int M = bluestein_m(N);
         if (M != curM) {
-            fill_stage_twiddles(tw, a.plans[slot]);
+            if (threadIdx.x == 0) make_plan(M, &pl, 16);
+            __syncthreads();
+            fill_stage_twiddles(tw, pl);
             curM = M;
         }
+        const float2* Bc = a.chirp && a.chirp_off[N] >= 0 ? a.chirp + a.chirp_off[N] : nullptr;
         load_pair(a, th, fbar_inv, ps, s1);
-        bluestein<false>(s1, s2, tw, N, M, a.plans[slot]);
+        bluestein<false>(s1, s2, tw, N, M, pl, Bc);
         // X1_m = (Z_m + Z*_{N-m})/2, X2_m = (Z_m - Z*_{N-m})/(2i), m = 0..N/2
         const float norm = (float)(a.dx / (double)N);
         const int half = N / 2;
@@ -301,17 +327,20 @@ __global__ void __launch_bounds__(FIT_T) fit_adjoint_kernel(const FitArgs a) {
     const double fbar = a.acc[acc_ftot(a.nzb)] / (double)a.n_total;
     const float fbar_inv = (float)(1.0 / fbar);
     const double kfac = 2.0 * (3.14159265358979323846 / a.dx);
+    __shared__ FftPlan pl;
     int curM = 0;
     while (next_pair(a, &item_sh, &ps)) {
         const int N = ps.N;
-        int slot;
-        const int M = bluestein_m(N, &slot);
+        const int M = bluestein_m(N);
         if (M != curM) {
-            fill_stage_twiddles(tw, a.plans[slot]);
+            if (threadIdx.x == 0) make_plan(M, &pl, 16);
+            __syncthreads();
+            fill_stage_twiddles(tw, pl);
             curM = M;
         }
+        const float2* Bc = a.chirp && a.chirp_off[N] >= 0 ? a.chirp + a.chirp_off[N] : nullptr;
         load_pair(a, th, fbar_inv, ps, s1);
-        bluestein<false>(s1, s2, tw, N, M, a.plans[slot]);
+        bluestein<false>(s1, s2, tw, N, M, pl, Bc);
         // V_t (Hermitian): V_m = w_m X_m (0<m<N/2), V_{N-m} = conj; V_0, V_{N/2} = 2 Re(w X);
         // packed W = V_1 + i V_2; the unnormalised inverse DFT of W is gdF_1 + i gdF_2.
         const float norm = (float)(a.dx / (double)N);
@@ -335,7 +364,7 @@ __global__ void __launch_bounds__(FIT_T) fit_adjoint_kernel(const FitArgs a) {
         __syncthreads();
         for (int n = threadIdx.x; n < N; n += FIT_T) s1[n] = s2[n];
         __syncthreads();
-        bluestein<true>(s1, s2, tw, N, M, a.plans[slot]);
+        bluestein<true>(s1, s2, tw, N, M, pl, Bc);
         // per pixel: gF~ = gM_j + gdF / <F>; dF/da = -tau1 F, dF/db = -a tau1 G g F,
         // dF/dc = -a tau1 b G eta F
         // per-thread FP32 partials for the current redshift bin, flushed to the block's FP64
@@ -400,6 +429,26 @@ __global__ void __launch_bounds__(FIT_T) fit_adjoint_kernel(const FitArgs a) {
     if (threadIdx.x == 0) atomicAdd(a.acc + acc_S(a.nzb, a.nkb), sS);
 }
 
+// FFT_M of the forward chirp of each length (one block per length), in the order the engine
+// leaves a forward transform: the same arithmetic as bluestein() without a table.
+__global__ void __launch_bounds__(FIT_T) fit_chirp_kernel(const int32_t* lengths, const int64_t* offsets,
+                                                          float2* out) {
+    extern __shared__ float2 smem[];
+    float2* s = smem;
+    float2* tw = smem + FFT_MAX_N;
+    __shared__ FftPlan pl;
+    const int N = lengths[blockIdx.x];
+    const int M = bluestein_m(N);
+    if (threadIdx.x == 0) make_plan(M, &pl, 16);
+    __syncthreads();
+    fill_stage_twiddles(tw, pl);
+    for (int n = threadIdx.x; n < M; n += FIT_T) s[n] = chirp_b(n, N, M);
+    __syncthreads();
+    fft_tile<false, 1, 1, FIT_T, 16>(s, tw, pl);
+    float2* o = out + offsets[blockIdx.x];
+    for (int n = threadIdx.x; n < M; n += FIT_T) o[n] = s[n];
+}
+
 static int fit_grid(const void* kernel, size_t smem, int64_t items, int* grid) {
     int dev = 0, nsm = 0, per_sm = 0;
     cudaGetDevice(&dev);
@@ -420,6 +469,20 @@ using namespace smk;
 extern "C" {
 
 int smk_fit_acc_len(int32_t nzb, int32_t nkb) { return acc_len(nzb, nkb); }
+
+int smk_fit_bluestein_m(int32_t n) { return n >= 1 && n <= FFT_MAX_N / 2 ? bluestein_m(n) : 0; }
+
+int smk_fit_chirps(int32_t n_lengths, const int32_t* lengths, const int64_t* offsets, float* out, void* stream) {
+    if (n_lengths < 0 || (n_lengths > 0 && (!lengths || !offsets || !out)))
+        return fail(SMK_EINVAL, "smk_fit_chirps: null argument");
+    if (n_lengths == 0) return SMK_OK;
+    if ((uintptr_t)out & 7) return fail(SMK_EINVAL, "smk_fit_chirps: out must be 8-byte aligned");
+    const size_t smem = 2 * FFT_MAX_N * sizeof(float2);
+    if (cudaFuncSetAttribute(fit_chirp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return check_launch("cudaFuncSetAttribute(fit_chirp)");
+    fit_chirp_kernel<<<n_lengths, FIT_T, smem, (cudaStream_t)stream>>>(lengths, offsets, reinterpret_cast<float2*>(out));
+    return check_launch("fit_chirp_kernel");
+}
 
 int smk_fit_schedule(int64_t n, const int32_t* npix_host, int32_t* order_out, int64_t* n_slots_out) {
     if (n < 0 || (n > 0 && (!npix_host || !order_out)) || !n_slots_out)
@@ -469,8 +532,9 @@ static int fit_args(const SmkFitProblem* fp, const float* theta, double* acc, co
     a->gM = gM;
     a->gP = gP;
     a->counter = counter;
-    make_plan(2048, &a->plans[0], 16);
-    make_plan(4096, &a->plans[1], 16);
+    a->chirp = reinterpret_cast<const float2*>(fp->chirp);
+    a->chirp_off = fp->chirp_off;
+    if (!a->chirp != !a->chirp_off) return fail(SMK_EINVAL, "smk_fit: give chirp and chirp_off together");
     return SMK_OK;
 }
 

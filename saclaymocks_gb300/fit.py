@@ -63,6 +63,17 @@ class FitProblem:
         self.d_off = torch.from_numpy(self.offset).to(dv)
         self.d_npix = torch.from_numpy(self.lengths).to(dv)
         self.d_kedges = torch.from_numpy(self.kedges).to(dv)
+        # chirp spectra of every distinct length (independent of theta): one table, built once
+        uniq = np.unique(self.lengths).astype(np.int32)
+        msz = np.array([lib.smk_fit_bluestein_m(int(N)) for N in uniq], np.int64)
+        offs = np.concatenate([[0], np.cumsum(msz[:-1])]).astype(np.int64)
+        self.chirp = torch.empty(2 * int(msz.sum()), dtype=torch.float32, device=dv)
+        off_by_n = np.full(2049, -1, np.int64)
+        off_by_n[uniq] = offs
+        self.d_chirp_off = torch.from_numpy(off_by_n).to(dv)
+        d_uniq, d_offs = torch.from_numpy(uniq).to(dv), torch.from_numpy(offs).to(dv)
+        _lib.check(lib.smk_fit_chirps(len(uniq), d_uniq.data_ptr(), d_offs.data_ptr(), self.chirp.data_ptr(),
+                                      stream_handle()), "smk_fit_chirps")
         self.acc = torch.zeros(lib.smk_fit_acc_len(self.nzb, self.nkb), dtype=torch.float64, device=dv)
         self.ws = torch.zeros(32, dtype=torch.int64, device=dv)
         self.d_gM = torch.zeros(self.nzb, dtype=torch.float64, device=dv)
@@ -85,7 +96,14 @@ class FitProblem:
             G=self.G.data_ptr() if self.G is not None else None, zbin=self.zbin.data_ptr(),
             offset=self.d_off.data_ptr(), npix=self.d_npix.data_ptr(), order=self.d_order.data_ptr(),
             n_slots=ns.value, n_total=self.n_total, nzb=self.nzb, nkb=self.nkb,
-            kedges=self.d_kedges.data_ptr(), dx=self.dx)
+            kedges=self.d_kedges.data_ptr(), dx=self.dx, chirp=self.chirp.data_ptr(),
+            chirp_off=self.d_chirp_off.data_ptr())
+
+    def without_chirp_table(self):
+        """Let the kernels compute the chirp spectra themselves (the form without the table)."""
+        self.fp.chirp = None
+        self.fp.chirp_off = None
+        return self
 
     # ---------------------------------------------------------------- passes
     def _set_theta(self, theta):

@@ -204,19 +204,21 @@ def test_boxes_spectra_merge_chain(ok, tmp_path, golden):
     p1d = str(tmp_path / "pk.fits")
     (fits.FitsWriter(p1d).image(ptab["z"], extname="z").image(ptab["k"], extname="k")
      .image(ptab["pk"], extname="pk").image(ptab["sigma"], extname="sigma").close())
-    paths = merge_spectra.main(["-inDir", str(sdir), "-outDir", str(mdir), "-i", "0", "-aa", "0.1", "-bb", "1.6",
-                                "-cc", "0.5", "-seed", "7", "--store-g", "True", "-p1dfile", p1d, "-nside", "1"])
-    spec = []
+    # merge_spectra -i k takes the files whose last number is k: the spectra of QSO-file HDU k
     for hdu in (0, 1):
+        paths = merge_spectra.main(["-inDir", str(sdir), "-outDir", str(mdir), "-i", str(hdu), "-aa", "0.1",
+                                    "-bb", "1.6", "-cc", "0.5", "-seed", "7", "--store-g", "True", "-p1dfile", p1d,
+                                    "-nside", "1"])
         hd = {h.name: h.data for h in fits.read_fits(str(sdir / f"spectra-0-{hdu}.fits.gz"))}
+        spec = []
         for r in range(len(hd["METADATA"])):
             ok_ = hd["LAMBDA"][r] > 0
             spec.append(dict(tid=int(hd["METADATA"]["THING_ID"][r]), wav=hd["LAMBDA"][r][ok_],
                              delta_l=hd["DELTA_L"][r][ok_], eta_par=hd["ETA_PAR"][r][ok_],
                              z=hd["REDSHIFT"][r][ok_], zq=float(hd["METADATA"]["Z"][r])))
-    spec.sort(key=lambda d: d["tid"])
-    fo, dso = osk.merge_spectra_loop(spec, np.random.RandomState(7), ptab=ptab, abc=(0.1, 1.6, 0.5))
-    hd = {h.name: h.data for h in fits.read_fits(paths[0])}
-    np.testing.assert_array_equal(hd["METADATA"]["THING_ID"], [d["tid"] for d in spec])
-    np.testing.assert_allclose(hd["FLUX"], np.array(fo), rtol=0, atol=2e-6)
-    np.testing.assert_allclose(hd["DELTA_S"], np.array(dso), rtol=0, atol=2e-6)
+        spec.sort(key=lambda d: d["tid"])
+        fo, dso = osk.merge_spectra_loop(spec, np.random.RandomState(7 + hdu), ptab=ptab, abc=(0.1, 1.6, 0.5))
+        md = {h.name: h.data for h in fits.read_fits(paths[0])}
+        np.testing.assert_array_equal(md["METADATA"]["THING_ID"], [d["tid"] for d in spec])
+        np.testing.assert_allclose(md["FLUX"], np.array(fo), rtol=0, atol=2e-6)
+        np.testing.assert_allclose(md["DELTA_S"], np.array(dso), rtol=0, atol=2e-6)

@@ -68,6 +68,44 @@ def test_autograd_function(problem_pair):
     np.testing.assert_allclose(th.grad.numpy(), og, rtol=0, atol=2e-4 * np.abs(og).max())
 
 
+def test_adjoint_matches_torch_autograd_of_fp64_restatement(problem_pair):
+    """The adjoint gradient against torch.autograd through an FP64 torch restatement of the same
+    loss (oracle.fit.torch_loss), within the FP32 tolerance 2e-4 max|g|."""
+    gp, op, mz, pk = problem_pair
+    theta = np.tile([0.14, 1.45, 0.45], (10, 1)) * np.linspace(0.97, 1.03, 10)[:, None]
+    th = torch.tensor(theta, dtype=torch.float64, requires_grad=True)
+    ofit.torch_loss(op, th, mz, pk).backward()
+    _, g = gp.loss_grad(theta, mz, pk)
+    ref = th.grad.numpy()
+    np.testing.assert_allclose(g, ref, rtol=0, atol=2e-4 * np.abs(ref).max())
+
+
+def test_chirp_table_gives_identical_results(problem_pair):
+    """The precomputed chirp spectra (one Bluestein transform saved) give the same reductions
+    and gradient, bit for bit, as the chirps transformed in the kernels; every Bluestein length
+    is the smallest 2^a 3^b 5^c >= 2N - 1."""
+    import copy
+    from saclaymocks_gb300 import _lib
+    gp, op, mz, pk = problem_pair
+    lib = _lib.load()
+    for N in (1, 2, 40, 400, 1024, 1025, 1200, 2048):
+        M = lib.smk_fit_bluestein_m(N)
+        assert M >= 2 * N - 1 and lib.smk_fft_supported(M)
+        assert all(not lib.smk_fft_supported(m) for m in range(max(2, 2 * N - 1), M))
+    theta = np.tile([0.15, 1.3, 0.4], (10, 1))
+    L1, g1 = gp.loss_grad(theta, mz, pk)
+    r1 = gp.reductions(theta)
+    gq = copy.copy(gp)
+    gq.fp = type(gp.fp).from_buffer_copy(gp.fp)
+    gq.without_chirp_table()
+    L0, g0 = gq.loss_grad(theta, mz, pk)
+    r0 = gq.reductions(theta)
+    assert L1 == L0
+    np.testing.assert_array_equal(g1, g0)
+    for a, b in zip(r1, r0):
+        np.testing.assert_array_equal(a, b)
+
+
 def test_adjoint_and_fd_fits_agree(problem_pair):
     """Adam from (0.15, 1.3, 0.4) with adjoint and with finite-difference gradients (fourth-order
     stencil, relative step 1e-2: truncation and the float32 rounding of the loss together keep the

@@ -40,3 +40,22 @@ def test_two_replicas_gloo():
     for r in range(world):
         assert res[r][1] == [2.5, 10.0]                      # max over ranks, element-wise
         assert res[r][2] == pytest.approx(2 * 100.0 / 2.5)   # all units over the slowest time
+
+
+def test_bench_spawns_replicas_without_a_launcher():
+    """`python bench.py --gpus 2` with no WORLD_SIZE in the environment starts two replica
+    processes itself (here the gloo self-test leg, no GPU) and prints one line for the job."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--gpus", "2", "--selftest-replicas"],
+                       capture_output=True, text=True, env=env, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["n_gpus"] == 2 and d["parallelism"] == "replicas"
+    assert d["seeds"] == [1, 2] and d["max_s"] == 0.75
+    assert d["value"] == pytest.approx(2 * 100.0 / 0.75)
