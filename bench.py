@@ -267,8 +267,9 @@ def run_ours(args, cfg):
                                  pmiss=spectra.pmiss_gauss(0.05, 2.0), seed=seed,
                                  abc_mode=_lib.SMK_ABC_POWERLAW, a=0.1, a_zref1=3.2, a_power=4.5,
                                  b=1.58, c=0.6, z_lo=1.8, z_hi=3.6)
+    xi = xi_chunk(args, cfg["nz"])
     chunk = pipeline.MockChunk(cfg["nx"], cfg["ny"], cfg["nz"], cfg["dcell"], seed=seed,
-                               cfg=scfg)
+                               cfg=scfg, xi_chunk_kz=xi)
     runner = chunk._prepare(table.start, table.direction, table.npix)
     boxes, ws = chunk.boxes, chunk.ws
     tuned = None
@@ -276,14 +277,15 @@ def run_ours(args, cfg):
         tuned = set_variants(args.variants, cfg["nx"], cfg["ny"], cfg["nz"])
     elif not args.no_tune:
         from saclaymocks_gb300 import tune
-        tuned = tune.tune_grf(cfg["nx"], cfg["ny"], cfg["nz"], cfg["dcell"], out=boxes, workspace=ws)
+        tuned = tune.tune_grf(cfg["nx"], cfg["ny"], cfg["nz"], cfg["dcell"], out=boxes, workspace=ws,
+                              xi_chunk_kz=xi, use_cache=xi == 0)
     nx, ny, nz = cfg["nx"], cfg["ny"], cfg["nz"]
     cells = nx * ny * nz
     pixels = table.total_pixels
 
     def device_step(ev=None, sk_ev=None):
         out = grf.make_boxes(nx, ny, nz, cfg["dcell"], seed=seed, amp=chunk.amp,
-                             out=boxes, workspace=ws, pass_events=ev)
+                             out=boxes, workspace=ws, pass_events=ev, xi_chunk_kz=xi)
         if sk_ev:
             sk_ev[0].record()
         runner.run(out.delta_pad[0], out.eta_pad[0], nx=nx, ny=ny, nz=nz, pitch=out.pitch,
@@ -760,6 +762,13 @@ def precision_leg(n=1536, seed=3, nsk=100_000, npix=1024, dcell=2.19, k0=0.02, n
     return res
 
 
+def xi_chunk(args, nz):
+    """k_z columns per chunk of the x pass's blocked intermediate: --xi-chunk (0: x pass in
+    place; -1: one chunk for the whole half spectrum)."""
+    v = args.xi_chunk
+    return (nz // 2 + 1) if v < 0 else v
+
+
 def set_variants(spec, nx, ny, nz):
     """--variants xgen=5,line=5,zinv=4: fixed tile variants per GRF pass instead of tuning
     (so a profile replays the tile choice of an earlier tuned run)."""
@@ -796,21 +805,22 @@ def run_grf_only(args, shape):
         tuned = set_variants(args.variants, nx, ny, nz)
     elif not args.no_tune:
         from saclaymocks_gb300 import tune
-        tuned = tune.tune_grf(nx, ny, nz, out=boxes, workspace=ws, use_cache=False)
+        tuned = tune.tune_grf(nx, ny, nz, out=boxes, workspace=ws, use_cache=False, xi_chunk_kz=xi_chunk(args, nz))
+    xi = xi_chunk(args, nz)
     for _ in range(args.warmup):
-        grf.make_boxes(nx, ny, nz, seed=1, amp=amp, out=boxes, workspace=ws, want_eta=want_eta)
+        grf.make_boxes(nx, ny, nz, seed=1, amp=amp, out=boxes, workspace=ws, want_eta=want_eta, xi_chunk_kz=xi)
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(args.steps)]
     for e in [x for row in evs for x in row]:
         e.record()
     torch.cuda.synchronize()
     for k in range(args.steps):
         out = grf.make_boxes(nx, ny, nz, seed=1, amp=amp, out=boxes, workspace=ws, pass_events=evs[k],
-                             want_eta=want_eta)
+                             want_eta=want_eta, xi_chunk_kz=xi)
     torch.cuda.synchronize()
     out.check()
     pass_ms = np.mean([[evs[k][i].elapsed_time(evs[k][i + 1]) for i in range(5)]
                        for k in range(args.steps)], axis=0)
-    print(json.dumps({"grf_shape": shape, "pass_ms": [round(float(x), 4) for x in pass_ms], "tuned": tuned,
+    print(json.dumps({"grf_shape": shape, "xi_chunk_kz": xi, "pass_ms": [round(float(x), 4) for x in pass_ms], "tuned": tuned,
                       "grf_cells_per_s": nx * ny * nz / (pass_ms.sum() * 1e-3)}))
 
 
@@ -832,6 +842,9 @@ def main():
                     help="only the FP32-vs-FP64 precision report: N,skewers,pixels (default 1536^3, 1e5 x 1024)")
     ap.add_argument("--variants", default=None,
                     help="fixed tile variants, e.g. xgen=5,line=5,zinv=4 (no autotuning)")
+    ap.add_argument("--xi-chunk", type=int, default=0,
+                    help="GPU-noise x pass into a blocked intermediate, this many k_z columns per chunk "
+                         "(0: in place, -1: one chunk)")
     ap.add_argument("--no-fit", action="store_true", help="skip the (a,b,c) fit leg")
     ap.add_argument("--no-host-noise", action="store_true", help="skip the host-noise (5-pass) GRF leg")
     ap.add_argument("--fit-steps", type=int, default=20, help="Adam steps of the fit leg")

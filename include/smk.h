@@ -84,13 +84,21 @@ typedef struct {
     int32_t n_pass_events;    /* first HBM pass and after each of the five (0: none)          */
     int32_t eta_comp;     /* SMK_ETA_*: which eta_ij or velocity the eta box holds (0 = zz)  */
     double vel_factor;    /* SMK_ETA_VX/VY/VZ: H0 * dD/dz(z = 0) (km/s/(Mpc/h) per unit z)    */
+    int32_t xi_chunk_kz;  /* GPU noise: > 0 runs the x pass into a blocked intermediate in the  */
+                          /* workspace (each mode drawn once, both fields in one launch, the   */
+                          /* rows of a tile ny x 32..64 bytes apart instead of ny x pitch x 4) */
+                          /* that the y pass reads as contiguous runs, xi_chunk_kz k_z columns */
+                          /* at a time (rounded up to 16); 0: the x pass writes the boxes in   */
+                          /* place.  The boxes are the same, bit for bit.                      */
 } SmkGrfParams;
 
 /* Row pitch (floats) of the padded box layout for a z extent nz. */
 int64_t smk_grf_pitch(int32_t nz);
 /* Floats of one padded output box array (all batch members). */
 int64_t smk_grf_box_floats(const SmkGrfParams* p);
-/* Workspace bytes smk_grf_boxes needs: 256 (the FP64 normalisation accumulator). */
+/* Workspace bytes smk_grf_boxes needs: 256 (the FP64 normalisation accumulator), plus, for a
+ * GPU-noise call with xi_chunk_kz > 0, the intermediate of one chunk: fields (2 with eta, else
+ * 1) x batch x nx x ny x min(roundup(xi_chunk_kz, 16), roundup(nz/2+1, 16)) complex floats. */
 size_t smk_grf_workspace_size(const SmkGrfParams* p);
 
 /*

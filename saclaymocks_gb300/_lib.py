@@ -43,7 +43,7 @@ class SmkGrfParams(C.Structure):
                 ("amp", C.c_double), ("pk_grid", C.c_void_p), ("noise_mode", C.c_int32),
                 ("noise", C.c_void_p), ("seed", C.c_uint64), ("want_eta", C.c_int32),
                 ("pass_events", C.c_void_p), ("n_pass_events", C.c_int32), ("eta_comp", C.c_int32),
-                ("vel_factor", C.c_double)]
+                ("vel_factor", C.c_double), ("xi_chunk_kz", C.c_int32)]
 
 
 class SmkSkewers(C.Structure):

@@ -130,9 +130,19 @@ int64_t smk_grf_box_floats(const SmkGrfParams* p) {
     return (int64_t)p->batch * p->nx * p->ny * smk_grf_pitch(p->nz);
 }
 
+// k_z columns per chunk of the x pass's blocked intermediate (0: in place).
+static int64_t xi_chunk_cols(const SmkGrfParams* p) {
+    if (!p || p->noise_mode != SMK_NOISE_PHILOX || p->xi_chunk_kz <= 0 || p->nz < 2) return 0;
+    const int64_t nzh16 = (p->nz / 2 + 1 + 15) / 16 * 16;
+    return std::min<int64_t>(((int64_t)p->xi_chunk_kz + 15) / 16 * 16, nzh16);
+}
+
 size_t smk_grf_workspace_size(const SmkGrfParams* p) {
-    (void)p;
-    return 256;  // [0] FP64 mode sum, [1] amplitude A
+    // [0] FP64 mode sum, [1] amplitude A; then the intermediate of one chunk
+    const int64_t cols = xi_chunk_cols(p);
+    if (!cols) return 256;
+    const int64_t nf = p->want_eta ? 2 : 1;
+    return 256 + (size_t)(nf * p->batch * (int64_t)p->nx * p->ny * cols) * sizeof(float2);
 }
 
 int smk_pk_normalisation(int32_t nx, int32_t ny, int32_t nz, double dcell, double k0, double* amp_dev,
@@ -284,20 +294,69 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         ga.seed = p->seed;
         ga.eta_comp = p->eta_comp;
         ga.vfac = (float)p->vel_factor;
-        // A tile writes all nx rows of its columns, so one wave of tiles touches rows spread over
-        // the whole of each output box.  Past ~64 GiB for the two boxes together (2 x 40 GB at
-        // 2560x2560x1536) that spread outruns the GPU's address-translation reach and the pass
-        // slows by 1.7x; writing delta and eta in two launches keeps each wave within one box.
-        const double pair_bytes = 2.0 * 4.0 * (double)p->batch * p->nx * p->ny * (double)pitch;
-        const int sm = g_xgen_split.load();
-        const bool split = p->want_eta && (sm < 0 ? pair_bytes > 64.0 * (1ull << 30) : sm == 1);
-        ga.fields = !p->want_eta ? XGEN_DELTA : (split ? XGEN_DELTA : XGEN_BOTH);
-        if ((rc = run_xgen(vx, ga, st))) return rc;
-        if (split) {
-            ga.fields = XGEN_ETA;
+        const int nf = p->want_eta ? 2 : 1;
+        const int wx = variant_table(PASS_XGEN)[vx].w, wy = variant_table(PASS_LINE)[vy].w;
+        const int kb = wx / nf;   // k_z columns per block of the intermediate
+        const int64_t xcols = xi_chunk_cols(p);
+        if (xcols > 0 && (!workspace || workspace_bytes < smk_grf_workspace_size(p)))
+            return fail(SMK_EWORKSPACE, "smk_grf_boxes: xi_chunk_kz needs %zu workspace bytes",
+                        smk_grf_workspace_size(p));
+        const bool staged = xcols > 0 && kb >= 2 && kb % 2 == 0 && wy % kb == 0 && xcols % wy == 0;
+        if (staged) {
+            // Chunks of xcols k_z columns: the x pass of both fields into the intermediate (each
+            // mode drawn once; the rows of a tile ny * kb * 8 bytes apart instead of ny * pitch *
+            // 4), then the y pass reading its tiles from the intermediate as contiguous runs.
+            float2* I0 = reinterpret_cast<float2*>(reinterpret_cast<char*>(workspace) + 256);
+            const int64_t nouter = (int64_t)p->batch * p->nx;
+            ga.I[0] = I0;
+            ga.I[1] = p->want_eta ? I0 + nouter * p->ny * xcols : nullptr;
+            ga.fields = p->want_eta ? XGEN_BOTH : XGEN_DELTA;
+            LineArgs yi = ya;
+            yi.nbuf = nf;
+            yi.src[0] = ga.I[0];
+            yi.src[1] = ga.I[1];
+            yi.src_kb = kb;
+            if (yi.tma == 2) yi.tma = 1;   // stores go to the boxes; the maps cover the intermediate
+            const int per = wy / kb;         // intermediate blocks per y tile
+            const uint64_t dims[5] = {(uint64_t)kb, (uint64_t)per, (uint64_t)p->ny, (uint64_t)nouter,
+                                      (uint64_t)(xcols / wy)};
+            const uint64_t strides[5] = {1, (uint64_t)(nouter * p->ny * kb), (uint64_t)kb, (uint64_t)p->ny * kb,
+                                         (uint64_t)(per * nouter * p->ny * kb)};
+            const uint32_t box[5] = {(uint32_t)kb, (uint32_t)per, (uint32_t)std::max(ya.box_rows, 1), 1, 1};
+            for (int f = 0; f < nf && yi.tma; ++f)
+                if (!encode_map_5d_8b(&yi.tmap[f], ga.I[f], dims, strides, box)) yi.tma = 0;
+            const bool one_chunk = xcols >= nzh;
+            for (int64_t c0 = 0; c0 < nzh; c0 += xcols) {
+                ga.cb0 = (int)(c0 / kb);
+                ga.ncb = (int)ceil_div(std::min<int64_t>(xcols, nzh - c0), kb);
+                if ((rc = run_xgi(vx, ga, st))) return rc;
+                if (one_chunk && (rc = mark(3))) return rc;
+                yi.col0 = (int)c0;
+                yi.ncol = (int)std::min<int64_t>(xcols, nzh - c0);
+                if ((rc = run_line(vy, yi, true, st))) return rc;
+            }
+            if ((!one_chunk && (rc = mark(3))) || (rc = mark(4))) return rc;
+        } else {
+            // A tile writes all nx rows of its columns, so one wave of tiles touches rows spread
+            // over the whole of each output box.  Past ~64 GiB for the two boxes together (2 x 40
+            // GB at 2560x2560x1536) that spread outruns the GPU's address-translation reach and
+            // the pass slows by 1.7x; writing delta and eta in two launches keeps each wave
+            // within one box.
+            const double pair_bytes = 2.0 * 4.0 * (double)p->batch * p->nx * p->ny * (double)pitch;
+            const int sm = g_xgen_split.load();
+            const bool split = p->want_eta && (sm < 0 ? pair_bytes > 64.0 * (1ull << 30) : sm == 1);
+            ga.fields = !p->want_eta ? XGEN_DELTA : (split ? XGEN_DELTA : XGEN_BOTH);
             if ((rc = run_xgen(vx, ga, st))) return rc;
+            if (split) {
+                ga.fields = XGEN_ETA;
+                if ((rc = run_xgen(vx, ga, st))) return rc;
+            }
+            if ((rc = mark(3))) return rc;
+            // 4. c2c along y, inverse, on delta (and eta)
+            ya.nbuf = nf;
+            if ((rc = run_line(vy, ya, true, st))) return rc;
+            if ((rc = mark(4))) return rc;
         }
-        if ((rc = mark(3))) return rc;
     } else {
         // 1. r2c along z of the caller's noise
         ZFwdArgs za;
@@ -333,12 +392,11 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         xa.vfac = (float)p->vel_factor;
         if ((rc = run_xpass(vx, xa, st))) return rc;
         if ((rc = mark(3))) return rc;
+        // 4. c2c along y, inverse, on delta (and eta)
+        ya.nbuf = p->want_eta ? 2 : 1;
+        if ((rc = run_line(vy, ya, true, st))) return rc;
+        if ((rc = mark(4))) return rc;
     }
-
-    // 4. c2c along y, inverse, on delta (and eta)
-    ya.nbuf = p->want_eta ? 2 : 1;
-    if ((rc = run_line(vy, ya, true, st))) return rc;
-    if ((rc = mark(4))) return rc;
 
     // 5. c2r along z, / N, statistics
     ZInvArgs ia;

@@ -136,6 +136,14 @@ struct LineArgs {
     int tma_extra_tx;
     long long tma_wait_limit;
     CUtensorMap tmap[2];
+    // Source of the tiles: in place (src[0] null) or the blocked intermediate of the x pass
+    // (xgi_kernel): column c of the launch (0 <= c < ncol) of line o, element e at
+    // src[buf] + (((c / src_kb) * n_outer + o) * n + e) * src_kb + c % src_kb.  With TMA, tmap is
+    // a 5D map (src_kb, W / src_kb, n, n_outer, column tiles) over the source.  Output columns
+    // start at col0 in every row.
+    const float2* src[2];
+    int src_kb;
+    int col0;
 };
 
 // Forward: natural -> digit-reversed order along the axis (kept in HBM); inverse: back.
@@ -167,14 +175,20 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
         const int64_t t = tile - buf * tpb;
         const int64_t o = t / ncolt;
         const int cb = (int)(t - o * ncolt);
-        float2* base = a.base[buf] + o * a.ostride + (int64_t)cb * W;
+        float2* base = a.base[buf] + o * a.ostride + a.col0 + (int64_t)cb * W;
         const int cols = min(W, a.ncol - cb * W);
+        const float2* src = a.src[buf];
         if (a.tma) {
             // n / box_rows tensor boxes of W columns (columns past ncol read as zeros)
             if (threadIdx.x == 0) {
                 if (a.tma == 2) bulk_wait_read_all();   // the previous tile's stores have read s
                 mbar_arrive_expect_tx(&bar, (unsigned)(n * W * sizeof(float2)) + (unsigned)a.tma_extra_tx);
-                for (int e0 = 0; e0 < n; e0 += a.box_rows) tma_load_3d(s + e0 * W, &a.tmap[buf], &bar, cb * W, e0, (int)o);
+                for (int e0 = 0; e0 < n; e0 += a.box_rows) {
+                    if (src)
+                        tma_load_5d(s + e0 * W, &a.tmap[buf], &bar, 0, 0, e0, (int)o, cb);
+                    else
+                        tma_load_3d(s + e0 * W, &a.tmap[buf], &bar, cb * W, e0, (int)o);
+                }
             }
             // bounded wait (~1 s at 2 GHz): on time-out the tile is poisoned with NaN, which the
             // z pass counts as non-finite cells (SMK_ENULLBOX from smk_grf_check), and the
@@ -188,18 +202,40 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
                 for (int i = threadIdx.x; i < n * W; i += T) s[i] = make_float2(__int_as_float(0x7fc00000), 0.f);
                 __syncthreads();
             }
+        } else if (src) {
+            // W / src_kb contiguous runs of n * src_kb complex values, 16 bytes per copy
+            const int kb = a.src_kb, G = W / 2;
+            for (int idx = threadIdx.x; idx < n * G; idx += T) {
+                const int e = idx / G, w = 2 * (idx % G);
+                const int c = cb * W + w;
+                cp_async<16>(s + e * W + w, src + (((int64_t)(c / kb) * a.n_outer + o) * n + e) * kb + c % kb, 16);
+            }
+            cp_async_wait_all();
+            __syncthreads();
         } else {
             load_cols_async<W, T>(s, base, n, a.estride, cols);
             cp_async_wait_all();
             __syncthreads();
         }
-        if (a.prefetch && tile + gridDim.x < ntiles) {
+        if (src) {
+            // the next tile's source runs into L2
+            if (a.prefetch && threadIdx.x == 0 && tile + gridDim.x < ntiles) {
+                const int64_t tn = tile + gridDim.x;
+                const int bn = (int)(tn / tpb);
+                const int64_t un = tn - bn * tpb;
+                const int64_t on = un / ncolt;
+                const int cbn = (int)(un - on * ncolt);
+                for (int q = 0; q < W / a.src_kb; ++q)
+                    prefetch_l2_bulk(a.src[bn] + (((int64_t)cbn * (W / a.src_kb) + q) * a.n_outer + on) * n * a.src_kb,
+                                     (uint32_t)(n * a.src_kb * sizeof(float2)));
+            }
+        } else if (a.prefetch && tile + gridDim.x < ntiles) {
             // the next tile of this block: one line per row segment of its W columns
             const int64_t tn = tile + gridDim.x;
             const int bn = (int)(tn / tpb);
             const int64_t un = tn - bn * tpb;
             const int64_t on = un / ncolt;
-            const float2* nb = a.base[bn] + on * a.ostride + (un - on * ncolt) * W;
+            const float2* nb = a.base[bn] + on * a.ostride + a.col0 + (un - on * ncolt) * W;
             for (int e = threadIdx.x; e < n; e += T) prefetch_l2(nb + (int64_t)e * a.estride);
         }
         if (INV && a.tma == 2) {
@@ -384,6 +420,12 @@ struct XGenArgs {
     float vfac;
     int fields;            // XGEN_BOTH: W/2 delta + W/2 eta lines per tile; XGEN_DELTA / XGEN_ETA:
                            // W lines of one field (two launches; see xgen_split)
+    // Intermediate output (xgi_kernel): field f of k_z column block kb (kb - cb0 within this
+    // chunk; blocks of KB = W / fields columns) at I[f] + (((kb - cb0) * batch * nx + b * nx + x)
+    // * ny + yslot) * KB + kz % KB: the x rows of a tile lie ny * KB * 8 bytes apart, and the y
+    // line of one column block is one contiguous run for the y pass
+    float2* I[2];
+    int cb0, ncb;          // column blocks of this chunk
 };
 
 // GPU-noise mode arithmetic (no bit-level reference: the FP64 oracle restates the drawn modes
@@ -574,6 +616,86 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
                 }
             }
         }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ GPU-noise x pass into the
+// blocked intermediate
+// Tiles (box b, column block kb, y slot), y slot fastest: a tile draws the modes of its WC k_z
+// columns for every x slot once, forms delta_k (and eta_k with XGEN_BOTH), takes the x inverse
+// of its W lines and stores the last stage from registers into I (see XGenArgs).  Tiles that
+// run together hold neighbouring y slots, so their 8 * KB-byte pieces of a row of I are
+// assembled into whole lines in L2.
+// smem: s[n*W] | tw[n] | kx[n] | ix[n] | kzt[nzh]
+template <class C>
+__global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
+    constexpr int W = C::W, T = C::T;
+    extern __shared__ float2 smem[];
+    const bool both = a.fields == XGEN_BOTH;
+    const int WC = both ? W / 2 : W;          // k_z columns per tile (= KB)
+    const int NP = WC / 2;
+    const int n = a.pl.n;  // == nx
+    float2* s = smem;
+    float2* tw = s + n * W;
+    float* kx = reinterpret_cast<float*>(tw + n);
+    int* ix = reinterpret_cast<int*>(kx + n);
+    float* kzt = reinterpret_cast<float*>(ix + n);
+    fill_stage_twiddles(tw, a.pl);
+    for (int e = threadIdx.x; e < n; e += T) {
+        const int f = freq_of_slot(a.pl, e);
+        ix[e] = f;
+        kx[e] = kaxis(f, n, a.kfac, true);
+    }
+    for (int z = threadIdx.x; z < a.nzh; z += T) kzt[z] = kaxis(z, a.nz, a.kfac, false);
+    __syncthreads();
+    const float scale_c = pk_scale_c(a);
+    const int64_t ntiles = (int64_t)a.batch * a.ncb * a.ny;
+    const int64_t nouter = (int64_t)a.batch * a.nx;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int yslot = (int)(tile % a.ny);
+        const int64_t r = tile / a.ny;
+        const int kbl = (int)(r % a.ncb);      // block within the chunk
+        const int64_t b = r / a.ncb;
+        const int cb = a.cb0 + kbl;
+        const int iy = freq_of_slot(a.ply, yslot);
+        const int iym = iy == 0 ? 0 : a.ny - iy;
+        const float ky = kaxis(iy, a.ny, a.kfac, true);
+        const uint64_t seed = a.seed + (uint64_t)b;
+        auto draw = [&](auto chk) {
+#pragma unroll 2
+            for (int idx = threadIdx.x; idx < n * NP; idx += T) {
+                const int e = idx / NP, pr = idx % NP;
+                const int c0 = 2 * pr, kz0 = cb * WC + c0;
+                const float kxv = kx[e];
+                const ModePair mp = draw_pair<decltype(chk)::value>(a, seed, ix[e], iy, iym, kxv, ky, kz0, kzt, scale_c);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (both) {
+                        s[e * W + c0 + h] = mp.d[h];
+                        s[e * W + WC + c0 + h] = eta_from_inv_k2(a.eta_comp, mp.d[h], kxv, ky, mp.kz[h], mp.ikk[h], a.vfac);
+                    } else {
+                        s[e * W + c0 + h] = a.fields == XGEN_DELTA
+                            ? mp.d[h] : eta_from_inv_k2(a.eta_comp, mp.d[h], kxv, ky, mp.kz[h], mp.ikk[h], a.vfac);
+                    }
+                }
+            }
+        };
+        if (tile_needs_check(a, cb * WC, WC))
+            draw(std::true_type{});
+        else
+            draw(std::false_type{});
+        __syncthreads();
+        const int cols = min(WC, a.nzh - cb * WC);
+        const int64_t row0 = ((int64_t)kbl * nouter + b * a.nx) * a.ny + yslot;
+        float2* d0 = a.I[0] + row0 * WC;
+        float2* d1 = both ? a.I[1] + row0 * WC : nullptr;
+        const int64_t es = (int64_t)a.ny * WC;
+        ifft_tile_out<W, W, T, C::RMAX>(s, tw, a.pl, [&](int e, int w, float2 v) {
+            const int f = both && w >= WC;
+            const int c = w - f * WC;
+            if (c < cols) (f ? d1 : d0)[e * es + c] = v;
+        });
         __syncthreads();
     }
 }
@@ -925,6 +1047,18 @@ static int launch_xpass(const XArgs& a, cudaStream_t st) {
 }
 
 template <class C>
+static int launch_xgi(const XGenArgs& a, cudaStream_t st) {
+    if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xgi_kernel");
+    const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 +
+                        (size_t)a.nzh * 4 + 16;
+    const int64_t ntiles = (int64_t)a.batch * a.ncb * a.ny;
+    int grid = 0, rc;
+    if ((rc = persistent_grid(xgi_kernel<C>, C::T, smem, ntiles, &grid))) return rc;
+    xgi_kernel<C><<<grid, C::T, smem, st>>>(a);
+    return check_launch("xgi_kernel");
+}
+
+template <class C>
 static int launch_xgen(const XGenArgs& a, cudaStream_t st) {
     if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xgen_kernel");
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 +
@@ -974,5 +1108,6 @@ int run_zinv(int v, const ZInvArgs& a, int64_t rows_per_box, cudaStream_t st);
 int run_line(int v, const LineArgs& a, bool inv, cudaStream_t st);
 int run_xpass(int v, const XArgs& a, cudaStream_t st);
 int run_xgen(int v, const XGenArgs& a, cudaStream_t st);
+int run_xgi(int v, const XGenArgs& a, cudaStream_t st);
 
 }  // namespace smk

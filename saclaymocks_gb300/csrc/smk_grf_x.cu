@@ -21,4 +21,13 @@ int run_xgen(int v, const XGenArgs& a, cudaStream_t st) {
     return fail(SMK_EINVAL, "xgen: no tile variant %d", v);
 }
 
+int run_xgi(int v, const XGenArgs& a, cudaStream_t st) {
+    int i = 0;
+#define X(W, T, N, R, B) \
+    if (v == i++) return launch_xgi<TileCfg<W, T, R, B>>(a, st);
+    SMK_XGEN_VARIANTS(X)
+#undef X
+    return fail(SMK_EINVAL, "xgi: no tile variant %d", v);
+}
+
 }  // namespace smk

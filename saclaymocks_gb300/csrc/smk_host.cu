@@ -63,6 +63,28 @@ bool encode_map_3d_8b(CUtensorMap* m, const void* base, uint64_t d0, uint64_t d1
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// 5D map of 8-byte elements: dims d[0..4] (d[0] innermost, contiguous), element strides
+// st[1..4] (multiples of 2 elements), box b[0..4]; out-of-range elements read as zero.
+bool encode_map_5d_8b(CUtensorMap* m, const void* base, const uint64_t* d, const uint64_t* st, const uint32_t* b) {
+    const EncodeTiledFn fn = encode_tiled_fn();
+    if (!fn || ((uintptr_t)base & 15) || ((b[0] * 8) & 15)) return false;
+    cuuint64_t dims[5], strides[4];
+    cuuint32_t box[5], es[5];
+    for (int i = 0; i < 5; ++i) {
+        if (b[i] < 1 || b[i] > 256 || d[i] < 1) return false;
+        dims[i] = d[i];
+        box[i] = b[i];
+        es[i] = 1;
+        if (i > 0) {
+            if ((st[i] * 8) & 15) return false;
+            strides[i - 1] = st[i] * 8;
+        }
+    }
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 5, const_cast<void*>(base), dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 }  // namespace smk
 
 extern "C" {

@@ -29,8 +29,9 @@ class _PendingFlux:
 
 class MockChunk:
     def __init__(self, nx, ny, nz, dcell=2.19, *, seed=1, k0=0.02, want_eta=True,
-                 cfg: spectra.SpectraConfig | None = None, dpix=0.2, device="cuda"):
+                 cfg: spectra.SpectraConfig | None = None, dpix=0.2, device="cuda", xi_chunk_kz: int = 0):
         self.nx, self.ny, self.nz, self.dcell = nx, ny, nz, dcell
+        self.xi_chunk_kz = xi_chunk_kz     # grf.make_boxes: blocked x-pass intermediate (0: in place)
         self.seed, self.k0, self.dpix = seed, k0, dpix
         self.cfg = cfg or spectra.SpectraConfig()
         self.device = torch.device(device)
@@ -94,7 +95,7 @@ class MockChunk:
         slot = self._step & 1
         out = grf.make_boxes(self.nx, self.ny, self.nz, self.dcell, seed=self.seed, k0=self.k0,
                              amp=self.amp, want_eta=self.boxes[1] is not None, out=self.boxes,
-                             workspace=self.ws, pass_events=pass_events)
+                             workspace=self.ws, pass_events=pass_events, xi_chunk_kz=self.xi_chunk_kz)
         r = self._prepare(start, direction, npix, slot)
         if self._d2h_done[slot] is not None:
             self.stream.wait_event(self._d2h_done[slot])   # the flux buffer's last copy is done

@@ -80,8 +80,9 @@ def _store(choices: dict):
 
 
 def tune_grf(nx: int, ny: int, nz: int, dcell: float = 2.19, gpu_noise: bool = True, reps: int = 2,
-             out=None, workspace=None, use_cache: bool = True) -> dict:
-    """Pick the fastest tile variant of every pass of smk_grf_boxes for this shape.
+             out=None, workspace=None, use_cache: bool = True, xi_chunk_kz: int = 0) -> dict:
+    """Pick the fastest tile variant of every pass of smk_grf_boxes for this shape (with the x
+    pass in place or, xi_chunk_kz > 0, into the blocked intermediate).
     Returns {"choices": {pass name: (variant, W, T)}, "ms": {pass name: {variant: ms}}}."""
     if gpu_noise:
         passes = [(_lib.SMK_PASS_XGEN, nx, 3), (_lib.SMK_PASS_LINE, ny, 4), (_lib.SMK_PASS_ZINV, nz, 5)]
@@ -113,6 +114,7 @@ def tune_grf(nx: int, ny: int, nz: int, dcell: float = 2.19, gpu_noise: bool = T
         acc = {p: [] for p, _, _ in passes}
         for k in range(1 + reps):
             grf.make_boxes(nx, ny, nz, dcell, seed=1, noise=noise, amp=amp, out=out, workspace=workspace,
+                           xi_chunk_kz=xi_chunk_kz,
                            pass_events=evs)
             torch.cuda.synchronize()
             if k == 0:

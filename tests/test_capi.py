@@ -142,6 +142,15 @@ def test_grf_workspace_size_and_alignment_need_no_gpu(lib):
     p.noise_mode, p.pk_mode, p.k0, p.amp, p.want_eta = _lib.SMK_NOISE_PHILOX, _lib.SMK_PK_ANALYTIC, 0.02, 1.0, 1
     lib.smk_grf_workspace_size.restype = C.c_size_t
     assert lib.smk_grf_workspace_size(C.byref(p)) == 256
+    # blocked x-pass intermediate: one chunk of roundup(xi_chunk_kz, 16) k_z columns (at most
+    # roundup(nz/2+1, 16)) for each field
+    p.xi_chunk_kz = 20
+    assert lib.smk_grf_workspace_size(C.byref(p)) == 256 + 2 * 2 * 10 * 6 * 32 * 8
+    p.xi_chunk_kz = 5000
+    assert lib.smk_grf_workspace_size(C.byref(p)) == 256 + 2 * 2 * 10 * 6 * 32 * 8
+    p.want_eta = 0
+    assert lib.smk_grf_workspace_size(C.byref(p)) == 256 + 2 * 10 * 6 * 32 * 8
+    p.want_eta, p.xi_chunk_kz = 1, 0
     base = 1 << 20   # never dereferenced: the call returns before touching memory
     for d, e, w in ((base + 8, base + 4096, None), (base, base + 4100, None), (base, base + 4096, base + 4)):
         assert lib.smk_grf_boxes(C.byref(p), d, e, None, w, 0, None) == _lib.SMK_EINVAL

@@ -60,6 +60,47 @@ def test_xgen_one_launch_equals_split_launches(G, shape):
     np.testing.assert_array_equal(got.sigma(), ref.sigma())
 
 
+@pytest.mark.parametrize("shape", [(40, 24, 36), (45, 18, 50), (64, 20, 12), (30, 6, 160), (24, 2560, 40),
+                                   (6, 1536, 96)])
+@pytest.mark.parametrize("chunk", [16, 4096])
+def test_blocked_intermediate_x_pass_equals_in_place(G, shape, chunk):
+    """The x pass into the blocked intermediate (each mode drawn once, the y pass reading
+    contiguous runs), in one chunk or several, gives the same boxes, bit for bit, as the x pass
+    in place: both fields, a batch, delta alone, a velocity component, odd nx, k_z extents that
+    end inside a block, y lines loaded by TMA (2560, 1536) and by cp.async."""
+    nx, ny, nz = shape
+    for kw in (dict(batch=2), dict(want_eta=False), dict(eta_comp="vz", vel_factor=90.0)):
+        ref = G.make_boxes(nx, ny, nz, 2.19, seed=37, **kw)
+        got = G.make_boxes(nx, ny, nz, 2.19, seed=37, xi_chunk_kz=chunk, **kw)
+        torch.cuda.synchronize()
+        assert torch.equal(got.delta, ref.delta), kw
+        if ref.eta is not None:
+            assert torch.equal(got.eta, ref.eta), kw
+        np.testing.assert_array_equal(got.sigma(), ref.sigma())
+
+
+def test_blocked_intermediate_every_tile_variant_is_exact(G):
+    """Every x-pass tile variant run into the intermediate matches the FP64 oracle."""
+    import ctypes as C
+    from saclaymocks_gb300 import _lib, tune
+    lib = _lib.load()
+    pid = _lib.SMK_PASS_XGEN
+    for v, w, t in tune.variants(pid, 2):
+        nm = C.c_int32()
+        lib.smk_tune_info(pid, v, None, None, C.byref(nm))
+        nx, ny, nz = CLASS_LEN[nm.value], 8, 72
+        _lib.check(lib.smk_tune_set(pid, nx, v))
+        try:
+            out = G.make_boxes(nx, ny, nz, 2.19, seed=19, xi_chunk_kz=32)
+            torch.cuda.synchronize()
+        finally:
+            lib.smk_tune_set(pid, nx, -1)
+        nk = ophilox.kspace_noise(nx, ny, nz, 19)
+        o64 = ograf.grf_from_modes(nk, nz, 2.19, 0.02, eta=("zz",), precision="f64")
+        _check(out.delta[0].cpu().numpy(), o64["delta"], f"xgi variant {v} (W={w}, T={t})")
+        _check(out.eta[0].cpu().numpy(), o64["eta_zz"], f"xgi variant {v} eta")
+
+
 @pytest.mark.parametrize("shape", [(24, 2560, 40), (6, 1536, 96), (10, 600, 72), (8, 45, 24)])
 def test_y_pass_tma_loads_equal_cp_async(G, shape):
     """The y pass loading its tiles with TMA tensor copies gives the same boxes, bit for bit, as
