@@ -11,8 +11,16 @@ files, velocity factor H0 * dD/dz(z=0) from the growth-rate table of -dgrowthfil
 $SACLAYMOCKS_BASE/etc/dgrowth.fits).  Without a P-grid file the analytic spectrum
 A k/(1+(k/k0)^2)^2 with E[var delta] = 1 is used (no lognormal boxes).  -ncpu is accepted and
 ignored.  Extra flags: --noise numpy|gpu (numpy, the default: the reference's MT19937
-plane-order draws, bit-identical input; gpu: Fourier modes drawn on the GPU), -k0, --eta-only-zz (write only the
-eta_zz box the trilinear skewer read uses), --no-write.
+plane-order draws, bit-identical input; gpu: Fourier modes drawn on the GPU), -k0,
+--eta-only-zz (write only the eta_zz box the trilinear skewer read uses), --no-write,
+--write-boxk True|False.
+
+Checkpoint (bin/make_boxes.py:206-245, 241-352): every run writes seed_boxk.npy, and with
+--write-boxk True also boxk.npy (the unnormalised r2c of the noise, complex64 [NX][NY][NZ/2+1],
+computed on the host; the default skips it because the GPU redraws the modes from the seed in
+less time than reading them back takes).  A run in an outDir that holds seed_boxk.npy takes
+that seed; one that holds only boxk.npy (e.g. from the reference, P0-scaled or not) recovers the
+noise from it; either way a box family whose files all exist is skipped.
 """
 from __future__ import annotations
 
@@ -51,6 +59,7 @@ def parser():
     p.add_argument("--noise", choices=["numpy", "gpu"], default="numpy")
     p.add_argument("--eta-only-zz", action="store_true")
     p.add_argument("--no-write", action="store_true")
+    p.add_argument("--write-boxk", default="False")
     return p
 
 
@@ -85,6 +94,12 @@ def write_planes(prefix, box, dcell, sigma, seed, nhdu=None):
         fits.write_image(f"{prefix}-{i}.fits", np.ascontiguousarray(part), hdr)
 
 
+def family_done(outdir, prefix, nfiles):
+    """True when every file {prefix}-{i}.fits, i < nfiles, exists (the file count the reference
+    checks before it skips a box family on a resumed run, bin/make_boxes.py:241-352)."""
+    return all(os.path.exists(os.path.join(outdir, f"{prefix}-{i}.fits")) for i in range(nfiles))
+
+
 def main(argv=None):
     from saclaymocks_gb300 import fits, grf
     args = parser().parse_args(argv)
@@ -94,14 +109,47 @@ def main(argv=None):
     rsd = str2bool(args.rsd)
     seed = args.seed if args.seed is not None else int(np.random.randint(2 ** 31 - 1))
     t0 = time.time()
+    # checkpoint of a previous run in outDir (bin/make_boxes.py:206-245): the seed of its noise
+    # (seed_boxk.npy) or, without it, the Fourier transform of its noise (boxk.npy)
+    boxk_file = os.path.join(args.outDir, "boxk.npy")
+    seed_file = os.path.join(args.outDir, "seed_boxk.npy")
+    resumed = os.path.isfile(boxk_file) or os.path.isfile(seed_file)
+    noise_box = None
+    if os.path.isfile(seed_file):
+        seed = int(np.load(seed_file))
+        print(f"{seed_file} found: resuming with seed {seed}")
+    elif os.path.isfile(boxk_file):
+        if args.noise != "numpy":
+            raise SystemExit("make_boxes: resuming from boxk.npy needs --noise numpy")
+        boxk = np.load(boxk_file).astype(np.complex128)
+        if boxk.shape != (NX, NY, NZ // 2 + 1):
+            raise SystemExit(f"make_boxes: {boxk_file} has shape {boxk.shape}, not {(NX, NY, NZ // 2 + 1)}")
+        if boxk.std() > 70 * NX:
+            # saved after the P0 multiply (:284-287): undo it with the P-grid file
+            fn = pgrid_file(args.PkDir, NX, NY, NZ) if args.PkDir else None
+            if not fn or not os.path.exists(fn):
+                raise SystemExit("make_boxes: boxk.npy holds the P0-scaled modes; the P-grid file of -PkDir "
+                                 "is needed to undo the scaling")
+            p0 = np.asarray(fits.read(fn, "P0"), np.float64)
+            boxk = np.divide(boxk, p0, out=np.zeros_like(boxk), where=p0 != 0)
+        noise_box = np.fft.irfftn(boxk, s=(NX, NY, NZ)).astype(np.float32)
+        print(f"{boxk_file} found: noise recovered from the saved modes")
     noise = None
     if args.noise == "numpy":
-        rs = np.random.RandomState(seed)        # the plane order of bin/make_boxes.py:46-48
-        box = np.zeros((NX, NY, NZ), dtype=np.float32)
-        for iz in range(NZ):
-            box[:, :, iz] = np.float32(rs.normal(size=[NX, NY]))
-        noise = torch.from_numpy(box).cuda()
-        del box
+        if noise_box is None:
+            rs = np.random.RandomState(seed)        # the plane order of bin/make_boxes.py:46-48
+            noise_box = np.zeros((NX, NY, NZ), dtype=np.float32)
+            for iz in range(NZ):
+                noise_box[:, :, iz] = np.float32(rs.normal(size=[NX, NY]))
+        noise = torch.from_numpy(noise_box).cuda()
+    if not args.no_write:
+        os.makedirs(args.outDir, exist_ok=True)
+        np.save(seed_file, np.int64(seed))
+        if str2bool(args.write_boxk) and not os.path.isfile(boxk_file):
+            if noise_box is None:
+                raise SystemExit("make_boxes: --write-boxk True needs --noise numpy (the real-space noise)")
+            np.save(boxk_file, np.fft.rfftn(noise_box.astype(np.float64)).astype(np.complex64))
+    del noise_box
     grids = {}
     if args.PkDir:
         fn = pgrid_file(args.PkDir, NX, NY, NZ)
@@ -129,9 +177,15 @@ def main(argv=None):
         if write:
             write_planes(os.path.join(outdir, prefix), field[0], args.pixel, field[1], seed, nhdu)
 
+    def skip(prefix, nfiles):
+        if resumed and write and family_done(outdir, prefix, nfiles):
+            print(f"{os.path.join(outdir, prefix)} files already exist ! Skiping this step.")
+            return True
+        return False
+
     # lognormal boxes: raw modes x Pln grids (bin/make_boxes.py:241-275)
     for i in (1, 2, 3):
-        if f"Pln{i}" in grids:
+        if f"Pln{i}" in grids and not skip(f"boxln_{i}", args.nHDU):
             o = grf.make_boxes(NX, NY, NZ, args.pixel, pk_grid=grids[f"Pln{i}"], want_eta=False, **common)
             o.check()
             emit(f"boxln_{i}", (o.delta[0].cpu().numpy(), o.sigma()[0]), args.nHDU)
@@ -141,16 +195,22 @@ def main(argv=None):
         comps = ["zz"] if args.eta_only_zz else ["xx", "yy", "zz", "xy", "xz", "yz", "vx", "vy", "vz"]
     pk = grids.get("P0")
     out = None
+    names = {c: (c if c[0] == "v" else f"eta_{c}") for c in comps}
+    box_done = skip("box", NX)
+    comps = [c for c in comps if not skip(names[c], args.nHDU if c[0] == "v" else NX)]
+    if box_done and not comps:
+        print("every box family already exists")
+        return None
     for j, c in enumerate(comps or [None]):
         o = grf.make_boxes(NX, NY, NZ, args.pixel, pk_grid=pk, want_eta=c is not None,
                            eta_comp=c or "zz", vel_factor=vfac if c and c[0] == "v" else None, **common)
         o.check()
         if j == 0:
             out = o
-            emit("box", (o.delta[0].cpu().numpy(), o.sigma()[0]))
+            if not box_done:
+                emit("box", (o.delta[0].cpu().numpy(), o.sigma()[0]))
         if c is not None:
-            name = c if c[0] == "v" else f"eta_{c}"
-            emit(name, (o.eta[0].cpu().numpy(), o.sigma(1)[0]), args.nHDU if c[0] == "v" else None)
+            emit(names[c], (o.eta[0].cpu().numpy(), o.sigma(1)[0]), args.nHDU if c[0] == "v" else None)
     torch.cuda.synchronize()
     print(f"boxes {NX}x{NY}x{NZ}: {1 + len(comps) + sum(f'Pln{i}' in grids for i in (1, 2, 3))} fields "
           f"in {time.time() - t0:.2f} s, sigma = {out.sigma()[0]:.6f}" + (f", written to {outdir}" if write else ""))

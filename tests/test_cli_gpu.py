@@ -62,6 +62,34 @@ def test_make_boxes_files_match_reference_golden(ok, tmp_path, golden):
     assert h["SIGMA"] == pytest.approx(float(f["sigma"]), rel=1e-5) and h["SEED"] == 0
 
 
+def test_make_boxes_checkpoint_and_resume(ok, tmp_path):
+    """seed_boxk.npy / boxk.npy checkpoint: a rerun in the same directory takes the saved seed
+    (not -seed) and skips the families whose files all exist, regenerating a removed family
+    bit for bit; a directory holding only boxk.npy gives the same boxes from the saved modes."""
+    from saclaymocks_gb300 import fits
+    from saclaymocks_gb300.bin import make_boxes
+    out = tmp_path / "out"
+    args = ["-NX", "12", "-NY", "10", "-NZ", "16", "-seed", "5", "-outDir", str(out), "-rsd", "True",
+            "--eta-only-zz", "--write-boxk", "True"]
+    make_boxes.main(args)
+    box = np.concatenate([fits.read(str(out / f"box-{i}.fits")) for i in range(12)])
+    eta = np.concatenate([fits.read(str(out / f"eta_zz-{i}.fits")) for i in range(12)])
+    assert int(np.load(out / "seed_boxk.npy")) == 5
+    boxk = np.load(out / "boxk.npy")
+    assert boxk.shape == (12, 10, 9) and boxk.dtype == np.complex64
+    os.remove(out / "eta_zz-3.fits")
+    make_boxes.main(args[:7] + ["99"] + args[8:])               # another -seed: the saved one wins
+    eta2 = np.concatenate([fits.read(str(out / f"eta_zz-{i}.fits")) for i in range(12)])
+    np.testing.assert_array_equal(eta2, eta)
+    # only boxk.npy: noise = irfftn(boxk), the same boxes to float32 rounding of the round trip
+    other = tmp_path / "other"
+    other.mkdir()
+    np.save(other / "boxk.npy", boxk)
+    make_boxes.main(["-NX", "12", "-NY", "10", "-NZ", "16", "-outDir", str(other), "-rsd", "True", "--eta-only-zz"])
+    box3 = np.concatenate([fits.read(str(other / f"box-{i}.fits")) for i in range(12)])
+    assert np.abs(box3 - box).max() < 1e-5 * box.std()
+
+
 ETA6 = ("xx", "yy", "zz", "xy", "xz", "yz")
 
 
