@@ -216,8 +216,14 @@ def main(argv=None):
         buf = np.concatenate(draws) if draws else np.zeros(1)
         noise = (torch.from_numpy(buf.astype(np.float32)).cuda(), torch.from_numpy(offs).cuda())
     r = spectra.SkewerRunner(table, cfg, pixels=pix_in)
-    F, dtot, _, _ = r.run(noise=noise, want_fields=True)
-    F, dtot = spectra.split(F, table), spectra.split(dtot, table)
+    F = spectra.split(r.run(noise=noise), table)
+    dsm = None
+    if store_g:
+        # delta_s itself: the same launch on delta_l = 0 (same noise, the same small-scale field),
+        # since (delta_l + delta_s) - delta_l loses delta_s where delta_l = -1e6 beyond the forest
+        r.pixels = (torch.zeros_like(pix_in[0]), pix_in[1], pix_in[2])
+        _, ds_dev, _, _ = r.run(noise=noise, want_fields=True)
+        dsm = spectra.split(ds_dev, table)
 
     g24 = float(fgrowth(2.4))
     names = ["RA", "DEC", "Z_noRSD", "Z", "HDU", "THING_ID", "PLATE", "MJD", "FIBERID", "PMF"]
@@ -256,7 +262,7 @@ def main(argv=None):
             w.image(np.array([spectra_list[k]["eta"] if rsd else np.zeros(npixeltot) for k in good], np.float32),
                     extname="ETA_PAR")
             w.image(last["z"].astype(np.float32), extname="Z")
-            w.image(np.array([dtot[k] - spectra_list[k]["delta_l"] for k in good], np.float32), extname="DELTA_S")
+            w.image(np.array([dsm[k] for k in good], np.float32), extname="DELTA_S")
         w.close()
         paths.append(path)
         written += len(good)
