@@ -385,6 +385,18 @@ def run_ours(args, cfg):
         batch_res = batching_leg()
     if rank != 0:
         return
+    pitch = boxes[0].shape[-1]
+    h2d_bytes, d2h_bytes = chunk.h2d_bytes(), chunk.d2h_bytes()
+    prec_res = None
+    if not args.no_precision and not args.small:
+        # the precision configuration (1536^3, FP32 path vs FP64 restatement) once the
+        # production buffers are released
+        sec_pre = skewer_sector_bytes(table, nx, ny, nz, pitch, cfg["dcell"])
+        del chunk, boxes, ws, out
+        torch.cuda.empty_cache()
+        prec_res = precision_leg()
+    else:
+        sec_pre = None
     peak, peak_kind = hbm_peak()
     nzh = nz // 2 + 1
     modes = nx * ny * nzh
@@ -418,7 +430,7 @@ def run_ours(args, cfg):
              "basis": "ncu smsp__inst_executed.sum per mode and field, scaled; peak SMs x 4 x SM clock"}
     # skewer stage: 4 B of flux per pixel + the distinct 32-byte sectors of delta and eta the
     # trilinear corners touch (Philox small scales: no noise bytes)
-    sec = skewer_sector_bytes(table, nx, ny, nz, boxes[0].shape[-1], cfg["dcell"])
+    sec = sec_pre if sec_pre is not None else skewer_sector_bytes(table, nx, ny, nz, pitch, cfg["dcell"])
     sk_bytes = 4.0 * pixels + 2.0 * sec
     sk_roof = {"kernel": "skewer_kernel", "algorithmic_bytes": sk_bytes / 1e9,
                "achieved": sk_bytes / (sk_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
@@ -444,13 +456,14 @@ def run_ours(args, cfg):
                         "issue": issue, "skewer": sk_roof},
            "host_noise": host_res,
            "e2e": {"value": aggregate_value(cells, world, e2e_s), "unit": "cells/s",
-                   "h2d_bytes_per_step": chunk.h2d_bytes(), "d2h_bytes_per_step": chunk.d2h_bytes(),
+                   "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
                    "ms_per_step": e2e_s * 1e3},
            "gpu_launches": args.steps * (grf.grf_launches(nx, ny, nz) + 1),
            "tile_variants": tuned,
            "clocks": clk_sum,
            "fit": fit_res,
-           "batching": batch_res}
+           "batching": batch_res,
+           "precision": prec_res}
     if not args.no_cpu:
         workers = os.cpu_count() or 1
         r = cpu_baseline(cfg, 64 if not args.small else 8, workers)
@@ -862,6 +875,7 @@ def main():
     ap.add_argument("--xi-chunk", type=int, default=0,
                     help="GPU-noise x pass into a blocked intermediate, this many k_z columns per chunk "
                          "(0: in place, -1: one chunk)")
+    ap.add_argument("--no-precision", action="store_true", help="skip the 1536^3 FP32-vs-FP64 precision leg")
     ap.add_argument("--no-fit", action="store_true", help="skip the (a,b,c) fit leg")
     ap.add_argument("--no-host-noise", action="store_true", help="skip the host-noise (5-pass) GRF leg")
     ap.add_argument("--fit-steps", type=int, default=20, help="Adam steps of the fit leg")
