@@ -854,6 +854,39 @@ def run_grf_only(args, shape):
                       "grf_cells_per_s": nx * ny * nz / (pass_ms.sum() * 1e-3)}))
 
 
+def run_skewers_only(args, spec):
+    """The skewer stage alone (the ncu profiling case): GPU-noise boxes of NX,NY,NZ, NSK skewers
+    of the production chunk's kind (400-1200 pixels within 10 deg of +z, Philox small scales on
+    2048 points, a(z) power law), W + K launches timed with CUDA events."""
+    import numpy as np
+    import torch
+
+    from saclaymocks_gb300 import _lib, grf, spectra
+    nx, ny, nz, nsk = spec
+    out = grf.make_boxes(nx, ny, nz, seed=1)
+    table = spectra.skewers_cone(nsk, np.array([nx, ny, nz]) * 2.19, seed=1, npix_range=(400, 1200))
+    scfg = spectra.SpectraConfig(ss_mode=_lib.SMK_SS_PHILOX, ss_nz=2048, pmiss=spectra.pmiss_gauss(0.05, 2.0),
+                                 seed=1, abc_mode=_lib.SMK_ABC_POWERLAW, a=0.1, a_zref1=3.2, a_power=4.5,
+                                 b=1.58, c=0.6, z_lo=1.8, z_hi=3.6)
+    r = spectra.SkewerRunner(table, scfg)
+    flux = torch.empty(table.total_pixels, dtype=torch.float32, device="cuda")
+
+    def step():
+        r.run(out.delta_pad[0], out.eta_pad[0], nx=nx, ny=ny, nz=nz, pitch=out.pitch, dcell=2.19, flux=flux)
+    for _ in range(args.warmup):
+        step()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    print(json.dumps({"skewer_shape": list(spec), "pixels": table.total_pixels, "ms": ms,
+                      "pixels_per_s": table.total_pixels / (ms * 1e-3)}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -872,13 +905,15 @@ def main():
                     help="only the FP32-vs-FP64 precision report: N,skewers,pixels (default 1536^3, 1e5 x 1024)")
     ap.add_argument("--variants", default=None,
                     help="fixed tile variants, e.g. xgen=5,line=5,zinv=4 (no autotuning)")
-    ap.add_argument("--xi-chunk", type=int, default=0,
+    ap.add_argument("--xi-chunk", type=int, default=-1,
                     help="GPU-noise x pass into a blocked intermediate, this many k_z columns per chunk "
                          "(0: in place, -1: one chunk)")
     ap.add_argument("--no-precision", action="store_true", help="skip the 1536^3 FP32-vs-FP64 precision leg")
     ap.add_argument("--no-fit", action="store_true", help="skip the (a,b,c) fit leg")
     ap.add_argument("--no-host-noise", action="store_true", help="skip the host-noise (5-pass) GRF leg")
     ap.add_argument("--fit-steps", type=int, default=20, help="Adam steps of the fit leg")
+    ap.add_argument("--skewer-shape", default=None,
+                    help="NX,NY,NZ,NSK: time only the skewer stage on boxes of this shape (profiling case)")
     ap.add_argument("--grf-shape", default=None,
                     help="NX,NY,NZ: time only the GRF boxes of this shape (profiling case)")
     ap.add_argument("--selftest-replicas", action="store_true", help=argparse.SUPPRESS)
@@ -892,6 +927,9 @@ def main():
     cfg = SMALL if args.small else PRODUCTION
     if args.grf_shape:
         run_grf_only(args, [int(x) for x in args.grf_shape.split(",")])
+        return
+    if args.skewer_shape:
+        run_skewers_only(args, [int(x) for x in args.skewer_shape.split(",")])
         return
     if args.precision:
         n, nsk, npix = (int(x) for x in args.precision.split(","))

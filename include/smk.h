@@ -313,6 +313,8 @@ typedef struct {
                             /* of each Bluestein DFT saved), or NULL                        */
     const int64_t* chirp_off; /* [2049]: offset (complex elements) of length N's spectrum in */
                               /* chirp, or -1 (then computed in the kernel)                    */
+    int32_t n_max;          /* largest npix of the problem (sizes the kernels' shared memory */
+                            /* to its Bluestein length); 0: up to 2048                      */
 } SmkFitProblem;
 
 /* Cyclic convolution length of the Bluestein DFT of a length-n skewer: the smallest

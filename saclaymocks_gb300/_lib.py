@@ -71,7 +71,8 @@ class SmkFitProblem(C.Structure):
     _fields_ = [("delta", C.c_void_p), ("eta", C.c_void_p), ("G", C.c_void_p), ("zbin", C.c_void_p),
                 ("offset", C.c_void_p), ("npix", C.c_void_p), ("order", C.c_void_p),
                 ("n_slots", C.c_int64), ("n_total", C.c_int64), ("nzb", C.c_int32), ("nkb", C.c_int32),
-                ("kedges", C.c_void_p), ("dx", C.c_double), ("chirp", C.c_void_p), ("chirp_off", C.c_void_p)]
+                ("kedges", C.c_void_p), ("dx", C.c_double), ("chirp", C.c_void_p), ("chirp_off", C.c_void_p),
+                ("n_max", C.c_int32)]
 
 
 # (name, restype, argtypes) of every exported entry point

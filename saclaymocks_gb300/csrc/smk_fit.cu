@@ -42,6 +42,7 @@ struct FitArgs {
     const double* gM;      // backward: dL/d<F>_j / n_j            [nzb]
     const double* gP;      // backward: dL/dP_b / count_b          [nkb]
     unsigned long long* counter;
+    int mmax;              // largest Bluestein length of the problem: smem = s1 | s2 | tw of mmax each
     const float2* chirp;   // optional: FFT_M of the forward chirp of every length N, digit-reversed
     const int64_t* chirp_off;  // [FFT_MAX_N / 2 + 1]: offset (complex) of length N in chirp, or -1
 };
@@ -249,8 +250,8 @@ __device__ __forceinline__ float warp_sum(float v) {
 __global__ void __launch_bounds__(FIT_T) fit_p1d_kernel(const FitArgs a) {
     extern __shared__ float2 smem[];
     float2* s1 = smem;
-    float2* s2 = smem + FFT_MAX_N;
-    float2* tw = smem + 2 * FFT_MAX_N;
+    float2* s2 = smem + a.mmax;
+    float2* tw = smem + 2 * a.mmax;
     __shared__ double psum[FIT_MAX_BINS];
     __shared__ double psq[FIT_MAX_BINS];
     __shared__ double edges[FIT_MAX_BINS + 1];
@@ -267,6 +268,13 @@ __global__ void __launch_bounds__(FIT_T) fit_p1d_kernel(const FitArgs a) {
     while (next_pair(a, &item_sh, &ps)) {
         const int N = ps.N;
         const int M = bluestein_m(N);
+        if (M > a.mmax) {
+            // a skewer longer than SmkFitProblem.n_max: not transformed (its Bluestein length
+            // does not fit the shared memory), the power sums are made NaN instead
+            if (threadIdx.x == 0) psum[0] = __longlong_as_double(0x7ff8000000000000LL);
+            __syncthreads();
+            continue;
+        }
         if (M != curM) {
             if (threadIdx.x == 0) make_plan(M, &pl, 16);
             __syncthreads();
@@ -308,8 +316,8 @@ __global__ void __launch_bounds__(FIT_T) fit_p1d_kernel(const FitArgs a) {
 __global__ void __launch_bounds__(FIT_T) fit_adjoint_kernel(const FitArgs a) {
     extern __shared__ float2 smem[];
     float2* s1 = smem;
-    float2* s2 = smem + FFT_MAX_N;
-    float2* tw = smem + 2 * FFT_MAX_N;
+    float2* s2 = smem + a.mmax;
+    float2* tw = smem + 2 * a.mmax;
     __shared__ double sA[3 * FIT_MAX_BINS], sB[3 * FIT_MAX_BINS], sS;
     __shared__ double edges[FIT_MAX_BINS + 1], gP[FIT_MAX_BINS], gM[FIT_MAX_BINS];
     __shared__ float th[3 * FIT_MAX_BINS];
@@ -332,6 +340,12 @@ __global__ void __launch_bounds__(FIT_T) fit_adjoint_kernel(const FitArgs a) {
     while (next_pair(a, &item_sh, &ps)) {
         const int N = ps.N;
         const int M = bluestein_m(N);
+        if (M > a.mmax) {
+            // a skewer longer than SmkFitProblem.n_max: skipped, the gradient is made NaN
+            if (threadIdx.x == 0) sS = __longlong_as_double(0x7ff8000000000000LL);
+            __syncthreads();
+            continue;
+        }
         if (M != curM) {
             if (threadIdx.x == 0) make_plan(M, &pl, 16);
             __syncthreads();
@@ -532,6 +546,9 @@ static int fit_args(const SmkFitProblem* fp, const float* theta, double* acc, co
     a->gM = gM;
     a->gP = gP;
     a->counter = counter;
+    // Bluestein lengths of the problem's skewers (n_max = 0: any length up to 2048)
+    const int nmax = fp->n_max > 0 ? std::min(fp->n_max, FFT_MAX_N / 2) : FFT_MAX_N / 2;
+    a->mmax = (bluestein_m(nmax) + 15) / 16 * 16;
     a->chirp = reinterpret_cast<const float2*>(fp->chirp);
     a->chirp_off = fp->chirp_off;
     if (!a->chirp != !a->chirp_off) return fail(SMK_EINVAL, "smk_fit: give chirp and chirp_off together");
@@ -554,7 +571,7 @@ int smk_fit_forward(const SmkFitProblem* fp, const float* theta, double* acc, vo
     const int g1 = (int)std::min<int64_t>((a.n_total + FIT_T * 16 - 1) / (FIT_T * 16), 8LL * nsm);
     fit_flux_kernel<<<std::max(g1, 1), FIT_T, 0, st>>>(a);
     if ((rc = check_launch("fit_flux_kernel"))) return rc;
-    const size_t smem = 3 * FFT_MAX_N * sizeof(float2);
+    const size_t smem = 3 * (size_t)a.mmax * sizeof(float2);
     int grid = 0;
     if ((rc = fit_grid((const void*)fit_p1d_kernel, smem, a.n_items, &grid))) return rc;
     fit_p1d_kernel<<<grid, FIT_T, smem, st>>>(a);
@@ -573,7 +590,7 @@ int smk_fit_backward(const SmkFitProblem* fp, const float* theta, double* acc, c
     if (cudaMemsetAsync(acc + off, 0, sizeof(double) * (acc_psq(a.nzb, a.nkb) - off), st) != cudaSuccess ||
         cudaMemsetAsync(workspace, 0, 8, st) != cudaSuccess)
         return check_launch("smk_fit_backward: memset");
-    const size_t smem = 3 * FFT_MAX_N * sizeof(float2);
+    const size_t smem = 3 * (size_t)a.mmax * sizeof(float2);
     int grid = 0;
     if ((rc = fit_grid((const void*)fit_adjoint_kernel, smem, a.n_items, &grid))) return rc;
     fit_adjoint_kernel<<<grid, FIT_T, smem, st>>>(a);

@@ -97,7 +97,7 @@ class FitProblem:
             offset=self.d_off.data_ptr(), npix=self.d_npix.data_ptr(), order=self.d_order.data_ptr(),
             n_slots=ns.value, n_total=self.n_total, nzb=self.nzb, nkb=self.nkb,
             kedges=self.d_kedges.data_ptr(), dx=self.dx, chirp=self.chirp.data_ptr(),
-            chirp_off=self.d_chirp_off.data_ptr())
+            chirp_off=self.d_chirp_off.data_ptr(), n_max=int(self.lengths.max()))
 
     def without_chirp_table(self):
         """Let the kernels compute the chirp spectra themselves (the form without the table)."""

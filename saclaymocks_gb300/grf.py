@@ -103,7 +103,7 @@ def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: flo
                amp: float | None = None, pk_grid: torch.Tensor | None = None,
                want_eta: bool = True, batch: int = 1, out=None, workspace: GrfWorkspace | None = None,
                stream=None, pass_events=None, eta_comp: str = "zz",
-               vel_factor: float | None = None, xi_chunk_kz: int = 0) -> GrfBoxes:
+               vel_factor: float | None = None, xi_chunk_kz: int = 128) -> GrfBoxes:
     """Draw delta (and eta_zz) boxes on the current CUDA device.
 
     noise:   None -> Philox white noise drawn on the GPU from ``seed`` (box b: seed + b);
@@ -118,7 +118,8 @@ def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: flo
     xi_chunk_kz: GPU noise: > 0 runs the x pass into a blocked intermediate in the workspace
              (each mode drawn once, the y pass reading contiguous runs), that many k_z columns
              at a time (the workspace grows to about 16 * batch * nx * ny * xi_chunk_kz bytes
-             with eta); 0 writes the boxes in place.  Same boxes, bit for bit.
+             with eta: 13 GB at 2560 x 2560 for the default 128); 0 writes the boxes in place.
+             Same boxes, bit for bit.
     eta_comp: which eta_ij = irfftn(k_i k_j / k^2 delta_k) the eta box holds ("zz", "xx",
              "yy", "xy", "xz", "yz"; bin/make_boxes.py:315-391), or a velocity
              v_i = irfftn(-i k_i / k^2 * vel_factor * delta_k) ("vx", "vy", "vz";

@@ -29,7 +29,7 @@ class _PendingFlux:
 
 class MockChunk:
     def __init__(self, nx, ny, nz, dcell=2.19, *, seed=1, k0=0.02, want_eta=True,
-                 cfg: spectra.SpectraConfig | None = None, dpix=0.2, device="cuda", xi_chunk_kz: int = 0):
+                 cfg: spectra.SpectraConfig | None = None, dpix=0.2, device="cuda", xi_chunk_kz: int = 128):
         self.nx, self.ny, self.nz, self.dcell = nx, ny, nz, dcell
         self.xi_chunk_kz = xi_chunk_kz     # grf.make_boxes: blocked x-pass intermediate (0: in place)
         self.seed, self.k0, self.dpix = seed, k0, dpix

@@ -80,7 +80,7 @@ def _store(choices: dict):
 
 
 def tune_grf(nx: int, ny: int, nz: int, dcell: float = 2.19, gpu_noise: bool = True, reps: int = 2,
-             out=None, workspace=None, use_cache: bool = True, xi_chunk_kz: int = 0) -> dict:
+             out=None, workspace=None, use_cache: bool = True, xi_chunk_kz: int = 128) -> dict:
     """Pick the fastest tile variant of every pass of smk_grf_boxes for this shape (with the x
     pass in place or, xi_chunk_kz > 0, into the blocked intermediate).
     Returns {"choices": {pass name: (variant, W, T)}, "ms": {pass name: {variant: ms}}}."""

@@ -108,6 +108,25 @@ def test_chirp_table_gives_identical_results(problem_pair):
         np.testing.assert_array_equal(a, b)
 
 
+def test_fit_kernels_sized_by_longest_skewer(problem_pair):
+    """The kernels' shared memory holds the Bluestein length of SmkFitProblem.n_max; a problem
+    that understates it gets NaN power sums and gradient (the too-long pairs are skipped), and
+    the next call with the right n_max is correct again."""
+    import copy
+    gp, op, mz, pk = problem_pair
+    theta = np.tile([0.15, 1.3, 0.4], (10, 1))
+    _, g_ok = gp.loss_grad(theta, mz, pk)
+    bad = copy.copy(gp)
+    bad.fp = type(gp.fp).from_buffer_copy(gp.fp)
+    bad.fp.n_max = 200                     # lengths go up to 2048
+    _, pk_bad, _ = bad.reductions(theta)
+    assert np.isnan(pk_bad).any()
+    _, g_bad = bad.loss_grad(theta, mz, pk)
+    assert np.isnan(g_bad).all()
+    _, g_again = gp.loss_grad(theta, mz, pk)
+    np.testing.assert_allclose(g_again, g_ok, rtol=0, atol=1e-6 * np.abs(g_ok).max())
+
+
 def test_adjoint_and_fd_fits_agree(problem_pair):
     """Adam from (0.15, 1.3, 0.4) with adjoint and with finite-difference gradients (fourth-order
     stencil, relative step 1e-2: truncation and the float32 rounding of the loss together keep the

@@ -46,11 +46,11 @@ def test_xgen_one_launch_equals_split_launches(G, shape):
     nx, ny, nz = shape
     ps = _lib.xgen_split(1)
     try:
-        ref = G.make_boxes(nx, ny, nz, 2.19, seed=23, batch=2)
-        refv = G.make_boxes(nx, ny, nz, 2.19, seed=24, eta_comp="vy", vel_factor=100.0)
+        ref = G.make_boxes(nx, ny, nz, 2.19, seed=23, batch=2, xi_chunk_kz=0)
+        refv = G.make_boxes(nx, ny, nz, 2.19, seed=24, eta_comp="vy", vel_factor=100.0, xi_chunk_kz=0)
         _lib.xgen_split(0)
-        got = G.make_boxes(nx, ny, nz, 2.19, seed=23, batch=2)
-        gotv = G.make_boxes(nx, ny, nz, 2.19, seed=24, eta_comp="vy", vel_factor=100.0)
+        got = G.make_boxes(nx, ny, nz, 2.19, seed=23, batch=2, xi_chunk_kz=0)
+        gotv = G.make_boxes(nx, ny, nz, 2.19, seed=24, eta_comp="vy", vel_factor=100.0, xi_chunk_kz=0)
         torch.cuda.synchronize()
     finally:
         _lib.xgen_split(ps)
@@ -70,7 +70,7 @@ def test_blocked_intermediate_x_pass_equals_in_place(G, shape, chunk):
     end inside a block, y lines loaded by TMA (2560, 1536) and by cp.async."""
     nx, ny, nz = shape
     for kw in (dict(batch=2), dict(want_eta=False), dict(eta_comp="vz", vel_factor=90.0)):
-        ref = G.make_boxes(nx, ny, nz, 2.19, seed=37, **kw)
+        ref = G.make_boxes(nx, ny, nz, 2.19, seed=37, xi_chunk_kz=0, **kw)
         got = G.make_boxes(nx, ny, nz, 2.19, seed=37, xi_chunk_kz=chunk, **kw)
         torch.cuda.synchronize()
         assert torch.equal(got.delta, ref.delta), kw
@@ -315,7 +315,7 @@ def test_every_tile_variant_is_exact(G, pname):
         _lib.check(lib.smk_tune_set(pid, n, v))
         try:
             if gpu_noise:
-                out = G.make_boxes(nx, ny, nz, 2.19, seed=17)
+                out = G.make_boxes(nx, ny, nz, 2.19, seed=17, xi_chunk_kz=0)   # the in-place x pass
                 nk = ophilox.kspace_noise(nx, ny, nz, 17)
                 o64 = ograf.grf_from_modes(nk, nz, 2.19, 0.02, eta=("zz",), precision="f64")
             else:
