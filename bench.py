@@ -364,13 +364,14 @@ def run_ours(args, cfg):
             e.record()                          # materialise the raw event handles
         for k in range(3):
             hout = grf.make_boxes(nx, ny, nz, cfg["dcell"], noise=noise, amp=chunk.amp, out=boxes, workspace=ws,
-                                  pass_events=hev[k])
+                                  pass_events=hev[k], xi_chunk_kz=xi)
         torch.cuda.synchronize()
         hout.check()
         hp = np.mean([[hev[k][i].elapsed_time(hev[k][i + 1]) for i in range(5)] for k in (1, 2)], axis=0)
         del noise, hout
         torch.cuda.empty_cache()
         host_res = {"grf_ms": round(float(hp.sum()), 3),
+                    "x_pass": "blocked intermediate" if xi else "in place",
                     "pass_ms": dict(zip(["zfwd_r2c", "y_fwd", "x_fwd_scale_inv(x2)", "y_inv(x2)", "zinv_c2r(x2)"],
                                         [round(float(x), 3) for x in hp])),
                     "ms_per_step": round(float(hp.sum()) + sk_ms, 3),
@@ -410,20 +411,20 @@ def run_ours(args, cfg):
     dom = int(np.argmax(pass_ms))
     achieved = pass_bytes[dom] / (pass_ms[dom] * 1e-3) / 1e9
     # DRAM bytes per unit from ncu captures of the same kernels on boxes with the production
-    # line lengths (2560 x 128 x 1536 for the x pass, 128 x 2560 x 1536 for y and z), scaled
-    # by the units of this launch: x 7.81 B per mode and field, y 16.0 and z 16.1 B per mode
-    # and field
-    traffic = [7.81 * modes * 2, 16.0 * modes * 2, 16.14 * modes * 2][dom] / 1e9
+    # line lengths (2560 x 128 x 1536 for the x pass, 128 x 2560 x 1536 for y and z), scaled by
+    # the units of this launch: x (xgi_kernel, both fields) 15.84 B per mode, y 16.97 and z
+    # 16.14 B per mode and field
+    traffic = [15.84 * modes, 16.97 * modes * 2, 16.14 * modes * 2][dom] / 1e9
     grf_ms = float(np.sum(pass_ms))
     step_ms = ms / args.steps
     # The x pass is instruction-bound, so its issue-slot roofline is reported beside the HBM one:
-    # warp instructions per mode and field from the same ncu capture (1.311e9 for 2560x128x769
-    # modes, one field), scaled by the modes of this launch; peak = SMs x 4 schedulers x the
-    # median SM clock sampled during the timed region
+    # warp instructions per mode from the same ncu capture (2.0697e9 for 2560x128x769 modes, both
+    # fields), scaled by the modes of this launch; peak = SMs x 4 schedulers x the median SM clock
+    # sampled during the timed region
     clk_sum = clk.summary()
     sm_hz = float(clk_sum.get("sm_mhz") or 2070.0) * 1e6
     nsm = torch.cuda.get_device_properties(dev).multi_processor_count
-    x_winst = 1.311e9 / (2560 * 128 * 769) * modes * 2
+    x_winst = 2.0697e9 / (2560 * 128 * 769) * modes
     issue = {"kernel": "x_gen", "warp_instructions": x_winst,
              "achieved_per_s": x_winst / (pass_ms[0] * 1e-3), "peak_per_s": nsm * 4 * sm_hz,
              "frac": x_winst / (pass_ms[0] * 1e-3) / (nsm * 4 * sm_hz),
@@ -458,7 +459,7 @@ def run_ours(args, cfg):
            "e2e": {"value": aggregate_value(cells, world, e2e_s), "unit": "cells/s",
                    "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
                    "ms_per_step": e2e_s * 1e3},
-           "gpu_launches": args.steps * (grf.grf_launches(nx, ny, nz) + 1),
+           "gpu_launches": args.steps * (grf.grf_launches(nx, ny, nz, xi_chunk_kz=xi) + 1),
            "tile_variants": tuned,
            "clocks": clk_sum,
            "fit": fit_res,
@@ -887,6 +888,35 @@ def run_skewers_only(args, spec):
                       "pixels_per_s": table.total_pixels / (ms * 1e-3)}))
 
 
+def run_fit_only(args, nsk):
+    """The fit kernels alone (the ncu profiling case): NSK skewers of 400-1200 pixels with
+    Gaussian fields, 10 z bins x (a, b, c), 32 log-k bins; W + K loss-and-gradient evaluations."""
+    import numpy as np
+    import torch
+
+    from saclaymocks_gb300 import fit
+    rng = np.random.RandomState(0)
+    lengths = rng.randint(400, 1201, nsk).astype(np.int32)
+    n = int(lengths.sum())
+    delta = torch.randn(n, device="cuda") * 1.2
+    eta = torch.randn(n, device="cuda") * 0.4
+    z = torch.rand(n, device="cuda", dtype=torch.float64) * 1.8 + 1.8
+    prob = fit.FitProblem(delta, eta, None, z, lengths, np.linspace(1.8, 3.6, 11),
+                          np.logspace(np.log10(0.05), np.log10(15.0), 33), 0.2)
+    truth = np.tile([0.1, 1.58, 0.6], (10, 1))
+    mz, pk, _ = prob.reductions(truth)
+    th0 = np.tile([0.15, 1.3, 0.4], (10, 1))
+    for _ in range(args.warmup):
+        prob.loss_grad(th0, mz, pk)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        prob.loss_grad(th0, mz, pk)
+    torch.cuda.synchronize()
+    s = (time.perf_counter() - t0) / args.steps
+    print(json.dumps({"fit_case": nsk, "pixels": n, "s_per_grad": s}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -912,6 +942,8 @@ def main():
     ap.add_argument("--no-fit", action="store_true", help="skip the (a,b,c) fit leg")
     ap.add_argument("--no-host-noise", action="store_true", help="skip the host-noise (5-pass) GRF leg")
     ap.add_argument("--fit-steps", type=int, default=20, help="Adam steps of the fit leg")
+    ap.add_argument("--fit-case", type=int, default=0,
+                    help="NSK: time only the fit's loss + gradient on NSK random skewers (profiling case)")
     ap.add_argument("--skewer-shape", default=None,
                     help="NX,NY,NZ,NSK: time only the skewer stage on boxes of this shape (profiling case)")
     ap.add_argument("--grf-shape", default=None,
@@ -927,6 +959,9 @@ def main():
     cfg = SMALL if args.small else PRODUCTION
     if args.grf_shape:
         run_grf_only(args, [int(x) for x in args.grf_shape.split(",")])
+        return
+    if args.fit_case:
+        run_fit_only(args, args.fit_case)
         return
     if args.skewer_shape:
         run_skewers_only(args, [int(x) for x in args.skewer_shape.split(",")])

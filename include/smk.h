@@ -84,9 +84,9 @@ typedef struct {
     int32_t n_pass_events;    /* first HBM pass and after each of the five (0: none)          */
     int32_t eta_comp;     /* SMK_ETA_*: which eta_ij or velocity the eta box holds (0 = zz)  */
     double vel_factor;    /* SMK_ETA_VX/VY/VZ: H0 * dD/dz(z = 0) (km/s/(Mpc/h) per unit z)    */
-    int32_t xi_chunk_kz;  /* GPU noise: > 0 runs the x pass into a blocked intermediate in the  */
-                          /* workspace (each mode drawn once, both fields in one launch, the   */
-                          /* rows of a tile ny x 32..64 bytes apart instead of ny x pitch x 4) */
+    int32_t xi_chunk_kz;  /* > 0 runs the x pass into a blocked intermediate in the workspace */
+                          /* (both fields from one launch, each GPU-noise mode drawn once, the */
+                          /* rows of a tile ny x 16..64 bytes apart instead of ny x pitch x 4) */
                           /* that the y pass reads as contiguous runs, xi_chunk_kz k_z columns */
                           /* at a time (rounded up to 16); 0: the x pass writes the boxes in   */
                           /* place.  The boxes are the same, bit for bit.                      */
@@ -96,9 +96,9 @@ typedef struct {
 int64_t smk_grf_pitch(int32_t nz);
 /* Floats of one padded output box array (all batch members). */
 int64_t smk_grf_box_floats(const SmkGrfParams* p);
-/* Workspace bytes smk_grf_boxes needs: 256 (the FP64 normalisation accumulator), plus, for a
- * GPU-noise call with xi_chunk_kz > 0, the intermediate of one chunk: fields (2 with eta, else
- * 1) x batch x nx x ny x min(roundup(xi_chunk_kz, 16), roundup(nz/2+1, 16)) complex floats. */
+/* Workspace bytes smk_grf_boxes needs: 256 (the FP64 normalisation accumulator), plus, with
+ * xi_chunk_kz > 0, the intermediate of one chunk: fields (2 with eta, else 1) x batch x nx x
+ * ny x min(roundup(xi_chunk_kz, 16), roundup(nz/2+1, 16)) complex floats. */
 size_t smk_grf_workspace_size(const SmkGrfParams* p);
 
 /*
@@ -185,7 +185,7 @@ typedef struct {
     const float* dir;      /* [n][3] unit direction (or dir64)                           */
     const int32_t* npix;   /* [n] pixels                                                 */
     const int64_t* offset; /* [n] index of the skewer's first pixel in the packed outputs */
-    double dpix;           /* pixel spacing along the skewer, Mpc/h                      */
+    double dpix;           /* pixel spacing along the skewer, Mpc/h (at most 64 cells)   */
     const int32_t* order;  /* [n_slots] schedule from smk_skewer_schedule (device)       */
     int64_t n_slots;       /* 2 * work items                                             */
     const float* pix_delta;/* SMK_INTERP_PIXELS: packed delta_l per pixel                */
@@ -239,7 +239,7 @@ typedef struct {
 } SmkSpectraParams;
 #define SMK_SS_SET_FLOATS 3973 /* sum over nz = 256<<j, j = 0..4, of nz/2+1 */
 
-/* Host: build the work schedule of smk_skewers_flux from the host copy of npix.  Skewers
+/* Host: build the work schedule of smk_skewers_flux from the host copy of npix (each 0..2^24).  Skewers
  * are grouped by small-scale FFT length, longest first, in pairs of equal length (one
  * complex FFT carries two skewers); order_out must hold 2*n + 16 ints, n_slots_out gets
  * the used length (even; empty slots are -1).  ss_nz is SmkSpectraParams.ss_nz: 0 applies

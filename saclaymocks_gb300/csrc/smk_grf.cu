@@ -132,7 +132,7 @@ int64_t smk_grf_box_floats(const SmkGrfParams* p) {
 
 // k_z columns per chunk of the x pass's blocked intermediate (0: in place).
 static int64_t xi_chunk_cols(const SmkGrfParams* p) {
-    if (!p || p->noise_mode != SMK_NOISE_PHILOX || p->xi_chunk_kz <= 0 || p->nz < 2) return 0;
+    if (!p || p->xi_chunk_kz <= 0 || p->nz < 2) return 0;
     const int64_t nzh16 = (p->nz / 2 + 1 + 15) / 16 * 16;
     return std::min<int64_t>(((int64_t)p->xi_chunk_kz + 15) / 16 * 16, nzh16);
 }
@@ -172,6 +172,26 @@ int smk_grf_check(const double* st, int64_t ncells, double* sigma_out) {
     if (st[2] > 0) return fail(SMK_ENULLBOX, "box holds %.0f non-finite cells", st[2]);
     if (st[1] == 0.0) return fail(SMK_ENULLBOX, "box is all zero");
     return SMK_OK;
+}
+
+// y inverse reading the blocked intermediate I of a chunk of xcols columns (blocks of kb
+// columns, nf fields): the in-place arguments with the source, and 5-D TMA maps over I.
+static LineArgs staged_y(const LineArgs& ya, float2* const* I, int nf, int kb, int wy, int64_t xcols,
+                         int64_t nouter, int ny) {
+    LineArgs yi = ya;
+    yi.nbuf = nf;
+    yi.src[0] = I[0];
+    yi.src[1] = nf > 1 ? I[1] : nullptr;
+    yi.src_kb = kb;
+    if (yi.tma == 2) yi.tma = 1;   // stores go to the boxes; the maps cover the intermediate
+    const int per = wy / kb;         // intermediate blocks per y tile
+    const uint64_t dims[5] = {(uint64_t)kb, (uint64_t)per, (uint64_t)ny, (uint64_t)nouter, (uint64_t)(xcols / wy)};
+    const uint64_t strides[5] = {1, (uint64_t)(nouter * ny * kb), (uint64_t)kb, (uint64_t)ny * kb,
+                                 (uint64_t)(per * nouter * ny * kb)};
+    const uint32_t box[5] = {(uint32_t)kb, (uint32_t)per, (uint32_t)std::max(ya.box_rows, 1), 1, 1};
+    for (int f = 0; f < nf && yi.tma; ++f)
+        if (!encode_map_5d_8b(&yi.tmap[f], I[f], dims, strides, box)) yi.tma = 0;
+    return yi;
 }
 
 int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats, void* workspace,
@@ -311,20 +331,7 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
             ga.I[0] = I0;
             ga.I[1] = p->want_eta ? I0 + nouter * p->ny * xcols : nullptr;
             ga.fields = p->want_eta ? XGEN_BOTH : XGEN_DELTA;
-            LineArgs yi = ya;
-            yi.nbuf = nf;
-            yi.src[0] = ga.I[0];
-            yi.src[1] = ga.I[1];
-            yi.src_kb = kb;
-            if (yi.tma == 2) yi.tma = 1;   // stores go to the boxes; the maps cover the intermediate
-            const int per = wy / kb;         // intermediate blocks per y tile
-            const uint64_t dims[5] = {(uint64_t)kb, (uint64_t)per, (uint64_t)p->ny, (uint64_t)nouter,
-                                      (uint64_t)(xcols / wy)};
-            const uint64_t strides[5] = {1, (uint64_t)(nouter * p->ny * kb), (uint64_t)kb, (uint64_t)p->ny * kb,
-                                         (uint64_t)(per * nouter * p->ny * kb)};
-            const uint32_t box[5] = {(uint32_t)kb, (uint32_t)per, (uint32_t)std::max(ya.box_rows, 1), 1, 1};
-            for (int f = 0; f < nf && yi.tma; ++f)
-                if (!encode_map_5d_8b(&yi.tmap[f], ga.I[f], dims, strides, box)) yi.tma = 0;
+            LineArgs yi = staged_y(ya, ga.I, nf, kb, wy, xcols, nouter, p->ny);
             const bool one_chunk = xcols >= nzh;
             for (int64_t c0 = 0; c0 < nzh; c0 += xcols) {
                 ga.cb0 = (int)(c0 / kb);
@@ -390,12 +397,40 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         xa.inv_vcell = inv_vcell;
         xa.eta_comp = p->eta_comp;
         xa.vfac = (float)p->vel_factor;
-        if ((rc = run_xpass(vx, xa, st))) return rc;
-        if ((rc = mark(3))) return rc;
-        // 4. c2c along y, inverse, on delta (and eta)
-        ya.nbuf = p->want_eta ? 2 : 1;
-        if ((rc = run_line(vy, ya, true, st))) return rc;
-        if ((rc = mark(4))) return rc;
+        const int nf = p->want_eta ? 2 : 1;
+        const int wxp = variant_table(PASS_XPASS)[vx].w, wy = variant_table(PASS_LINE)[vy].w;
+        const int kb = p->want_eta ? wxp / 2 : wxp;
+        const int64_t xcols = xi_chunk_cols(p);
+        if (xcols > 0 && (!workspace || workspace_bytes < smk_grf_workspace_size(p)))
+            return fail(SMK_EWORKSPACE, "smk_grf_boxes: xi_chunk_kz needs %zu workspace bytes",
+                        smk_grf_workspace_size(p));
+        if (xcols > 0 && kb >= 2 && kb % 2 == 0 && wy % kb == 0 && xcols % wy == 0) {
+            // chunks of xcols k_z columns: the x pass reads one field in place and writes both
+            // into the blocked intermediate, the y inverse reads it as contiguous runs
+            float2* I0 = reinterpret_cast<float2*>(reinterpret_cast<char*>(workspace) + 256);
+            const int64_t nouter = (int64_t)p->batch * p->nx;
+            xa.I[0] = I0;
+            xa.I[1] = p->want_eta ? I0 + nouter * p->ny * xcols : nullptr;
+            LineArgs yi = staged_y(ya, xa.I, nf, kb, wy, xcols, nouter, p->ny);
+            const bool one_chunk = xcols >= nzh;
+            for (int64_t c0 = 0; c0 < nzh; c0 += xcols) {
+                xa.cb0 = (int)(c0 / kb);
+                xa.ncb = (int)ceil_div(std::min<int64_t>(xcols, nzh - c0), kb);
+                if ((rc = run_xpi(vx, xa, st))) return rc;
+                if (one_chunk && (rc = mark(3))) return rc;
+                yi.col0 = (int)c0;
+                yi.ncol = (int)std::min<int64_t>(xcols, nzh - c0);
+                if ((rc = run_line(vy, yi, true, st))) return rc;
+            }
+            if ((!one_chunk && (rc = mark(3))) || (rc = mark(4))) return rc;
+        } else {
+            if ((rc = run_xpass(vx, xa, st))) return rc;
+            if ((rc = mark(3))) return rc;
+            // 4. c2c along y, inverse, on delta (and eta)
+            ya.nbuf = nf;
+            if ((rc = run_line(vy, ya, true, st))) return rc;
+            if ((rc = mark(4))) return rc;
+        }
     }
 
     // 5. c2r along z, / N, statistics

@@ -281,6 +281,10 @@ struct XArgs {
     float inv_k0, inv_vcell;
     int eta_comp;          // SMK_ETA_*: eta_ij = k_i k_j / k^2 delta_k, or a velocity component
     float vfac;            // velocity: H0 * dD/dz(0)
+    // xpi_kernel: the blocked intermediate of XGenArgs (I[0] delta, I[1] eta or null) and the
+    // k_z column blocks [cb0, cb0 + ncb) of this chunk
+    float2* I[2];
+    int cb0, ncb;
 };
 
 // k_i k_j of the eta component (SMK_ETA_*), float32 product as numpy forms kx*ky
@@ -392,6 +396,97 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpass_kernel(const XArgs a) {
             store_cols<W, T>(s, pb, n, estride, cols);
             __syncthreads();
         }
+    }
+}
+
+// ------------------------------------------------------------------ host-noise x pass into the
+// blocked intermediate
+// Tiles (box b, column block kb, y slot), y slot fastest, of KB = W/2 k_z columns (W with delta
+// only): load the KB columns of the noise spectrum (after the y forward pass) for every x,
+// forward x FFT of those KB lines (tile pitch W), x sqrt(P/Vcell) and the eta split into lines
+// KB..W-1 of the same tile, inverse x FFT of the W lines, last stage stored from registers into
+// the intermediate (layout of XGenArgs::I).  Same arithmetic as xpass_kernel per line.
+// smem: s[n*W] | tw[n] | kx[n] | ix[n] | kt[W+1]
+template <class C>
+__global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
+    constexpr int W = C::W, T = C::T;
+    constexpr int KB = W / 2;
+    extern __shared__ float2 smem[];
+    const int n = a.pl.n;  // == nx
+    float2* s = smem;
+    float2* tw = s + n * W;
+    float* kx = reinterpret_cast<float*>(tw + n);
+    int* ix = reinterpret_cast<int*>(kx + n);
+    float* kt = reinterpret_cast<float*>(ix + n);
+    fill_stage_twiddles(tw, a.pl);
+    for (int e = threadIdx.x; e < n; e += T) {
+        const int f = freq_of_slot(a.pl, e);
+        ix[e] = f;
+        kx[e] = kaxis(f, n, a.kfac, true);
+    }
+    float amp = 0.f;
+    if (a.pk_mode == SMK_PK_ANALYTIC) amp = (float)(a.amp_host > 0.0 ? a.amp_host : *a.amp_dev);
+    const bool both = a.I[1] != nullptr;
+    const int WC = both ? KB : W;     // k_z columns per tile
+    const int64_t ntiles = (int64_t)a.batch * a.ncb * a.ny;
+    const int64_t nouter = (int64_t)a.batch * a.nx;
+    const int64_t estride = (int64_t)a.ny * a.cp;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int yslot = (int)(tile % a.ny);
+        const int64_t r = tile / a.ny;
+        const int kbl = (int)(r % a.ncb);
+        const int64_t b = r / a.ncb;
+        const int cb = a.cb0 + kbl;
+        const int cols = min(WC, a.nzh - cb * WC);
+        const float2* pa = a.A + b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)cb * WC;
+        // WC columns (16-byte copies of column pairs, zero past nzh) into lines 0..WC-1 of the tile
+        for (int idx = threadIdx.x; idx < n * (WC / 2); idx += T) {
+            const int e = idx / (WC / 2), w = 2 * (idx % (WC / 2));
+            const int bytes = w < cols ? (w + 1 < cols ? 16 : 8) : 0;
+            cp_async<16>(s + e * W + w, bytes ? pa + e * estride + w : pa, bytes);
+        }
+        const int iy = freq_of_slot(a.ply, yslot);
+        if (threadIdx.x == 0) kt[0] = kaxis(iy, a.ny, a.kfac, true);
+        if (threadIdx.x < WC) kt[1 + threadIdx.x] = kaxis(cb * WC + threadIdx.x, 2 * (a.nzh - 1), a.kfac, false);
+        cp_async_wait_all();
+        __syncthreads();
+        if (both)
+            fft_tile<false, KB, W, T, C::RMAX>(s, tw, a.pl);
+        else
+            fft_tile<false, W, W, T, C::RMAX>(s, tw, a.pl);
+        const float ky = kt[0];
+        for (int idx = threadIdx.x; idx < n * WC; idx += T) {
+            const int e = idx / WC, w = idx % WC;
+            const float kxv = kx[e], kz = kt[1 + w];
+            // k^2 in float32 without contraction, as numpy evaluates kx*kx + ky*ky + kz*kz
+            const float kk = __fadd_rn(__fadd_rn(__fmul_rn(kxv, kxv), __fmul_rn(ky, ky)), __fmul_rn(kz, kz));
+            float sc;
+            if (a.pk_mode == SMK_PK_GRID) {
+                sc = w < cols ? __ldg(a.grid + ((int64_t)ix[e] * a.ny + iy) * a.nzh + cb * WC + w) : 0.f;
+            } else {
+                const float k = __fsqrt_rn(kk);
+                const float kr = k * a.inv_k0;
+                const float den = fmaf(kr, kr, 1.0f);
+                sc = sqrtf(amp * k / (den * den) * a.inv_vcell);
+            }
+            const float2 d = cscale(s[e * W + w], sc);
+            s[e * W + w] = d;
+            if (both) {
+                const float kk1 = (kk == 0.0f) ? 1.0f : kk;  // k^2[0,0,0] = 1 (bin/make_boxes.py:306)
+                s[e * W + KB + w] = eta_apply<true>(a.eta_comp, d, kxv, ky, kz, kk1, a.vfac);
+            }
+        }
+        __syncthreads();
+        const int64_t row0 = ((int64_t)kbl * nouter + b * a.nx) * a.ny + yslot;
+        float2* d0 = a.I[0] + row0 * WC;
+        float2* d1 = both ? a.I[1] + row0 * WC : nullptr;
+        const int64_t es = (int64_t)a.ny * WC;
+        ifft_tile_out<W, W, T, C::RMAX>(s, tw, a.pl, [&](int e, int w, float2 v) {
+            const int f = both && w >= WC;
+            const int c = w - f * WC;
+            if (c < cols) (f ? d1 : d0)[e * es + c] = v;
+        });
+        __syncthreads();
     }
 }
 
@@ -1047,6 +1142,17 @@ static int launch_xpass(const XArgs& a, cudaStream_t st) {
 }
 
 template <class C>
+static int launch_xpi(const XArgs& a, cudaStream_t st) {
+    if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xpi_kernel");
+    const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 + (C::W + 1) * 4;
+    const int64_t ntiles = (int64_t)a.batch * a.ncb * a.ny;
+    int grid = 0, rc;
+    if ((rc = persistent_grid(xpi_kernel<C>, C::T, smem, ntiles, &grid))) return rc;
+    xpi_kernel<C><<<grid, C::T, smem, st>>>(a);
+    return check_launch("xpi_kernel");
+}
+
+template <class C>
 static int launch_xgi(const XGenArgs& a, cudaStream_t st) {
     if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xgi_kernel");
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 +
@@ -1109,5 +1215,6 @@ int run_line(int v, const LineArgs& a, bool inv, cudaStream_t st);
 int run_xpass(int v, const XArgs& a, cudaStream_t st);
 int run_xgen(int v, const XGenArgs& a, cudaStream_t st);
 int run_xgi(int v, const XGenArgs& a, cudaStream_t st);
+int run_xpi(int v, const XArgs& a, cudaStream_t st);
 
 }  // namespace smk

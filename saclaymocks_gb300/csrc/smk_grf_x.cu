@@ -1,16 +1,7 @@
-// Tile variants of the x passes (host noise: xpass; GPU noise: xgen).
+// Tile variants of the GPU-noise x passes (xgen: into the boxes, xgi: into the blocked intermediate).
 #include "smk_grf_kernels.cuh"
 
 namespace smk {
-
-int run_xpass(int v, const XArgs& a, cudaStream_t st) {
-    int i = 0;
-#define X(W, T, N, R, B) \
-    if (v == i++) return launch_xpass<TileCfg<W, T, R, B>>(a, st);
-    SMK_X_VARIANTS(X)
-#undef X
-    return fail(SMK_EINVAL, "xpass: no tile variant %d", v);
-}
 
 int run_xgen(int v, const XGenArgs& a, cudaStream_t st) {
     int i = 0;

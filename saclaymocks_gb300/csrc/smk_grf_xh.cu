@@ -1,0 +1,24 @@
+// Tile variants of the host-noise x passes (xpass: in place, xpi: into the blocked intermediate).
+#include "smk_grf_kernels.cuh"
+
+namespace smk {
+
+int run_xpass(int v, const XArgs& a, cudaStream_t st) {
+    int i = 0;
+#define X(W, T, N, R, B) \
+    if (v == i++) return launch_xpass<TileCfg<W, T, R, B>>(a, st);
+    SMK_X_VARIANTS(X)
+#undef X
+    return fail(SMK_EINVAL, "xpass: no tile variant %d", v);
+}
+
+int run_xpi(int v, const XArgs& a, cudaStream_t st) {
+    int i = 0;
+#define X(W, T, N, R, B) \
+    if (v == i++) return launch_xpi<TileCfg<W, T, R, B>>(a, st);
+    SMK_X_VARIANTS(X)
+#undef X
+    return fail(SMK_EINVAL, "xpi: no tile variant %d", v);
+}
+
+}  // namespace smk

@@ -120,7 +120,8 @@ int smk_skewer_schedule(int64_t n, const int32_t* npix_host, int32_t ss_nz, int3
     std::vector<Key> key((size_t)n);
     for (int64_t s = 0; s < n; ++s) {
         const int32_t np = npix_host[s];
-        if (np < 0) return smk::fail(SMK_EINVAL, "smk_skewer_schedule: negative npix");
+        if (np < 0 || np > (1 << 24))
+            return smk::fail(SMK_EINVAL, "smk_skewer_schedule: npix %d outside 0..2^24", np);
         int32_t nz = ss_nz;
         if (nz < 0) {
             nz = 0;  // no small-scale field: one class, pairs by length only

@@ -83,6 +83,13 @@ __device__ __forceinline__ int wrap(int64_t c, int n) {
     return (int)(r < 0 ? r + n : r);
 }
 
+// The same for a 32-bit cell index (a wrapped start cell plus the cells a skewer advances, or a
+// neighbour offset): one 32-bit remainder instead of the emulated 64-bit one.
+__device__ __forceinline__ int wrap32(int c, int n) {
+    const int r = c % n;
+    return r < 0 ? r + n : r;
+}
+
 // Pixel positions in cells along each axis as 32.32 fixed point: q_i = f0 + i * step exactly
 // in int64, cell = i0 + (q_i >> 32), fraction = low 32 bits (error < 2e-7 cells at 1e3 pixels,
 // where float32 i*step would lose ~1e-5 cells).
@@ -101,7 +108,7 @@ constexpr int SK_SS_SET = 129 + 257 + 513 + 1025 + 2049;
 __device__ __forceinline__ float pixel_z_box(const SkArgs& a, const SkewerGeo& g, int i) {
     const long long q = g.f0[0] + (long long)i * g.step[0];
     const float fr = (float)(unsigned)(q & 0xffffffffLL) * 2.3283064365386963e-10f;
-    float xc = (float)wrap((int64_t)g.i0[0] + (q >> 32), a.nx) + fr + 0.5f;
+    float xc = (float)wrap32(g.i0[0] + (int)(q >> 32), a.nx) + fr + 0.5f;
     if (xc >= (float)a.nx) xc -= (float)a.nx;
     return a.z_lo + (a.z_hi - a.z_lo) * (xc / (float)a.nx);
 }
@@ -343,7 +350,7 @@ __global__ void __launch_bounds__(SK_T, GR ? 2 : 4) skewer_kernel(const SkArgs a
                     // p/dcell = i0 + q 2^-32 + 0.5: shift by half a cell to get floor(p/dcell)
                     const long long q = g.f0[d] + (long long)i * g.step[d] + (1LL << 31);
                     const float fu = (float)(unsigned)(q & 0xffffffffLL) * 2.3283064365386963e-10f;
-                    ci[d] = wrap((int64_t)g.i0[d] + (q >> 32), dims[d]);
+                    ci[d] = wrap32(g.i0[d] + (int)(q >> 32), dims[d]);
                     rpos[d] = ((double)(g.i0u[d] + (q >> 32)) + (double)fu) * a.dcell - a.obs[d];
                     if (d == 0) fux = fu;
 #pragma unroll
@@ -359,15 +366,19 @@ __global__ void __launch_bounds__(SK_T, GR ? 2 : 4) skewer_kernel(const SkArgs a
                     sy += ew[1][c];
                     sz += ew[2][c];
                 }
-                int izs[2 * GR + 1 + !GAUSS];
+                int ixs[2 * GR + 1 + !GAUSS], iys[2 * GR + 1 + !GAUSS], izs[2 * GR + 1 + !GAUSS];
 #pragma unroll
-                for (int c = 0; c < 2 * GR + 1; ++c) izs[c] = wrap((int64_t)ci[2] + c - GR, dims[2]);
+                for (int c = 0; c < 2 * GR + 1; ++c) {
+                    ixs[c] = wrap32(ci[0] + c - GR, dims[0]);
+                    iys[c] = wrap32(ci[1] + c - GR, dims[1]);
+                    izs[c] = wrap32(ci[2] + c - GR, dims[2]);
+                }
                 const bool rsd = a.eta6[0] != nullptr;
                 float acc[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
                 for (int cx = -GR; cx <= GR; ++cx) {
-                    const int ixw = wrap((int64_t)ci[0] + cx, dims[0]);
+                    const int ixw = ixs[cx + GR];
                     for (int cy = -GR; cy <= GR; ++cy) {
-                        const int iyw = wrap((int64_t)ci[1] + cy, dims[1]);
+                        const int iyw = iys[cy + GR];
                         const float wxy = ew[0][cx + GR] * ew[1][cy + GR];
                         const int64_t row = ((int64_t)ixw * a.ny + iyw) * a.pitch;
 #pragma unroll
@@ -403,7 +414,7 @@ __global__ void __launch_bounds__(SK_T, GR ? 2 : 4) skewer_kernel(const SkArgs a
                 for (int d = 0; d < 3; ++d) {
                     const long long q = g.f0[d] + (long long)i * g.step[d];
                     fr[d] = (float)(unsigned)(q & 0xffffffffLL) * 2.3283064365386963e-10f;  // 2^-32
-                    c0[d] = wrap((int64_t)g.i0[d] + (q >> 32), dims[d]);
+                    c0[d] = wrap32(g.i0[d] + (int)(q >> 32), dims[d]);
                     c1[d] = c0[d] + 1 == dims[d] ? 0 : c0[d] + 1;
                 }
                 const int64_t r00 = ((int64_t)c0[0] * a.ny + c0[1]) * a.pitch;
@@ -493,6 +504,9 @@ int smk_skewers_flux(const SmkSkewers* sk, const SmkSpectraParams* p, const floa
             return fail(SMK_EINVAL, "smk_skewers_flux: null start/dir");
         if (p->nx < 1 || p->ny < 1 || p->nz < 1 || p->pitch < p->nz || !(p->dcell > 0) || !(sk->dpix > 0))
             return fail(SMK_EINVAL, "smk_skewers_flux: bad box geometry");
+        // a skewer then advances fewer than 2^30 cells (npix <= 2^24), the kernel's 32-bit index range
+        if (sk->dpix > 64.0 * p->dcell)
+            return fail(SMK_EINVAL, "smk_skewers_flux: pixel spacing above 64 cells");
     } else if (p->interp != SMK_INTERP_PIXELS) {
         return fail(SMK_EINVAL, "smk_skewers_flux: unknown interp");
     }

@@ -115,11 +115,11 @@ def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: flo
     out:     optional (delta_pad, eta_pad) from :func:`alloc_boxes` to reuse storage.
     pass_events: optional list of 6 recorded torch.cuda.Event, marked before the first HBM
              pass and after each of the five (per-pass timing).
-    xi_chunk_kz: GPU noise: > 0 runs the x pass into a blocked intermediate in the workspace
-             (each mode drawn once, the y pass reading contiguous runs), that many k_z columns
-             at a time (the workspace grows to about 16 * batch * nx * ny * xi_chunk_kz bytes
-             with eta: 13 GB at 2560 x 2560 for the default 128); 0 writes the boxes in place.
-             Same boxes, bit for bit.
+    xi_chunk_kz: > 0 runs the x pass into a blocked intermediate in the workspace (both fields
+             from one launch, GPU-noise modes drawn once, the y pass reading contiguous runs),
+             that many k_z columns at a time (the workspace grows to about
+             16 * batch * nx * ny * xi_chunk_kz bytes with eta: 13 GB at 2560 x 2560 for the
+             default 128); 0 writes the boxes in place.  Same boxes, bit for bit.
     eta_comp: which eta_ij = irfftn(k_i k_j / k^2 delta_k) the eta box holds ("zz", "xx",
              "yy", "xy", "xz", "yz"; bin/make_boxes.py:315-391), or a velocity
              v_i = irfftn(-i k_i / k^2 * vel_factor * delta_k) ("vx", "vy", "vz";
@@ -136,7 +136,7 @@ def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: flo
     p.want_eta = 1 if want_eta else 0
     p.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
     p.eta_comp = _lib.SMK_ETA[eta_comp]
-    p.xi_chunk_kz = int(xi_chunk_kz) if noise is None else 0
+    p.xi_chunk_kz = int(xi_chunk_kz)
     if eta_comp in ("vx", "vy", "vz"):
         if vel_factor is None:
             raise ValueError("velocity boxes need vel_factor = H0 * dD/dz(z=0)")
@@ -184,10 +184,18 @@ def make_boxes(nx: int, ny: int | None = None, nz: int | None = None, dcell: flo
                     dcell=float(dcell))
 
 
-def grf_launches(nx: int, ny: int, nz: int, batch: int = 1, want_eta: bool = True, gpu_noise: bool = True) -> int:
-    """Kernel launches of one smk_grf_boxes call as make_boxes issues it by default (GPU noise:
-    x pass, y inverse, z inverse, with the x pass in two launches when delta + eta exceed
-    SPLIT_MIN_PAIR_BYTES; host noise: z forward, y forward, x, y inverse, z inverse)."""
+def grf_launches(nx: int, ny: int, nz: int, batch: int = 1, want_eta: bool = True, gpu_noise: bool = True,
+                 xi_chunk_kz: int = 128) -> int:
+    """Kernel launches of one smk_grf_boxes call as make_boxes issues it (x pass in place: x, y
+    inverse, z inverse, the GPU-noise x pass in two launches when delta + eta exceed
+    SPLIT_MIN_PAIR_BYTES, and host noise adding the z and y forward passes; blocked
+    intermediate: one x launch and one y launch per chunk of xi_chunk_kz columns rounded up to
+    16, then the z inverse)."""
+    fwd = 0 if gpu_noise else 2
+    if xi_chunk_kz > 0:
+        nzh = nz // 2 + 1
+        cols = min((xi_chunk_kz + 15) // 16 * 16, (nzh + 15) // 16 * 16)
+        return fwd + 2 * (-(-nzh // cols)) + 1
     if not gpu_noise:
         return 5
     pair = 2 * 4 * batch * nx * ny * pitch_of(nz)

@@ -66,10 +66,13 @@ def test_xgen_one_launch_equals_split_launches(G, shape):
 def test_blocked_intermediate_x_pass_equals_in_place(G, shape, chunk):
     """The x pass into the blocked intermediate (each mode drawn once, the y pass reading
     contiguous runs), in one chunk or several, gives the same boxes, bit for bit, as the x pass
-    in place: both fields, a batch, delta alone, a velocity component, odd nx, k_z extents that
-    end inside a block, y lines loaded by TMA (2560, 1536) and by cp.async."""
+    in place, with GPU noise and with host noise: both fields, a batch, delta alone, a velocity
+    component, odd nx, k_z extents that end inside a block, y lines loaded by TMA (2560, 1536)
+    and by cp.async."""
     nx, ny, nz = shape
-    for kw in (dict(batch=2), dict(want_eta=False), dict(eta_comp="vz", vel_factor=90.0)):
+    noise = torch.from_numpy(np.random.RandomState(6).normal(size=(nx, ny, nz)).astype(np.float32)).cuda()
+    for kw in (dict(batch=2), dict(want_eta=False), dict(eta_comp="vz", vel_factor=90.0), dict(noise=noise),
+               dict(noise=noise, want_eta=False), dict(noise=noise, eta_comp="xy")):
         ref = G.make_boxes(nx, ny, nz, 2.19, seed=37, xi_chunk_kz=0, **kw)
         got = G.make_boxes(nx, ny, nz, 2.19, seed=37, xi_chunk_kz=chunk, **kw)
         torch.cuda.synchronize()
