@@ -1195,7 +1195,7 @@ struct TileVariant {
     X(0, 512, 4096, 16, 1) X(0, 256, 2560, 32, 1)
 // y pass (line): W = columns per tile
 #define SMK_LINE_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) \
-    X(4, 512, 4096, 16, 1) X(8, 256, 2560, 16, 1)
+    X(4, 512, 4096, 16, 1) X(8, 256, 2560, 16, 1) X(4, 256, 2560, 16, 2)
 // x pass of host noise: W = columns per tile
 #define SMK_X_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(4, 512, 4096, 16, 1)
 // x pass of GPU noise: W = lines per tile (one field per launch: W columns; both fields: W/2 + W/2)
