@@ -156,6 +156,11 @@ int smk_tune_get(int32_t pass, int32_t n);
  * expect 16 bytes more than its copies deliver, with a ~10 ms limit, so each wait runs out; the
  * pass then writes NaN and smk_grf_check reports SMK_ENULLBOX.  Nothing faults or hangs. */
 #define SMK_TUNE_TMA_WAIT_TEST 4
+/* Tile order of the host-noise x pass into the blocked intermediate (xi_chunk_kz > 0): y slot
+ * fastest (0, default: neighbouring tiles fill lines of the intermediate in L2) or k_z column
+ * block fastest (1: neighbouring tiles read neighbouring pieces of the same noise rows).  Same
+ * boxes either way. */
+#define SMK_TUNE_XPI_ORDER 5
 int smk_tune_flag(int32_t flag, int32_t value, int32_t* previous);
 
 /* ---------------------------------------------------------------- skewers (make_spectra +

@@ -247,11 +247,12 @@ __device__ __forceinline__ float warp_sum(float v) {
 }
 
 // ------------------------------------------------------------------ pass 2: binned P1D
-__global__ void __launch_bounds__(FIT_T) fit_p1d_kernel(const FitArgs a) {
+__global__ void __launch_bounds__(FIT_T, 3) fit_p1d_kernel(const FitArgs a) {
     extern __shared__ float2 smem[];
     float2* s1 = smem;
-    float2* s2 = smem + a.mmax;
-    float2* tw = smem + 2 * a.mmax;
+    // with the chirp table the Bluestein transforms need no second buffer
+    float2* s2 = a.chirp ? nullptr : smem + a.mmax;
+    float2* tw = smem + (a.chirp ? 1 : 2) * a.mmax;
     __shared__ double psum[FIT_MAX_BINS];
     __shared__ double psq[FIT_MAX_BINS];
     __shared__ double edges[FIT_MAX_BINS + 1];
@@ -282,6 +283,12 @@ __global__ void __launch_bounds__(FIT_T) fit_p1d_kernel(const FitArgs a) {
             curM = M;
         }
         const float2* Bc = a.chirp && a.chirp_off[N] >= 0 ? a.chirp + a.chirp_off[N] : nullptr;
+        if (!Bc && !s2) {
+            // a length missing from the chirp table (and no room to transform its chirp here)
+            if (threadIdx.x == 0) psum[0] = __longlong_as_double(0x7ff8000000000000LL);
+            __syncthreads();
+            continue;
+        }
         load_pair(a, th, fbar_inv, ps, s1);
         bluestein<false>(s1, s2, tw, N, M, pl, Bc);
         // X1_m = (Z_m + Z*_{N-m})/2, X2_m = (Z_m - Z*_{N-m})/(2i), m = 0..N/2
@@ -313,11 +320,12 @@ __global__ void __launch_bounds__(FIT_T) fit_p1d_kernel(const FitArgs a) {
 }
 
 // ------------------------------------------------------------------ backward
-__global__ void __launch_bounds__(FIT_T) fit_adjoint_kernel(const FitArgs a) {
+__global__ void __launch_bounds__(FIT_T, 3) fit_adjoint_kernel(const FitArgs a) {
     extern __shared__ float2 smem[];
     float2* s1 = smem;
-    float2* s2 = smem + a.mmax;
-    float2* tw = smem + 2 * a.mmax;
+    // with the chirp table the Bluestein transforms need no second buffer
+    float2* s2 = a.chirp ? nullptr : smem + a.mmax;
+    float2* tw = smem + (a.chirp ? 1 : 2) * a.mmax;
     __shared__ double sA[3 * FIT_MAX_BINS], sB[3 * FIT_MAX_BINS], sS;
     __shared__ double edges[FIT_MAX_BINS + 1], gP[FIT_MAX_BINS], gM[FIT_MAX_BINS];
     __shared__ float th[3 * FIT_MAX_BINS];
@@ -353,6 +361,12 @@ __global__ void __launch_bounds__(FIT_T) fit_adjoint_kernel(const FitArgs a) {
             curM = M;
         }
         const float2* Bc = a.chirp && a.chirp_off[N] >= 0 ? a.chirp + a.chirp_off[N] : nullptr;
+        if (!Bc && !s2) {
+            // a length missing from the chirp table (and no room to transform its chirp here)
+            if (threadIdx.x == 0) sS = __longlong_as_double(0x7ff8000000000000LL);
+            __syncthreads();
+            continue;
+        }
         load_pair(a, th, fbar_inv, ps, s1);
         bluestein<false>(s1, s2, tw, N, M, pl, Bc);
         // V_t (Hermitian): V_m = w_m X_m (0<m<N/2), V_{N-m} = conj; V_0, V_{N/2} = 2 Re(w X);
@@ -367,16 +381,14 @@ __global__ void __launch_bounds__(FIT_T) fit_adjoint_kernel(const FitArgs a) {
             if (ps.sid[1] < 0) x2 = make_float2(0.f, 0.f);
             x1 = cscale(x1, wgt);
             x2 = cscale(x2, wgt);
-            // results written to s2 first (s1 still read by other threads)
+            // in place: this thread alone reads and writes the slots m and N - m
             if (m == 0 || 2 * m == N) {
-                s2[m] = make_float2(2.f * x1.x, 2.f * x2.x);
+                s1[m] = make_float2(2.f * x1.x, 2.f * x2.x);
             } else {
-                s2[m] = make_float2(x1.x - x2.y, x1.y + x2.x);          // V1_m + i V2_m
-                s2[N - m] = make_float2(x1.x + x2.y, x2.x - x1.y);      // conj(V1_m) + i conj(V2_m)
+                s1[m] = make_float2(x1.x - x2.y, x1.y + x2.x);          // V1_m + i V2_m
+                s1[N - m] = make_float2(x1.x + x2.y, x2.x - x1.y);      // conj(V1_m) + i conj(V2_m)
             }
         }
-        __syncthreads();
-        for (int n = threadIdx.x; n < N; n += FIT_T) s1[n] = s2[n];
         __syncthreads();
         bluestein<true>(s1, s2, tw, N, M, pl, Bc);
         // per pixel: gF~ = gM_j + gdF / <F>; dF/da = -tau1 F, dF/db = -a tau1 G g F,
@@ -571,7 +583,7 @@ int smk_fit_forward(const SmkFitProblem* fp, const float* theta, double* acc, vo
     const int g1 = (int)std::min<int64_t>((a.n_total + FIT_T * 16 - 1) / (FIT_T * 16), 8LL * nsm);
     fit_flux_kernel<<<std::max(g1, 1), FIT_T, 0, st>>>(a);
     if ((rc = check_launch("fit_flux_kernel"))) return rc;
-    const size_t smem = 3 * (size_t)a.mmax * sizeof(float2);
+    const size_t smem = (a.chirp ? 2 : 3) * (size_t)a.mmax * sizeof(float2);
     int grid = 0;
     if ((rc = fit_grid((const void*)fit_p1d_kernel, smem, a.n_items, &grid))) return rc;
     fit_p1d_kernel<<<grid, FIT_T, smem, st>>>(a);
@@ -590,7 +602,7 @@ int smk_fit_backward(const SmkFitProblem* fp, const float* theta, double* acc, c
     if (cudaMemsetAsync(acc + off, 0, sizeof(double) * (acc_psq(a.nzb, a.nkb) - off), st) != cudaSuccess ||
         cudaMemsetAsync(workspace, 0, 8, st) != cudaSuccess)
         return check_launch("smk_fit_backward: memset");
-    const size_t smem = 3 * (size_t)a.mmax * sizeof(float2);
+    const size_t smem = (a.chirp ? 2 : 3) * (size_t)a.mmax * sizeof(float2);
     int grid = 0;
     if ((rc = fit_grid((const void*)fit_adjoint_kernel, smem, a.n_items, &grid))) return rc;
     fit_adjoint_kernel<<<grid, FIT_T, smem, st>>>(a);

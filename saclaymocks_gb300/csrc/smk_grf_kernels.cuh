@@ -282,9 +282,12 @@ struct XArgs {
     int eta_comp;          // SMK_ETA_*: eta_ij = k_i k_j / k^2 delta_k, or a velocity component
     float vfac;            // velocity: H0 * dD/dz(0)
     // xpi_kernel: the blocked intermediate of XGenArgs (I[0] delta, I[1] eta or null) and the
-    // k_z column blocks [cb0, cb0 + ncb) of this chunk
+    // k_z column blocks [cb0, cb0 + ncb) of this chunk; col_fast: tiles ordered column block
+    // fastest (neighbouring tiles read neighbouring 32-byte pieces of the same rows) instead of
+    // y slot fastest (neighbouring tiles fill lines of the intermediate)
     float2* I[2];
     int cb0, ncb;
+    int col_fast;
 };
 
 // k_i k_j of the eta component (SMK_ETA_*), float32 product as numpy forms kx*ky
@@ -432,10 +435,19 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
     const int64_t nouter = (int64_t)a.batch * a.nx;
     const int64_t estride = (int64_t)a.ny * a.cp;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int yslot = (int)(tile % a.ny);
-        const int64_t r = tile / a.ny;
-        const int kbl = (int)(r % a.ncb);
-        const int64_t b = r / a.ncb;
+        int yslot, kbl;
+        int64_t b;
+        if (a.col_fast) {
+            kbl = (int)(tile % a.ncb);
+            const int64_t r = tile / a.ncb;
+            yslot = (int)(r % a.ny);
+            b = r / a.ny;
+        } else {
+            yslot = (int)(tile % a.ny);
+            const int64_t r = tile / a.ny;
+            kbl = (int)(r % a.ncb);
+            b = r / a.ncb;
+        }
         const int cb = a.cb0 + kbl;
         const int cols = min(WC, a.nzh - cb * WC);
         const float2* pa = a.A + b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)cb * WC;
