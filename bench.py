@@ -458,6 +458,7 @@ def run_ours(args, cfg):
                                           for n, b, m in zip(pass_names, pass_bytes, pass_ms)},
                         "issue": issue, "skewer": sk_roof},
            "host_noise": host_res,
+           "host_noise_ms_per_step": host_res["ms_per_step"] if host_res else None,
            "e2e": {"value": aggregate_value(cells, world, e2e_s), "unit": "cells/s",
                    "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
                    "ms_per_step": e2e_s * 1e3},
