@@ -359,8 +359,6 @@ def run_ours(args, cfg):
     host_res = None
     if not args.no_host_noise and rank == 0:
         noise = torch.randn(nx * ny * nz, dtype=torch.float32, device="cuda").view(nx, ny, nz)
-        if args.xpi_order is not None:
-            _lib.tune_flag(_lib.SMK_TUNE_XPI_ORDER, args.xpi_order)
         hev = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(3)]
         for e in [x for row in hev for x in row]:
             e.record()                          # materialise the raw event handles
@@ -942,8 +940,6 @@ def main():
                     help="GPU-noise x pass into a blocked intermediate, this many k_z columns per chunk "
                          "(0: in place, -1: one chunk)")
     ap.add_argument("--no-precision", action="store_true", help="skip the 1536^3 FP32-vs-FP64 precision leg")
-    ap.add_argument("--xpi-order", type=int, default=None, choices=[0, 1],
-                    help="host-noise x pass into the intermediate: tiles y slot fastest (0) or column block fastest (1)")
     ap.add_argument("--no-fit", action="store_true", help="skip the (a,b,c) fit leg")
     ap.add_argument("--no-host-noise", action="store_true", help="skip the host-noise (5-pass) GRF leg")
     ap.add_argument("--fit-steps", type=int, default=20, help="Adam steps of the fit leg")

@@ -146,8 +146,8 @@ int smk_tune_get(int32_t pass, int32_t n);
  *     launches of one field each (1), or by footprint (-1, default: two launches when the
  *     delta + eta boxes span more than 64 GiB, where one launch's spread of rows outruns
  *     address translation);
- *   SMK_TUNE_PREFETCH: the y and z passes pull their next tile into L2 while transforming the
- *     current one (1, default) or not (0). */
+ *   SMK_TUNE_PREFETCH: the x (host noise, into the intermediate), y and z passes pull their
+ *     next tile into L2 while transforming the current one (1, default) or not (0). */
 #define SMK_TUNE_XGEN_SPLIT 0
 #define SMK_TUNE_PREFETCH 1
 #define SMK_TUNE_TMA 3  /* y pass tiles loaded by TMA tensor copies (1, default), loaded and */
@@ -156,11 +156,6 @@ int smk_tune_get(int32_t pass, int32_t n);
  * expect 16 bytes more than its copies deliver, with a ~10 ms limit, so each wait runs out; the
  * pass then writes NaN and smk_grf_check reports SMK_ENULLBOX.  Nothing faults or hangs. */
 #define SMK_TUNE_TMA_WAIT_TEST 4
-/* Tile order of the host-noise x pass into the blocked intermediate (xi_chunk_kz > 0): y slot
- * fastest (0, default: neighbouring tiles fill lines of the intermediate in L2) or k_z column
- * block fastest (1: neighbouring tiles read neighbouring pieces of the same noise rows).  Same
- * boxes either way. */
-#define SMK_TUNE_XPI_ORDER 5
 int smk_tune_flag(int32_t flag, int32_t value, int32_t* previous);
 
 /* ---------------------------------------------------------------- skewers (make_spectra +

@@ -148,7 +148,7 @@ def load(path: str | None = None):
     return lib
 
 
-SMK_TUNE_XGEN_SPLIT, SMK_TUNE_PREFETCH, SMK_TUNE_TMA, SMK_TUNE_TMA_WAIT_TEST, SMK_TUNE_XPI_ORDER = 0, 1, 3, 4, 5
+SMK_TUNE_XGEN_SPLIT, SMK_TUNE_PREFETCH, SMK_TUNE_TMA, SMK_TUNE_TMA_WAIT_TEST = 0, 1, 3, 4
 
 
 def tune_flag(flag: int, value: int) -> int:

@@ -73,7 +73,6 @@ static std::atomic<int> g_xgen_split{-1};  // -1: by footprint, 0: never, 1: alw
 static std::atomic<int> g_prefetch{1};     // L2 prefetch of the next tile in the y and z passes
 static std::atomic<int> g_tma{1};          // TMA tensor loads of the y pass's tiles
 static std::atomic<int> g_tma_wait_test{0};  // y-pass TMA waits made to run out (failure test)
-static std::atomic<int> g_xpi_order{0};      // host-noise x pass into the intermediate: 0 y slot fastest, 1 column block fastest
 
 static int length_class(int n) { return n <= 512 ? 0 : n <= 1024 ? 1 : n <= 2560 ? 2 : 3; }
 
@@ -412,7 +411,7 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
             const int64_t nouter = (int64_t)p->batch * p->nx;
             xa.I[0] = I0;
             xa.I[1] = p->want_eta ? I0 + nouter * p->ny * xcols : nullptr;
-            xa.col_fast = g_xpi_order.load();
+            xa.prefetch = g_prefetch.load();
             LineArgs yi = staged_y(ya, xa.I, nf, kb, wy, xcols, nouter, p->ny);
             const bool one_chunk = xcols >= nzh;
             for (int64_t c0 = 0; c0 < nzh; c0 += xcols) {
@@ -455,9 +454,6 @@ int smk_tune_flag(int32_t flag, int32_t value, int32_t* previous) {
     if (flag == SMK_TUNE_XGEN_SPLIT) {
         if (value < -1 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: XGEN_SPLIT must be -1, 0 or 1");
         old = g_xgen_split.exchange(value);
-    } else if (flag == SMK_TUNE_XPI_ORDER) {
-        if (value < 0 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: XPI_ORDER must be 0 or 1");
-        old = g_xpi_order.exchange(value);
     } else if (flag == SMK_TUNE_TMA_WAIT_TEST) {
         if (value < 0 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: TMA_WAIT_TEST must be 0 or 1");
         old = g_tma_wait_test.exchange(value);

@@ -282,12 +282,11 @@ struct XArgs {
     int eta_comp;          // SMK_ETA_*: eta_ij = k_i k_j / k^2 delta_k, or a velocity component
     float vfac;            // velocity: H0 * dD/dz(0)
     // xpi_kernel: the blocked intermediate of XGenArgs (I[0] delta, I[1] eta or null) and the
-    // k_z column blocks [cb0, cb0 + ncb) of this chunk; col_fast: tiles ordered column block
-    // fastest (neighbouring tiles read neighbouring 32-byte pieces of the same rows) instead of
-    // y slot fastest (neighbouring tiles fill lines of the intermediate)
+    // k_z column blocks [cb0, cb0 + ncb) of this chunk; prefetch: pull the next tile's rows into
+    // L2 while transforming the current one
     float2* I[2];
     int cb0, ncb;
-    int col_fast;
+    int prefetch;
 };
 
 // k_i k_j of the eta component (SMK_ETA_*), float32 product as numpy forms kx*ky
@@ -435,19 +434,10 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
     const int64_t nouter = (int64_t)a.batch * a.nx;
     const int64_t estride = (int64_t)a.ny * a.cp;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        int yslot, kbl;
-        int64_t b;
-        if (a.col_fast) {
-            kbl = (int)(tile % a.ncb);
-            const int64_t r = tile / a.ncb;
-            yslot = (int)(r % a.ny);
-            b = r / a.ny;
-        } else {
-            yslot = (int)(tile % a.ny);
-            const int64_t r = tile / a.ny;
-            kbl = (int)(r % a.ncb);
-            b = r / a.ncb;
-        }
+        const int yslot = (int)(tile % a.ny);
+        const int64_t r = tile / a.ny;
+        const int kbl = (int)(r % a.ncb);
+        const int64_t b = r / a.ncb;
         const int cb = a.cb0 + kbl;
         const int cols = min(WC, a.nzh - cb * WC);
         const float2* pa = a.A + b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)cb * WC;
@@ -462,6 +452,14 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
         if (threadIdx.x < WC) kt[1 + threadIdx.x] = kaxis(cb * WC + threadIdx.x, 2 * (a.nzh - 1), a.kfac, false);
         cp_async_wait_all();
         __syncthreads();
+        if (a.prefetch && tile + gridDim.x < ntiles) {
+            // the next tile's nx row pieces (one line each) into L2
+            const int64_t tn = tile + gridDim.x;
+            const int64_t rn = tn / a.ny;
+            const float2* pn = a.A + (rn / a.ncb) * (int64_t)a.nx * estride + (int64_t)(tn % a.ny) * a.cp +
+                               (int64_t)(a.cb0 + (int)(rn % a.ncb)) * WC;
+            for (int e = threadIdx.x; e < n; e += T) prefetch_l2(pn + e * estride);
+        }
         if (both)
             fft_tile<false, KB, W, T, C::RMAX>(s, tw, a.pl);
         else
@@ -1207,7 +1205,7 @@ struct TileVariant {
     X(0, 512, 4096, 16, 1) X(0, 256, 2560, 32, 1)
 // y pass (line): W = columns per tile
 #define SMK_LINE_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) \
-    X(4, 512, 4096, 16, 1) X(8, 256, 2560, 16, 1) X(4, 256, 2560, 16, 2)
+    X(4, 512, 4096, 16, 1) X(8, 256, 2560, 16, 1)
 // x pass of host noise: W = columns per tile
 #define SMK_X_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(4, 512, 4096, 16, 1)
 // x pass of GPU noise: W = lines per tile (one field per launch: W columns; both fields: W/2 + W/2)
