@@ -512,6 +512,17 @@ def fit_leg(args, runner, out, table, cfg):
         nt.loss_grad(th0, mz, pk)
     t_adj_nt = (time.perf_counter() - t0) / 3
     del nt
+    # and with the backward transforming every pair again (no stored forward spectra)
+    ns = copy.copy(prob)
+    ns.fp = type(prob.fp).from_buffer_copy(prob.fp)
+    ns.without_spectrum_store()
+    ns.loss_grad(th0, mz, pk)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        ns.loss_grad(th0, mz, pk)
+    t_adj_ns = (time.perf_counter() - t0) / 3
+    del ns
     # finite-difference comparator: central differences, relative step 1e-4, 2 * 30 loss evaluations
     t0 = time.perf_counter()
     g_fd = prob.fd_grad(th0, mz, pk, h=1e-4, points=2)
@@ -521,12 +532,15 @@ def fit_leg(args, runner, out, table, cfg):
     steps = args.fit_steps
     ta, la, sa, _ = fit.adam_fit(prob, th0, mz, pk, steps=steps, lr=0.02, grad="adjoint", eps_rel=1e-2)
     # algorithmic bytes of one gradient: delta + eta (4 B each) + z bin (2 B) per pixel read by the
-    # mean-flux pass, the P1D pass and twice by the adjoint pass (pair load + accumulation)
-    grad_bytes = 4 * 10.0 * prob.n_total
+    # mean-flux pass, the P1D pass and the adjoint pass (accumulation), plus the pair spectra
+    # (N complex per pair of N-pixel skewers: 4 B per pixel) written by the P1D pass and read
+    # back by the adjoint pass
+    grad_bytes = (3 * 10.0 + 2 * 4.0) * prob.n_total
     res = {"params": "10 z bins x (a,b,c)", "pixels": prob.n_total, "adjoint_s_per_grad": t_adj,
            "adjoint_s_per_grad_without_chirp_table": t_adj_nt,
+           "adjoint_s_per_grad_without_spectrum_store": t_adj_ns,
            "adjoint_gbs": grad_bytes / t_adj / 1e9,
-           "adjoint_bytes_basis": "10 B/pixel (delta, eta, z bin) x 4 reads per gradient",
+           "adjoint_bytes_basis": "10 B/pixel (delta, eta, z bin) x 3 reads + 4 B/pixel spectra written and read",
            "fd": "central differences, relative step 1e-4 (60 loss evaluations per gradient)",
            "fd_s_per_grad": t_fd, "grad_speedup": t_fd / t_adj,
            "grad_rel_diff_median": float(np.median(rel)), "grad_rel_diff_max": float(rel.max()),

@@ -129,14 +129,16 @@ int smk_pk_normalisation(int32_t nx, int32_t ny, int32_t nz, double dcell, doubl
  * pass has a table of variants (tile width W and threads per block T, valid up to a line
  * length); smk_tune_set picks the variant used for the lengths of n's class (<=512, <=1024,
  * <=2560, <=4096; v = -1 restores the built-in choice).  Process-wide setting.  The built-in
- * choice is the first variant whose length covers n; for SMK_PASS_ZINV the first such variant
- * with W = 0 (one warp per row pair, as many warps per block as fit, up to T/32). */
+ * choice is a variant compiled for exactly n if there is one, else the first variant whose
+ * length covers n; for SMK_PASS_ZINV the first such variant with W = 0 (one warp per row pair,
+ * as many warps per block as fit, up to T/32). */
 #define SMK_PASS_ZFWD 0  /* r2c along z (host noise)                              */
 #define SMK_PASS_LINE 1  /* c2c along y                                            */
 #define SMK_PASS_XPASS 2 /* x pass of host noise                                   */
 #define SMK_PASS_XGEN 3  /* x pass drawing the GPU noise                           */
 #define SMK_PASS_ZINV 4  /* c2r along z + statistics                               */
 int smk_tune_count(int32_t pass);
+/* n_max < 0: the variant runs the length -n_max only (its FFT plan fixed at compile time). */
 int smk_tune_info(int32_t pass, int32_t variant, int32_t* w, int32_t* threads, int32_t* n_max);
 int smk_tune_set(int32_t pass, int32_t n, int32_t variant);
 int smk_tune_get(int32_t pass, int32_t n);
@@ -293,7 +295,8 @@ int smk_skewers_flux_static(const SmkSkewers* sk, const int32_t* npix_host, cons
  * per-redshift-bin loss L = sum_j (<F>_j - Fbar*_j)^2 + sum_b ((P_b - P*_b)/P*_b)^2 and its
  * exact gradient, so Migrad's finite differences become one adjoint pass.  The reductions run
  * on the GPU (FP64 accumulators); the loss itself is assembled on the host from them.
- * Pixels are recomputed from the fields in every pass, never stored.
+ * Pixels are recomputed from the fields in every pass, never stored (only, optionally, the
+ * forward pass's spectra, for the backward).
  */
 typedef struct {
     const float* delta;     /* [n_total] delta_l + delta_s                                */
@@ -315,6 +318,11 @@ typedef struct {
                               /* chirp, or -1 (then computed in the kernel)                    */
     int32_t n_max;          /* largest npix of the problem (sizes the kernels' shared memory */
                             /* to its Bluestein length); 0: up to 2048                      */
+    float* spectrum;        /* optional [2 n_total] (8-byte aligned): smk_fit_forward stores  */
+                            /* the packed DFT of every pair of skewers there (N complex at  */
+                            /* the pair's first offset) and smk_fit_backward reads it back   */
+                            /* instead of transforming the pair again, so the backward must */
+                            /* follow a forward with the same theta; NULL: recomputed        */
 } SmkFitProblem;
 
 /* Cyclic convolution length of the Bluestein DFT of a length-n skewer: the smallest

@@ -72,7 +72,7 @@ class SmkFitProblem(C.Structure):
                 ("offset", C.c_void_p), ("npix", C.c_void_p), ("order", C.c_void_p),
                 ("n_slots", C.c_int64), ("n_total", C.c_int64), ("nzb", C.c_int32), ("nkb", C.c_int32),
                 ("kedges", C.c_void_p), ("dx", C.c_double), ("chirp", C.c_void_p), ("chirp_off", C.c_void_p),
-                ("n_max", C.c_int32)]
+                ("n_max", C.c_int32), ("spectrum", C.c_void_p)]
 
 
 # (name, restype, argtypes) of every exported entry point

@@ -45,7 +45,7 @@ struct FftPlan {
 // rmax 8: 8s, then 4s / 2.  3s and 5s follow.
 // Returns false unless 2 <= n <= FFT_MAX_N and n = 2^a 3^b 5^c.
 // mid: a three-stage plan (R, R, x) becomes (R, x, R) (the warp z pass's conflict-free order).
-__host__ __device__ inline bool make_plan(int n, FftPlan* p, int rmax = 16, bool mid = false) {
+__host__ __device__ constexpr bool make_plan(int n, FftPlan* p, int rmax = 16, bool mid = false) {
     if (n < 2 || n > FFT_MAX_N) return false;
     int m = n, p2 = 0, p3 = 0, p5 = 0;
     while (m % 2 == 0) { m /= 2; ++p2; }
@@ -55,7 +55,7 @@ __host__ __device__ inline bool make_plan(int n, FftPlan* p, int rmax = 16, bool
     // rmax >= 16: radix-16 stages (a radix-32 one when one factor 2 is left over and
     // rmax >= 32), then 8, 4 or 2 for the rest of the power of two; rmax 8: 8s, then 4s / 2.
     // 3s and 5s follow.
-    int rad[32], nr = 0;
+    int rad[32] = {}, nr = 0;
     if (rmax >= 16) {
         while (p2 >= 4) { rad[nr++] = 16; p2 -= 4; }
         if (p2 == 1 && nr > 0 && rmax >= 32) {
@@ -95,6 +95,26 @@ __host__ __device__ inline bool make_plan(int n, FftPlan* p, int rmax = 16, bool
     }
     for (int s = nr; s < FFT_MAX_STAGES; ++s) p->twoff[s] = tw;
     p->twn = tw;
+    return true;
+}
+
+// The plan of a length fixed at compile time (FixedPlan<n, rmax>::P.r[st] etc. are constants).
+template <int N, int RMAX, bool MID = false>
+struct FixedPlan {
+    __host__ __device__ static constexpr FftPlan make() {
+        FftPlan p{};
+        make_plan(N, &p, RMAX, MID);
+        return p;
+    }
+    static constexpr FftPlan P = make();
+    static_assert(P.n == N, "FixedPlan: length not supported by the engine");
+};
+
+// True when two plans have the same stages (the tables of one serve the other).
+__host__ __device__ inline bool same_plan(const FftPlan& a, const FftPlan& b) {
+    if (a.n != b.n || a.nst != b.nst) return false;
+    for (int s = 0; s < a.nst; ++s)
+        if (a.r[s] != b.r[s]) return false;
     return true;
 }
 
@@ -340,17 +360,32 @@ struct NoOut {
 struct NoPre {
     __device__ __forceinline__ float2 operator()(int, int, float2 v) const { return v; }
 };
-template <int R, bool INV, int W, int SN, int T, bool OUT = false, bool PRE = false, class Out = NoOut,
-          class Pre = NoPre>
-__device__ __forceinline__ void fft_stage(float2* __restrict__ s, const float2* __restrict__ tw,
-                                          const FftPlan& pl, const int st, Out&& out = Out{}, Pre&& pre = Pre{}) {
-    const int m = pl.m[st];
-    const int nb = (pl.n / R) * W;
-    const float2* tws = tw + pl.twoff[st] - 1;
+// Stage geometry: from the plan at run time (RtStage), or compile-time constants (CtStage: the
+// strides become immediate offsets and the block division a constant one).  Both give the same
+// butterflies in the same order, so the results are identical.
+struct RtStage {
+    int m, n, twoff;
+    uint32_t magic;
+    __device__ __forceinline__ RtStage(const FftPlan& pl, int st)
+        : m(pl.m[st]), n(pl.n), twoff(pl.twoff[st]), magic(pl.magic[st]) {}
+    __device__ __forceinline__ int div(int x) const { return m == 1 ? x : (int)__umulhi((unsigned)x, magic); }
+};
+template <int M, int N, int TWOFF>
+struct CtStage {
+    static constexpr int m = M, n = N, twoff = TWOFF;
+    __device__ __forceinline__ static int div(int x) { return M == 1 ? x : x / M; }
+};
+
+template <int R, bool INV, int W, int SN, int T, bool OUT, bool PRE, class SP, class Out, class Pre>
+__device__ __forceinline__ void fft_stage_body(float2* __restrict__ s, const float2* __restrict__ tw, const SP& sp,
+                                               Out&& out, Pre&& pre) {
+    const int m = sp.m;
+    const int nb = (sp.n / R) * W;
+    const float2* tws = tw + sp.twoff - 1;
 #pragma unroll(T >= 1024 ? 1 : 2)
     for (int bf = threadIdx.x; bf < nb; bf += T) {
         const int j = bf / W, w = bf % W;
-        const int blk = div_m(pl, st, j);
+        const int blk = sp.div(j);
         const int q = j - blk * m;
         float2* p = s + (blk * R * m + q) * SN + w;
         float2 v[R];
@@ -386,6 +421,24 @@ __device__ __forceinline__ void fft_stage(float2* __restrict__ s, const float2* 
     if constexpr (!OUT) __syncthreads();
 }
 
+template <int R, bool INV, int W, int SN, int T, bool OUT = false, bool PRE = false, class Out = NoOut,
+          class Pre = NoPre>
+__device__ __forceinline__ void fft_stage(float2* __restrict__ s, const float2* __restrict__ tw,
+                                          const FftPlan& pl, const int st, Out&& out = Out{}, Pre&& pre = Pre{}) {
+    fft_stage_body<R, INV, W, SN, T, OUT, PRE>(s, tw, RtStage(pl, st), out, pre);
+}
+
+// Stage st of the compile-time plan of length NF.
+template <int NF, int RMAX, int ST, bool INV, int W, int SN, int T, bool OUT = false, bool PRE = false,
+          class Out = NoOut, class Pre = NoPre>
+__device__ __forceinline__ void fft_stage_fixed(float2* __restrict__ s, const float2* __restrict__ tw,
+                                                Out&& out = Out{}, Pre&& pre = Pre{}) {
+    using FP = FixedPlan<NF, RMAX>;
+    constexpr int R = FP::P.r[ST];
+    static_assert(R <= RMAX, "fixed plan radix above the kernel's");
+    fft_stage_body<R, INV, W, SN, T, OUT, PRE>(s, tw, CtStage<FP::P.m[ST], NF, FP::P.twoff[ST]>{}, out, pre);
+}
+
 template <bool INV, int W, int SN, int T, int RMAX, bool OUT = false, bool PRE = false, class Out = NoOut,
           class Pre = NoPre>
 __device__ __forceinline__ void fft_stage_any(float2* s, const float2* tw, const FftPlan& pl, int st,
@@ -416,10 +469,16 @@ __device__ __forceinline__ void fft_stage_any(float2* s, const float2* tw, const
 // (fill_stage_twiddles).  The caller synchronises after filling s; on
 // return the block is synchronised.  The plan's radices must be <= RMAX (plan_fits; the
 // launchers check it), larger radices are not compiled into the kernel.
-template <bool INV, int W, int SN, int T, int RMAX = fft_max_radix(T)>
+template <bool INV, int W, int SN, int T, int RMAX = fft_max_radix(T), int NF = 0>
 __device__ __forceinline__ void fft_tile(float2* __restrict__ s, const float2* __restrict__ tw,
                                          const FftPlan& pl) {
-    if (!INV) {
+    if constexpr (NF > 0) {
+        constexpr int NST = FixedPlan<NF, RMAX>::P.nst;
+        static_for<0, NST>([&](auto c) {
+            constexpr int st = INV ? NST - 1 - decltype(c)::value : decltype(c)::value;
+            fft_stage_fixed<NF, RMAX, st, INV, W, SN, T>(s, tw);
+        });
+    } else if (!INV) {
         for (int st = 0; st < pl.nst; ++st) fft_stage_any<false, W, SN, T, RMAX>(s, tw, pl, st);
     } else {
         for (int st = pl.nst - 1; st >= 0; --st) fft_stage_any<true, W, SN, T, RMAX>(s, tw, pl, st);
@@ -429,24 +488,19 @@ __device__ __forceinline__ void fft_tile(float2* __restrict__ s, const float2* _
 // Inverse of the W lines with the last stage's natural-order results handed to out(e, w, v)
 // (element e of line w) instead of written back: every stage but the last ends with a block
 // barrier; the caller synchronises before it reuses s.
-template <int W, int SN, int T, int RMAX, class Out>
+template <int W, int SN, int T, int RMAX, int NF = 0, class Out>
 __device__ __forceinline__ void ifft_tile_out(float2* __restrict__ s, const float2* __restrict__ tw,
                                               const FftPlan& pl, Out&& out) {
-    for (int st = pl.nst - 1; st >= 1; --st) fft_stage_any<true, W, SN, T, RMAX>(s, tw, pl, st);
-    fft_stage_any<true, W, SN, T, RMAX, true>(s, tw, pl, 0, out);
-}
-
-// The same with pre(e, w, v) applied to every input value as the first stage loads it.
-template <int W, int SN, int T, int RMAX, class Pre, class Out>
-__device__ __forceinline__ void ifft_tile_pre_out(float2* __restrict__ s, const float2* __restrict__ tw,
-                                                  const FftPlan& pl, Pre&& pre, Out&& out) {
-    if (pl.nst == 1) {
-        fft_stage_any<true, W, SN, T, RMAX, true, true>(s, tw, pl, 0, out, pre);
-        return;
+    if constexpr (NF > 0) {
+        constexpr int NST = FixedPlan<NF, RMAX>::P.nst;
+        static_for<0, NST - 1>([&](auto c) {
+            fft_stage_fixed<NF, RMAX, NST - 1 - decltype(c)::value, true, W, SN, T>(s, tw);
+        });
+        fft_stage_fixed<NF, RMAX, 0, true, W, SN, T, true>(s, tw, out);
+    } else {
+        for (int st = pl.nst - 1; st >= 1; --st) fft_stage_any<true, W, SN, T, RMAX>(s, tw, pl, st);
+        fft_stage_any<true, W, SN, T, RMAX, true>(s, tw, pl, 0, out);
     }
-    fft_stage_any<true, W, SN, T, RMAX, false, true>(s, tw, pl, pl.nst - 1, NoOut{}, pre);
-    for (int st = pl.nst - 2; st >= 1; --st) fft_stage_any<true, W, SN, T, RMAX>(s, tw, pl, st);
-    fft_stage_any<true, W, SN, T, RMAX, true>(s, tw, pl, 0, out);
 }
 
 // Per-stage twiddle tables of the plan (FftPlan::twoff; fewer than n entries), filled by the

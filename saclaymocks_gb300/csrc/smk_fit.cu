@@ -9,8 +9,9 @@
 //   fit_flux_kernel     F per pixel -> sum F per z bin and over all pixels (FP64)
 //   fit_p1d_kernel      per pair of equal-length skewers: dF, length-N DFT by Bluestein's chirp
 //                       transform on the FFT engine, |X_m|^2 dx/N binned in log-k (FP64)
-//   fit_adjoint_kernel  per pair: recompute X, back-propagate the P1D weights through the
-//                       inverse DFT (Bluestein again), then accumulate per bin
+//   fit_adjoint_kernel  per pair: X (read back from the forward's store, or recomputed),
+//                       back-propagate the P1D weights through the inverse DFT (Bluestein
+//                       again), then accumulate per bin
 //                       A_j = sum (gM_j + gdF/<F>) dF/dtheta_j, B_j = sum dF/dtheta_j and
 //                       S = sum gdF * F, so that dL/dtheta_j = A_j - S B_j / (n <F>^2)
 //                       (the coupling through the global mean <F> needs no second pass).
@@ -45,6 +46,8 @@ struct FitArgs {
     int mmax;              // largest Bluestein length of the problem: smem = s1 | s2 | tw of mmax each
     const float2* chirp;   // optional: FFT_M of the forward chirp of every length N, digit-reversed
     const int64_t* chirp_off;  // [FFT_MAX_N / 2 + 1]: offset (complex) of length N in chirp, or -1
+    float2* spec;          // optional: the forward stores each pair's DFT at its first offset,
+                           // the backward reads it back (no second forward transform)
 };
 
 // accumulator layout (doubles)
@@ -291,6 +294,10 @@ __global__ void __launch_bounds__(FIT_T, 3) fit_p1d_kernel(const FitArgs a) {
         }
         load_pair(a, th, fbar_inv, ps, s1);
         bluestein<false>(s1, s2, tw, N, M, pl, Bc);
+        if (a.spec) {   // the packed spectrum Z for the backward (s1 is only read below)
+            float2* z = a.spec + ps.off[0];
+            for (int m = threadIdx.x; m < N; m += FIT_T) z[m] = s1[m];
+        }
         // X1_m = (Z_m + Z*_{N-m})/2, X2_m = (Z_m - Z*_{N-m})/(2i), m = 0..N/2
         const float norm = (float)(a.dx / (double)N);
         const int half = N / 2;
@@ -340,8 +347,8 @@ __global__ void __launch_bounds__(FIT_T, 3) fit_adjoint_kernel(const FitArgs a) 
     for (int i = threadIdx.x; i < a.nkb; i += FIT_T) gP[i] = a.gP[i];
     for (int i = threadIdx.x; i < a.nzb; i += FIT_T) gM[i] = a.gM[i];
     if (threadIdx.x == 0) sS = 0.0;
-    const double fbar = a.acc[acc_ftot(a.nzb)] / (double)a.n_total;
-    const float fbar_inv = (float)(1.0 / fbar);
+    // the same FP32 1/<F> as the forward pass (the stored spectra were made with it)
+    const float fbar_inv = (float)((double)a.n_total / a.acc[acc_ftot(a.nzb)]);
     const double kfac = 2.0 * (3.14159265358979323846 / a.dx);
     __shared__ FftPlan pl;
     int curM = 0;
@@ -367,8 +374,14 @@ __global__ void __launch_bounds__(FIT_T, 3) fit_adjoint_kernel(const FitArgs a) 
             __syncthreads();
             continue;
         }
-        load_pair(a, th, fbar_inv, ps, s1);
-        bluestein<false>(s1, s2, tw, N, M, pl, Bc);
+        if (a.spec) {   // Z as the forward pass with the same theta left it
+            const float2* z = a.spec + ps.off[0];
+            for (int m = threadIdx.x; m < N; m += FIT_T) s1[m] = z[m];
+            __syncthreads();
+        } else {
+            load_pair(a, th, fbar_inv, ps, s1);
+            bluestein<false>(s1, s2, tw, N, M, pl, Bc);
+        }
         // V_t (Hermitian): V_m = w_m X_m (0<m<N/2), V_{N-m} = conj; V_0, V_{N/2} = 2 Re(w X);
         // packed W = V_1 + i V_2; the unnormalised inverse DFT of W is gdF_1 + i gdF_2.
         const float norm = (float)(a.dx / (double)N);
@@ -564,6 +577,8 @@ static int fit_args(const SmkFitProblem* fp, const float* theta, double* acc, co
     a->chirp = reinterpret_cast<const float2*>(fp->chirp);
     a->chirp_off = fp->chirp_off;
     if (!a->chirp != !a->chirp_off) return fail(SMK_EINVAL, "smk_fit: give chirp and chirp_off together");
+    a->spec = reinterpret_cast<float2*>(fp->spectrum);
+    if ((uintptr_t)a->spec & 7) return fail(SMK_EINVAL, "smk_fit: spectrum must be 8-byte aligned");
     return SMK_OK;
 }
 

@@ -102,14 +102,17 @@ int variant_for(int pass, int n) {
     const TileVariant* t = variant_table(pass);
     const int cnt = variant_count(pass);
     const int c = g_choice[pass][length_class(n)].load();
-    if (c >= 0 && c < cnt && t[c].nmax >= n) return c;
-    // built-in choice: the z inverse prefers the one-warp-per-row-pair engine (W = 0), every
-    // pass otherwise the first variant whose line length covers n
+    if (c >= 0 && c < cnt && variant_fits(t[c], n)) return c;
+    // built-in choice: a variant compiled for exactly this length, else the z inverse prefers
+    // the one-warp-per-row-pair engine (W = 0), every pass otherwise the first variant whose
+    // line length covers n
+    for (int i = 0; i < cnt; ++i)
+        if (t[i].nmax == -n) return i;
     if (pass == PASS_ZINV)
         for (int i = 0; i < cnt; ++i)
-            if (t[i].w == 0 && t[i].nmax >= n) return i;
+            if (t[i].w == 0 && variant_fits(t[i], n)) return i;
     for (int i = 0; i < cnt; ++i)
-        if (t[i].nmax >= n) return i;
+        if (variant_fits(t[i], n)) return i;
     return cnt - 1;
 }
 
@@ -484,7 +487,7 @@ int smk_tune_info(int32_t pass, int32_t v, int32_t* w, int32_t* t, int32_t* nmax
 int smk_tune_set(int32_t pass, int32_t n, int32_t v) {
     const TileVariant* tab = variant_table(pass);
     if (!tab || n < 2 || n > FFT_MAX_N) return fail(SMK_EINVAL, "smk_tune_set: bad pass or length");
-    if (v >= variant_count(pass) || (v >= 0 && tab[v].nmax < n))
+    if (v >= variant_count(pass) || (v >= 0 && !variant_fits(tab[v], n)))
         return fail(SMK_EINVAL, "smk_tune_set: variant %d cannot run length %d", v, n);
     g_choice[pass][length_class(n)].store(v < 0 ? -1 : v);
     return SMK_OK;

@@ -25,11 +25,19 @@ namespace smk {
 namespace cg = cooperative_groups;
 
 // W lines (or row pairs) per tile, T threads, largest FFT radix R in registers, at least B
-// resident blocks per SM requested from the register allocator.
-template <int W_, int T_, int R_ = fft_max_radix(T_), int B_ = 1>
+// resident blocks per SM requested from the register allocator; F > 0: the line length is F and
+// the FFT plan is a compile-time constant (FixedPlan<F, R>), else the plan is read at run time.
+template <int W_, int T_, int R_ = fft_max_radix(T_), int B_ = 1, int F_ = 0>
 struct TileCfg {
-    static constexpr int W = W_, T = T_, RMAX = R_, MINB = B_;
+    static constexpr int W = W_, T = T_, RMAX = R_, MINB = B_, NF = F_;
 };
+
+// The launch's plan is the one a fixed-length variant was compiled for (always true otherwise).
+template <class C>
+inline bool fixed_plan_ok(const FftPlan& pl) {
+    if constexpr (C::NF > 0) return same_plan(pl, FixedPlan<C::NF, C::RMAX>::P);
+    else return true;
+}
 
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
@@ -105,7 +113,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) zfwd_kernel(const ZFwdArgs a) {
         }
         cp_async_wait_all();
         __syncthreads();
-        fft_tile<false, W, SN, T, C::RMAX>(s, tw, a.pl);
+        fft_tile<false, W, SN, T, C::RMAX, C::NF>(s, tw, a.pl);
         // split the two real transforms packed as re/im and store the half spectra
         for (int idx = threadIdx.x; idx < W * nh; idx += T) {
             const int k = idx / W, w = idx % W;
@@ -241,7 +249,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
         if (INV && a.tma == 2) {
             // transform in shared memory, then TMA tensor stores of the tile (columns past ncol
             // are not written); the next load waits until these stores have read s
-            fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
+            fft_tile<true, W, W, T, C::RMAX, C::NF>(s, tw, a.pl);
             fence_proxy_async_smem();
             __syncthreads();
             if (threadIdx.x == 0) {
@@ -251,11 +259,11 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
         } else if constexpr (INV) {
             // the last stage stores straight from registers
             const int64_t es = a.estride;
-            ifft_tile_out<W, W, T, C::RMAX>(s, tw, a.pl, [&](int e, int w, float2 v) {
+            ifft_tile_out<W, W, T, C::RMAX, C::NF>(s, tw, a.pl, [&](int e, int w, float2 v) {
                 if (w < cols) base[e * es + w] = v;
             });
         } else {
-            fft_tile<INV, W, W, T, C::RMAX>(s, tw, a.pl);
+            fft_tile<INV, W, W, T, C::RMAX, C::NF>(s, tw, a.pl);
             store_cols<W, T>(s, base, n, a.estride, cols);
         }
         if (a.tma) fence_proxy_async_smem();   // this tile's shared accesses before the next TMA writes
@@ -360,7 +368,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpass_kernel(const XArgs a) {
         if (threadIdx.x < W) kt[1 + threadIdx.x] = kaxis(cb * W + threadIdx.x, 2 * (a.nzh - 1), a.kfac, false);
         cp_async_wait_all();
         __syncthreads();
-        fft_tile<false, W, W, T, C::RMAX>(s, tw, a.pl);
+        fft_tile<false, W, W, T, C::RMAX, C::NF>(s, tw, a.pl);
         const float ky = kt[0];
         for (int idx = threadIdx.x; idx < n * W; idx += T) {
             const int e = idx / W, w = idx % W;
@@ -384,7 +392,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpass_kernel(const XArgs a) {
             }
         }
         __syncthreads();
-        fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
+        fft_tile<true, W, W, T, C::RMAX, C::NF>(s, tw, a.pl);
         store_cols<W, T>(s, pa, n, estride, cols);
         __syncthreads();
         if (pb) {
@@ -394,7 +402,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpass_kernel(const XArgs a) {
                 s[idx] = w < cols ? __ldcg(pb + e * estride + w) : make_float2(0.f, 0.f);
             }
             __syncthreads();
-            fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
+            fft_tile<true, W, W, T, C::RMAX, C::NF>(s, tw, a.pl);
             store_cols<W, T>(s, pb, n, estride, cols);
             __syncthreads();
         }
@@ -461,9 +469,9 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
             for (int e = threadIdx.x; e < n; e += T) prefetch_l2(pn + e * estride);
         }
         if (both)
-            fft_tile<false, KB, W, T, C::RMAX>(s, tw, a.pl);
+            fft_tile<false, KB, W, T, C::RMAX, C::NF>(s, tw, a.pl);
         else
-            fft_tile<false, W, W, T, C::RMAX>(s, tw, a.pl);
+            fft_tile<false, W, W, T, C::RMAX, C::NF>(s, tw, a.pl);
         const float ky = kt[0];
         for (int idx = threadIdx.x; idx < n * WC; idx += T) {
             const int e = idx / WC, w = idx % WC;
@@ -491,7 +499,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
         float2* d0 = a.I[0] + row0 * WC;
         float2* d1 = both ? a.I[1] + row0 * WC : nullptr;
         const int64_t es = (int64_t)a.ny * WC;
-        ifft_tile_out<W, W, T, C::RMAX>(s, tw, a.pl, [&](int e, int w, float2 v) {
+        ifft_tile_out<W, W, T, C::RMAX, C::NF>(s, tw, a.pl, [&](int e, int w, float2 v) {
             const int f = both && w >= WC;
             const int c = w - f * WC;
             if (c < cols) (f ? d1 : d0)[e * es + c] = v;
@@ -707,11 +715,11 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
         if constexpr (ONE) {
             // the last stage stores straight from registers
             float2* dst = (a.fields == XGEN_DELTA ? a.A : a.B) + off;
-            ifft_tile_out<W, W, T, C::RMAX>(s, tw, a.pl, [&](int e, int w, float2 v) {
+            ifft_tile_out<W, W, T, C::RMAX, C::NF>(s, tw, a.pl, [&](int e, int w, float2 v) {
                 if (w < cols) dst[e * estride + w] = v;
             });
         } else {
-            fft_tile<true, W, W, T, C::RMAX>(s, tw, a.pl);
+            fft_tile<true, W, W, T, C::RMAX, C::NF>(s, tw, a.pl);
             for (int idx = threadIdx.x; idx < n * W; idx += T) {
                 const int e = idx / W, l = idx % W;
                 const int c = l < WC ? l : l - WC;
@@ -796,7 +804,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
         float2* d0 = a.I[0] + row0 * WC;
         float2* d1 = both ? a.I[1] + row0 * WC : nullptr;
         const int64_t es = (int64_t)a.ny * WC;
-        ifft_tile_out<W, W, T, C::RMAX>(s, tw, a.pl, [&](int e, int w, float2 v) {
+        ifft_tile_out<W, W, T, C::RMAX, C::NF>(s, tw, a.pl, [&](int e, int w, float2 v) {
             const int f = both && w >= WC;
             const int c = w - f * WC;
             if (c < cols) (f ? d1 : d0)[e * es + c] = v;
@@ -1079,6 +1087,7 @@ static size_t zpass_smem(int n) {
 template <class C>
 static int launch_zfwd(ZFwdArgs a, int64_t rows_per_box, cudaStream_t st) {
     if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "zfwd_kernel");
+    if (!fixed_plan_ok<C>(a.pl)) return fail(SMK_EINVAL, "%s: length %d is not the variant's fixed length", "zfwd_kernel", a.pl.n);
     a.zt.init(rows_per_box, C::W);
     const size_t smem = zpass_smem<C>(a.pl.n);
     const int64_t ntiles = a.zt.tiles_per_box * a.batch;
@@ -1093,6 +1102,7 @@ static int launch_zfwd(ZFwdArgs a, int64_t rows_per_box, cudaStream_t st) {
 template <class C>
 static int launch_zinvw(ZInvArgs a, int64_t rows_per_box, cudaStream_t st) {
     if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "zinvw_kernel");
+    if (!fixed_plan_ok<C>(a.pl)) return fail(SMK_EINVAL, "%s: length %d is not the variant's fixed length", "zinvw_kernel", a.pl.n);
     a.zt.rows_per_box = rows_per_box;
     a.zt.tiles_per_box = 0;
     // layout: XOR swizzle with the odd radix mid-plan, except power-of-two lengths >= 2048
@@ -1127,6 +1137,7 @@ static int launch_zinv(ZInvArgs a, int64_t rows_per_box, cudaStream_t st) {
 template <class C>
 static int launch_line(const LineArgs& a, bool inv, cudaStream_t st) {
     if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "line_kernel");
+    if (!fixed_plan_ok<C>(a.pl)) return fail(SMK_EINVAL, "%s: length %d is not the variant's fixed length", "line_kernel", a.pl.n);
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2);
     const int64_t ntiles = a.n_outer * ceil_div(a.ncol, C::W) * a.nbuf;
     int grid = 0, rc;
@@ -1143,6 +1154,7 @@ static int launch_line(const LineArgs& a, bool inv, cudaStream_t st) {
 template <class C>
 static int launch_xpass(const XArgs& a, cudaStream_t st) {
     if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xpass_kernel");
+    if (!fixed_plan_ok<C>(a.pl)) return fail(SMK_EINVAL, "%s: length %d is not the variant's fixed length", "xpass_kernel", a.pl.n);
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 + (C::W + 1) * 4;
     const int64_t ntiles = (int64_t)a.batch * a.ny * ceil_div(a.nzh, C::W);
     int grid = 0, rc;
@@ -1154,6 +1166,7 @@ static int launch_xpass(const XArgs& a, cudaStream_t st) {
 template <class C>
 static int launch_xpi(const XArgs& a, cudaStream_t st) {
     if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xpi_kernel");
+    if (!fixed_plan_ok<C>(a.pl)) return fail(SMK_EINVAL, "%s: length %d is not the variant's fixed length", "xpi_kernel", a.pl.n);
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 + (C::W + 1) * 4;
     const int64_t ntiles = (int64_t)a.batch * a.ncb * a.ny;
     int grid = 0, rc;
@@ -1165,6 +1178,7 @@ static int launch_xpi(const XArgs& a, cudaStream_t st) {
 template <class C>
 static int launch_xgi(const XGenArgs& a, cudaStream_t st) {
     if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xgi_kernel");
+    if (!fixed_plan_ok<C>(a.pl)) return fail(SMK_EINVAL, "%s: length %d is not the variant's fixed length", "xgi_kernel", a.pl.n);
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 +
                         (size_t)a.nzh * 4 + 16;
     const int64_t ntiles = (int64_t)a.batch * a.ncb * a.ny;
@@ -1177,6 +1191,7 @@ static int launch_xgi(const XGenArgs& a, cudaStream_t st) {
 template <class C>
 static int launch_xgen(const XGenArgs& a, cudaStream_t st) {
     if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "xgen_kernel");
+    if (!fixed_plan_ok<C>(a.pl)) return fail(SMK_EINVAL, "%s: length %d is not the variant's fixed length", "xgen_kernel", a.pl.n);
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 +
                         (size_t)a.nzh * 4 + 16;
     const bool one = a.fields != XGEN_BOTH;
@@ -1195,8 +1210,12 @@ static int launch_xgen(const XGenArgs& a, cudaStream_t st) {
 // ------------------------------------------------------------------ tile variants
 struct TileVariant {
     int w, t, nmax;  // columns (line pairs for z passes, lines for xgen) per tile, threads, max length
+                     // (nmax < 0: the length -nmax only, with its FFT plan fixed at compile time)
     int rmax, minb;  // largest FFT radix, requested resident blocks per SM
 };
+// TileCfg's fixed length of a table entry
+#define SMK_NFIX(N) ((N) < 0 ? -(N) : 0)
+inline bool variant_fits(const TileVariant& v, int n) { return v.nmax < 0 ? n == -v.nmax : v.nmax >= n; }
 // r2c along z of host noise (zfwd): W = row pairs per tile
 #define SMK_Z_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(4, 512, 2560, 16, 1) \
     X(2, 128, 2560, 16, 4) X(4, 512, 4096, 16, 1)
@@ -1205,12 +1224,13 @@ struct TileVariant {
     X(0, 512, 4096, 16, 1) X(0, 256, 2560, 32, 1)
 // y pass (line): W = columns per tile
 #define SMK_LINE_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) \
-    X(4, 512, 4096, 16, 1) X(8, 256, 2560, 16, 1)
+    X(4, 512, 4096, 16, 1) X(8, 256, 2560, 16, 1) X(8, 512, -2560, 16, 1)
 // x pass of host noise: W = columns per tile
-#define SMK_X_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(4, 512, 4096, 16, 1)
+#define SMK_X_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(4, 512, 4096, 16, 1) \
+    X(8, 512, -2560, 16, 1)
 // x pass of GPU noise: W = lines per tile (one field per launch: W columns; both fields: W/2 + W/2)
 #define SMK_XGEN_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) \
-    X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1)
+    X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1) X(8, 512, -2560, 16, 1)
 
 enum { PASS_ZFWD = 0, PASS_LINE = 1, PASS_XPASS = 2, PASS_XGEN = 3, PASS_ZINV = 4, NPASS = 5 };
 

@@ -6,7 +6,7 @@ namespace smk {
 int run_line(int v, const LineArgs& a, bool inv, cudaStream_t st) {
     int i = 0;
 #define X(W, T, N, R, B) \
-    if (v == i++) return launch_line<TileCfg<W, T, R, B>>(a, inv, st);
+    if (v == i++) return launch_line<TileCfg<W, T, R, B, SMK_NFIX(N)>>(a, inv, st);
     SMK_LINE_VARIANTS(X)
 #undef X
     return fail(SMK_EINVAL, "line: no tile variant %d", v);

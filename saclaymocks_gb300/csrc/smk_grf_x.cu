@@ -6,7 +6,7 @@ namespace smk {
 int run_xgen(int v, const XGenArgs& a, cudaStream_t st) {
     int i = 0;
 #define X(W, T, N, R, B) \
-    if (v == i++) return launch_xgen<TileCfg<W, T, R, B>>(a, st);
+    if (v == i++) return launch_xgen<TileCfg<W, T, R, B, SMK_NFIX(N)>>(a, st);
     SMK_XGEN_VARIANTS(X)
 #undef X
     return fail(SMK_EINVAL, "xgen: no tile variant %d", v);
@@ -15,7 +15,7 @@ int run_xgen(int v, const XGenArgs& a, cudaStream_t st) {
 int run_xgi(int v, const XGenArgs& a, cudaStream_t st) {
     int i = 0;
 #define X(W, T, N, R, B) \
-    if (v == i++) return launch_xgi<TileCfg<W, T, R, B>>(a, st);
+    if (v == i++) return launch_xgi<TileCfg<W, T, R, B, SMK_NFIX(N)>>(a, st);
     SMK_XGEN_VARIANTS(X)
 #undef X
     return fail(SMK_EINVAL, "xgi: no tile variant %d", v);

@@ -6,7 +6,7 @@ namespace smk {
 int run_xpass(int v, const XArgs& a, cudaStream_t st) {
     int i = 0;
 #define X(W, T, N, R, B) \
-    if (v == i++) return launch_xpass<TileCfg<W, T, R, B>>(a, st);
+    if (v == i++) return launch_xpass<TileCfg<W, T, R, B, SMK_NFIX(N)>>(a, st);
     SMK_X_VARIANTS(X)
 #undef X
     return fail(SMK_EINVAL, "xpass: no tile variant %d", v);
@@ -15,7 +15,7 @@ int run_xpass(int v, const XArgs& a, cudaStream_t st) {
 int run_xpi(int v, const XArgs& a, cudaStream_t st) {
     int i = 0;
 #define X(W, T, N, R, B) \
-    if (v == i++) return launch_xpi<TileCfg<W, T, R, B>>(a, st);
+    if (v == i++) return launch_xpi<TileCfg<W, T, R, B, SMK_NFIX(N)>>(a, st);
     SMK_X_VARIANTS(X)
 #undef X
     return fail(SMK_EINVAL, "xpi: no tile variant %d", v);

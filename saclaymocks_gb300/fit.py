@@ -37,7 +37,7 @@ class FitProblem:
     """Fixed fields of the fit on the GPU: per-pixel delta (= delta_l + delta_s), eta_par,
     growth G and redshift, skewer lengths (packed layout), z and log-k bin edges."""
 
-    def __init__(self, delta, eta, G, z, lengths, zedges, kedges, dx=0.2, device="cuda"):
+    def __init__(self, delta, eta, G, z, lengths, zedges, kedges, dx=0.2, device="cuda", store_spectrum=True):
         dv = torch.device(device)
         self.device = dv
         to_dev = lambda x, dt: None if x is None else torch.as_tensor(x).to(device=dv, dtype=dt).contiguous()  # noqa: E731
@@ -98,11 +98,23 @@ class FitProblem:
             n_slots=ns.value, n_total=self.n_total, nzb=self.nzb, nkb=self.nkb,
             kedges=self.d_kedges.data_ptr(), dx=self.dx, chirp=self.chirp.data_ptr(),
             chirp_off=self.d_chirp_off.data_ptr(), n_max=int(self.lengths.max()))
+        # the forward pass's pair spectra (8 B per pixel), read back by the backward of the same
+        # theta instead of a second forward transform
+        self.spec = torch.empty(2 * self.n_total, dtype=torch.float32, device=dv) if store_spectrum else None
+        self.fp.spectrum = self.spec.data_ptr() if store_spectrum else None
+        self._spec_theta = None
 
     def without_chirp_table(self):
         """Let the kernels compute the chirp spectra themselves (the form without the table)."""
         self.fp.chirp = None
         self.fp.chirp_off = None
+        return self
+
+    def without_spectrum_store(self):
+        """Let the backward transform every pair again (the form without the stored spectra)."""
+        self.fp.spectrum = None
+        self.spec = None
+        self._spec_theta = None
         return self
 
     # ---------------------------------------------------------------- passes
@@ -117,6 +129,7 @@ class FitProblem:
         _lib.check(lib.smk_fit_forward(C.byref(self.fp), self.d_theta.data_ptr(), self.acc.data_ptr(),
                                        self.ws.data_ptr(), self.ws.numel() * 8, stream_handle()),
                    "smk_fit_forward")
+        self._spec_theta = np.asarray(theta, np.float32).reshape(self.nzb, 3).copy() if self.spec is not None else None
         acc = self.acc.cpu().numpy()
         nzb, nkb = self.nzb, self.nkb
         with np.errstate(invalid="ignore", divide="ignore"):
@@ -162,7 +175,13 @@ class FitProblem:
         self.d_gP.copy_(torch.from_numpy(np.nan_to_num(gP)))
         self._set_theta(state["theta"])
         self.acc[self.nzb] = state["fbar"] * self.n_total   # <F> of this state's forward pass
-        _lib.check(lib.smk_fit_backward(C.byref(self.fp), self.d_theta.data_ptr(), self.acc.data_ptr(),
+        fp = self.fp
+        th32 = np.asarray(state["theta"], np.float32).reshape(self.nzb, 3)
+        if self.spec is not None and (self._spec_theta is None or not np.array_equal(self._spec_theta, th32)):
+            # the stored spectra belong to another theta's forward: transform again
+            fp = type(self.fp).from_buffer_copy(self.fp)
+            fp.spectrum = None
+        _lib.check(lib.smk_fit_backward(C.byref(fp), self.d_theta.data_ptr(), self.acc.data_ptr(),
                                         self.d_gM.data_ptr(), self.d_gP.data_ptr(), self.ws.data_ptr(),
                                         self.ws.numel() * 8, stream_handle()), "smk_fit_backward")
         acc = self.acc.cpu().numpy()

@@ -32,7 +32,7 @@ def variants(pass_id: int, n: int) -> list:
     w, t, nm = C.c_int32(), C.c_int32(), C.c_int32()
     for v in range(lib.smk_tune_count(pass_id)):
         _lib.check(lib.smk_tune_info(pass_id, v, C.byref(w), C.byref(t), C.byref(nm)))
-        if nm.value >= n:
+        if nm.value >= n or nm.value == -n:     # n_max < 0: that length only
             out.append((v, w.value, t.value))
     return out
 

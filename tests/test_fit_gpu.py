@@ -108,6 +108,28 @@ def test_chirp_table_gives_identical_results(problem_pair):
         np.testing.assert_array_equal(a, b)
 
 
+def test_stored_spectra_give_the_recomputed_gradient(problem_pair):
+    """The backward that reads the pair spectra stored by the forward pass gives the gradient of
+    the backward that transforms every pair again (1e-6 max|g|); after a forward at another
+    theta the stored spectra are stale and the backward of the first state transforms again."""
+    import copy
+    gp, op, mz, pk = problem_pair
+    assert gp.spec is not None
+    t1 = np.tile([0.15, 1.3, 0.4], (10, 1))
+    t2 = np.tile([0.11, 1.6, 0.7], (10, 1))
+    L1, g1 = gp.loss_grad(t1, mz, pk)
+    nq = copy.copy(gp)
+    nq.fp = type(gp.fp).from_buffer_copy(gp.fp)
+    nq.without_spectrum_store()
+    L0, g0 = nq.loss_grad(t1, mz, pk)
+    assert L1 == L0
+    np.testing.assert_allclose(g1, g0, rtol=0, atol=1e-6 * np.abs(g0).max())
+    _, s1 = gp.forward(t1, mz, pk)
+    gp.forward(t2, mz, pk)                 # overwrites the stored spectra
+    g_stale = gp.backward(s1)
+    np.testing.assert_allclose(g_stale, g0, rtol=0, atol=1e-6 * np.abs(g0).max())
+
+
 def test_fit_kernels_sized_by_longest_skewer(problem_pair):
     """The kernels' shared memory holds the Bluestein length of SmkFitProblem.n_max; a problem
     that understates it gets NaN power sums and gradient (the too-long pairs are skipped), and

@@ -88,10 +88,8 @@ def test_blocked_intermediate_every_tile_variant_is_exact(G):
     from saclaymocks_gb300 import _lib, tune
     lib = _lib.load()
     pid = _lib.SMK_PASS_XGEN
-    for v, w, t in tune.variants(pid, 2):
-        nm = C.c_int32()
-        lib.smk_tune_info(pid, v, None, None, C.byref(nm))
-        nx, ny, nz = CLASS_LEN[nm.value], 8, 72
+    for v, w, t, n in _all_variants(pid):
+        nx, ny, nz = n, 8, 72
         _lib.check(lib.smk_tune_set(pid, nx, v))
         try:
             out = G.make_boxes(nx, ny, nz, 2.19, seed=19, xi_chunk_kz=32)
@@ -300,6 +298,60 @@ VARIANT_AXES = {  # pass -> which axis is its line, shapes per length class
 CLASS_LEN = {512: 40, 1024: 600, 2560: 1536, 4096: 4000}
 
 
+def _all_variants(pid):
+    """(variant, W, threads, test length) of every variant of a pass: a length of its class, or
+    the one length of a variant compiled for a fixed length (n_max < 0)."""
+    import ctypes as C
+    from saclaymocks_gb300 import _lib
+    lib = _lib.load()
+    out = []
+    w, t, nm = C.c_int32(), C.c_int32(), C.c_int32()
+    for v in range(lib.smk_tune_count(pid)):
+        _lib.check(lib.smk_tune_info(pid, v, C.byref(w), C.byref(t), C.byref(nm)))
+        out.append((v, w.value, t.value, -nm.value if nm.value < 0 else CLASS_LEN[nm.value]))
+    return out
+
+
+def test_fixed_length_variants_equal_run_time_plan_variants(G):
+    """A variant compiled for one length (its FFT plan as constants) gives the same boxes, bit
+    for bit, as the variant of the same tile (W, threads) that reads the plan at run time."""
+    import ctypes as C
+    from saclaymocks_gb300 import _lib
+    lib = _lib.load()
+    checked = 0
+    for pid, axis in ((_lib.SMK_PASS_LINE, 1), (_lib.SMK_PASS_XGEN, 0), (_lib.SMK_PASS_XPASS, 0)):
+        info = {}
+        w, t, nm = C.c_int32(), C.c_int32(), C.c_int32()
+        for v in range(lib.smk_tune_count(pid)):
+            _lib.check(lib.smk_tune_info(pid, v, C.byref(w), C.byref(t), C.byref(nm)))
+            info[v] = (w.value, t.value, nm.value)
+        for vf, (wf, tf, nf) in info.items():
+            if nf >= 0:
+                continue
+            n = -nf
+            twin = [v for v, (wv, tv, nv) in info.items() if (wv, tv) == (wf, tf) and nv >= n]
+            assert twin, f"pass {pid}: no run-time-plan twin of variant {vf}"
+            shape = [6, 4, 8]
+            shape[axis] = n
+            noise = None
+            if pid == _lib.SMK_PASS_XPASS:
+                noise = torch.from_numpy(np.random.RandomState(3).normal(size=shape).astype(np.float32)).cuda()
+            res = []
+            for v in (vf, twin[0]):
+                _lib.check(lib.smk_tune_set(pid, n, v))
+                try:
+                    for xi in (0, 32):
+                        o = G.make_boxes(*shape, 2.19, seed=23, noise=noise, xi_chunk_kz=xi)
+                        torch.cuda.synchronize()
+                        res.append((o.delta[0].clone(), o.eta[0].clone()))
+                finally:
+                    lib.smk_tune_set(pid, n, -1)
+            for (d0, e0), (d1, e1) in zip(res[:2], res[2:]):
+                assert torch.equal(d0, d1) and torch.equal(e0, e1), f"pass {pid} variant {vf} vs {twin[0]}"
+            checked += 1
+    assert checked >= 3
+
+
 @pytest.mark.parametrize("pname", ["zfwd", "line", "xpass", "xgen", "zinv"])
 def test_every_tile_variant_is_exact(G, pname):
     """Each tile variant (W, threads) of each pass reproduces the FP64 oracle."""
@@ -307,11 +359,7 @@ def test_every_tile_variant_is_exact(G, pname):
     pid = {v: k for k, v in tune.PASS_NAMES.items()}[pname]
     lib = _lib.load()
     gpu_noise = pname == "xgen"
-    for v, w, t in tune.variants(pid, 2):
-        import ctypes as C
-        nm = C.c_int32()
-        lib.smk_tune_info(pid, v, None, None, C.byref(nm))
-        n = CLASS_LEN[nm.value]
+    for v, w, t, n in _all_variants(pid):
         shape = [6, 4, 8]
         shape[VARIANT_AXES[pname]] = n
         nx, ny, nz = shape
