@@ -905,7 +905,9 @@ def run_skewers_only(args, spec):
 
 def run_fit_only(args, nsk):
     """The fit kernels alone (the ncu profiling case): NSK skewers of 400-1200 pixels with
-    Gaussian fields, 10 z bins x (a, b, c), 32 log-k bins; W + K loss-and-gradient evaluations."""
+    Gaussian fields, redshift rising along each skewer (3e-4 per pixel from a uniform start in
+    1.8-3.4, as on a line of sight), 10 z bins x (a, b, c), 32 log-k bins; W + K
+    loss-and-gradient evaluations."""
     import numpy as np
     import torch
 
@@ -915,7 +917,10 @@ def run_fit_only(args, nsk):
     n = int(lengths.sum())
     delta = torch.randn(n, device="cuda") * 1.2
     eta = torch.randn(n, device="cuda") * 0.4
-    z = torch.rand(n, device="cuda", dtype=torch.float64) * 1.8 + 1.8
+    z0 = rng.uniform(1.8, 3.4, nsk)
+    first = np.concatenate([[0], np.cumsum(lengths[:-1], dtype=np.int64)])
+    idx = np.arange(n) - np.repeat(first, lengths)
+    z = torch.from_numpy(np.minimum(np.repeat(z0, lengths) + 3e-4 * idx, 3.6)).cuda()
     prob = fit.FitProblem(delta, eta, None, z, lengths, np.linspace(1.8, 3.6, 11),
                           np.logspace(np.log10(0.05), np.log10(15.0), 33), 0.2)
     truth = np.tile([0.1, 1.58, 0.6], (10, 1))
