@@ -72,33 +72,75 @@ __device__ __forceinline__ float flux_of(const FitArgs& a, int64_t o, const floa
     return expf(-pa * t);
 }
 
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// Warp-cooperative flush of per-lane FP32 partials v[0..K) that belong to redshift bin jw: the
+// lanes with `flush` set (and jw >= 0) are grouped by bin, each group warp-summed and added by
+// lane 0 to dst(bin, q) (FP64 shared memory) -- one atomic per distinct bin and value instead of
+// one per lane, so the lanes of a block that all sit in one bin do not queue on one address.
+// Those lanes leave with zeroed partials and jw = -1.  All 32 lanes must call it.
+template <int K, class Dst>
+__device__ __forceinline__ void warp_flush(bool flush, int& jw, float (&v)[K], Dst&& dst) {
+    for (;;) {
+        const unsigned act = __ballot_sync(0xffffffffu, flush && jw >= 0);
+        if (!act) break;
+        const int jl = __shfl_sync(0xffffffffu, jw, __ffs(act) - 1);
+        const bool mine = flush && jw == jl;
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            const float sum = warp_sum(mine ? v[q] : 0.f);
+            if ((threadIdx.x & 31) == 0) atomicAdd(dst(jl, q), (double)sum);
+        }
+        if (mine) {
+#pragma unroll
+            for (int q = 0; q < K; ++q) v[q] = 0.f;
+            jw = -1;
+        }
+    }
+}
+
 // ------------------------------------------------------------------ pass 1: mean flux
+constexpr int FIT_RUN = 32 * 16;   // pixels per warp work run of the mean-flux pass
+
 __global__ void __launch_bounds__(FIT_T) fit_flux_kernel(const FitArgs a) {
     __shared__ double sb[FIT_MAX_BINS + 1];
     __shared__ float th[3 * FIT_MAX_BINS];
     for (int i = threadIdx.x; i <= a.nzb; i += FIT_T) sb[i] = 0.0;
     for (int i = threadIdx.x; i < 3 * a.nzb; i += FIT_T) th[i] = a.theta[i];
     __syncthreads();
-    // per-thread FP32 partials over a short run of pixels, FP64 in shared memory
-    for (int64_t base = (blockIdx.x * (int64_t)FIT_T + threadIdx.x) * 16; base < a.n_total;
-         base += (int64_t)gridDim.x * FIT_T * 16) {
-        const int64_t end = min(base + 16, a.n_total);
-        int jcur = a.zbin[base];
-        float part = 0.f, tot = 0.f;
-        for (int64_t o = base; o < end; ++o) {
-            float t1, g;
-            const float F = flux_of(a, o, th, &t1, &g);
-            const int j = a.zbin[o];
-            if (j != jcur) {
-                atomicAdd(&sb[jcur], (double)part);
-                part = 0.f;
-                jcur = j;
+    // warps take runs of FIT_RUN consecutive pixels, lanes on consecutive pixels; each lane keeps
+    // an FP32 partial of its current bin (16 pixels at most), flushed in FP64 per bin change
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = (int64_t)gridDim.x * (FIT_T / 32);
+    for (int64_t base = (blockIdx.x * (int64_t)(FIT_T / 32) + (threadIdx.x >> 5)) * FIT_RUN; base < a.n_total;
+         base += nw * FIT_RUN) {
+        const int64_t end = min(base + (int64_t)FIT_RUN, a.n_total);
+        float part[1] = {0.f}, tot[1] = {0.f};
+        int jw = -1, jt = 0;
+        for (int64_t o0 = base; o0 < end; o0 += 32) {   // warp-uniform trip count
+            const int64_t o = o0 + lane;
+            const bool ok = o < end;
+            float F = 0.f;
+            int j = -1;
+            if (ok) {
+                float t1, g;
+                F = flux_of(a, o, th, &t1, &g);
+                j = a.zbin[o];
             }
-            part += F;
-            tot += F;
+            const bool change = ok && jw >= 0 && j != jw;
+            if (__any_sync(0xffffffffu, change)) warp_flush(change, jw, part, [&](int b, int) { return &sb[b]; });
+            if (ok) {
+                if (jw < 0) jw = j;
+                part[0] += F;
+                tot[0] += F;
+            }
         }
-        atomicAdd(&sb[jcur], (double)part);
-        atomicAdd(&sb[a.nzb], (double)tot);
+        warp_flush(true, jw, part, [&](int b, int) { return &sb[b]; });
+        warp_flush(true, jt, tot, [&](int, int) { return &sb[a.nzb]; });
     }
     __syncthreads();
     for (int i = threadIdx.x; i <= a.nzb; i += FIT_T) atomicAdd(a.acc + i, sb[i]);
@@ -176,16 +218,38 @@ __device__ void bluestein(float2* s1, float2* s2, const float2* tw, int N, int M
     __syncthreads();
 }
 
-// bin of frequency m of a length-N spectrum: numpy's rfftfreq(N)*2*k_ny in FP64 and
-// searchsorted(edges, k, 'right') - 1 with the last edge inclusive; -1 outside
-__device__ __forceinline__ int kbin(int m, int N, double kfac, const double* edges, int nkb) {
-    const double k = ((double)m * (1.0 / (double)N)) * kfac;
-    if (k < edges[0] || k > edges[nkb]) return -1;
-    if (k == edges[nkb]) return nkb - 1;
-    int lo = 0, hi = nkb;  // edges[lo] <= k < edges[hi]
+// Frequency k_m of mode m of a length-N spectrum: numpy's rfftfreq(N)*2*k_ny in FP64.  Its bin
+// is searchsorted(edges, k_m, 'right') - 1 with the last edge inclusive, -1 outside the edges.
+__device__ __forceinline__ double kfreq(int m, int N, double kfac) { return ((double)m * (1.0 / (double)N)) * kfac; }
+
+// The bins as integer thresholds on m, once per length (k_m is nondecreasing in m):
+// thr[b] (b < nkb) = the smallest m with k_m >= edges[b], thr[nkb] = the smallest m with
+// k_m > edges[nkb] (m up to N/2 + 1).  Block-synchronous.
+__device__ void kbin_thresholds(int N, double kfac, const double* edges, int nkb, int* thr) {
+    const int half = N / 2;
+    for (int b = threadIdx.x; b <= nkb; b += FIT_T) {
+        const double e = edges[b];
+        int m = (int)fmin(fmax(floor(e * (double)N / kfac), 0.0), (double)(half + 1));
+        if (b < nkb) {
+            while (m > 0 && kfreq(m - 1, N, kfac) >= e) --m;
+            while (m <= half && kfreq(m, N, kfac) < e) ++m;
+        } else {
+            while (m > 0 && kfreq(m - 1, N, kfac) > e) --m;
+            while (m <= half && kfreq(m, N, kfac) <= e) ++m;
+        }
+        thr[b] = m;
+    }
+    __syncthreads();
+}
+
+// The bin of mode m from the thresholds: the largest b < nkb with thr[b] <= m, -1 outside
+// [thr[0], thr[nkb]).
+__device__ __forceinline__ int kbin_thr(int m, const int* thr, int nkb) {
+    if (m < thr[0] || m >= thr[nkb]) return -1;
+    int lo = 0, hi = nkb;  // thr[lo] <= m, and hi == nkb or thr[hi] > m
     while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
-        if (edges[mid] <= k) lo = mid;
+        if (thr[mid] <= m) lo = mid;
         else hi = mid;
     }
     return lo;
@@ -243,11 +307,6 @@ __device__ __forceinline__ void warp_bin_add(double* sbins, int bin, float v) {
     if (bin >= 0 && (lane == 0 || bprev != bin)) atomicAdd(&sbins[bin], (double)v);
 }
 
-__device__ __forceinline__ float warp_sum(float v) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    return v;
-}
 
 // ------------------------------------------------------------------ pass 2: binned P1D
 __global__ void __launch_bounds__(FIT_T, 3) fit_p1d_kernel(const FitArgs a) {
@@ -268,10 +327,15 @@ __global__ void __launch_bounds__(FIT_T, 3) fit_p1d_kernel(const FitArgs a) {
     const float fbar_inv = (float)((double)a.n_total / a.acc[acc_ftot(a.nzb)]);
     const double kfac = 2.0 * (3.14159265358979323846 / a.dx);
     __shared__ FftPlan pl;
-    int curM = 0;
+    __shared__ int thr[FIT_MAX_BINS + 1];
+    int curM = 0, curN = 0;
     while (next_pair(a, &item_sh, &ps)) {
         const int N = ps.N;
         const int M = bluestein_m(N);
+        if (N != curN) {
+            kbin_thresholds(N, kfac, edges, a.nkb, thr);
+            curN = N;
+        }
         if (M > a.mmax) {
             // a skewer longer than SmkFitProblem.n_max: not transformed (its Bluestein length
             // does not fit the shared memory), the power sums are made NaN instead
@@ -306,7 +370,7 @@ __global__ void __launch_bounds__(FIT_T, 3) fit_p1d_kernel(const FitArgs a) {
             int b = -1;
             float p = 0.f, q = 0.f;
             if (m <= half) {
-                b = kbin(m, N, kfac, edges, a.nkb);
+                b = kbin_thr(m, thr, a.nkb);
                 const float2 zk = s1[m], zm = s1[m == 0 ? 0 : N - m];
                 const float x1r = 0.5f * (zk.x + zm.x), x1i = 0.5f * (zk.y - zm.y);
                 const float x2r = 0.5f * (zk.y + zm.y), x2i = -0.5f * (zk.x - zm.x);
@@ -351,10 +415,15 @@ __global__ void __launch_bounds__(FIT_T, 3) fit_adjoint_kernel(const FitArgs a) 
     const float fbar_inv = (float)((double)a.n_total / a.acc[acc_ftot(a.nzb)]);
     const double kfac = 2.0 * (3.14159265358979323846 / a.dx);
     __shared__ FftPlan pl;
-    int curM = 0;
+    __shared__ int thr[FIT_MAX_BINS + 1];
+    int curM = 0, curN = 0;
     while (next_pair(a, &item_sh, &ps)) {
         const int N = ps.N;
         const int M = bluestein_m(N);
+        if (N != curN) {
+            kbin_thresholds(N, kfac, edges, a.nkb, thr);
+            curN = N;
+        }
         if (M > a.mmax) {
             // a skewer longer than SmkFitProblem.n_max: skipped, the gradient is made NaN
             if (threadIdx.x == 0) sS = __longlong_as_double(0x7ff8000000000000LL);
@@ -387,7 +456,7 @@ __global__ void __launch_bounds__(FIT_T, 3) fit_adjoint_kernel(const FitArgs a) 
         const float norm = (float)(a.dx / (double)N);
         for (int m = threadIdx.x; m <= N / 2; m += FIT_T) {
             const float2 zk = s1[m], zm = s1[m == 0 ? 0 : N - m];
-            const int b = kbin(m, N, kfac, edges, a.nkb);
+            const int b = kbin_thr(m, thr, a.nkb);
             const float wgt = b >= 0 ? (float)gP[b] * norm : 0.f;
             float2 x1 = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
             float2 x2 = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
@@ -405,57 +474,56 @@ __global__ void __launch_bounds__(FIT_T, 3) fit_adjoint_kernel(const FitArgs a) 
         __syncthreads();
         bluestein<true>(s1, s2, tw, N, M, pl, Bc);
         // per pixel: gF~ = gM_j + gdF / <F>; dF/da = -tau1 F, dF/db = -a tau1 G g F,
-        // dF/dc = -a tau1 b G eta F
-        // per-thread FP32 partials for the current redshift bin, flushed to the block's FP64
-        // accumulators when the bin changes and, warp-reduced, at the end of the pair
-        float acc6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, accS = 0.f;
-        int jw = -1;
-        for (int i = threadIdx.x; i < 2 * N; i += FIT_T) {
-            const int t = i < N ? 0 : 1;
-            const int ii = i - t * N;
-            if (ps.sid[t] < 0) continue;
-            const int64_t o = ps.off[t] + ii;
-            float t1, g;
-            const float F = flux_of(a, o, th, &t1, &g);
-            const float gdF = t ? s1[ii].y : s1[ii].x;
-            const int j = a.zbin[o];
-            if (jw >= 0 && j != jw) {
+        // dF/dc = -a tau1 b G eta F.  Each warp walks a contiguous run of the pair's 2N pixel
+        // slots (lanes on consecutive pixels); per-lane FP32 partials of the current redshift bin
+        // are flushed to the block's FP64 accumulators when the bin changes (warp_flush)
+        {
+            const int total = 2 * N;
+            const int per_warp = ((total + FIT_T / 32 - 1) / (FIT_T / 32) + 31) & ~31;
+            const int lane = threadIdx.x & 31;
+            const int beg = (threadIdx.x >> 5) * per_warp, end = min(total, beg + per_warp);
+            float acc6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, accS[1] = {0.f};
+            int jw = -1, js = 0;
+            auto dst6 = [&](int b, int q) { return q < 3 ? &sA[3 * b + q] : &sB[3 * b + q - 3]; };
+            for (int i0 = beg; i0 < end; i0 += 32) {   // warp-uniform trip count
+                const int i = i0 + lane;
+                const int t = i < N ? 0 : 1;
+                const int ii = i - t * N;
+                const bool ok = i < end && ps.sid[t] >= 0;
+                int j = -1;
+                float v6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, vS = 0.f;
+                if (ok) {
+                    const int64_t o = ps.off[t] + ii;
+                    float t1, g;
+                    const float F = flux_of(a, o, th, &t1, &g);
+                    const float gdF = t ? s1[ii].y : s1[ii].x;
+                    j = a.zbin[o];
+                    const float pa = th[3 * j], pb = th[3 * j + 1];
+                    const float e = a.eta ? __ldg(a.eta + o) : 0.f;
+                    const float G = a.G ? __ldg(a.G + o) : 1.f;
+                    const float dFa = -t1 * F;
+                    const float dFb = -pa * t1 * G * g * F;
+                    const float dFc = -pa * t1 * pb * G * e * F;
+                    const float gF = (float)gM[j] + gdF * fbar_inv;
+                    v6[0] = gF * dFa;
+                    v6[1] = gF * dFb;
+                    v6[2] = gF * dFc;
+                    v6[3] = dFa;
+                    v6[4] = dFb;
+                    v6[5] = dFc;
+                    vS = gdF * F;
+                }
+                const bool change = ok && jw >= 0 && j != jw;
+                if (__any_sync(0xffffffffu, change)) warp_flush(change, jw, acc6, dst6);
+                if (ok) {
+                    if (jw < 0) jw = j;
 #pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    atomicAdd(&sA[3 * jw + q], (double)acc6[q]);
-                    atomicAdd(&sB[3 * jw + q], (double)acc6[3 + q]);
-                    acc6[q] = acc6[3 + q] = 0.f;
+                    for (int q = 0; q < 6; ++q) acc6[q] += v6[q];
+                    accS[0] += vS;
                 }
             }
-            jw = j;
-            const float pa = th[3 * j], pb = th[3 * j + 1];
-            const float e = a.eta ? __ldg(a.eta + o) : 0.f;
-            const float G = a.G ? __ldg(a.G + o) : 1.f;
-            const float dFa = -t1 * F;
-            const float dFb = -pa * t1 * G * g * F;
-            const float dFc = -pa * t1 * pb * G * e * F;
-            const float gF = (float)gM[j] + gdF * fbar_inv;
-            acc6[0] = fmaf(gF, dFa, acc6[0]);
-            acc6[1] = fmaf(gF, dFb, acc6[1]);
-            acc6[2] = fmaf(gF, dFc, acc6[2]);
-            acc6[3] += dFa;
-            acc6[4] += dFb;
-            acc6[5] += dFc;
-            accS = fmaf(gdF, F, accS);
-        }
-        const float wS = warp_sum(accS);
-        if ((threadIdx.x & 31) == 0) atomicAdd(&sS, (double)wS);
-        for (;;) {  // warp-uniform loop over the distinct bins still held by the lanes
-            const unsigned act = __ballot_sync(0xffffffffu, jw >= 0);
-            if (!act) break;
-            const int jl = __shfl_sync(0xffffffffu, jw, __ffs(act) - 1);
-            const bool mine = jw == jl;
-#pragma unroll
-            for (int q = 0; q < 6; ++q) {
-                const float v = warp_sum(mine ? acc6[q] : 0.f);
-                if ((threadIdx.x & 31) == 0) atomicAdd(q < 3 ? &sA[3 * jl + q] : &sB[3 * jl + q - 3], (double)v);
-            }
-            if (mine) jw = -1;
+            warp_flush(true, jw, acc6, dst6);
+            warp_flush(true, js, accS, [&](int, int) { return &sS; });
         }
         __syncthreads();
     }

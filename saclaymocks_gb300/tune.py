@@ -94,40 +94,38 @@ def tune_grf(nx: int, ny: int, nz: int, dcell: float = 2.19, gpu_noise: bool = T
         if len(found) == len(passes):
             return {"choices": {PASS_NAMES[p]: found[(p, n)] for p, n, _ in passes}, "ms": {}, "cached": True}
     cands = {p: variants(p, n) for p, n, _ in passes}
-    rounds = max(len(v) for v in cands.values())
     if out is None:
         out = grf.alloc_boxes(nx, ny, nz)
     if workspace is None:
         workspace = grf.GrfWorkspace(1)
     amp = grf.pk_normalisation(nx, ny, nz, dcell)
     noise = None if gpu_noise else torch.randn(nx * ny * nz, device="cuda").reshape(nx, ny, nz)
-    times = {p: {} for p, _, _ in passes}
-    for r in range(rounds):
-        cur = {}
-        for p, n, _ in passes:
-            v = cands[p][min(r, len(cands[p]) - 1)][0]
-            cur[(p, n)] = v
-        apply(cur)
-        evs = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
-        for e in evs:
-            e.record()
-        acc = {p: [] for p, _, _ in passes}
-        for k in range(1 + reps):
-            grf.make_boxes(nx, ny, nz, dcell, seed=1, noise=noise, amp=amp, out=out, workspace=workspace,
-                           xi_chunk_kz=xi_chunk_kz,
-                           pass_events=evs)
-            torch.cuda.synchronize()
-            if k == 0:
-                continue           # first call of a variant: launch set-up, cold caches
-            for p, n, mark in passes:
-                acc[p].append(evs[mark - 1].elapsed_time(evs[mark]))
-        for p, n, _ in passes:
-            v = cur[(p, n)]
-            times[p].setdefault(v, float(np.mean(acc[p])))
+    lib = _lib.load()
+    # coordinate descent in pass order: the candidates of one pass are timed with the other passes
+    # at their current choice (the x pass's tile decides the intermediate's layout that the y
+    # pass reads, so passes are not timed independently of each other)
     best = {}
     for p, n, _ in passes:
-        v = min(times[p], key=times[p].get)
-        best[(p, n)] = v
+        _lib.check(lib.smk_tune_set(p, n, -1))
+        best[(p, n)] = lib.smk_tune_get(p, n)
+    times = {p: {} for p, _, _ in passes}
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+    for e in evs:
+        e.record()
+    for p, n, mark in passes:
+        for v, _, _ in cands[p]:
+            cur = dict(best)
+            cur[(p, n)] = v
+            apply(cur)
+            acc = []
+            for k in range(1 + reps):
+                grf.make_boxes(nx, ny, nz, dcell, seed=1, noise=noise, amp=amp, out=out, workspace=workspace,
+                               xi_chunk_kz=xi_chunk_kz, pass_events=evs)
+                torch.cuda.synchronize()
+                if k:                  # the first call of a variant: launch set-up, cold caches
+                    acc.append(evs[mark - 1].elapsed_time(evs[mark]))
+            times[p][v] = float(np.mean(acc))
+        best[(p, n)] = min(times[p], key=times[p].get)
     apply(best)
     _store(best)
     info = {p: {v: (w, t) for v, w, t in cands[p]} for p, _, _ in passes}
