@@ -412,9 +412,9 @@ def run_ours(args, cfg):
     achieved = pass_bytes[dom] / (pass_ms[dom] * 1e-3) / 1e9
     # DRAM bytes per unit from ncu captures of the same kernels on boxes with the production
     # line lengths (2560 x 128 x 1536 for the x pass, 128 x 2560 x 1536 for y and z), scaled by
-    # the units of this launch: x (xgi_kernel, both fields) 15.84 B per mode, y 16.97 and z
-    # 16.14 B per mode and field
-    traffic = [15.84 * modes, 16.97 * modes * 2, 16.14 * modes * 2][dom] / 1e9
+    # the units of this launch: x (xgi_kernel, both fields) 15.84 B per mode, y (compile-time
+    # plan variant) 16.92 and z 16.14 B per mode and field
+    traffic = [15.84 * modes, 16.92 * modes * 2, 16.14 * modes * 2][dom] / 1e9
     grf_ms = float(np.sum(pass_ms))
     step_ms = ms / args.steps
     # The x pass is instruction-bound, so its issue-slot roofline is reported beside the HBM one:

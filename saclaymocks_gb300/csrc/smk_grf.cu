@@ -377,11 +377,9 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         za.out = delta;
         if ((rc = run_zfwd(vzf, za, rows_per_box, st))) return rc;
         if ((rc = mark(1))) return rc;
-        // 2. c2c along y, forward (the y spectrum stays in digit-reversed order)
-        if ((rc = run_line(vy, ya, false, st))) return rc;
-        if ((rc = mark(2))) return rc;
-        // 3. x: forward, P(k) scaling + eta split, inverse
-        XArgs xa;
+        // 2. c2c along y, forward (the y spectrum stays in digit-reversed order); 3. x: forward,
+        // P(k) scaling + eta split, inverse
+        XArgs xa = {};
         xa.pl = plx;
         xa.ply = ply;
         xa.A = d2;
@@ -407,27 +405,42 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         if (xcols > 0 && (!workspace || workspace_bytes < smk_grf_workspace_size(p)))
             return fail(SMK_EWORKSPACE, "smk_grf_boxes: xi_chunk_kz needs %zu workspace bytes",
                         smk_grf_workspace_size(p));
-        if (xcols > 0 && kb >= 2 && kb % 2 == 0 && wy % kb == 0 && xcols % wy == 0) {
-            // chunks of xcols k_z columns: the x pass reads one field in place and writes both
-            // into the blocked intermediate, the y inverse reads it as contiguous runs
+        if (xcols > 0 && kb >= 2 && kb % 2 == 0 && wy % kb == 0 && wy / kb <= 8 && xcols % wy == 0) {
+            // chunks of xcols k_z columns: the y forward of the chunk's columns writes the blocked
+            // layout of the intermediate's first field, the x pass reads it there as rows
+            // ny * kb * 8 bytes apart (not ny * pitch * 4) and writes both fields back into the
+            // intermediate, and the y inverse reads them as contiguous runs
             float2* I0 = reinterpret_cast<float2*>(reinterpret_cast<char*>(workspace) + 256);
             const int64_t nouter = (int64_t)p->batch * p->nx;
             xa.I[0] = I0;
             xa.I[1] = p->want_eta ? I0 + nouter * p->ny * xcols : nullptr;
             xa.prefetch = g_prefetch.load();
+            xa.src_blocked = 1;
+            LineArgs yf = ya;
+            yf.nbuf = 1;
+            yf.dst = I0;
+            yf.dst_kb = kb;
+            if (yf.tma == 2) yf.tma = 1;
             LineArgs yi = staged_y(ya, xa.I, nf, kb, wy, xcols, nouter, p->ny);
             const bool one_chunk = xcols >= nzh;
             for (int64_t c0 = 0; c0 < nzh; c0 += xcols) {
+                const int ncol = (int)std::min<int64_t>(xcols, nzh - c0);
+                yf.col0 = (int)c0;
+                yf.ncol = ncol;
+                if ((rc = run_line(vy, yf, false, st))) return rc;
+                if (one_chunk && (rc = mark(2))) return rc;
                 xa.cb0 = (int)(c0 / kb);
-                xa.ncb = (int)ceil_div(std::min<int64_t>(xcols, nzh - c0), kb);
+                xa.ncb = (int)ceil_div(ncol, kb);
                 if ((rc = run_xpi(vx, xa, st))) return rc;
                 if (one_chunk && (rc = mark(3))) return rc;
                 yi.col0 = (int)c0;
-                yi.ncol = (int)std::min<int64_t>(xcols, nzh - c0);
+                yi.ncol = ncol;
                 if ((rc = run_line(vy, yi, true, st))) return rc;
             }
-            if ((!one_chunk && (rc = mark(3))) || (rc = mark(4))) return rc;
+            if ((!one_chunk && ((rc = mark(2)) || (rc = mark(3)))) || (rc = mark(4))) return rc;
         } else {
+            if ((rc = run_line(vy, ya, false, st))) return rc;
+            if ((rc = mark(2))) return rc;
             if ((rc = run_xpass(vx, xa, st))) return rc;
             if ((rc = mark(3))) return rc;
             // 4. c2c along y, inverse, on delta (and eta)

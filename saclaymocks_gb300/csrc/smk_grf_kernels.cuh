@@ -73,6 +73,32 @@ __device__ __forceinline__ void store_cols(const float2* s, float2* base, int n,
     }
 }
 
+// The tile's W columns (column block cb of the launch, line o) into the blocked layout
+// dst[((c / kb) * n_outer + o) * n + e][c % kb], c = cb W + w: each of the W / kb blocks is one
+// contiguous run of n * kb values, written as 16-byte pieces (kb even, dst 16-byte aligned).
+// Columns past the launch's count carry the zeros the load put there.
+template <int W, int T, int KB>
+__device__ __forceinline__ void store_blocked(const float2* s, float2* dst, int n, int64_t n_outer, int64_t o,
+                                              int cb) {
+    constexpr int HK = KB / 2;
+    for (int q = 0; q < W / KB; ++q) {
+        float2* run = dst + (((int64_t)cb * (W / KB) + q) * n_outer + o) * n * KB;
+        for (int idx = threadIdx.x; idx < n * HK; idx += T) {
+            const int e = idx / HK, w2 = 2 * (idx % HK);
+            const float2 v0 = s[e * W + q * KB + w2], v1 = s[e * W + q * KB + w2 + 1];
+            *reinterpret_cast<float4*>(run + (int64_t)e * KB + w2) = make_float4(v0.x, v0.y, v1.x, v1.y);
+        }
+    }
+}
+template <int W, int T>
+__device__ __forceinline__ void store_blocked(const float2* s, float2* dst, int n, int kb, int64_t n_outer,
+                                              int64_t o, int cb) {
+    if constexpr (W >= 2) { if (kb == W) { store_blocked<W, T, W>(s, dst, n, n_outer, o, cb); return; } }
+    if constexpr (W >= 4) { if (kb == W / 2) { store_blocked<W, T, W / 2>(s, dst, n, n_outer, o, cb); return; } }
+    if constexpr (W >= 8) { if (kb == W / 4) { store_blocked<W, T, W / 4>(s, dst, n, n_outer, o, cb); return; } }
+    if constexpr (W >= 16) { if (kb == W / 8) { store_blocked<W, T, W / 8>(s, dst, n, n_outer, o, cb); return; } }
+}
+
 struct ZFwdArgs {
     FftPlan pl;
     ZTiling zt;             // set by the launcher from its tile width
@@ -152,6 +178,10 @@ struct LineArgs {
     const float2* src[2];
     int src_kb;
     int col0;
+    // Destination of a forward launch (one buffer): in place (null) or the blocked layout above
+    // with dst_kb columns per block (the host-noise x pass reads it as contiguous rows)
+    float2* dst;
+    int dst_kb;
 };
 
 // Forward: natural -> digit-reversed order along the axis (kept in HBM); inverse: back.
@@ -195,7 +225,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
                     if (src)
                         tma_load_5d(s + e0 * W, &a.tmap[buf], &bar, 0, 0, e0, (int)o, cb);
                     else
-                        tma_load_3d(s + e0 * W, &a.tmap[buf], &bar, cb * W, e0, (int)o);
+                        tma_load_3d(s + e0 * W, &a.tmap[buf], &bar, a.col0 + cb * W, e0, (int)o);
                 }
             }
             // bounded wait (~1 s at 2 GHz): on time-out the tile is poisoned with NaN, which the
@@ -226,7 +256,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
             __syncthreads();
         }
         if (src) {
-            // the next tile's source runs into L2
+            // the next tile's source runs into L2 (two tiles ahead measured slower)
             if (a.prefetch && threadIdx.x == 0 && tile + gridDim.x < ntiles) {
                 const int64_t tn = tile + gridDim.x;
                 const int bn = (int)(tn / tpb);
@@ -264,7 +294,10 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
             });
         } else {
             fft_tile<INV, W, W, T, C::RMAX, C::NF>(s, tw, a.pl);
-            store_cols<W, T>(s, base, n, a.estride, cols);
+            if (a.dst)
+                store_blocked<W, T>(s, a.dst, n, a.dst_kb, a.n_outer, o, cb);
+            else
+                store_cols<W, T>(s, base, n, a.estride, cols);
         }
         if (a.tma) fence_proxy_async_smem();   // this tile's shared accesses before the next TMA writes
         __syncthreads();
@@ -295,6 +328,10 @@ struct XArgs {
     float2* I[2];
     int cb0, ncb;
     int prefetch;
+    // xpi_kernel source: the boxes (null) or the blocked layout of I[0] that the y forward wrote
+    // (the tile's rows ny * WC * 8 bytes apart instead of ny * pitch * 4; read, then overwritten
+    // by the tile itself)
+    int src_blocked;
 };
 
 // k_i k_j of the eta component (SMK_ETA_*), float32 product as numpy forms kx*ky
@@ -448,12 +485,16 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
         const int64_t b = r / a.ncb;
         const int cb = a.cb0 + kbl;
         const int cols = min(WC, a.nzh - cb * WC);
-        const float2* pa = a.A + b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)cb * WC;
+        const int64_t row0 = ((int64_t)kbl * nouter + b * a.nx) * a.ny + yslot;
+        const int64_t es = (int64_t)a.ny * WC;
         // WC columns (16-byte copies of column pairs, zero past nzh) into lines 0..WC-1 of the tile
+        const float2* pa = a.src_blocked ? a.I[0] + row0 * WC
+                                         : a.A + b * (int64_t)a.nx * estride + (int64_t)yslot * a.cp + (int64_t)cb * WC;
+        const int64_t rs = a.src_blocked ? es : estride;
         for (int idx = threadIdx.x; idx < n * (WC / 2); idx += T) {
             const int e = idx / (WC / 2), w = 2 * (idx % (WC / 2));
             const int bytes = w < cols ? (w + 1 < cols ? 16 : 8) : 0;
-            cp_async<16>(s + e * W + w, bytes ? pa + e * estride + w : pa, bytes);
+            cp_async<16>(s + e * W + w, bytes ? pa + e * rs + w : pa, bytes);
         }
         const int iy = freq_of_slot(a.ply, yslot);
         if (threadIdx.x == 0) kt[0] = kaxis(iy, a.ny, a.kfac, true);
@@ -464,9 +505,11 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
             // the next tile's nx row pieces (one line each) into L2
             const int64_t tn = tile + gridDim.x;
             const int64_t rn = tn / a.ny;
-            const float2* pn = a.A + (rn / a.ncb) * (int64_t)a.nx * estride + (int64_t)(tn % a.ny) * a.cp +
-                               (int64_t)(a.cb0 + (int)(rn % a.ncb)) * WC;
-            for (int e = threadIdx.x; e < n; e += T) prefetch_l2(pn + e * estride);
+            const float2* pn = a.src_blocked
+                ? a.I[0] + (((int64_t)(rn % a.ncb) * nouter + (rn / a.ncb) * a.nx) * a.ny + tn % a.ny) * WC
+                : a.A + (rn / a.ncb) * (int64_t)a.nx * estride + (int64_t)(tn % a.ny) * a.cp +
+                      (int64_t)(a.cb0 + (int)(rn % a.ncb)) * WC;
+            for (int e = threadIdx.x; e < n; e += T) prefetch_l2(pn + e * rs);
         }
         if (both)
             fft_tile<false, KB, W, T, C::RMAX, C::NF>(s, tw, a.pl);
@@ -495,10 +538,8 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
             }
         }
         __syncthreads();
-        const int64_t row0 = ((int64_t)kbl * nouter + b * a.nx) * a.ny + yslot;
         float2* d0 = a.I[0] + row0 * WC;
         float2* d1 = both ? a.I[1] + row0 * WC : nullptr;
-        const int64_t es = (int64_t)a.ny * WC;
         ifft_tile_out<W, W, T, C::RMAX, C::NF>(s, tw, a.pl, [&](int e, int w, float2 v) {
             const int f = both && w >= WC;
             const int c = w - f * WC;
