@@ -398,7 +398,8 @@ __global__ void __launch_bounds__(FIT_T, 3) fit_adjoint_kernel(const FitArgs a) 
     float2* s2 = a.chirp ? nullptr : smem + a.mmax;
     float2* tw = smem + (a.chirp ? 1 : 2) * a.mmax;
     __shared__ double sA[3 * FIT_MAX_BINS], sB[3 * FIT_MAX_BINS], sS;
-    __shared__ double edges[FIT_MAX_BINS + 1], gP[FIT_MAX_BINS], gM[FIT_MAX_BINS];
+    __shared__ double edges[FIT_MAX_BINS + 1];
+    __shared__ float gP[FIT_MAX_BINS], gM[FIT_MAX_BINS];   // the weights in FP32 (no FP64 per pixel)
     __shared__ float th[3 * FIT_MAX_BINS];
     __shared__ long long item_sh;
     __shared__ PairSetup ps;
@@ -408,8 +409,8 @@ __global__ void __launch_bounds__(FIT_T, 3) fit_adjoint_kernel(const FitArgs a) 
         th[i] = a.theta[i];
     }
     for (int i = threadIdx.x; i <= a.nkb; i += FIT_T) edges[i] = a.kedges[i];
-    for (int i = threadIdx.x; i < a.nkb; i += FIT_T) gP[i] = a.gP[i];
-    for (int i = threadIdx.x; i < a.nzb; i += FIT_T) gM[i] = a.gM[i];
+    for (int i = threadIdx.x; i < a.nkb; i += FIT_T) gP[i] = (float)a.gP[i];
+    for (int i = threadIdx.x; i < a.nzb; i += FIT_T) gM[i] = (float)a.gM[i];
     if (threadIdx.x == 0) sS = 0.0;
     // the same FP32 1/<F> as the forward pass (the stored spectra were made with it)
     const float fbar_inv = (float)((double)a.n_total / a.acc[acc_ftot(a.nzb)]);
@@ -457,7 +458,7 @@ __global__ void __launch_bounds__(FIT_T, 3) fit_adjoint_kernel(const FitArgs a) 
         for (int m = threadIdx.x; m <= N / 2; m += FIT_T) {
             const float2 zk = s1[m], zm = s1[m == 0 ? 0 : N - m];
             const int b = kbin_thr(m, thr, a.nkb);
-            const float wgt = b >= 0 ? (float)gP[b] * norm : 0.f;
+            const float wgt = b >= 0 ? gP[b] * norm : 0.f;
             float2 x1 = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
             float2 x2 = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
             if (ps.sid[1] < 0) x2 = make_float2(0.f, 0.f);
@@ -504,7 +505,7 @@ __global__ void __launch_bounds__(FIT_T, 3) fit_adjoint_kernel(const FitArgs a) 
                     const float dFa = -t1 * F;
                     const float dFb = -pa * t1 * G * g * F;
                     const float dFc = -pa * t1 * pb * G * e * F;
-                    const float gF = (float)gM[j] + gdF * fbar_inv;
+                    const float gF = gM[j] + gdF * fbar_inv;
                     v6[0] = gF * dFa;
                     v6[1] = gF * dFb;
                     v6[2] = gF * dFc;
