@@ -295,6 +295,15 @@ def run_ours(args, cfg):
         from saclaymocks_gb300 import tune
         tuned = tune.tune_grf(cfg["nx"], cfg["ny"], cfg["nz"], cfg["dcell"], out=boxes, workspace=ws,
                               xi_chunk_kz=xi, use_cache=xi == 0)
+        # the skewer stage's schedule (paired or one per item) and blocks per SM, on the boxes
+        # the GRF tuning left
+        sk_tuned = tune.tune_skewers(table, scfg, (boxes[0][0], boxes[1][0]), cfg["nx"], cfg["ny"], cfg["nz"],
+                                     grf.pitch_of(cfg["nz"]), cfg["dcell"], use_cache=False)
+        if sk_tuned["choice"]["pair"] != chunk.pair:
+            chunk.pair = sk_tuned["choice"]["pair"]
+            chunk._runner = None
+            runner = chunk._prepare(table.start, table.direction, table.npix)
+        tuned = dict(tuned, skewers=sk_tuned)
     nx, ny, nz = cfg["nx"], cfg["ny"], cfg["nz"]
     cells = nx * ny * nz
     pixels = table.total_pixels

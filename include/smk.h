@@ -158,6 +158,9 @@ int smk_tune_get(int32_t pass, int32_t n);
  * expect 16 bytes more than its copies deliver, with a ~10 ms limit, so each wait runs out; the
  * pass then writes NaN and smk_grf_check reports SMK_ENULLBOX.  Nothing faults or hangs. */
 #define SMK_TUNE_TMA_WAIT_TEST 4
+/* Resident blocks per SM of smk_skewers_flux's persistent launch: 0 (default) as many as fit,
+ * k in 1..32 at most k (the skewer autotuner's knob). */
+#define SMK_TUNE_SKEWER_BLOCKS 5
 int smk_tune_flag(int32_t flag, int32_t value, int32_t* previous);
 
 /* ---------------------------------------------------------------- skewers (make_spectra +
@@ -312,8 +315,8 @@ typedef struct {
     const double* kedges;   /* [nkb+1] k bin edges, h/Mpc (device)                        */
     double dx;              /* pixel size, Mpc/h                                          */
     const float* chirp;     /* optional (with chirp_off): smk_fit_chirps' table of the chirp */
-                            /* spectra of the problem's lengths (one transform of the three  */
-                            /* of each Bluestein DFT saved), or NULL                        */
+                            /* spectra and chirps of the problem's lengths (one transform of */
+                            /* the three of each Bluestein DFT saved), or NULL              */
     const int64_t* chirp_off; /* [2049]: offset (complex elements) of length N's spectrum in */
                               /* chirp, or -1 (then computed in the kernel)                    */
     int32_t n_max;          /* largest npix of the problem (sizes the kernels' shared memory */
@@ -328,11 +331,12 @@ typedef struct {
 /* Cyclic convolution length of the Bluestein DFT of a length-n skewer: the smallest
  * 2^a 3^b 5^c >= 2n - 1 (0 outside 1..2048).  No counterpart in the reference. */
 int smk_fit_bluestein_m(int32_t n);
-/* Chirp spectra of the Bluestein DFTs (they depend on the skewer lengths only, not on theta):
- * for i < n_lengths, out[2*offsets[i] .. 2*(offsets[i] + M_i)) receives the complex FFT_M of
- * the length-lengths[i] chirp, M_i = smk_fit_bluestein_m(lengths[i]) (device arrays, offsets
- * in complex elements).  SmkFitProblem.chirp_off[N] = offsets[i] for N = lengths[i], -1 for
- * lengths without an entry.  No counterpart in the reference. */
+/* Chirp tables of the Bluestein DFTs (they depend on the skewer lengths only, not on theta):
+ * for i < n_lengths, out[2*offsets[i] .. 2*(offsets[i] + M_i + N_i)) receives the complex FFT_M
+ * of the length-N_i chirp (N_i = lengths[i], M_i = smk_fit_bluestein_m(N_i)) followed by the
+ * chirp w_n = exp(-i pi n^2 / N_i) itself for n < N_i (device arrays, offsets in complex
+ * elements).  SmkFitProblem.chirp_off[N] = offsets[i] for N = lengths[i], -1 for lengths
+ * without an entry.  No counterpart in the reference. */
 int smk_fit_chirps(int32_t n_lengths, const int32_t* lengths, const int64_t* offsets, float* out,
                    void* stream);
 /* Host: pairs of equal-length skewers for the fit kernels (order_out: 2n + 16 ints). */

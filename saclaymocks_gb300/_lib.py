@@ -149,6 +149,7 @@ def load(path: str | None = None):
 
 
 SMK_TUNE_XGEN_SPLIT, SMK_TUNE_PREFETCH, SMK_TUNE_TMA, SMK_TUNE_TMA_WAIT_TEST = 0, 1, 3, 4
+SMK_TUNE_SKEWER_BLOCKS = 5
 
 
 def tune_flag(flag: int, value: int) -> int:

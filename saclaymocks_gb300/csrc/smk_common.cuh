@@ -6,9 +6,15 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "../../include/smk.h"
 
 namespace smk {
+
+// Process-wide cap on the skewer kernel's resident blocks per SM (SMK_TUNE_SKEWER_BLOCKS; 0:
+// as many as fit), defined in smk_skewers.cu.
+extern std::atomic<int> g_skewer_blocks;
 
 // ------------------------------------------------------------------ status (host)
 // Records a message for smk_last_error() and returns the code.

@@ -147,10 +147,11 @@ __global__ void __launch_bounds__(FIT_T) fit_flux_kernel(const FitArgs a) {
 }
 
 // ------------------------------------------------------------------ Bluestein DFT helpers
-// chirp w_n = exp(-i pi n^2 / N) = exp(-2 pi i r / 2N), r = n^2 mod 2N (exact integers)
+// chirp w_n = exp(-i pi n^2 / N) = exp(-2 pi i r / 2N), r = n^2 mod 2N (exact integers;
+// n < N <= 2048, so n^2 fits 32 bits)
 __device__ __forceinline__ float2 chirp(int n, int N) {
-    const long long r = ((long long)n * n) % (2LL * N);
-    return twiddle((int)r, 2 * N);
+    const int r = (n * n) % (2 * N);
+    return twiddle(r, 2 * N);
 }
 
 // Smallest M = 2^a 3^b 5^c >= 2N - 1 (N <= 2048, so M <= 4096): the cyclic convolution length
@@ -178,15 +179,16 @@ __device__ __forceinline__ float2 chirp_b(int n, int N, int M) {
 // Unnormalised length-N DFT of the complex sequence held in s1[0..N) (natural order),
 // forward (e^{-}) or inverse (e^{+}); result left in s1[0..N) in natural order.  s2 is
 // scratch of M elements; tw the twiddle table of M.  Bc (may be null): FFT_M of the forward
-// chirp in the engine's digit-reversed order, which saves one of the three transforms.
-// Block-synchronous.
+// chirp in the engine's digit-reversed order, which saves one of the three transforms, followed
+// by the chirp w_n itself for n < N (the same values chirp() computes).  Block-synchronous.
 template <bool INV>
 __device__ void bluestein(float2* s1, float2* s2, const float2* tw, int N, int M, const FftPlan& pl,
                           const float2* __restrict__ Bc) {
+    const float2* __restrict__ Wt = Bc ? Bc + M : nullptr;
     // a_n = x_n w_n (INV: x_n conj(w_n)); b = the chirp (INV: its conjugate)
     for (int n = threadIdx.x; n < M; n += FIT_T) {
         if (n < N) {
-            const float2 w = chirp(n, N);
+            const float2 w = Wt ? __ldg(Wt + n) : chirp(n, N);
             s1[n] = INV ? cmulc(s1[n], w) : cmul(s1[n], w);
         } else {
             s1[n] = make_float2(0.f, 0.f);
@@ -211,7 +213,7 @@ __device__ void bluestein(float2* s1, float2* s2, const float2* tw, int N, int M
     fft_tile<true, 1, 1, FIT_T, 16>(s1, tw, pl);
     const float inv_m = 1.0f / (float)M;
     for (int k = threadIdx.x; k < N; k += FIT_T) {
-        const float2 w = chirp(k, N);
+        const float2 w = Wt ? __ldg(Wt + k) : chirp(k, N);
         const float2 c = cscale(s1[k], inv_m);
         s1[k] = INV ? cmulc(c, w) : cmul(c, w);
     }
@@ -538,7 +540,8 @@ __global__ void __launch_bounds__(FIT_T, 3) fit_adjoint_kernel(const FitArgs a) 
 }
 
 // FFT_M of the forward chirp of each length (one block per length), in the order the engine
-// leaves a forward transform: the same arithmetic as bluestein() without a table.
+// leaves a forward transform: the same arithmetic as bluestein() without a table; then the
+// chirp w_n itself for n < N.
 __global__ void __launch_bounds__(FIT_T) fit_chirp_kernel(const int32_t* lengths, const int64_t* offsets,
                                                           float2* out) {
     extern __shared__ float2 smem[];
@@ -555,6 +558,7 @@ __global__ void __launch_bounds__(FIT_T) fit_chirp_kernel(const int32_t* lengths
     fft_tile<false, 1, 1, FIT_T, 16>(s, tw, pl);
     float2* o = out + offsets[blockIdx.x];
     for (int n = threadIdx.x; n < M; n += FIT_T) o[n] = s[n];
+    for (int n = threadIdx.x; n < N; n += FIT_T) o[M + n] = chirp(n, N);
 }
 
 static int fit_grid(const void* kernel, size_t smem, int64_t items, int* grid) {

@@ -476,6 +476,9 @@ int smk_tune_flag(int32_t flag, int32_t value, int32_t* previous) {
     } else if (flag == SMK_TUNE_TMA) {
         if (value < 0 || value > 2) return fail(SMK_EINVAL, "smk_tune_flag: TMA must be 0, 1 or 2");
         old = g_tma.exchange(value);
+    } else if (flag == SMK_TUNE_SKEWER_BLOCKS) {
+        if (value < 0 || value > 32) return fail(SMK_EINVAL, "smk_tune_flag: SKEWER_BLOCKS must be 0..32");
+        old = g_skewer_blocks.exchange(value);
     } else if (flag == SMK_TUNE_PREFETCH) {
         if (value < 0 || value > 1) return fail(SMK_EINVAL, "smk_tune_flag: PREFETCH must be 0 or 1");
         old = g_prefetch.exchange(value);

@@ -16,6 +16,8 @@
 
 namespace smk {
 
+std::atomic<int> g_skewer_blocks{0};
+
 constexpr int SK_T = 256;
 constexpr int SK_NCLASS = 5;  // small-scale FFT lengths 256 << j
 
@@ -623,7 +625,10 @@ int smk_skewers_flux(const SmkSkewers* sk, const SmkSpectraParams* p, const floa
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, SK_T, smem) != cudaSuccess)
         return check_launch("occupancy(skewer_kernel)");
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(a.n_items, (int64_t)std::max(per_sm, 1) * nsm));
+    int per = std::max(per_sm, 1);
+    const int cap = g_skewer_blocks.load();
+    if (cap > 0) per = std::min(per, cap);
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(a.n_items, (int64_t)per * nsm));
     kern<<<grid, SK_T, smem, st>>>(a);
     return check_launch("skewer_kernel");
 }

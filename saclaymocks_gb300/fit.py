@@ -63,9 +63,10 @@ class FitProblem:
         self.d_off = torch.from_numpy(self.offset).to(dv)
         self.d_npix = torch.from_numpy(self.lengths).to(dv)
         self.d_kedges = torch.from_numpy(self.kedges).to(dv)
-        # chirp spectra of every distinct length (independent of theta): one table, built once
+        # chirp spectra and chirps of every distinct length (independent of theta): one table,
+        # built once, M + N complex values per length
         uniq = np.unique(self.lengths).astype(np.int32)
-        msz = np.array([lib.smk_fit_bluestein_m(int(N)) for N in uniq], np.int64)
+        msz = np.array([lib.smk_fit_bluestein_m(int(N)) + int(N) for N in uniq], np.int64)
         offs = np.concatenate([[0], np.cumsum(msz[:-1])]).astype(np.int64)
         self.chirp = torch.empty(2 * int(msz.sum()), dtype=torch.float32, device=dv)
         off_by_n = np.full(2049, -1, np.int64)

@@ -29,8 +29,10 @@ class _PendingFlux:
 
 class MockChunk:
     def __init__(self, nx, ny, nz, dcell=2.19, *, seed=1, k0=0.02, want_eta=True,
-                 cfg: spectra.SpectraConfig | None = None, dpix=0.2, device="cuda", xi_chunk_kz: int = 128):
+                 cfg: spectra.SpectraConfig | None = None, dpix=0.2, device="cuda", xi_chunk_kz: int = 128,
+                 pair: bool = True):
         self.nx, self.ny, self.nz, self.dcell = nx, ny, nz, dcell
+        self.pair = pair                   # skewer schedule: pairs of equal FFT length (False: one per item)
         self.xi_chunk_kz = xi_chunk_kz     # grf.make_boxes: blocked x-pass intermediate (0: in place)
         self.seed, self.k0, self.dpix = seed, k0, dpix
         self.cfg = cfg or spectra.SpectraConfig()
@@ -50,7 +52,7 @@ class MockChunk:
         table = spectra.SkewerTable(start, direction, npix, dpix=self.dpix)
         key = (table.n, table.total_pixels)
         if self._runner is None or self._key != key:
-            self._runner = spectra.SkewerRunner(table, self.cfg, device=self.device)
+            self._runner = spectra.SkewerRunner(table, self.cfg, device=self.device, pair=self.pair)
             self._pin_in = [[torch.empty(x.shape, dtype=t, pin_memory=True) for x, t in
                              ((table.start, torch.float32), (table.direction, torch.float32),
                               (table.npix, torch.int32), (table.offset, torch.int64))] for _ in range(2)]

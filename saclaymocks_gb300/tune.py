@@ -132,3 +132,56 @@ def tune_grf(nx: int, ny: int, nz: int, dcell: float = 2.19, gpu_noise: bool = T
     return {"choices": {PASS_NAMES[p]: (best[(p, n)], *info[p][best[(p, n)]]) for p, n, _ in passes},
             "ms": {PASS_NAMES[p]: {int(v): round(m, 3) for v, m in times[p].items()} for p, _, _ in passes},
             "cached": False}
+
+
+def tune_skewers(table, cfg, boxes, nx: int, ny: int, nz: int, pitch: int, dcell: float, reps: int = 3,
+                 blocks=(0, 1, 2, 3), use_cache: bool = True) -> dict:
+    """Pick the skewer stage's launch shape for this table: the paired schedule (two skewers of
+    one small-scale FFT length per work item) or one skewer per item, and the resident blocks per
+    SM of the persistent launch (SMK_TUNE_SKEWER_BLOCKS; 0: as many as fit), by timing
+    smk_skewers_flux on `boxes` = (delta_pad, eta_pad).  Applies the block cap and returns
+    {"choice": {"pair": bool, "blocks": int}, "ms": {"pair=..,blocks=..": ms}}; the caller builds
+    its runner with the chosen schedule."""
+    from . import spectra
+    key = f"skewers:{int(cfg.ss_nz)}:{int(cfg.ss_mode)}"
+    if use_cache:
+        try:
+            with open(CACHE) as f:
+                dev = json.load(f).get(_device_key(), {})
+        except (OSError, ValueError):
+            dev = {}
+        if key in dev:
+            code = int(dev[key])
+            _lib.tune_flag(_lib.SMK_TUNE_SKEWER_BLOCKS, code >> 1)
+            return {"choice": {"pair": bool(code & 1), "blocks": code >> 1}, "ms": {}, "cached": True}
+    flux = torch.empty(table.total_pixels, dtype=torch.float32, device="cuda")
+    kw = dict(nx=nx, ny=ny, nz=nz, pitch=pitch, dcell=dcell, flux=flux)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    times = {}
+    for pair in (True, False):
+        runner = spectra.SkewerRunner(table, cfg, pair=pair)
+        for b in blocks:
+            _lib.tune_flag(_lib.SMK_TUNE_SKEWER_BLOCKS, int(b))
+            runner.run(boxes[0], boxes[1], **kw)            # launch set-up
+            torch.cuda.synchronize()
+            ev[0].record()
+            for _ in range(reps):
+                runner.run(boxes[0], boxes[1], **kw)
+            ev[1].record()
+            torch.cuda.synchronize()
+            times[(pair, int(b))] = ev[0].elapsed_time(ev[1]) / reps
+        del runner
+    pair, b = min(times, key=times.get)
+    _lib.tune_flag(_lib.SMK_TUNE_SKEWER_BLOCKS, b)
+    try:
+        with open(CACHE) as f:
+            cache = json.load(f)
+    except (OSError, ValueError):
+        cache = {}
+    cache.setdefault(_device_key(), {})[key] = 2 * b + int(pair)
+    os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+    with open(CACHE, "w") as f:
+        json.dump(cache, f, indent=1, sort_keys=True)
+    return {"choice": {"pair": pair, "blocks": b},
+            "ms": {f"pair={int(p)},blocks={k}": round(t, 3) for (p, k), t in times.items()}, "cached": False}
+

@@ -120,10 +120,11 @@ def test_tune_flags(lib):
 
 
 def test_tma_flags(lib):
-    """The y pass's TMA mode and the TMA wait test switch are host-only settings with checked
-    ranges."""
+    """The y pass's TMA mode, the TMA wait test switch and the skewer kernel's block cap are
+    host-only settings with checked ranges."""
     for flag, good, bad in ((_lib.SMK_TUNE_TMA, (0, 1, 2), (3, -1)),
-                            (_lib.SMK_TUNE_TMA_WAIT_TEST, (0, 1), (2, -1))):
+                            (_lib.SMK_TUNE_TMA_WAIT_TEST, (0, 1), (2, -1)),
+                            (_lib.SMK_TUNE_SKEWER_BLOCKS, (0, 1, 4, 32), (33, -1))):
         first = _lib.tune_flag(flag, good[0])
         for v in good[1:]:
             _lib.tune_flag(flag, v)

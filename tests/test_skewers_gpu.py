@@ -356,3 +356,34 @@ def test_longest_skewer_of_the_fft_rule(env, boxes):
     ref = _oracle(boxes, t, dict(kind="const", a=0.1, b=1.6, c=0.5),
                   small=dict(pixsize=0.2, nz="rule", pmiss=pm), noise1d=[x.astype(np.float64) for x in noise1d])
     _cmp(g, ref, np.std(boxes["d"]))
+
+
+def test_skewer_tuner_choice_and_block_cap(env, boxes):
+    """The skewer autotuner times the paired and one-per-item schedules at several resident-block
+    caps and applies its choice; a block cap changes only how many blocks share the work
+    (flux identical bit for bit), the schedule only the packing of the small-scale FFTs (flux
+    within float32 rounding)."""
+    _lib, _, spectra = env
+    from saclaymocks_gb300 import tune
+    L = np.array([boxes["nx"], boxes["ny"], boxes["nz"]]) * boxes["dx"]
+    t = spectra.skewers_cone(60, L, seed=7, npix_range=(100, 600))
+    cfg = spectra.SpectraConfig(ss_mode=_lib.SMK_SS_PHILOX, ss_nz=2048, seed=5, a=0.1, b=1.6, c=0.5)
+    out = boxes["out"]
+    kw = dict(nx=boxes["nx"], ny=boxes["ny"], nz=boxes["nz"], pitch=out.pitch, dcell=boxes["dx"])
+    try:
+        _lib.tune_flag(_lib.SMK_TUNE_SKEWER_BLOCKS, 0)
+        f0 = spectra.SkewerRunner(t, cfg).run(out.delta_pad[0], out.eta_pad[0], **kw).clone()
+        _lib.tune_flag(_lib.SMK_TUNE_SKEWER_BLOCKS, 1)
+        f1 = spectra.SkewerRunner(t, cfg).run(out.delta_pad[0], out.eta_pad[0], **kw).clone()
+        torch.cuda.synchronize()
+        assert torch.equal(f0, f1)
+        res = tune.tune_skewers(t, cfg, (out.delta_pad[0], out.eta_pad[0]), reps=1, use_cache=False, **kw)
+        ch = res["choice"]
+        assert ch["blocks"] in (0, 1, 2, 3) and isinstance(ch["pair"], bool)
+        assert len(res["ms"]) == 8 and all(v > 0 for v in res["ms"].values())
+        assert _lib.tune_flag(_lib.SMK_TUNE_SKEWER_BLOCKS, ch["blocks"]) == ch["blocks"]
+        fc = spectra.SkewerRunner(t, cfg, pair=ch["pair"]).run(out.delta_pad[0], out.eta_pad[0], **kw)
+        torch.cuda.synchronize()
+        assert float((fc - f0).abs().max()) <= F_ATOL
+    finally:
+        _lib.tune_flag(_lib.SMK_TUNE_SKEWER_BLOCKS, 0)
