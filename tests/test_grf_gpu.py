@@ -320,7 +320,7 @@ def test_fixed_length_variants_equal_run_time_plan_variants(G):
     lib = _lib.load()
     checked = 0
     for pid, axis in ((_lib.SMK_PASS_LINE, 1), (_lib.SMK_PASS_XGEN, 0), (_lib.SMK_PASS_XPASS, 0),
-                      (_lib.SMK_PASS_ZFWD, 2), (_lib.SMK_PASS_ZINV, 2)):
+                      (_lib.SMK_PASS_ZFWD, 2)):
         info = {}
         w, t, nm = C.c_int32(), C.c_int32(), C.c_int32()
         for v in range(lib.smk_tune_count(pid)):
