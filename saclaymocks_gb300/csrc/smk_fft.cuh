@@ -376,14 +376,17 @@ struct CtStage {
     __device__ __forceinline__ static int div(int x) { return M == 1 ? x : x / M; }
 };
 
-template <int R, bool INV, int W, int SN, int T, bool OUT, bool PRE, class SP, class Out, class Pre>
+// Butterflies [bf0, bf1) of the stage (bf1 < 0: all); SYNC: a block barrier at the end (in-place
+// stages only).
+template <int R, bool INV, int W, int SN, int T, bool OUT, bool PRE, class SP, class Out, class Pre,
+          bool SYNC = true>
 __device__ __forceinline__ void fft_stage_body(float2* __restrict__ s, const float2* __restrict__ tw, const SP& sp,
-                                               Out&& out, Pre&& pre) {
+                                               Out&& out, Pre&& pre, const int bf0 = 0, const int bf1 = -1) {
     const int m = sp.m;
-    const int nb = (sp.n / R) * W;
+    const int nb = bf1 < 0 ? (sp.n / R) * W : bf1;
     const float2* tws = tw + sp.twoff - 1;
 #pragma unroll(T >= 1024 ? 1 : 2)
-    for (int bf = threadIdx.x; bf < nb; bf += T) {
+    for (int bf = bf0 + threadIdx.x; bf < nb; bf += T) {
         const int j = bf / W, w = bf % W;
         const int blk = sp.div(j);
         const int q = j - blk * m;
@@ -418,7 +421,7 @@ __device__ __forceinline__ void fft_stage_body(float2* __restrict__ s, const flo
             for (int r = 0; r < R; ++r) p[r * m * SN] = v[r];
         }
     }
-    if constexpr (!OUT) __syncthreads();
+    if constexpr (!OUT && SYNC) __syncthreads();
 }
 
 template <int R, bool INV, int W, int SN, int T, bool OUT = false, bool PRE = false, class Out = NoOut,
@@ -483,6 +486,32 @@ __device__ __forceinline__ void fft_tile(float2* __restrict__ s, const float2* _
     } else {
         for (int st = pl.nst - 1; st >= 0; --st) fft_stage_any<true, W, SN, T, RMAX>(s, tw, pl, st);
     }
+}
+
+// The inverse of ifft_tile_out for a fixed plan whose first executed stage works on contiguous
+// groups (m = 1) that split evenly at n / 2: that stage runs on the first half of the elements,
+// then mid() (which must leave the second half in s and end with a block barrier), then on the
+// second half, then the other stages.  Lets the second half of a tile still be arriving while
+// the first is transformed.
+template <int W, int SN, int T, int RMAX, int NF, class Mid, class Out>
+__device__ __forceinline__ void ifft_tile_out_split(float2* __restrict__ s, const float2* __restrict__ tw,
+                                                    Mid&& mid, Out&& out) {
+    using FP = FixedPlan<NF, RMAX>;
+    constexpr int NST = FP::P.nst;
+    constexpr int S0 = NST - 1;
+    constexpr int R0 = FP::P.r[S0];
+    static_assert(NST >= 2 && FP::P.m[S0] == 1 && (NF / 2) % R0 == 0, "split needs contiguous first groups");
+    constexpr int HALF = (NF / 2 / R0) * W;
+    const CtStage<1, NF, FP::P.twoff[S0]> sp0{};
+    fft_stage_body<R0, true, W, SN, T, false, false, CtStage<1, NF, FP::P.twoff[S0]>, NoOut, NoPre, false>(
+        s, tw, sp0, NoOut{}, NoPre{}, 0, HALF);
+    mid();
+    fft_stage_body<R0, true, W, SN, T, false, false, CtStage<1, NF, FP::P.twoff[S0]>, NoOut, NoPre, true>(
+        s, tw, sp0, NoOut{}, NoPre{}, HALF, (NF / R0) * W);
+    static_for<1, NST - 1>([&](auto c) {
+        fft_stage_fixed<NF, RMAX, NST - 1 - decltype(c)::value, true, W, SN, T>(s, tw);
+    });
+    fft_stage_fixed<NF, RMAX, 0, true, W, SN, T, true>(s, tw, out);
 }
 
 // Inverse of the W lines with the last stage's natural-order results handed to out(e, w, v)

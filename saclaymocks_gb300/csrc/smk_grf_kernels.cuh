@@ -190,7 +190,8 @@ template <class C, bool INV>
 __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_constant__ LineArgs a) {
     constexpr int W = C::W, T = C::T;
     extern __shared__ __align__(128) float2 smem[];
-    __shared__ __align__(8) uint64_t bar;   // TMA completion of the current tile
+    __shared__ __align__(8) uint64_t bar;    // TMA completion of the current tile (its first half if split)
+    __shared__ __align__(8) uint64_t bar2;   // second half of the tile (split)
     __shared__ int timed_out;
     const int n = a.pl.n;
     float2* s = smem;
@@ -200,11 +201,16 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
         timed_out = 0;
         if (a.tma) {
             mbar_init(&bar, 1);
+            mbar_init(&bar2, 1);
             mbar_fence_init();
         }
     }
     __syncthreads();
     unsigned parity = 0;
+    // Split tile (inverse with a compile-time plan whose first stage works on contiguous groups,
+    // TMA loads into shared memory): the first half of the rows completes on bar, the second on
+    // bar2, and the first stage runs on the first half while the second is still arriving.
+    const bool split = INV && C::NF > 0 && a.tma == 1 && (n / 2) % a.box_rows == 0;
     const int64_t ncolt = ceil_div(a.ncol, W);
     const int64_t tpb = a.n_outer * ncolt;
     const int64_t ntiles = tpb * a.nbuf;
@@ -220,25 +226,34 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
             // n / box_rows tensor boxes of W columns (columns past ncol read as zeros)
             if (threadIdx.x == 0) {
                 if (a.tma == 2) bulk_wait_read_all();   // the previous tile's stores have read s
-                mbar_arrive_expect_tx(&bar, (unsigned)(n * W * sizeof(float2)) + (unsigned)a.tma_extra_tx);
-                for (int e0 = 0; e0 < n; e0 += a.box_rows) {
-                    if (src)
-                        tma_load_5d(s + e0 * W, &a.tmap[buf], &bar, 0, 0, e0, (int)o, cb);
-                    else
-                        tma_load_3d(s + e0 * W, &a.tmap[buf], &bar, a.col0 + cb * W, e0, (int)o);
+                const int nh = split ? n / 2 : n;
+                for (int part = 0; part < (split ? 2 : 1); ++part) {
+                    uint64_t* b = part ? &bar2 : &bar;
+                    const int e_lo = part ? nh : 0, e_hi = part ? n : nh;
+                    mbar_arrive_expect_tx(b, (unsigned)((e_hi - e_lo) * W * sizeof(float2)) +
+                                                 (part ? 0u : (unsigned)a.tma_extra_tx));
+                    for (int e0 = e_lo; e0 < e_hi; e0 += a.box_rows) {
+                        if (src)
+                            tma_load_5d(s + e0 * W, &a.tmap[buf], b, 0, 0, e0, (int)o, cb);
+                        else
+                            tma_load_3d(s + e0 * W, &a.tmap[buf], b, a.col0 + cb * W, e0, (int)o);
+                    }
                 }
             }
             // bounded wait (~1 s at 2 GHz): on time-out the tile is poisoned with NaN, which the
             // z pass counts as non-finite cells (SMK_ENULLBOX from smk_grf_check), and the
-            // block stops after a last bounded wait for its copies
+            // block stops after a last bounded wait for its copies (split: the second half's wait
+            // and the poisoning happen inside the transform, after its first stage's first half)
             if (!mbar_wait_bounded(&bar, parity, a.tma_wait_limit)) timed_out = 1;
-            parity ^= 1u;
-            __syncthreads();
-            if (timed_out) {
-                if (threadIdx.x == 0) mbar_wait_bounded(&bar, parity ^ 1u, a.tma_wait_limit);
+            if (!split) {
+                parity ^= 1u;
                 __syncthreads();
-                for (int i = threadIdx.x; i < n * W; i += T) s[i] = make_float2(__int_as_float(0x7fc00000), 0.f);
-                __syncthreads();
+                if (timed_out) {
+                    if (threadIdx.x == 0) mbar_wait_bounded(&bar, parity ^ 1u, a.tma_wait_limit);
+                    __syncthreads();
+                    for (int i = threadIdx.x; i < n * W; i += T) s[i] = make_float2(__int_as_float(0x7fc00000), 0.f);
+                    __syncthreads();
+                }
             }
         } else if (src) {
             // W / src_kb contiguous runs of n * src_kb complex values, 16 bytes per copy
@@ -289,9 +304,31 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
         } else if constexpr (INV) {
             // the last stage stores straight from registers
             const int64_t es = a.estride;
-            ifft_tile_out<W, W, T, C::RMAX, C::NF>(s, tw, a.pl, [&](int e, int w, float2 v) {
+            auto store = [&](int e, int w, float2 v) {
                 if (w < cols) base[e * es + w] = v;
-            });
+            };
+            if constexpr (C::NF > 0) {
+                if (split) {
+                    ifft_tile_out_split<W, W, T, C::RMAX, C::NF>(s, tw, [&]() {
+                        if (!mbar_wait_bounded(&bar2, parity, a.tma_wait_limit)) timed_out = 1;
+                        parity ^= 1u;
+                        __syncthreads();
+                        if (timed_out) {
+                            if (threadIdx.x == 0) {
+                                mbar_wait_bounded(&bar, parity ^ 1u, a.tma_wait_limit);
+                                mbar_wait_bounded(&bar2, parity ^ 1u, a.tma_wait_limit);
+                            }
+                            __syncthreads();
+                            for (int i = threadIdx.x; i < n * W; i += T) s[i] = make_float2(__int_as_float(0x7fc00000), 0.f);
+                            __syncthreads();
+                        }
+                    }, store);
+                } else {
+                    ifft_tile_out<W, W, T, C::RMAX, C::NF>(s, tw, a.pl, store);
+                }
+            } else {
+                ifft_tile_out<W, W, T, C::RMAX, C::NF>(s, tw, a.pl, store);
+            }
         } else {
             fft_tile<INV, W, W, T, C::RMAX, C::NF>(s, tw, a.pl);
             if (a.dst)

@@ -126,13 +126,15 @@ def test_y_pass_tma_loads_equal_cp_async(G, shape):
         _lib.tune_flag(_lib.SMK_TUNE_TMA, prev)
 
 
-def test_y_pass_tma_wait_running_out_is_reported(G):
+@pytest.mark.parametrize("shape", [(8, 512, 16), (4, 2560, 8)])
+def test_y_pass_tma_wait_running_out_is_reported(G, shape):
     """A y-pass TMA wait that runs out (the barrier made to expect more bytes than its copies
     bring) ends within its limit, leaves NaN that the box check reports as SMK_ENULLBOX, and
-    the next call on the same context is correct again."""
+    the next call on the same context is correct again; at y = 2560 the tile load is split in
+    two halves (the first stage starts on the first) and the first half's wait runs out."""
     from saclaymocks_gb300 import _lib
     from saclaymocks_gb300._lib import SmkError
-    nx, ny, nz = 8, 512, 16
+    nx, ny, nz = shape
     good = G.make_boxes(nx, ny, nz, 2.19, seed=7)
     torch.cuda.synchronize()
     prev = _lib.tune_flag(_lib.SMK_TUNE_TMA, 1)
