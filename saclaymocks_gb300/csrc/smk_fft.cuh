@@ -489,25 +489,27 @@ __device__ __forceinline__ void fft_tile(float2* __restrict__ s, const float2* _
 }
 
 // The inverse of ifft_tile_out for a fixed plan whose first executed stage works on contiguous
-// groups (m = 1) that split evenly at n / 2: that stage runs on the first half of the elements,
-// then mid() (which must leave the second half in s and end with a block barrier), then on the
-// second half, then the other stages.  Lets the second half of a tile still be arriving while
-// the first is transformed.
-template <int W, int SN, int T, int RMAX, int NF, class Mid, class Out>
-__device__ __forceinline__ void ifft_tile_out_split(float2* __restrict__ s, const float2* __restrict__ tw,
-                                                    Mid&& mid, Out&& out) {
+// groups (m = 1), with the elements in ns equal parts (each a whole number of groups): that
+// stage runs part by part, wait(p) called before part p >= 1 (the caller has the first part),
+// then after() once every part is done (after a block barrier), then the other stages.  Lets
+// the later parts of a tile still be arriving while the first are transformed.
+template <int W, int SN, int T, int RMAX, int NF, class Wait, class After, class Out>
+__device__ __forceinline__ void ifft_tile_out_parts(float2* __restrict__ s, const float2* __restrict__ tw,
+                                                    const int ns, Wait&& wait, After&& after, Out&& out) {
     using FP = FixedPlan<NF, RMAX>;
     constexpr int NST = FP::P.nst;
     constexpr int S0 = NST - 1;
     constexpr int R0 = FP::P.r[S0];
-    static_assert(NST >= 2 && FP::P.m[S0] == 1 && (NF / 2) % R0 == 0, "split needs contiguous first groups");
-    constexpr int HALF = (NF / 2 / R0) * W;
-    const CtStage<1, NF, FP::P.twoff[S0]> sp0{};
-    fft_stage_body<R0, true, W, SN, T, false, false, CtStage<1, NF, FP::P.twoff[S0]>, NoOut, NoPre, false>(
-        s, tw, sp0, NoOut{}, NoPre{}, 0, HALF);
-    mid();
-    fft_stage_body<R0, true, W, SN, T, false, false, CtStage<1, NF, FP::P.twoff[S0]>, NoOut, NoPre, true>(
-        s, tw, sp0, NoOut{}, NoPre{}, HALF, (NF / R0) * W);
+    static_assert(NST >= 2 && FP::P.m[S0] == 1, "parts need contiguous first groups");
+    using SP0 = CtStage<1, NF, FP::P.twoff[S0]>;
+    const int pb = (NF / R0 / ns) * W;   // butterflies per part
+    for (int p = 0; p < ns; ++p) {
+        if (p) wait(p);
+        fft_stage_body<R0, true, W, SN, T, false, false, SP0, NoOut, NoPre, false>(s, tw, SP0{}, NoOut{}, NoPre{},
+                                                                                    p * pb, (p + 1) * pb);
+    }
+    __syncthreads();
+    after();
     static_for<1, NST - 1>([&](auto c) {
         fft_stage_fixed<NF, RMAX, NST - 1 - decltype(c)::value, true, W, SN, T>(s, tw);
     });

@@ -184,14 +184,15 @@ struct LineArgs {
     int dst_kb;
 };
 
+constexpr int LINE_PARTS = 4;   // most parts a y tile's TMA load is split into
+
 // Forward: natural -> digit-reversed order along the axis (kept in HBM); inverse: back.
 // smem: s[n*W] | tw[n]
 template <class C, bool INV>
 __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_constant__ LineArgs a) {
     constexpr int W = C::W, T = C::T;
     extern __shared__ __align__(128) float2 smem[];
-    __shared__ __align__(8) uint64_t bar;    // TMA completion of the current tile (its first half if split)
-    __shared__ __align__(8) uint64_t bar2;   // second half of the tile (split)
+    __shared__ __align__(8) uint64_t bar[LINE_PARTS];   // TMA completion of the tile (of each of its parts)
     __shared__ int timed_out;
     const int n = a.pl.n;
     float2* s = smem;
@@ -200,17 +201,27 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
     if (threadIdx.x == 0) {
         timed_out = 0;
         if (a.tma) {
-            mbar_init(&bar, 1);
-            mbar_init(&bar2, 1);
+            for (int p = 0; p < LINE_PARTS; ++p) mbar_init(&bar[p], 1);
             mbar_fence_init();
         }
     }
     __syncthreads();
     unsigned parity = 0;
-    // Split tile (inverse with a compile-time plan whose first stage works on contiguous groups,
-    // TMA loads into shared memory): the first half of the rows completes on bar, the second on
-    // bar2, and the first stage runs on the first half while the second is still arriving.
-    const bool split = INV && C::NF > 0 && a.tma == 1 && (n / 2) % a.box_rows == 0;
+    // Tile in parts (inverse with a compile-time plan whose first stage works on contiguous groups
+    // of R0, TMA loads into shared memory): part p of the rows completes on bar[p], and the first
+    // stage runs on the parts that have arrived while the others are still in flight.  Parts are
+    // whole boxes and whole groups: ns = the largest of LINE_PARTS, 2 with n / ns a multiple of
+    // box_rows and of R0 (1: one part).
+    int ns = 1;
+    if constexpr (INV && C::NF > 0) {
+        constexpr int R0 = FixedPlan<C::NF, C::RMAX>::P.r[FixedPlan<C::NF, C::RMAX>::P.nst - 1];
+        if (a.tma == 1)
+            for (int k = LINE_PARTS; k >= 2; k /= 2)
+                if (n % k == 0 && (n / k) % a.box_rows == 0 && (n / k) % R0 == 0) {
+                    ns = k;
+                    break;
+                }
+    }
     const int64_t ncolt = ceil_div(a.ncol, W);
     const int64_t tpb = a.n_outer * ncolt;
     const int64_t ntiles = tpb * a.nbuf;
@@ -226,10 +237,10 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
             // n / box_rows tensor boxes of W columns (columns past ncol read as zeros)
             if (threadIdx.x == 0) {
                 if (a.tma == 2) bulk_wait_read_all();   // the previous tile's stores have read s
-                const int nh = split ? n / 2 : n;
-                for (int part = 0; part < (split ? 2 : 1); ++part) {
-                    uint64_t* b = part ? &bar2 : &bar;
-                    const int e_lo = part ? nh : 0, e_hi = part ? n : nh;
+                const int pr = n / ns;
+                for (int part = 0; part < ns; ++part) {
+                    uint64_t* b = &bar[part];
+                    const int e_lo = part * pr, e_hi = e_lo + pr;
                     mbar_arrive_expect_tx(b, (unsigned)((e_hi - e_lo) * W * sizeof(float2)) +
                                                  (part ? 0u : (unsigned)a.tma_extra_tx));
                     for (int e0 = e_lo; e0 < e_hi; e0 += a.box_rows) {
@@ -242,14 +253,14 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
             }
             // bounded wait (~1 s at 2 GHz): on time-out the tile is poisoned with NaN, which the
             // z pass counts as non-finite cells (SMK_ENULLBOX from smk_grf_check), and the
-            // block stops after a last bounded wait for its copies (split: the second half's wait
-            // and the poisoning happen inside the transform, after its first stage's first half)
-            if (!mbar_wait_bounded(&bar, parity, a.tma_wait_limit)) timed_out = 1;
-            if (!split) {
+            // block stops after a last bounded wait for its copies (in parts: the later parts' waits
+            // and the poisoning happen inside the transform, after its first stage)
+            if (!mbar_wait_bounded(&bar[0], parity, a.tma_wait_limit)) timed_out = 1;
+            if (ns == 1) {
                 parity ^= 1u;
                 __syncthreads();
                 if (timed_out) {
-                    if (threadIdx.x == 0) mbar_wait_bounded(&bar, parity ^ 1u, a.tma_wait_limit);
+                    if (threadIdx.x == 0) mbar_wait_bounded(&bar[0], parity ^ 1u, a.tma_wait_limit);
                     __syncthreads();
                     for (int i = threadIdx.x; i < n * W; i += T) s[i] = make_float2(__int_as_float(0x7fc00000), 0.f);
                     __syncthreads();
@@ -308,16 +319,14 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
                 if (w < cols) base[e * es + w] = v;
             };
             if constexpr (C::NF > 0) {
-                if (split) {
-                    ifft_tile_out_split<W, W, T, C::RMAX, C::NF>(s, tw, [&]() {
-                        if (!mbar_wait_bounded(&bar2, parity, a.tma_wait_limit)) timed_out = 1;
+                if (ns > 1) {
+                    ifft_tile_out_parts<W, W, T, C::RMAX, C::NF>(s, tw, ns, [&](int p) {
+                        if (!mbar_wait_bounded(&bar[p], parity, a.tma_wait_limit)) timed_out = 1;
+                    }, [&]() {
                         parity ^= 1u;
-                        __syncthreads();
                         if (timed_out) {
-                            if (threadIdx.x == 0) {
-                                mbar_wait_bounded(&bar, parity ^ 1u, a.tma_wait_limit);
-                                mbar_wait_bounded(&bar2, parity ^ 1u, a.tma_wait_limit);
-                            }
+                            if (threadIdx.x == 0)
+                                for (int p = 0; p < ns; ++p) mbar_wait_bounded(&bar[p], parity ^ 1u, a.tma_wait_limit);
                             __syncthreads();
                             for (int i = threadIdx.x; i < n * W; i += T) s[i] = make_float2(__int_as_float(0x7fc00000), 0.f);
                             __syncthreads();
