@@ -225,6 +225,18 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
     const int64_t ncolt = ceil_div(a.ncol, W);
     const int64_t tpb = a.n_outer * ncolt;
     const int64_t ntiles = tpb * a.nbuf;
+    // the source runs of this block's next tile into L2 (intermediate source)
+    auto prefetch_src = [&](int64_t tile) {
+        if (tile + gridDim.x >= ntiles) return;
+        const int64_t tn = tile + gridDim.x;
+        const int bn = (int)(tn / tpb);
+        const int64_t un = tn - bn * tpb;
+        const int64_t on = un / ncolt;
+        const int cbn = (int)(un - on * ncolt);
+        for (int q = 0; q < W / a.src_kb; ++q)
+            prefetch_l2_bulk(a.src[bn] + (((int64_t)cbn * (W / a.src_kb) + q) * a.n_outer + on) * n * a.src_kb,
+                             (uint32_t)(n * a.src_kb * sizeof(float2)));
+    };
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int buf = (int)(tile / tpb);
         const int64_t t = tile - buf * tpb;
@@ -250,6 +262,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
                             tma_load_3d(s + e0 * W, &a.tmap[buf], b, a.col0 + cb * W, e0, (int)o);
                     }
                 }
+                if (src && a.prefetch) prefetch_src(tile);
             }
             // bounded wait (~1 s at 2 GHz): on time-out the tile is poisoned with NaN, which the
             // z pass counts as non-finite cells (SMK_ENULLBOX from smk_grf_check), and the
@@ -282,17 +295,9 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
             __syncthreads();
         }
         if (src) {
-            // the next tile's source runs into L2 (two tiles ahead measured slower)
-            if (a.prefetch && threadIdx.x == 0 && tile + gridDim.x < ntiles) {
-                const int64_t tn = tile + gridDim.x;
-                const int bn = (int)(tn / tpb);
-                const int64_t un = tn - bn * tpb;
-                const int64_t on = un / ncolt;
-                const int cbn = (int)(un - on * ncolt);
-                for (int q = 0; q < W / a.src_kb; ++q)
-                    prefetch_l2_bulk(a.src[bn] + (((int64_t)cbn * (W / a.src_kb) + q) * a.n_outer + on) * n * a.src_kb,
-                                     (uint32_t)(n * a.src_kb * sizeof(float2)));
-            }
+            // the next tile's source runs into L2 (two tiles ahead measured slower); with TMA
+            // issued with the current tile's loads, above
+            if (!a.tma && a.prefetch && threadIdx.x == 0) prefetch_src(tile);
         } else if (a.prefetch && tile + gridDim.x < ntiles) {
             // the next tile of this block: one line per row segment of its W columns
             const int64_t tn = tile + gridDim.x;
