@@ -370,12 +370,13 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         }
     } else {
         // 1. r2c along z of the caller's noise
-        ZFwdArgs za;
+        ZFwdArgs za = {};
         za.pl = plzf;
         za.batch = p->batch;
         za.pitch = pitch;
         za.noise = p->noise;
         za.out = delta;
+        za.prefetch = g_prefetch.load();
         if ((rc = run_zfwd(vzf, za, rows_per_box, st))) return rc;
         if ((rc = mark(1))) return rc;
         // 2. c2c along y, forward (the y spectrum stays in digit-reversed order); 3. x: forward,

@@ -106,6 +106,7 @@ struct ZFwdArgs {
     int64_t pitch;
     const float* noise;  // dense [batch][rows_per_box][nz]
     float* out;
+    int prefetch;        // one-warp-per-row-pair form: pull the next pair's rows into L2
 };
 
 // r2c along z of the caller's white noise (two rows per complex line).
@@ -262,7 +263,6 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
                             tma_load_3d(s + e0 * W, &a.tmap[buf], b, a.col0 + cb * W, e0, (int)o);
                     }
                 }
-                if (src && a.prefetch) prefetch_src(tile);
             }
             // bounded wait (~1 s at 2 GHz): on time-out the tile is poisoned with NaN, which the
             // z pass counts as non-finite cells (SMK_ENULLBOX from smk_grf_check), and the
@@ -295,9 +295,9 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
             __syncthreads();
         }
         if (src) {
-            // the next tile's source runs into L2 (two tiles ahead measured slower); with TMA
-            // issued with the current tile's loads, above
-            if (!a.tma && a.prefetch && threadIdx.x == 0) prefetch_src(tile);
+            // the next tile's source runs into L2, once the current tile's (first part) has
+            // arrived (issued with the current tile's loads, or two tiles ahead, measured slower)
+            if (a.prefetch && threadIdx.x == 0) prefetch_src(tile);
         } else if (a.prefetch && tile + gridDim.x < ntiles) {
             // the next tile of this block: one line per row segment of its W columns
             const int64_t tn = tile + gridDim.x;
@@ -1032,6 +1032,33 @@ __device__ __forceinline__ void warp_flush_stats(double s1, double s2, double ba
     }
 }
 
+// Forward transform of a warp's line (natural-order slots in, digit-reversed out), in place.
+template <int RMAX, int SWZ>
+__device__ __forceinline__ void warp_fft_fwd(float2* s, const float2* stw, const FftPlan& pl, const int lane) {
+    auto none = [](int, float2) {};
+    for (int st = 0; st < pl.nst; ++st) {
+        switch (pl.r[st]) {
+            case 32:
+                if constexpr (RMAX >= 32) warp_fft_stage<32, false, false, SWZ>(s, stw, pl, st, lane, none);
+                break;
+            case 16:
+                if constexpr (RMAX >= 16) warp_fft_stage<16, false, false, SWZ>(s, stw, pl, st, lane, none);
+                break;
+            case 10:
+                if constexpr (RMAX >= 16) warp_fft_stage<10, false, false, SWZ>(s, stw, pl, st, lane, none);
+                break;
+            case 6:
+                if constexpr (RMAX >= 16) warp_fft_stage<6, false, false, SWZ>(s, stw, pl, st, lane, none);
+                break;
+            case 8: warp_fft_stage<8, false, false, SWZ>(s, stw, pl, st, lane, none); break;
+            case 4: warp_fft_stage<4, false, false, SWZ>(s, stw, pl, st, lane, none); break;
+            case 2: warp_fft_stage<2, false, false, SWZ>(s, stw, pl, st, lane, none); break;
+            case 3: warp_fft_stage<3, false, false, SWZ>(s, stw, pl, st, lane, none); break;
+            default: warp_fft_stage<5, false, false, SWZ>(s, stw, pl, st, lane, none); break;
+        }
+    }
+}
+
 // Shared memory of zinvw_kernel for `warps` warps: stw[twn] | sof[n] | per-warp lines.
 __host__ __device__ inline size_t zinvw_line_slots(int n, int swz) {
     return swz ? (size_t)(n + 15) / 16 * 16 : (size_t)zpad(n - 1) + 1;
@@ -1171,23 +1198,126 @@ static int persistent_grid(K kernel, int threads, size_t smem, int64_t ntiles, i
     return SMK_OK;
 }
 
+// r2c along z of the caller's noise, one warp per row pair (variants with W = 0): the two real
+// rows packed as z = x1 + i x2 in the warp's private (swizzled) line, forward transform, the two
+// half spectra split out of Z_k and Z*_{n-k} and stored row by row.  Same shared-memory layout
+// as zinvw_kernel: stw[twn] | sof[n] | line[warp][zinvw_line_slots(n, SWZ)].
+template <class C, int SWZ>
+__global__ void __launch_bounds__(C::T, C::MINB) zfwdw_kernel(const ZFwdArgs a) {
+    extern __shared__ float2 smem[];
+    const int n = a.pl.n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    float2* stw = smem;
+    int* sof = reinterpret_cast<int*>(stw + a.pl.twn);
+    float2* sw = reinterpret_cast<float2*>(sof + n + (n & 1)) + (size_t)warp * zinvw_line_slots(n, SWZ);
+    fill_stage_twiddles(stw, a.pl);
+    for (int m = threadIdx.x; m < n; m += blockDim.x) sof[m] = zslot<SWZ>(slot_of_freq(a.pl, m));
+    __syncthreads();
+    const int nh = n / 2 + 1;
+    const int64_t rpb = a.zt.rows_per_box;
+    const int64_t ppb = (rpb + 1) / 2;                  // row pairs per box
+    const int64_t npairs = ppb * a.batch;
+    const int64_t cp = a.pitch / 2;
+    float2* out2 = reinterpret_cast<float2*>(a.out);
+    const bool pf = a.prefetch && (n & 3) == 0 && ((uintptr_t)a.noise & 15) == 0;
+    const int64_t gw = (int64_t)blockIdx.x * nwarp + warp, nw = (int64_t)gridDim.x * nwarp;
+    for (int64_t pi = gw; pi < npairs; pi += nw) {
+        const int64_t b = pi / ppb;
+        const int64_t lrow = 2 * (pi - b * ppb);        // first row of the pair inside box b
+        const bool two = lrow + 1 < rpb;
+        const int64_t row0 = b * rpb + lrow;
+        const float* in1 = a.noise + row0 * n;
+        const float* in2 = in1 + n;
+        if (pf && lane < 2 && pi + nw < npairs) {
+            // the next pair of this warp: one bulk L2 prefetch per row
+            const int64_t tn = pi + nw;
+            const int64_t bn = tn / ppb;
+            const int64_t rn = bn * rpb + 2 * (tn - bn * ppb) + lane;
+            if (rn < (bn + 1) * rpb) prefetch_l2_bulk(a.noise + rn * n, (uint32_t)(n * 4));
+        }
+        constexpr int U = 12;
+        for (int e0 = lane; e0 < n; e0 += 32 * U) {
+            float x1[U], x2[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int e = e0 + 32 * u;
+                x1[u] = x2[u] = 0.f;
+                if (e < n) {
+                    x1[u] = __ldcs(in1 + e);
+                    if (two) x2[u] = __ldcs(in2 + e);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int e = e0 + 32 * u;
+                if (e < n) sw[zslot<SWZ>(e)] = make_float2(x1[u], x2[u]);
+            }
+        }
+        __syncwarp();
+        warp_fft_fwd<C::RMAX, SWZ>(sw, stw, a.pl, lane);
+        // X1_k = (Z_k + Z*_{n-k})/2, X2_k = (Z_k - Z*_{n-k})/(2i)
+        float2* o1 = out2 + row0 * cp;
+        float2* o2 = o1 + cp;
+        for (int k = lane; k < nh; k += 32) {
+            const float2 zk = sw[sof[k]];
+            const float2 zm = sw[sof[k == 0 ? 0 : n - k]];
+            __stcs(o1 + k, make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y)));
+            if (two) __stcs(o2 + k, make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x)));
+        }
+        __syncwarp();
+    }
+}
+
 template <class C>
 static size_t zpass_smem(int n) {
     return (size_t)n * (C::W + 1) * sizeof(float2) + (size_t)n * sizeof(float2) + (size_t)(n + 1) * sizeof(int) +
            3 * (C::T / 32) * sizeof(double) + 8;
 }
 
+// One warp per row pair (variants with W = 0): as many warps per block as fit in shared
+// memory, up to C::T / 32; the plan and swizzle rule of zinvw_kernel.
+template <class C>
+static int launch_zfwdw(ZFwdArgs a, int64_t rows_per_box, cudaStream_t st) {
+    a.zt.rows_per_box = rows_per_box;
+    a.zt.tiles_per_box = 0;
+    const int n = a.pl.n;
+    const int swz = ((n & (n - 1)) != 0 || n < 2048) ? 1 : 0;
+    if (swz && !make_plan(n, &a.pl, C::RMAX, true)) return fail(SMK_ENOTSUPP, "zfwdw_kernel: no plan for %d", n);
+    int dev = 0, smem_max = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    int warps = C::T / 32;
+    while (warps > 1 && zinvw_smem(a.pl, warps, swz) > (size_t)smem_max) --warps;
+    const size_t smem = zinvw_smem(a.pl, warps, swz);
+    if (smem > (size_t)smem_max) return fail(SMK_ENOTSUPP, "zfwdw_kernel: line of %d does not fit", n);
+    auto kern = swz ? zfwdw_kernel<C, 1> : zfwdw_kernel<C, 0>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return check_launch("cudaFuncSetAttribute(zfwdw)");
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * warps, smem) != cudaSuccess)
+        return check_launch("cudaOccupancyMaxActiveBlocksPerMultiprocessor(zfwdw)");
+    if (per_sm < 1) return fail(SMK_ENOTSUPP, "zfwdw_kernel does not fit on an SM (smem %zu B)", smem);
+    const int64_t npairs = (rows_per_box + 1) / 2 * a.batch;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(npairs, warps), (int64_t)per_sm * sm_count()));
+    kern<<<grid, 32 * warps, smem, st>>>(a);
+    return check_launch("zfwdw_kernel");
+}
+
 template <class C>
 static int launch_zfwd(ZFwdArgs a, int64_t rows_per_box, cudaStream_t st) {
     if (!plan_fits(a.pl, C::RMAX)) return fail(SMK_EINVAL, "%s: plan radix above the variant's", "zfwd_kernel");
-    if (!fixed_plan_ok<C>(a.pl)) return fail(SMK_EINVAL, "%s: length %d is not the variant's fixed length", "zfwd_kernel", a.pl.n);
-    a.zt.init(rows_per_box, C::W);
-    const size_t smem = zpass_smem<C>(a.pl.n);
-    const int64_t ntiles = a.zt.tiles_per_box * a.batch;
-    int grid = 0, rc;
-    if ((rc = persistent_grid(zfwd_kernel<C>, C::T, smem, ntiles, &grid))) return rc;
-    zfwd_kernel<C><<<grid, C::T, smem, st>>>(a);
-    return check_launch("zfwd_kernel");
+    if constexpr (C::W == 0) {
+        return launch_zfwdw<C>(a, rows_per_box, st);
+    } else {
+        if (!fixed_plan_ok<C>(a.pl)) return fail(SMK_EINVAL, "%s: length %d is not the variant's fixed length", "zfwd_kernel", a.pl.n);
+        a.zt.init(rows_per_box, C::W);
+        const size_t smem = zpass_smem<C>(a.pl.n);
+        const int64_t ntiles = a.zt.tiles_per_box * a.batch;
+        int grid = 0, rc;
+        if ((rc = persistent_grid(zfwd_kernel<C>, C::T, smem, ntiles, &grid))) return rc;
+        zfwd_kernel<C><<<grid, C::T, smem, st>>>(a);
+        return check_launch("zfwd_kernel");
+    }
 }
 
 // One warp per row pair (variants with W = 0): as many warps per block as fit in shared
@@ -1311,7 +1441,7 @@ struct TileVariant {
 inline bool variant_fits(const TileVariant& v, int n) { return v.nmax < 0 ? n == -v.nmax : v.nmax >= n; }
 // r2c along z of host noise (zfwd): W = row pairs per tile
 #define SMK_Z_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(4, 512, 2560, 16, 1) \
-    X(2, 128, 2560, 16, 4) X(4, 512, 4096, 16, 1) X(8, 512, -1536, 16, 1)
+    X(2, 128, 2560, 16, 4) X(4, 512, 4096, 16, 1) X(8, 512, -1536, 16, 1) X(0, 512, 2560, 16, 1) X(0, 512, 4096, 16, 1)
 // z inverse: one warp per row pair (W = 0; as many warps per block as fit, up to T / 32)
 #define SMK_ZINV_VARIANTS(X) X(0, 512, 2560, 16, 1) X(0, 512, 1024, 16, 1) X(0, 256, 1024, 16, 2) \
     X(0, 512, 4096, 16, 1) X(0, 256, 2560, 32, 1)
