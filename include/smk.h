@@ -130,8 +130,8 @@ int smk_pk_normalisation(int32_t nx, int32_t ny, int32_t nz, double dcell, doubl
  * length); smk_tune_set picks the variant used for the lengths of n's class (<=512, <=1024,
  * <=2560, <=4096; v = -1 restores the built-in choice).  Process-wide setting.  The built-in
  * choice is a variant compiled for exactly n if there is one, else the first variant whose
- * length covers n; for SMK_PASS_ZINV the first such variant with W = 0 (one warp per row pair,
- * as many warps per block as fit, up to T/32). */
+ * length covers n; for SMK_PASS_ZFWD and SMK_PASS_ZINV the first such variant with W = 0 (one
+ * warp per row pair, as many warps per block as fit, up to T/32). */
 #define SMK_PASS_ZFWD 0  /* r2c along z (host noise)                              */
 #define SMK_PASS_LINE 1  /* c2c along y                                            */
 #define SMK_PASS_XPASS 2 /* x pass of host noise                                   */

@@ -103,12 +103,12 @@ int variant_for(int pass, int n) {
     const int cnt = variant_count(pass);
     const int c = g_choice[pass][length_class(n)].load();
     if (c >= 0 && c < cnt && variant_fits(t[c], n)) return c;
-    // built-in choice: a variant compiled for exactly this length, else the z inverse prefers
+    // built-in choice: a variant compiled for exactly this length, else the z passes prefer
     // the one-warp-per-row-pair engine (W = 0), every pass otherwise the first variant whose
     // line length covers n
     for (int i = 0; i < cnt; ++i)
         if (t[i].nmax == -n) return i;
-    if (pass == PASS_ZINV)
+    if (pass == PASS_ZINV || pass == PASS_ZFWD)
         for (int i = 0; i < cnt; ++i)
             if (t[i].w == 0 && variant_fits(t[i], n)) return i;
     for (int i = 0; i < cnt; ++i)
