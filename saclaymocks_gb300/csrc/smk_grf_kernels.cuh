@@ -505,7 +505,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpass_kernel(const XArgs a) {
 // KB..W-1 of the same tile, inverse x FFT of the W lines, last stage stored from registers into
 // the intermediate (layout of XGenArgs::I).  Same arithmetic as xpass_kernel per line.
 // smem: s[n*W] | tw[n] | kx[n] | ix[n] | kt[W+1]
-template <class C>
+template <class C, bool BOTH>
 __global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
     constexpr int W = C::W, T = C::T;
     constexpr int KB = W / 2;
@@ -524,8 +524,8 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
     }
     float amp = 0.f;
     if (a.pk_mode == SMK_PK_ANALYTIC) amp = (float)(a.amp_host > 0.0 ? a.amp_host : *a.amp_dev);
-    const bool both = a.I[1] != nullptr;
-    const int WC = both ? KB : W;     // k_z columns per tile
+    constexpr bool both = BOTH;       // both fields (I[1] set): the launcher's choice of instance
+    constexpr int WC = BOTH ? KB : W;  // k_z columns per tile
     const int64_t ntiles = (int64_t)a.batch * a.ncb * a.ny;
     const int64_t nouter = (int64_t)a.batch * a.nx;
     const int64_t estride = (int64_t)a.ny * a.cp;
@@ -839,7 +839,6 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
     extern __shared__ float2 smem[];
     const bool both = a.fields == XGEN_BOTH;
     const int WC = both ? W / 2 : W;          // k_z columns per tile (= KB)
-    const int NP = WC / 2;
     const int n = a.pl.n;  // == nx
     float2* s = smem;
     float2* tw = s + n * W;
@@ -867,18 +866,21 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
         const int iym = iy == 0 ? 0 : a.ny - iy;
         const float ky = kaxis(iy, a.ny, a.kfac, true);
         const uint64_t seed = a.seed + (uint64_t)b;
-        auto draw = [&](auto chk) {
+        // the column count per tile as a constant (BOTH: W/2 columns of each field, else W of one)
+        auto draw = [&](auto chk, auto both_c) {
+            constexpr bool BOTH = decltype(both_c)::value;
+            constexpr int WCC = BOTH ? W / 2 : W, NPC = WCC / 2;
 #pragma unroll 2
-            for (int idx = threadIdx.x; idx < n * NP; idx += T) {
-                const int e = idx / NP, pr = idx % NP;
-                const int c0 = 2 * pr, kz0 = cb * WC + c0;
+            for (int idx = threadIdx.x; idx < n * NPC; idx += T) {
+                const int e = idx / NPC, pr = idx % NPC;
+                const int c0 = 2 * pr, kz0 = cb * WCC + c0;
                 const float kxv = kx[e];
                 const ModePair mp = draw_pair<decltype(chk)::value>(a, seed, ix[e], iy, iym, kxv, ky, kz0, kzt, scale_c);
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
-                    if (both) {
+                    if constexpr (BOTH) {
                         s[e * W + c0 + h] = mp.d[h];
-                        s[e * W + WC + c0 + h] = eta_from_inv_k2(a.eta_comp, mp.d[h], kxv, ky, mp.kz[h], mp.ikk[h], a.vfac);
+                        s[e * W + WCC + c0 + h] = eta_from_inv_k2(a.eta_comp, mp.d[h], kxv, ky, mp.kz[h], mp.ikk[h], a.vfac);
                     } else {
                         s[e * W + c0 + h] = a.fields == XGEN_DELTA
                             ? mp.d[h] : eta_from_inv_k2(a.eta_comp, mp.d[h], kxv, ky, mp.kz[h], mp.ikk[h], a.vfac);
@@ -886,10 +888,13 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
                 }
             }
         };
-        if (tile_needs_check(a, cb * WC, WC))
-            draw(std::true_type{});
-        else
-            draw(std::false_type{});
+        if (tile_needs_check(a, cb * WC, WC)) {
+            if (both) draw(std::true_type{}, std::true_type{});
+            else draw(std::true_type{}, std::false_type{});
+        } else {
+            if (both) draw(std::false_type{}, std::true_type{});
+            else draw(std::false_type{}, std::false_type{});
+        }
         __syncthreads();
         const int cols = min(WC, a.nzh - cb * WC);
         const int64_t row0 = ((int64_t)kbl * nouter + b * a.nx) * a.ny + yslot;
@@ -1393,8 +1398,13 @@ static int launch_xpi(const XArgs& a, cudaStream_t st) {
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2) + (size_t)a.pl.n * 8 + (C::W + 1) * 4;
     const int64_t ntiles = (int64_t)a.batch * a.ncb * a.ny;
     int grid = 0, rc;
-    if ((rc = persistent_grid(xpi_kernel<C>, C::T, smem, ntiles, &grid))) return rc;
-    xpi_kernel<C><<<grid, C::T, smem, st>>>(a);
+    if (a.I[1]) {
+        if ((rc = persistent_grid(xpi_kernel<C, true>, C::T, smem, ntiles, &grid))) return rc;
+        xpi_kernel<C, true><<<grid, C::T, smem, st>>>(a);
+    } else {
+        if ((rc = persistent_grid(xpi_kernel<C, false>, C::T, smem, ntiles, &grid))) return rc;
+        xpi_kernel<C, false><<<grid, C::T, smem, st>>>(a);
+    }
     return check_launch("xpi_kernel");
 }
 
