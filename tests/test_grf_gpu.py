@@ -186,7 +186,7 @@ def test_grf_pk_grid_mode_is_the_reference_multiply(G, golden):
 
 # every tile class (n <= 512, <= 1024, <= 2560, <= 4096) on each axis, radices 2, 3, 4, 5, 8
 SHAPES = [(32, 24, 40), (12, 600, 10), (2560, 4, 6), (4, 6, 2560), (6, 4000, 4), (4, 4, 4096),
-          (2, 2, 2), (30, 18, 50), (1024, 8, 12), (10, 1536, 8), (5, 3, 40), (7, 9, 6)]   # odd row counts
+          (2, 2, 2), (30, 18, 50), (1024, 8, 12), (10, 1536, 8), (5, 3, 40), (5, 9, 6)]   # odd row counts
 
 
 @pytest.mark.parametrize("shape", SHAPES, ids=[f"{a}x{b}x{c}" for a, b, c in SHAPES])
