@@ -836,7 +836,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
 template <class C>
 __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
     constexpr int W = C::W, T = C::T;
-    extern __shared__ float2 smem[];
+    extern __shared__ __align__(16) float2 smem[];
     const bool both = a.fields == XGEN_BOTH;
     const int WC = both ? W / 2 : W;          // k_z columns per tile (= KB)
     const int n = a.pl.n;  // == nx
@@ -876,16 +876,22 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
                 const int c0 = 2 * pr, kz0 = cb * WCC + c0;
                 const float kxv = kx[e];
                 const ModePair mp = draw_pair<decltype(chk)::value>(a, seed, ix[e], iy, iym, kxv, ky, kz0, kzt, scale_c);
+                // the two modes of a field as one 16-byte store (rows are 64 B apart, so 8-byte stores
+                // of lanes on rows e and e + 2 met on the same banks)
+                float2 v[2][2];
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
+                    const float2 et = eta_from_inv_k2(a.eta_comp, mp.d[h], kxv, ky, mp.kz[h], mp.ikk[h], a.vfac);
                     if constexpr (BOTH) {
-                        s[e * W + c0 + h] = mp.d[h];
-                        s[e * W + WCC + c0 + h] = eta_from_inv_k2(a.eta_comp, mp.d[h], kxv, ky, mp.kz[h], mp.ikk[h], a.vfac);
+                        v[0][h] = mp.d[h];
+                        v[1][h] = et;
                     } else {
-                        s[e * W + c0 + h] = a.fields == XGEN_DELTA
-                            ? mp.d[h] : eta_from_inv_k2(a.eta_comp, mp.d[h], kxv, ky, mp.kz[h], mp.ikk[h], a.vfac);
+                        v[0][h] = a.fields == XGEN_DELTA ? mp.d[h] : et;
                     }
                 }
+                *reinterpret_cast<float4*>(s + e * W + c0) = make_float4(v[0][0].x, v[0][0].y, v[0][1].x, v[0][1].y);
+                if constexpr (BOTH)
+                    *reinterpret_cast<float4*>(s + e * W + WCC + c0) = make_float4(v[1][0].x, v[1][0].y, v[1][1].x, v[1][1].y);
             }
         };
         if (tile_needs_check(a, cb * WC, WC)) {
