@@ -509,7 +509,7 @@ template <class C, bool BOTH>
 __global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
     constexpr int W = C::W, T = C::T;
     constexpr int KB = W / 2;
-    extern __shared__ float2 smem[];
+    extern __shared__ __align__(128) float2 smem[];
     const int n = a.pl.n;  // == nx
     float2* s = smem;
     float2* tw = s + n * W;
@@ -567,26 +567,37 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
         else
             fft_tile<false, W, W, T, C::RMAX, C::NF>(s, tw, a.pl);
         const float ky = kt[0];
-        for (int idx = threadIdx.x; idx < n * WC; idx += T) {
-            const int e = idx / WC, w = idx % WC;
-            const float kxv = kx[e], kz = kt[1 + w];
-            // k^2 in float32 without contraction, as numpy evaluates kx*kx + ky*ky + kz*kz
-            const float kk = __fadd_rn(__fadd_rn(__fmul_rn(kxv, kxv), __fmul_rn(ky, ky)), __fmul_rn(kz, kz));
-            float sc;
-            if (a.pk_mode == SMK_PK_GRID) {
-                sc = w < cols ? __ldg(a.grid + ((int64_t)ix[e] * a.ny + iy) * a.nzh + cb * WC + w) : 0.f;
-            } else {
-                const float k = __fsqrt_rn(kk);
-                const float kr = k * a.inv_k0;
-                const float den = fmaf(kr, kr, 1.0f);
-                sc = sqrtf(amp * k / (den * den) * a.inv_vcell);
+        // two adjacent columns per thread, read and written as 16-byte pieces (rows are 64 B
+        // apart, so 8-byte accesses of lanes on rows e and e + 2 met on the same banks)
+        for (int idx = threadIdx.x; idx < n * (WC / 2); idx += T) {
+            const int e = idx / (WC / 2), w0 = 2 * (idx % (WC / 2));
+            const float kxv = kx[e];
+            const float4 in = *reinterpret_cast<const float4*>(s + e * W + w0);
+            float2 d[2] = {make_float2(in.x, in.y), make_float2(in.z, in.w)}, et[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int w = w0 + h;
+                const float kz = kt[1 + w];
+                // k^2 in float32 without contraction, as numpy evaluates kx*kx + ky*ky + kz*kz
+                const float kk = __fadd_rn(__fadd_rn(__fmul_rn(kxv, kxv), __fmul_rn(ky, ky)), __fmul_rn(kz, kz));
+                float sc;
+                if (a.pk_mode == SMK_PK_GRID) {
+                    sc = w < cols ? __ldg(a.grid + ((int64_t)ix[e] * a.ny + iy) * a.nzh + cb * WC + w) : 0.f;
+                } else {
+                    const float k = __fsqrt_rn(kk);
+                    const float kr = k * a.inv_k0;
+                    const float den = fmaf(kr, kr, 1.0f);
+                    sc = sqrtf(amp * k / (den * den) * a.inv_vcell);
+                }
+                d[h] = cscale(d[h], sc);
+                if (both) {
+                    const float kk1 = (kk == 0.0f) ? 1.0f : kk;  // k^2[0,0,0] = 1 (bin/make_boxes.py:306)
+                    et[h] = eta_apply<true>(a.eta_comp, d[h], kxv, ky, kz, kk1, a.vfac);
+                }
             }
-            const float2 d = cscale(s[e * W + w], sc);
-            s[e * W + w] = d;
-            if (both) {
-                const float kk1 = (kk == 0.0f) ? 1.0f : kk;  // k^2[0,0,0] = 1 (bin/make_boxes.py:306)
-                s[e * W + KB + w] = eta_apply<true>(a.eta_comp, d, kxv, ky, kz, kk1, a.vfac);
-            }
+            *reinterpret_cast<float4*>(s + e * W + w0) = make_float4(d[0].x, d[0].y, d[1].x, d[1].y);
+            if (both)
+                *reinterpret_cast<float4*>(s + e * W + KB + w0) = make_float4(et[0].x, et[0].y, et[1].x, et[1].y);
         }
         __syncthreads();
         float2* d0 = a.I[0] + row0 * WC;
@@ -836,7 +847,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
 template <class C>
 __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
     constexpr int W = C::W, T = C::T;
-    extern __shared__ __align__(16) float2 smem[];
+    extern __shared__ __align__(128) float2 smem[];
     const bool both = a.fields == XGEN_BOTH;
     const int WC = both ? W / 2 : W;          // k_z columns per tile (= KB)
     const int n = a.pl.n;  // == nx
