@@ -463,3 +463,40 @@ def test_lognormal_and_velocity_boxes_match_reference_golden(G, golden, tag):
         out = G.make_boxes(NX, NY, NZ, dx, seed=77, k0=k0, eta_comp=c, vel_factor=vf)
         torch.cuda.synchronize()
         _check(out.eta[0].cpu().numpy(), o64[c], f"philox {c}")
+
+
+@pytest.mark.parametrize("gpu_noise", [True, False])
+def test_tuner_choices_are_valid_and_exact(G, gpu_noise):
+    """tune.tune_grf times every candidate of each pass by coordinate descent (the x pass first:
+    its tile sets the intermediate's layout the y pass reads), applies the fastest, and the boxes
+    made with its choices match the FP64 oracle; the built-in choice comes back afterwards."""
+    from saclaymocks_gb300 import _lib, tune
+    lib = _lib.load()
+    nx, ny, nz = 48, 600, 40
+    noise = None if gpu_noise else np.random.RandomState(4).normal(size=(nx, ny, nz)).astype(np.float32)
+    passes = ([(_lib.SMK_PASS_XGEN, nx), (_lib.SMK_PASS_LINE, ny), (_lib.SMK_PASS_ZINV, nz)] if gpu_noise else
+              [(_lib.SMK_PASS_ZFWD, nz), (_lib.SMK_PASS_LINE, ny), (_lib.SMK_PASS_XPASS, nx), (_lib.SMK_PASS_ZINV, nz)])
+    builtin = {p: lib.smk_tune_get(p, n) for p, n in passes}
+    try:
+        res = tune.tune_grf(nx, ny, nz, 2.19, gpu_noise=gpu_noise, reps=1, use_cache=False, xi_chunk_kz=16)
+        for p, n in passes:
+            name = tune.PASS_NAMES[p]
+            cands = [v for v, _, _ in tune.variants(p, n)]
+            assert sorted(int(v) for v in res["ms"][name]) == sorted(cands)
+            v = res["choices"][name][0]
+            assert res["ms"][name][v] == min(res["ms"][name].values())
+            assert lib.smk_tune_get(p, n) == v
+        if gpu_noise:
+            out = G.make_boxes(nx, ny, nz, 2.19, seed=31, xi_chunk_kz=16)
+            nk = ophilox.kspace_noise(nx, ny, nz, 31)
+            o64 = ograf.grf_from_modes(nk, nz, 2.19, 0.02, eta=("zz",), precision="f64")
+        else:
+            out = G.make_boxes(nx, ny, nz, 2.19, noise=torch.from_numpy(noise).cuda(), xi_chunk_kz=16)
+            o64 = ograf.grf_boxes(noise, 2.19, 0.02, eta=("zz",), precision="f64")
+        torch.cuda.synchronize()
+        _check(out.delta[0].cpu().numpy(), o64["delta"], "tuned delta")
+        _check(out.eta[0].cpu().numpy(), o64["eta_zz"], "tuned eta")
+    finally:
+        for p, n in passes:
+            lib.smk_tune_set(p, n, -1)
+    assert {p: lib.smk_tune_get(p, n) for p, n in passes} == builtin
