@@ -447,6 +447,13 @@ def run_ours(args, cfg):
                "frac": sk_bytes / (sk_ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
                "box_sector_bytes": sec / 1e9, "naive_upper_bytes": 68.0 * pixels / 1e9,
                "basis": "4 B/pixel flux + distinct 32-B sectors of delta and eta touched by the 8 corners"}
+    # the stage is bound by instruction issue, not HBM: its issue-slot roofline from the warp
+    # instructions per pixel of an ncu capture of the same kernel (3.174e9 for the 2e5-skewer
+    # production set of 1.5995e8 pixels)
+    sk_winst = 3.174e9 / 1.5995e8 * pixels
+    sk_roof["issue"] = {"warp_instructions": sk_winst, "achieved_per_s": sk_winst / (sk_ms * 1e-3),
+                        "peak_per_s": nsm * 4 * sm_hz, "frac": sk_winst / (sk_ms * 1e-3) / (nsm * 4 * sm_hz),
+                        "basis": "ncu smsp__inst_executed.sum per pixel, scaled; peak SMs x 4 x SM clock"}
     value = aggregate_value(cells, world, step_ms * 1e-3)
     res = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
@@ -839,13 +846,16 @@ def set_variants(spec, nx, ny, nz):
 
 
 def run_grf_only(args, shape):
-    """GRF boxes of one shape, Philox noise, W + K calls (the ncu profiling case)."""
+    """GRF boxes of one shape, Philox noise (or, --host-noise, a dense device noise box through
+    the five-pass path), W + K calls (the ncu profiling case)."""
     import numpy as np
     import torch
 
     from saclaymocks_gb300 import grf
     nx, ny, nz = shape
     want_eta = not args.no_eta
+    host_noise = getattr(args, "host_noise", False)
+    noise = torch.randn(nx * ny * nz, device="cuda").reshape(nx, ny, nz) if host_noise else None
     if args.xgen_split is not None:
         from saclaymocks_gb300 import _lib
         _lib.xgen_split(args.xgen_split)
@@ -860,22 +870,25 @@ def run_grf_only(args, shape):
         tuned = set_variants(args.variants, nx, ny, nz)
     elif not args.no_tune:
         from saclaymocks_gb300 import tune
-        tuned = tune.tune_grf(nx, ny, nz, out=boxes, workspace=ws, use_cache=False, xi_chunk_kz=xi_chunk(args, nz))
+        tuned = tune.tune_grf(nx, ny, nz, gpu_noise=not host_noise, out=boxes, workspace=ws, use_cache=False,
+                              xi_chunk_kz=xi_chunk(args, nz))
     xi = xi_chunk(args, nz)
     for _ in range(args.warmup):
-        grf.make_boxes(nx, ny, nz, seed=1, amp=amp, out=boxes, workspace=ws, want_eta=want_eta, xi_chunk_kz=xi)
+        grf.make_boxes(nx, ny, nz, seed=1, noise=noise, amp=amp, out=boxes, workspace=ws, want_eta=want_eta,
+                       xi_chunk_kz=xi)
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(args.steps)]
     for e in [x for row in evs for x in row]:
         e.record()
     torch.cuda.synchronize()
     for k in range(args.steps):
-        out = grf.make_boxes(nx, ny, nz, seed=1, amp=amp, out=boxes, workspace=ws, pass_events=evs[k],
+        out = grf.make_boxes(nx, ny, nz, seed=1, noise=noise, amp=amp, out=boxes, workspace=ws, pass_events=evs[k],
                              want_eta=want_eta, xi_chunk_kz=xi)
     torch.cuda.synchronize()
     out.check()
     pass_ms = np.mean([[evs[k][i].elapsed_time(evs[k][i + 1]) for i in range(5)]
                        for k in range(args.steps)], axis=0)
-    print(json.dumps({"grf_shape": shape, "xi_chunk_kz": xi, "pass_ms": [round(float(x), 4) for x in pass_ms], "tuned": tuned,
+    print(json.dumps({"grf_shape": shape, "noise": "host" if host_noise else "gpu", "xi_chunk_kz": xi,
+                      "pass_ms": [round(float(x), 4) for x in pass_ms], "tuned": tuned,
                       "grf_cells_per_s": nx * ny * nz / (pass_ms.sum() * 1e-3)}))
 
 
@@ -977,6 +990,8 @@ def main():
                     help="NX,NY,NZ,NSK: time only the skewer stage on boxes of this shape (profiling case)")
     ap.add_argument("--grf-shape", default=None,
                     help="NX,NY,NZ: time only the GRF boxes of this shape (profiling case)")
+    ap.add_argument("--host-noise", action="store_true",
+                    help="--grf-shape: the five-pass path on a dense device noise box")
     ap.add_argument("--selftest-replicas", action="store_true", help=argparse.SUPPRESS)
     args = ap.parse_args()
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
