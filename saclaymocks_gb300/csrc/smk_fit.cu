@@ -176,46 +176,51 @@ __device__ __forceinline__ float2 chirp_b(int n, int N, int M) {
     return make_float2(w.x, -w.y);
 }
 
-// Unnormalised length-N DFT of the complex sequence held in s1[0..N) (natural order),
-// forward (e^{-}) or inverse (e^{+}); result left in s1[0..N) in natural order.  s2 is
-// scratch of M elements; tw the twiddle table of M.  Bc (may be null): FFT_M of the forward
-// chirp in the engine's digit-reversed order, which saves one of the three transforms, followed
-// by the chirp w_n itself for n < N (the same values chirp() computes).  Block-synchronous.
-template <bool INV>
+// Unnormalised length-N DFTs of the W complex sequences held in s1 (element n of line w at
+// s1[n W + w], natural order), forward (e^{-}) or inverse (e^{+}); results left in place in
+// natural order.  s2 is scratch of M elements; tw the twiddle table of M.  Bc (may be null):
+// FFT_M of the forward chirp in the engine's digit-reversed order, which saves one of the
+// three transforms, followed by the chirp w_n itself for n < N (the same values chirp()
+// computes).  Every line gets the same operations as a W = 1 call.  Block-synchronous.
+template <bool INV, int W>
 __device__ void bluestein(float2* s1, float2* s2, const float2* tw, int N, int M, const FftPlan& pl,
                           const float2* __restrict__ Bc) {
     const float2* __restrict__ Wt = Bc ? Bc + M : nullptr;
     // a_n = x_n w_n (INV: x_n conj(w_n)); b = the chirp (INV: its conjugate)
-    for (int n = threadIdx.x; n < M; n += FIT_T) {
+    for (int i = threadIdx.x; i < M * W; i += FIT_T) {
+        const int n = i / W;
         if (n < N) {
             const float2 w = Wt ? __ldg(Wt + n) : chirp(n, N);
-            s1[n] = INV ? cmulc(s1[n], w) : cmul(s1[n], w);
+            s1[i] = INV ? cmulc(s1[i], w) : cmul(s1[i], w);
         } else {
-            s1[n] = make_float2(0.f, 0.f);
+            s1[i] = make_float2(0.f, 0.f);
         }
-        if (!Bc) {
+    }
+    if (!Bc) {
+        for (int n = threadIdx.x; n < M; n += FIT_T) {
             const float2 b = chirp_b(n, N, M);
             s2[n] = INV ? make_float2(b.x, -b.y) : b;
         }
     }
     __syncthreads();
-    fft_tile<false, 1, 1, FIT_T, 16>(s1, tw, pl);
+    fft_tile<false, W, W, FIT_T, 16>(s1, tw, pl);
     if (Bc) {
-        for (int n = threadIdx.x; n < M; n += FIT_T) {
-            const float2 b = __ldg(Bc + n);
-            s1[n] = cmul(s1[n], INV ? make_float2(b.x, -b.y) : b);   // digit-reversed, same order
+        for (int i = threadIdx.x; i < M * W; i += FIT_T) {
+            const float2 b = __ldg(Bc + i / W);
+            s1[i] = cmul(s1[i], INV ? make_float2(b.x, -b.y) : b);   // digit-reversed, same order
         }
     } else {
         fft_tile<false, 1, 1, FIT_T, 16>(s2, tw, pl);
-        for (int n = threadIdx.x; n < M; n += FIT_T) s1[n] = cmul(s1[n], s2[n]);  // digit-reversed, same order
+        for (int i = threadIdx.x; i < M * W; i += FIT_T) s1[i] = cmul(s1[i], s2[i / W]);  // digit-reversed
     }
     __syncthreads();
-    fft_tile<true, 1, 1, FIT_T, 16>(s1, tw, pl);
+    fft_tile<true, W, W, FIT_T, 16>(s1, tw, pl);
     const float inv_m = 1.0f / (float)M;
-    for (int k = threadIdx.x; k < N; k += FIT_T) {
+    for (int i = threadIdx.x; i < N * W; i += FIT_T) {
+        const int k = i / W;
         const float2 w = Wt ? __ldg(Wt + k) : chirp(k, N);
-        const float2 c = cscale(s1[k], inv_m);
-        s1[k] = INV ? cmulc(c, w) : cmul(c, w);
+        const float2 c = cscale(s1[i], inv_m);
+        s1[i] = INV ? cmulc(c, w) : cmul(c, w);
     }
     __syncthreads();
 }
@@ -257,40 +262,82 @@ __device__ __forceinline__ int kbin_thr(int m, const int* thr, int nkb) {
     return lo;
 }
 
-struct PairSetup {
-    int sid[2];
-    int N;
-    int64_t off[2];
+// Work item of the fit kernels: two consecutive pairs of the schedule (pairs of equal-length
+// skewers, longest first).  Pair p holds skewers sid[2p] (always present) and sid[2p + 1] (or
+// -1); np = 1 when the schedule ended after the first pair.  Two pairs of one length run as the
+// two lines of one tile (W = 2), else one after the other (W = 1).
+struct Quad {
+    int sid[4];
+    int N[2];
+    int np;
+    int64_t off[4];
 };
 
-// Load the pair (dF of both skewers into s1 as re/im); returns via shared `ps`.
-__device__ void load_pair(const FitArgs& a, const float* th, float fbar_inv, const PairSetup& ps, float2* s1) {
-    for (int i = threadIdx.x; i < ps.N; i += FIT_T) {
+__device__ bool next_quad(const FitArgs& a, long long* item_sh, Quad* qd) {
+    if (threadIdx.x == 0) *item_sh = (long long)atomicAdd(a.counter, 1ULL);
+    __syncthreads();
+    const long long q = *item_sh;
+    if (q >= (a.n_items + 1) / 2) return false;
+    if (threadIdx.x < 4) {
+        const long long item = 2 * q + (threadIdx.x >> 1);
+        const int sid = item < a.n_items ? a.order[2 * item + (threadIdx.x & 1)] : -1;
+        qd->sid[threadIdx.x] = sid;
+        qd->off[threadIdx.x] = sid >= 0 ? a.offset[sid] : 0;
+        if ((threadIdx.x & 1) == 0) qd->N[threadIdx.x >> 1] = sid >= 0 ? a.npix[sid] : 0;
+        if (threadIdx.x == 0) qd->np = 2 * q + 1 < a.n_items ? 2 : 1;
+    }
+    __syncthreads();
+    return true;
+}
+
+// dF of the W pairs p0 .. p0 + W - 1 into s1: line w holds pair p0 + w's skewers as re / im
+// (element n at s1[n W + w]); each line's pixels are read consecutively.
+template <int W>
+__device__ void load_pairs(const FitArgs& a, const float* th, float fbar_inv, const Quad& qd, int p0, float2* s1) {
+    const int N = qd.N[p0];
+    for (int i = threadIdx.x; i < N * W; i += FIT_T) {
+        const int w = i / N, n = i - w * N;
         float v[2] = {0.f, 0.f};
 #pragma unroll
         for (int t = 0; t < 2; ++t) {
-            if (ps.sid[t] >= 0) {
+            const int q = 2 * (p0 + w) + t;
+            if (qd.sid[q] >= 0) {
                 float t1, g;
-                v[t] = flux_of(a, ps.off[t] + i, th, &t1, &g) * fbar_inv - 1.0f;
+                v[t] = flux_of(a, qd.off[q] + n, th, &t1, &g) * fbar_inv - 1.0f;
             }
         }
-        s1[i] = make_float2(v[0], v[1]);
+        s1[n * W + w] = make_float2(v[0], v[1]);
     }
     __syncthreads();
 }
 
-__device__ bool next_pair(const FitArgs& a, long long* item_sh, PairSetup* ps) {
-    if (threadIdx.x == 0) *item_sh = (long long)atomicAdd(a.counter, 1ULL);
-    __syncthreads();
-    const long long item = *item_sh;
-    if (item >= a.n_items) return false;
-    if (threadIdx.x < 2) {
-        const int sid = a.order[2 * item + threadIdx.x];
-        ps->sid[threadIdx.x] = sid;
-        ps->off[threadIdx.x] = sid >= 0 ? a.offset[sid] : 0;
-        if (threadIdx.x == 0) ps->N = a.npix[sid];
+// Per-length state of a block: the plan and twiddles of M, the k-bin thresholds of N.
+struct LengthState {
+    int curM, curN;
+};
+
+// Prepares a group of length N (Bluestein length M): false (and a NaN in *nan_at) when M is above
+// the shared memory's mmax or the chirp table lacks N and there is no room to transform it.
+__device__ bool prepare_length(const FitArgs& a, int N, int M, FftPlan& pl, float2* tw, int* thr, const double* edges,
+                               double kfac, float2* s2, LengthState& ls, double* nan_at, const float2** Bc) {
+    if (N != ls.curN) {
+        kbin_thresholds(N, kfac, edges, a.nkb, thr);
+        ls.curN = N;
     }
-    __syncthreads();
+    *Bc = a.chirp && a.chirp_off[N] >= 0 ? a.chirp + a.chirp_off[N] : nullptr;
+    if (M > a.mmax || (!*Bc && !s2)) {
+        // a skewer longer than SmkFitProblem.n_max (its Bluestein length does not fit the shared
+        // memory), or a length missing from the chirp table: not transformed, the sums made NaN
+        if (threadIdx.x == 0) *nan_at = __longlong_as_double(0x7ff8000000000000LL);
+        __syncthreads();
+        return false;
+    }
+    if (M != ls.curM) {
+        if (threadIdx.x == 0) make_plan(M, &pl, 16);
+        __syncthreads();
+        fill_stage_twiddles(tw, pl);
+        ls.curM = M;
+    }
     return true;
 }
 
@@ -311,18 +358,67 @@ __device__ __forceinline__ void warp_bin_add(double* sbins, int bin, float v) {
 
 
 // ------------------------------------------------------------------ pass 2: binned P1D
+// Shared memory of the fit kernels: s1 (two lines of mmax) | s2 (mmax, only without the chirp
+// table) | tw (mmax).
+struct FitSmem {
+    float2 *s1, *s2, *tw;
+    __device__ FitSmem(float2* smem, const FitArgs& a)
+        : s1(smem), s2(a.chirp ? nullptr : smem + 2 * a.mmax), tw(smem + (a.chirp ? 2 : 3) * a.mmax) {}
+};
+
+// The P1D of the W pairs p0 .. p0 + W - 1 of qd (one length N): transform, store the packed
+// spectra for the backward, bin |X_m|^2 dx/N of every skewer.
+template <int W>
+__device__ void p1d_group(const FitArgs& a, const Quad& qd, int p0, const FitSmem& sm, FftPlan& pl, int* thr,
+                          const double* edges, double kfac, const float* th, float fbar_inv, double* psum,
+                          double* psq, LengthState& ls) {
+    const int N = qd.N[p0];
+    const int M = bluestein_m(N);
+    const float2* Bc;
+    if (!prepare_length(a, N, M, pl, sm.tw, thr, edges, kfac, sm.s2, ls, &psum[0], &Bc)) return;
+    load_pairs<W>(a, th, fbar_inv, qd, p0, sm.s1);
+    bluestein<false, W>(sm.s1, sm.s2, sm.tw, N, M, pl, Bc);
+    if (a.spec) {   // the packed spectra Z for the backward (s1 is only read below)
+        for (int i = threadIdx.x; i < N * W; i += FIT_T) {
+            const int w = i / N, m = i - w * N;
+            a.spec[qd.off[2 * (p0 + w)] + m] = sm.s1[m * W + w];
+        }
+    }
+    // X1_m = (Z_m + Z*_{N-m})/2, X2_m = (Z_m - Z*_{N-m})/(2i), m = 0..N/2; one bin for all lines
+    const float norm = (float)(a.dx / (double)N);
+    const int half = N / 2;
+    for (int m0 = 0; m0 <= half; m0 += FIT_T) {    // block-uniform trip count
+        const int m = m0 + (int)threadIdx.x;
+        int b = -1;
+        float p = 0.f, q = 0.f;
+        if (m <= half) {
+            b = kbin_thr(m, thr, a.nkb);
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                const float2 zk = sm.s1[m * W + w], zm = sm.s1[(m == 0 ? 0 : N - m) * W + w];
+                const float x1r = 0.5f * (zk.x + zm.x), x1i = 0.5f * (zk.y - zm.y);
+                const float x2r = 0.5f * (zk.y + zm.y), x2i = -0.5f * (zk.x - zm.x);
+                const float p1 = (x1r * x1r + x1i * x1i) * norm;
+                const float p2 = qd.sid[2 * (p0 + w) + 1] >= 0 ? (x2r * x2r + x2i * x2i) * norm : 0.f;
+                p += p1 + p2;
+                q += p1 * p1 + p2 * p2;
+            }
+        }
+        warp_bin_add(psum, b, p);
+        warp_bin_add(psq, b, q);
+    }
+    __syncthreads();
+}
+
 __global__ void __launch_bounds__(FIT_T, 3) fit_p1d_kernel(const FitArgs a) {
     extern __shared__ float2 smem[];
-    float2* s1 = smem;
-    // with the chirp table the Bluestein transforms need no second buffer
-    float2* s2 = a.chirp ? nullptr : smem + a.mmax;
-    float2* tw = smem + (a.chirp ? 1 : 2) * a.mmax;
+    const FitSmem sm(smem, a);
     __shared__ double psum[FIT_MAX_BINS];
     __shared__ double psq[FIT_MAX_BINS];
     __shared__ double edges[FIT_MAX_BINS + 1];
     __shared__ float th[3 * FIT_MAX_BINS];
     __shared__ long long item_sh;
-    __shared__ PairSetup ps;
+    __shared__ Quad qd;
     for (int i = threadIdx.x; i < a.nkb; i += FIT_T) psum[i] = psq[i] = 0.0;
     for (int i = threadIdx.x; i <= a.nkb; i += FIT_T) edges[i] = a.kedges[i];
     for (int i = threadIdx.x; i < 3 * a.nzb; i += FIT_T) th[i] = a.theta[i];
@@ -330,61 +426,14 @@ __global__ void __launch_bounds__(FIT_T, 3) fit_p1d_kernel(const FitArgs a) {
     const double kfac = 2.0 * (3.14159265358979323846 / a.dx);
     __shared__ FftPlan pl;
     __shared__ int thr[FIT_MAX_BINS + 1];
-    int curM = 0, curN = 0;
-    while (next_pair(a, &item_sh, &ps)) {
-        const int N = ps.N;
-        const int M = bluestein_m(N);
-        if (N != curN) {
-            kbin_thresholds(N, kfac, edges, a.nkb, thr);
-            curN = N;
+    LengthState ls{0, 0};
+    while (next_quad(a, &item_sh, &qd)) {
+        if (qd.np == 2 && qd.N[1] == qd.N[0]) {
+            p1d_group<2>(a, qd, 0, sm, pl, thr, edges, kfac, th, fbar_inv, psum, psq, ls);
+        } else {
+            p1d_group<1>(a, qd, 0, sm, pl, thr, edges, kfac, th, fbar_inv, psum, psq, ls);
+            if (qd.np == 2) p1d_group<1>(a, qd, 1, sm, pl, thr, edges, kfac, th, fbar_inv, psum, psq, ls);
         }
-        if (M > a.mmax) {
-            // a skewer longer than SmkFitProblem.n_max: not transformed (its Bluestein length
-            // does not fit the shared memory), the power sums are made NaN instead
-            if (threadIdx.x == 0) psum[0] = __longlong_as_double(0x7ff8000000000000LL);
-            __syncthreads();
-            continue;
-        }
-        if (M != curM) {
-            if (threadIdx.x == 0) make_plan(M, &pl, 16);
-            __syncthreads();
-            fill_stage_twiddles(tw, pl);
-            curM = M;
-        }
-        const float2* Bc = a.chirp && a.chirp_off[N] >= 0 ? a.chirp + a.chirp_off[N] : nullptr;
-        if (!Bc && !s2) {
-            // a length missing from the chirp table (and no room to transform its chirp here)
-            if (threadIdx.x == 0) psum[0] = __longlong_as_double(0x7ff8000000000000LL);
-            __syncthreads();
-            continue;
-        }
-        load_pair(a, th, fbar_inv, ps, s1);
-        bluestein<false>(s1, s2, tw, N, M, pl, Bc);
-        if (a.spec) {   // the packed spectrum Z for the backward (s1 is only read below)
-            float2* z = a.spec + ps.off[0];
-            for (int m = threadIdx.x; m < N; m += FIT_T) z[m] = s1[m];
-        }
-        // X1_m = (Z_m + Z*_{N-m})/2, X2_m = (Z_m - Z*_{N-m})/(2i), m = 0..N/2
-        const float norm = (float)(a.dx / (double)N);
-        const int half = N / 2;
-        for (int m0 = 0; m0 <= half; m0 += FIT_T) {    // block-uniform trip count
-            const int m = m0 + (int)threadIdx.x;
-            int b = -1;
-            float p = 0.f, q = 0.f;
-            if (m <= half) {
-                b = kbin_thr(m, thr, a.nkb);
-                const float2 zk = s1[m], zm = s1[m == 0 ? 0 : N - m];
-                const float x1r = 0.5f * (zk.x + zm.x), x1i = 0.5f * (zk.y - zm.y);
-                const float x2r = 0.5f * (zk.y + zm.y), x2i = -0.5f * (zk.x - zm.x);
-                const float p1 = (x1r * x1r + x1i * x1i) * norm;
-                const float p2 = ps.sid[1] >= 0 ? (x2r * x2r + x2i * x2i) * norm : 0.f;
-                p = p1 + p2;
-                q = p1 * p1 + p2 * p2;
-            }
-            warp_bin_add(psum, b, p);
-            warp_bin_add(psq, b, q);
-        }
-        __syncthreads();
     }
     for (int i = threadIdx.x; i < a.nkb; i += FIT_T) {
         atomicAdd(a.acc + acc_psum(a.nzb) + i, psum[i]);
@@ -393,18 +442,129 @@ __global__ void __launch_bounds__(FIT_T, 3) fit_p1d_kernel(const FitArgs a) {
 }
 
 // ------------------------------------------------------------------ backward
+// Shared state of the adjoint pass's blocks.
+struct AdjShared {
+    double* sA;
+    double* sB;
+    double* sS;
+    const float* gP;
+    const float* gM;
+};
+
+// The adjoint of the W pairs p0 .. p0 + W - 1 of qd (one length N): their spectra (read back or
+// transformed again), the P1D weights applied, the inverse DFT (Bluestein), and the per-bin
+// accumulation of every pixel of the 2 W skewers.
+template <int W>
+__device__ void adjoint_group(const FitArgs& a, const Quad& qd, int p0, const FitSmem& sm, FftPlan& pl, int* thr,
+                              const double* edges, double kfac, const float* th, float fbar_inv,
+                              const AdjShared& sh, LengthState& ls) {
+    const int N = qd.N[p0];
+    const int M = bluestein_m(N);
+    const float2* Bc;
+    if (!prepare_length(a, N, M, pl, sm.tw, thr, edges, kfac, sm.s2, ls, sh.sS, &Bc)) return;
+    float2* s1 = sm.s1;
+    if (a.spec) {   // Z as the forward pass with the same theta left it
+        for (int i = threadIdx.x; i < N * W; i += FIT_T) {
+            const int w = i / N, m = i - w * N;
+            s1[m * W + w] = a.spec[qd.off[2 * (p0 + w)] + m];
+        }
+        __syncthreads();
+    } else {
+        load_pairs<W>(a, th, fbar_inv, qd, p0, s1);
+        bluestein<false, W>(s1, sm.s2, sm.tw, N, M, pl, Bc);
+    }
+    // V_t (Hermitian): V_m = w_m X_m (0<m<N/2), V_{N-m} = conj; V_0, V_{N/2} = 2 Re(w X);
+    // packed W = V_1 + i V_2; the unnormalised inverse DFT of W is gdF_1 + i gdF_2.
+    const float norm = (float)(a.dx / (double)N);
+    for (int m = threadIdx.x; m <= N / 2; m += FIT_T) {
+        const int b = kbin_thr(m, thr, a.nkb);
+        const float wgt = b >= 0 ? sh.gP[b] * norm : 0.f;
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            const float2 zk = s1[m * W + w], zm = s1[(m == 0 ? 0 : N - m) * W + w];
+            float2 x1 = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+            float2 x2 = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+            if (qd.sid[2 * (p0 + w) + 1] < 0) x2 = make_float2(0.f, 0.f);
+            x1 = cscale(x1, wgt);
+            x2 = cscale(x2, wgt);
+            // in place: this thread alone reads and writes the slots m and N - m of the line
+            if (m == 0 || 2 * m == N) {
+                s1[m * W + w] = make_float2(2.f * x1.x, 2.f * x2.x);
+            } else {
+                s1[m * W + w] = make_float2(x1.x - x2.y, x1.y + x2.x);          // V1_m + i V2_m
+                s1[(N - m) * W + w] = make_float2(x1.x + x2.y, x2.x - x1.y);    // conj(V1_m) + i conj(V2_m)
+            }
+        }
+    }
+    __syncthreads();
+    bluestein<true, W>(s1, sm.s2, sm.tw, N, M, pl, Bc);
+    // per pixel: gF~ = gM_j + gdF / <F>; dF/da = -tau1 F, dF/db = -a tau1 G g F,
+    // dF/dc = -a tau1 b G eta F.  Each warp walks a contiguous run of the group's 2 W N pixel
+    // slots (skewer by skewer, lanes on consecutive pixels); per-lane FP32 partials of the
+    // current redshift bin are flushed to the block's FP64 accumulators when the bin changes
+    // (warp_flush)
+    {
+        const int total = 2 * W * N;
+        const int per_warp = ((total + FIT_T / 32 - 1) / (FIT_T / 32) + 31) & ~31;
+        const int lane = threadIdx.x & 31;
+        const int beg = (threadIdx.x >> 5) * per_warp, end = min(total, beg + per_warp);
+        float acc6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, accS[1] = {0.f};
+        int jw = -1, js = 0;
+        auto dst6 = [&](int b, int q) { return q < 3 ? &sh.sA[3 * b + q] : &sh.sB[3 * b + q - 3]; };
+        for (int i0 = beg; i0 < end; i0 += 32) {   // warp-uniform trip count
+            const int i = i0 + lane;
+            const int sk = i / N;                   // skewer 0 .. 2W - 1 of the group
+            const int ii = i - sk * N;
+            const int w = sk >> 1, t = sk & 1;
+            const bool ok = i < end && qd.sid[2 * p0 + sk] >= 0;
+            int j = -1;
+            float v6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, vS = 0.f;
+            if (ok) {
+                const int64_t o = qd.off[2 * p0 + sk] + ii;
+                float t1, g;
+                const float F = flux_of(a, o, th, &t1, &g);
+                const float2 z = s1[ii * W + w];
+                const float gdF = t ? z.y : z.x;
+                j = a.zbin[o];
+                const float pa = th[3 * j], pb = th[3 * j + 1];
+                const float e = a.eta ? __ldg(a.eta + o) : 0.f;
+                const float G = a.G ? __ldg(a.G + o) : 1.f;
+                const float dFa = -t1 * F;
+                const float dFb = -pa * t1 * G * g * F;
+                const float dFc = -pa * t1 * pb * G * e * F;
+                const float gF = sh.gM[j] + gdF * fbar_inv;
+                v6[0] = gF * dFa;
+                v6[1] = gF * dFb;
+                v6[2] = gF * dFc;
+                v6[3] = dFa;
+                v6[4] = dFb;
+                v6[5] = dFc;
+                vS = gdF * F;
+            }
+            const bool change = ok && jw >= 0 && j != jw;
+            if (__any_sync(0xffffffffu, change)) warp_flush(change, jw, acc6, dst6);
+            if (ok) {
+                if (jw < 0) jw = j;
+#pragma unroll
+                for (int q = 0; q < 6; ++q) acc6[q] += v6[q];
+                accS[0] += vS;
+            }
+        }
+        warp_flush(true, jw, acc6, dst6);
+        warp_flush(true, js, accS, [&](int, int) { return sh.sS; });
+    }
+    __syncthreads();
+}
+
 __global__ void __launch_bounds__(FIT_T, 3) fit_adjoint_kernel(const FitArgs a) {
     extern __shared__ float2 smem[];
-    float2* s1 = smem;
-    // with the chirp table the Bluestein transforms need no second buffer
-    float2* s2 = a.chirp ? nullptr : smem + a.mmax;
-    float2* tw = smem + (a.chirp ? 1 : 2) * a.mmax;
+    const FitSmem sm(smem, a);
     __shared__ double sA[3 * FIT_MAX_BINS], sB[3 * FIT_MAX_BINS], sS;
     __shared__ double edges[FIT_MAX_BINS + 1];
     __shared__ float gP[FIT_MAX_BINS], gM[FIT_MAX_BINS];   // the weights in FP32 (no FP64 per pixel)
     __shared__ float th[3 * FIT_MAX_BINS];
     __shared__ long long item_sh;
-    __shared__ PairSetup ps;
+    __shared__ Quad qd;
     for (int i = threadIdx.x; i < 3 * a.nzb; i += FIT_T) {
         sA[i] = 0.0;
         sB[i] = 0.0;
@@ -419,116 +579,15 @@ __global__ void __launch_bounds__(FIT_T, 3) fit_adjoint_kernel(const FitArgs a) 
     const double kfac = 2.0 * (3.14159265358979323846 / a.dx);
     __shared__ FftPlan pl;
     __shared__ int thr[FIT_MAX_BINS + 1];
-    int curM = 0, curN = 0;
-    while (next_pair(a, &item_sh, &ps)) {
-        const int N = ps.N;
-        const int M = bluestein_m(N);
-        if (N != curN) {
-            kbin_thresholds(N, kfac, edges, a.nkb, thr);
-            curN = N;
-        }
-        if (M > a.mmax) {
-            // a skewer longer than SmkFitProblem.n_max: skipped, the gradient is made NaN
-            if (threadIdx.x == 0) sS = __longlong_as_double(0x7ff8000000000000LL);
-            __syncthreads();
-            continue;
-        }
-        if (M != curM) {
-            if (threadIdx.x == 0) make_plan(M, &pl, 16);
-            __syncthreads();
-            fill_stage_twiddles(tw, pl);
-            curM = M;
-        }
-        const float2* Bc = a.chirp && a.chirp_off[N] >= 0 ? a.chirp + a.chirp_off[N] : nullptr;
-        if (!Bc && !s2) {
-            // a length missing from the chirp table (and no room to transform its chirp here)
-            if (threadIdx.x == 0) sS = __longlong_as_double(0x7ff8000000000000LL);
-            __syncthreads();
-            continue;
-        }
-        if (a.spec) {   // Z as the forward pass with the same theta left it
-            const float2* z = a.spec + ps.off[0];
-            for (int m = threadIdx.x; m < N; m += FIT_T) s1[m] = z[m];
-            __syncthreads();
+    const AdjShared sh{sA, sB, &sS, gP, gM};
+    LengthState ls{0, 0};
+    while (next_quad(a, &item_sh, &qd)) {
+        if (qd.np == 2 && qd.N[1] == qd.N[0]) {
+            adjoint_group<2>(a, qd, 0, sm, pl, thr, edges, kfac, th, fbar_inv, sh, ls);
         } else {
-            load_pair(a, th, fbar_inv, ps, s1);
-            bluestein<false>(s1, s2, tw, N, M, pl, Bc);
+            adjoint_group<1>(a, qd, 0, sm, pl, thr, edges, kfac, th, fbar_inv, sh, ls);
+            if (qd.np == 2) adjoint_group<1>(a, qd, 1, sm, pl, thr, edges, kfac, th, fbar_inv, sh, ls);
         }
-        // V_t (Hermitian): V_m = w_m X_m (0<m<N/2), V_{N-m} = conj; V_0, V_{N/2} = 2 Re(w X);
-        // packed W = V_1 + i V_2; the unnormalised inverse DFT of W is gdF_1 + i gdF_2.
-        const float norm = (float)(a.dx / (double)N);
-        for (int m = threadIdx.x; m <= N / 2; m += FIT_T) {
-            const float2 zk = s1[m], zm = s1[m == 0 ? 0 : N - m];
-            const int b = kbin_thr(m, thr, a.nkb);
-            const float wgt = b >= 0 ? gP[b] * norm : 0.f;
-            float2 x1 = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
-            float2 x2 = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
-            if (ps.sid[1] < 0) x2 = make_float2(0.f, 0.f);
-            x1 = cscale(x1, wgt);
-            x2 = cscale(x2, wgt);
-            // in place: this thread alone reads and writes the slots m and N - m
-            if (m == 0 || 2 * m == N) {
-                s1[m] = make_float2(2.f * x1.x, 2.f * x2.x);
-            } else {
-                s1[m] = make_float2(x1.x - x2.y, x1.y + x2.x);          // V1_m + i V2_m
-                s1[N - m] = make_float2(x1.x + x2.y, x2.x - x1.y);      // conj(V1_m) + i conj(V2_m)
-            }
-        }
-        __syncthreads();
-        bluestein<true>(s1, s2, tw, N, M, pl, Bc);
-        // per pixel: gF~ = gM_j + gdF / <F>; dF/da = -tau1 F, dF/db = -a tau1 G g F,
-        // dF/dc = -a tau1 b G eta F.  Each warp walks a contiguous run of the pair's 2N pixel
-        // slots (lanes on consecutive pixels); per-lane FP32 partials of the current redshift bin
-        // are flushed to the block's FP64 accumulators when the bin changes (warp_flush)
-        {
-            const int total = 2 * N;
-            const int per_warp = ((total + FIT_T / 32 - 1) / (FIT_T / 32) + 31) & ~31;
-            const int lane = threadIdx.x & 31;
-            const int beg = (threadIdx.x >> 5) * per_warp, end = min(total, beg + per_warp);
-            float acc6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, accS[1] = {0.f};
-            int jw = -1, js = 0;
-            auto dst6 = [&](int b, int q) { return q < 3 ? &sA[3 * b + q] : &sB[3 * b + q - 3]; };
-            for (int i0 = beg; i0 < end; i0 += 32) {   // warp-uniform trip count
-                const int i = i0 + lane;
-                const int t = i < N ? 0 : 1;
-                const int ii = i - t * N;
-                const bool ok = i < end && ps.sid[t] >= 0;
-                int j = -1;
-                float v6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, vS = 0.f;
-                if (ok) {
-                    const int64_t o = ps.off[t] + ii;
-                    float t1, g;
-                    const float F = flux_of(a, o, th, &t1, &g);
-                    const float gdF = t ? s1[ii].y : s1[ii].x;
-                    j = a.zbin[o];
-                    const float pa = th[3 * j], pb = th[3 * j + 1];
-                    const float e = a.eta ? __ldg(a.eta + o) : 0.f;
-                    const float G = a.G ? __ldg(a.G + o) : 1.f;
-                    const float dFa = -t1 * F;
-                    const float dFb = -pa * t1 * G * g * F;
-                    const float dFc = -pa * t1 * pb * G * e * F;
-                    const float gF = gM[j] + gdF * fbar_inv;
-                    v6[0] = gF * dFa;
-                    v6[1] = gF * dFb;
-                    v6[2] = gF * dFc;
-                    v6[3] = dFa;
-                    v6[4] = dFb;
-                    v6[5] = dFc;
-                    vS = gdF * F;
-                }
-                const bool change = ok && jw >= 0 && j != jw;
-                if (__any_sync(0xffffffffu, change)) warp_flush(change, jw, acc6, dst6);
-                if (ok) {
-                    if (jw < 0) jw = j;
-#pragma unroll
-                    for (int q = 0; q < 6; ++q) acc6[q] += v6[q];
-                    accS[0] += vS;
-                }
-            }
-            warp_flush(true, jw, acc6, dst6);
-            warp_flush(true, js, accS, [&](int, int) { return &sS; });
-        }
-        __syncthreads();
     }
     double* A = a.acc + acc_A(a.nzb, a.nkb);
     double* B = a.acc + acc_B(a.nzb, a.nkb);
@@ -671,9 +730,9 @@ int smk_fit_forward(const SmkFitProblem* fp, const float* theta, double* acc, vo
     const int g1 = (int)std::min<int64_t>((a.n_total + FIT_T * 16 - 1) / (FIT_T * 16), 8LL * nsm);
     fit_flux_kernel<<<std::max(g1, 1), FIT_T, 0, st>>>(a);
     if ((rc = check_launch("fit_flux_kernel"))) return rc;
-    const size_t smem = (a.chirp ? 2 : 3) * (size_t)a.mmax * sizeof(float2);
+    const size_t smem = (a.chirp ? 3 : 4) * (size_t)a.mmax * sizeof(float2);   // two lines, tw (, s2)
     int grid = 0;
-    if ((rc = fit_grid((const void*)fit_p1d_kernel, smem, a.n_items, &grid))) return rc;
+    if ((rc = fit_grid((const void*)fit_p1d_kernel, smem, (a.n_items + 1) / 2, &grid))) return rc;
     fit_p1d_kernel<<<grid, FIT_T, smem, st>>>(a);
     return check_launch("fit_p1d_kernel");
 }
@@ -690,9 +749,9 @@ int smk_fit_backward(const SmkFitProblem* fp, const float* theta, double* acc, c
     if (cudaMemsetAsync(acc + off, 0, sizeof(double) * (acc_psq(a.nzb, a.nkb) - off), st) != cudaSuccess ||
         cudaMemsetAsync(workspace, 0, 8, st) != cudaSuccess)
         return check_launch("smk_fit_backward: memset");
-    const size_t smem = (a.chirp ? 2 : 3) * (size_t)a.mmax * sizeof(float2);
+    const size_t smem = (a.chirp ? 3 : 4) * (size_t)a.mmax * sizeof(float2);   // two lines, tw (, s2)
     int grid = 0;
-    if ((rc = fit_grid((const void*)fit_adjoint_kernel, smem, a.n_items, &grid))) return rc;
+    if ((rc = fit_grid((const void*)fit_adjoint_kernel, smem, (a.n_items + 1) / 2, &grid))) return rc;
     fit_adjoint_kernel<<<grid, FIT_T, smem, st>>>(a);
     return check_launch("fit_adjoint_kernel");
 }
