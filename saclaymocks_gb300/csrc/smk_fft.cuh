@@ -488,29 +488,55 @@ __device__ __forceinline__ void fft_tile(float2* __restrict__ s, const float2* _
     }
 }
 
-// The inverse of ifft_tile_out for a fixed plan whose first executed stage works on contiguous
-// groups (m = 1), with the elements in ns equal parts (each a whole number of groups): that
-// stage runs part by part, wait(p) called before part p >= 1 (the caller has the first part),
-// then after() once every part is done (after a block barrier), then the other stages.  Lets
-// the later parts of a tile still be arriving while the first are transformed.
-template <int W, int SN, int T, int RMAX, int NF, class Wait, class After, class Out>
+// Leading inverse stages (in execution order: NST-1, NST-2, ...) of the fixed plan whose groups of
+// L = R m elements lie inside one of ns equal parts of the line (L divides NF / ns), at most
+// NST - 1 (the last stage always runs on the whole line).
+template <int NF, int RMAX>
+__host__ __device__ constexpr int parts_depth(int ns) {
+    using FP = FixedPlan<NF, RMAX>;
+    int d = 0;
+    for (int st = FP::P.nst - 1; st >= 1; --st) {
+        const int L = FP::P.r[st] * FP::P.m[st];
+        if ((NF / ns) % L != 0) break;
+        ++d;
+    }
+    return d;
+}
+
+// Stage ST of the fixed plan on butterflies [bf0, bf1), no barrier.
+template <int NF, int RMAX, int ST, bool INV, int W, int SN, int T>
+__device__ __forceinline__ void fft_stage_fixed_range(float2* __restrict__ s, const float2* __restrict__ tw,
+                                                      int bf0, int bf1) {
+    using FP = FixedPlan<NF, RMAX>;
+    constexpr int R = FP::P.r[ST];
+    using SP = CtStage<FP::P.m[ST], NF, FP::P.twoff[ST]>;
+    fft_stage_body<R, INV, W, SN, T, false, false, SP, NoOut, NoPre, false>(s, tw, SP{}, NoOut{}, NoPre{}, bf0, bf1);
+}
+
+// The inverse of ifft_tile_out for a fixed plan, with the elements in ns equal parts: the D
+// leading stages whose groups lie inside one part (parts_depth) run part by part, wait(p) called
+// before part p >= 1 (the caller has the first part), then after() once every part is done
+// (after a block barrier), then the other stages.  Lets the later parts of a tile still be
+// arriving while the first are transformed.  D must be 1 or 2 (the plans of the tile variants).
+template <int W, int SN, int T, int RMAX, int NF, int D, class Wait, class After, class Out>
 __device__ __forceinline__ void ifft_tile_out_parts(float2* __restrict__ s, const float2* __restrict__ tw,
                                                     const int ns, Wait&& wait, After&& after, Out&& out) {
     using FP = FixedPlan<NF, RMAX>;
     constexpr int NST = FP::P.nst;
-    constexpr int S0 = NST - 1;
-    constexpr int R0 = FP::P.r[S0];
-    static_assert(NST >= 2 && FP::P.m[S0] == 1, "parts need contiguous first groups");
-    using SP0 = CtStage<1, NF, FP::P.twoff[S0]>;
-    const int pb = (NF / R0 / ns) * W;   // butterflies per part
+    static_assert(D >= 1 && D <= 2 && D <= NST - 1, "parts need one or two leading part-local stages");
+    constexpr int S0 = NST - 1, S1 = NST - 2;
+    constexpr int NB0 = (NF / FP::P.r[S0]) * W, NB1 = (NF / FP::P.r[S1 >= 0 ? S1 : 0]) * W;
     for (int p = 0; p < ns; ++p) {
         if (p) wait(p);
-        fft_stage_body<R0, true, W, SN, T, false, false, SP0, NoOut, NoPre, false>(s, tw, SP0{}, NoOut{}, NoPre{},
-                                                                                    p * pb, (p + 1) * pb);
+        fft_stage_fixed_range<NF, RMAX, S0, true, W, SN, T>(s, tw, p * (NB0 / ns), (p + 1) * (NB0 / ns));
+        if constexpr (D == 2) {
+            __syncthreads();
+            fft_stage_fixed_range<NF, RMAX, S1, true, W, SN, T>(s, tw, p * (NB1 / ns), (p + 1) * (NB1 / ns));
+        }
     }
     __syncthreads();
     after();
-    static_for<1, NST - 1>([&](auto c) {
+    static_for<D, NST - 1>([&](auto c) {
         fft_stage_fixed<NF, RMAX, NST - 1 - decltype(c)::value, true, W, SN, T>(s, tw);
     });
     fft_stage_fixed<NF, RMAX, 0, true, W, SN, T, true>(s, tw, out);

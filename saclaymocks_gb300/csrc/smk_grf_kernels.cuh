@@ -185,7 +185,7 @@ struct LineArgs {
     int dst_kb;
 };
 
-constexpr int LINE_PARTS = 4;   // most parts a y tile's TMA load is split into
+constexpr int LINE_PARTS = 2;   // most parts a y tile's TMA load is split into
 
 // Forward: natural -> digit-reversed order along the axis (kept in HBM); inverse: back.
 // smem: s[n*W] | tw[n]
@@ -208,20 +208,14 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
     }
     __syncthreads();
     unsigned parity = 0;
-    // Tile in parts (inverse with a compile-time plan whose first stage works on contiguous groups
-    // of R0, TMA loads into shared memory): part p of the rows completes on bar[p], and the first
-    // stage runs on the parts that have arrived while the others are still in flight.  Parts are
-    // whole boxes and whole groups: ns = the largest of LINE_PARTS, 2 with n / ns a multiple of
-    // box_rows and of R0 (1: one part).
+    // Tile in two halves (inverse with a compile-time plan whose first stages work on groups that
+    // stay inside a half, TMA loads into shared memory): half p of the rows completes on bar[p],
+    // and those stages run on the first half while the second is still in flight.  The halves
+    // are whole boxes (ns = 1 otherwise; four parts with 128-row boxes measured slower).
     int ns = 1;
     if constexpr (INV && C::NF > 0) {
-        constexpr int R0 = FixedPlan<C::NF, C::RMAX>::P.r[FixedPlan<C::NF, C::RMAX>::P.nst - 1];
-        if (a.tma == 1)
-            for (int k = LINE_PARTS; k >= 2; k /= 2)
-                if (n % k == 0 && (n / k) % a.box_rows == 0 && (n / k) % R0 == 0) {
-                    ns = k;
-                    break;
-                }
+        constexpr int d2 = parts_depth<C::NF, C::RMAX>(2);
+        if (d2 >= 1 && a.tma == 1 && n % 2 == 0 && (n / 2) % a.box_rows == 0) ns = 2;
     }
     const int64_t ncolt = ceil_div(a.ncol, W);
     const int64_t tpb = a.n_outer * ncolt;
@@ -324,8 +318,11 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
                 if (w < cols) base[e * es + w] = v;
             };
             if constexpr (C::NF > 0) {
+                // the leading stages whose groups stay inside a half run half by half (two for
+                // the plan 16,16,10 at 2560: groups of 10 and of 160 rows)
+                constexpr int D2 = parts_depth<C::NF, C::RMAX>(2) >= 2 ? 2 : 1;
                 if (ns > 1) {
-                    ifft_tile_out_parts<W, W, T, C::RMAX, C::NF>(s, tw, ns, [&](int p) {
+                    ifft_tile_out_parts<W, W, T, C::RMAX, C::NF, D2>(s, tw, ns, [&](int p) {
                         if (!mbar_wait_bounded(&bar[p], parity, a.tma_wait_limit)) timed_out = 1;
                     }, [&]() {
                         parity ^= 1u;
