@@ -1,15 +1,20 @@
 // GRF pass kernels of libsmk (make_boxes on GB300), shared by the translation units that
 // instantiate their tile variants:
 //
-//   zfwd   r2c along z of the caller's white noise, two rows per complex line
-//   line   c2c along y (forward: natural -> digit-reversed, inverse: back)
+//   zfwd   r2c along z of the caller's white noise, two rows per complex line (zfwdw: one
+//          warp per row pair, the built-in form; zfwd_kernel: block tiles)
+//   line   c2c along y (forward: natural -> digit-reversed, inverse: back), in place, from the
+//          blocked x-pass intermediate, or (forward) into it
 //   xpass  x forward, x sqrt(P/Vcell), eta_k = kz^2/k^2 delta_k, x inverse of both fields
+//          (xpi_kernel: read from and written to the blocked intermediate)
 //   xgen   GPU noise: Fourier modes of white noise drawn in place, x sqrt(P/Vcell), eta split,
-//          x inverse of both fields (replaces zfwd + line forward + xpass)
-//   zinv   c2r along z of row pairs of delta and eta, x 1/N, FP64 sum/sum^2/non-finite
+//          x inverse of both fields (replaces zfwd + line forward + xpass; xgi_kernel: into the
+//          blocked intermediate)
+//   zinv   c2r along z of row pairs of delta and eta, x 1/N, FP64 sum/sum^2/non-finite (zinvw:
+//          one warp per row pair)
 //
-// Every pass is a persistent kernel over tiles of W lines (see smk_fft.cuh) sized to the
-// resident-block count of the GPU; the tile variant (W, threads) of each pass is chosen per
+// Every pass is a persistent kernel over tiles of W lines (see smk_fft.cuh) or warps sized to
+// the resident-block count of the GPU; the tile variant (W, threads) of each pass is chosen per
 // line length from the tables below (smk_tune_set overrides the default).
 #pragma once
 
