@@ -660,8 +660,10 @@ __device__ __forceinline__ float mode_inv_k2(float kk) {
 
 // Second output of the GPU-noise x pass from delta_k and 1/k^2: eta_ij = k_i k_j / k^2 delta_k,
 // or velocity v_i = -i k_i / k^2 * vfac * delta_k (SMK_ETA_VX/VY/VZ).
-__device__ __forceinline__ float2 eta_from_inv_k2(int comp, float2 d, float kx, float ky, float kz, float ikk,
+template <int COMP = -1>   // COMP >= 0: the component fixed at compile time (no per-mode switch)
+__device__ __forceinline__ float2 eta_from_inv_k2(int comp_rt, float2 d, float kx, float ky, float kz, float ikk,
                                                   float vfac) {
+    const int comp = COMP >= 0 ? COMP : comp_rt;
     if (comp >= SMK_ETA_VX) {
         const float ki = comp == SMK_ETA_VX ? kx : (comp == SMK_ETA_VY ? ky : kz);
         const float f = ki * ikk * vfac;
@@ -688,7 +690,7 @@ struct ModePair {
     float2 d[2];
     float kz[2], ikk[2];
 };
-template <bool CHECK>
+template <bool CHECK, int PKM = -1>   // PKM >= 0: the P(k) mode fixed at compile time
 __device__ __forceinline__ ModePair draw_pair(const XGenArgs& a, uint64_t seed, int ixe, int iy, int iym,
                                               float kxv, float ky, int kz0, const float* kzt, float scale_c) {
     ModePair mp;
@@ -733,7 +735,7 @@ __device__ __forceinline__ ModePair draw_pair(const XGenArgs& a, uint64_t seed, 
         const float kz_ = kzt[kz];
         const float kk = mode_k2(kxv, ky, kz_);
         const float r = rsqrtf(kk);   // 1/k (+inf at k = 0)
-        if (a.pk_mode == SMK_PK_GRID) {
+        if ((PKM >= 0 ? PKM : a.pk_mode) == SMK_PK_GRID) {
             sc *= __ldg(a.grid + ((int64_t)ixe * a.ny + iy) * a.nzh + kz);
         } else {
             // sqrt(k)/den = 1/sqrt(den^2/k): one reciprocal square root (0 at k = 0)
@@ -879,22 +881,24 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
         const int iym = iy == 0 ? 0 : a.ny - iy;
         const float ky = kaxis(iy, a.ny, a.kfac, true);
         const uint64_t seed = a.seed + (uint64_t)b;
-        // the column count per tile as a constant (BOTH: W/2 columns of each field, else W of one)
-        auto draw = [&](auto chk, auto both_c) {
-            constexpr bool BOTH = decltype(both_c)::value;
+        // the column count per tile as a constant (BOTH: W/2 columns of each field, else W of one);
+        // FAST: analytic P(k) and eta_zz fixed at compile time (no per-mode switches)
+        auto draw = [&](auto chk, auto both_c, auto fast_c) {
+            constexpr bool BOTH = decltype(both_c)::value, FAST = decltype(fast_c)::value;
             constexpr int WCC = BOTH ? W / 2 : W, NPC = WCC / 2;
+            constexpr int PKM = FAST ? SMK_PK_ANALYTIC : -1, COMP = FAST ? SMK_ETA_ZZ : -1;
 #pragma unroll 2
             for (int idx = threadIdx.x; idx < n * NPC; idx += T) {
                 const int e = idx / NPC, pr = idx % NPC;
                 const int c0 = 2 * pr, kz0 = cb * WCC + c0;
                 const float kxv = kx[e];
-                const ModePair mp = draw_pair<decltype(chk)::value>(a, seed, ix[e], iy, iym, kxv, ky, kz0, kzt, scale_c);
+                const ModePair mp = draw_pair<decltype(chk)::value, PKM>(a, seed, ix[e], iy, iym, kxv, ky, kz0, kzt, scale_c);
                 // the two modes of a field as one 16-byte store (rows are 64 B apart, so 8-byte stores
                 // of lanes on rows e and e + 2 met on the same banks)
                 float2 v[2][2];
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
-                    const float2 et = eta_from_inv_k2(a.eta_comp, mp.d[h], kxv, ky, mp.kz[h], mp.ikk[h], a.vfac);
+                    const float2 et = eta_from_inv_k2<COMP>(a.eta_comp, mp.d[h], kxv, ky, mp.kz[h], mp.ikk[h], a.vfac);
                     if constexpr (BOTH) {
                         v[0][h] = mp.d[h];
                         v[1][h] = et;
@@ -907,23 +911,26 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
                     *reinterpret_cast<float4*>(s + e * W + WCC + c0) = make_float4(v[1][0].x, v[1][0].y, v[1][1].x, v[1][1].y);
             }
         };
+        const bool fast = a.pk_mode == SMK_PK_ANALYTIC && a.eta_comp == SMK_ETA_ZZ;
         if (tile_needs_check(a, cb * WC, WC)) {
-            if (both) draw(std::true_type{}, std::true_type{});
-            else draw(std::true_type{}, std::false_type{});
+            if (both) draw(std::true_type{}, std::true_type{}, std::false_type{});
+            else draw(std::true_type{}, std::false_type{}, std::false_type{});
         } else {
-            if (both) draw(std::false_type{}, std::true_type{});
-            else draw(std::false_type{}, std::false_type{});
+            if (both && fast) draw(std::false_type{}, std::true_type{}, std::true_type{});
+            else if (both) draw(std::false_type{}, std::true_type{}, std::false_type{});
+            else draw(std::false_type{}, std::false_type{}, std::false_type{});
         }
         __syncthreads();
-        const int cols = min(WC, a.nzh - cb * WC);
         const int64_t row0 = ((int64_t)kbl * nouter + b * a.nx) * a.ny + yslot;
         float2* d0 = a.I[0] + row0 * WC;
         float2* d1 = both ? a.I[1] + row0 * WC : nullptr;
         const int64_t es = (int64_t)a.ny * WC;
+        // I holds whole column blocks (a chunk is a multiple of 16 columns), so every column of the
+        // tile is stored: those past nzh carry the zero modes the draw gives there
         ifft_tile_out<W, W, T, C::RMAX, C::NF>(s, tw, a.pl, [&](int e, int w, float2 v) {
             const int f = both && w >= WC;
             const int c = w - f * WC;
-            if (c < cols) (f ? d1 : d0)[e * es + c] = v;
+            (f ? d1 : d0)[e * es + c] = v;
         });
         __syncthreads();
     }
@@ -1481,7 +1488,7 @@ inline bool variant_fits(const TileVariant& v, int n) { return v.nmax < 0 ? n ==
 #define SMK_X_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(4, 512, 4096, 16, 1)
 // x pass of GPU noise: W = lines per tile (one field per launch: W columns; both fields: W/2 + W/2)
 #define SMK_XGEN_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) \
-    X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1)
+    X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1) X(8, 512, -2560, 16, 1)
 
 enum { PASS_ZFWD = 0, PASS_LINE = 1, PASS_XPASS = 2, PASS_XGEN = 3, PASS_ZINV = 4, NPASS = 5 };
 
