@@ -169,6 +169,24 @@ __host__ __device__ __forceinline__ u32x4 philox4x32_10(u32x4 ctr, uint32_t k0, 
     return ctr;
 }
 
+// Hardware special functions on normal arguments (PTX .approx with .ftz: only subnormal inputs and
+// outputs would differ from rsqrtf / __log2f / __sinf / __cosf, and none arise where these are
+// used), without the subnormal range handling that the non-ftz forms add.
+__device__ __forceinline__ float hw_rsqrt(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float hw_log2(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ void hw_sincos(float x, float* s, float* c) {
+    asm("sin.approx.ftz.f32 %0, %1;" : "=f"(*s) : "f"(x));
+    asm("cos.approx.ftz.f32 %0, %1;" : "=f"(*c) : "f"(x));
+}
+
 // Stream tags keep the Fourier-mode noise of the boxes and the skewer noise in disjoint
 // counter spaces.
 enum : uint32_t { STREAM_KMODE = 0x4Bu, STREAM_SKEWER = 0x53u };
@@ -186,10 +204,10 @@ __device__ __forceinline__ void gauss4(u32x4 r, float g[4]) {
     for (int h = 0; h < 2; ++h) {
         const float u1 = 2.0f - __uint_as_float(0x3F800000u | (r.v[2 * h] >> 9));
         const float v = __uint_as_float(0x3F800000u | (r.v[2 * h + 1] >> 9));
-        const float x = -1.3862943611198906f * __log2f(u1);                             // -2 ln 2 log2(u)
-        const float rad = x > 0.0f ? x * rsqrtf(x) : 0.0f;
+        const float x = -1.3862943611198906f * hw_log2(u1);                             // -2 ln 2 log2(u)
+        const float rad = x > 0.0f ? x * hw_rsqrt(x) : 0.0f;
         float s, c;
-        __sincosf(fmaf(v, 6.28318530717958648f, -9.42477796076937972f), &s, &c);
+        hw_sincos(fmaf(v, 6.28318530717958648f, -9.42477796076937972f), &s, &c);
         g[2 * h] = -rad * c;
         g[2 * h + 1] = -rad * s;
     }

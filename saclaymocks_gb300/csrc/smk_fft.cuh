@@ -392,8 +392,25 @@ __device__ __forceinline__ void fft_stage_body(float2* __restrict__ s, const flo
         const int q = j - blk * m;
         float2* p = s + (blk * R * m + q) * SN + w;
         float2 v[R];
+        // 64-byte rows (W = 8), m = 1, even R: the 4 butterflies of a warp (rows blk R + r, all of
+        // one parity) met on the same banks; lanes of odd blk take their rows in the order r ^ 1
+        const bool m1 = W == 8 && SN == 8 && R % 2 == 0 && m == 1;
+        const bool fl = m1 && (blk & 1);
+        float2* pe = fl ? p + SN : p;
+        float2* po = fl ? p - SN : p;
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = p[r * m * SN];
+        for (int r = 0; r < R; ++r) v[r] = (r & 1 ? po : pe)[r * m * SN];
+        auto swap_pairs = [&]() {
+            if constexpr (R % 2 == 0) {
+#pragma unroll
+                for (int r = 0; r < R; r += 2) {
+                    const float2 a0 = v[r], a1 = v[r + 1];
+                    v[r] = fl ? a1 : a0;
+                    v[r + 1] = fl ? a0 : a1;
+                }
+            }
+        };
+        if (m1) swap_pairs();
         if constexpr (PRE) {
             const int e0 = blk * R * m + q;
 #pragma unroll
@@ -417,8 +434,9 @@ __device__ __forceinline__ void fft_stage_body(float2* __restrict__ s, const flo
 #pragma unroll
             for (int r = 0; r < R; ++r) out(q + r * m, w, v[r]);
         } else {
+            if (m1) swap_pairs();
 #pragma unroll
-            for (int r = 0; r < R; ++r) p[r * m * SN] = v[r];
+            for (int r = 0; r < R; ++r) (r & 1 ? po : pe)[r * m * SN] = v[r];
         }
     }
     if constexpr (!OUT && SYNC) __syncthreads();

@@ -654,7 +654,7 @@ __device__ __forceinline__ float mode_k2(float kxv, float ky, float kz) {
     return __fadd_rn(__fadd_rn(__fmul_rn(kxv, kxv), __fmul_rn(ky, ky)), __fmul_rn(kz, kz));
 }
 __device__ __forceinline__ float mode_inv_k2(float kk) {
-    const float r = rsqrtf(kk);
+    const float r = hw_rsqrt(kk);
     return kk > 0.0f ? r * r : 1.0f;
 }
 
@@ -734,13 +734,13 @@ __device__ __forceinline__ ModePair draw_pair(const XGenArgs& a, uint64_t seed, 
         }
         const float kz_ = kzt[kz];
         const float kk = mode_k2(kxv, ky, kz_);
-        const float r = rsqrtf(kk);   // 1/k (+inf at k = 0)
+        const float r = hw_rsqrt(kk);   // 1/k (+inf at k = 0)
         if ((PKM >= 0 ? PKM : a.pk_mode) == SMK_PK_GRID) {
             sc *= __ldg(a.grid + ((int64_t)ixe * a.ny + iy) * a.nzh + kz);
         } else {
             // sqrt(k)/den = 1/sqrt(den^2/k): one reciprocal square root (0 at k = 0)
             const float den = fmaf(kk, inv_k0sq, 1.0f);
-            sc *= rsqrtf(den * den * r);
+            sc *= hw_rsqrt(den * den * r);
         }
         mp.d[h] = cscale(X, sc);
         mp.kz[h] = kz_;
@@ -847,7 +847,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
 // of its W lines and stores the last stage from registers into I (see XGenArgs).  Tiles that
 // run together hold neighbouring y slots, so their 8 * KB-byte pieces of a row of I are
 // assembled into whole lines in L2.
-// smem: s[n*W] | tw[n] | kx[n] | ix[n] | kzt[nzh]
+// smem: s[n*W] | tw[n] | kxi[n] (k_x, frequency index) | kzt[nzh]
 template <class C>
 __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
     constexpr int W = C::W, T = C::T;
@@ -857,14 +857,12 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
     const int n = a.pl.n;  // == nx
     float2* s = smem;
     float2* tw = s + n * W;
-    float* kx = reinterpret_cast<float*>(tw + n);
-    int* ix = reinterpret_cast<int*>(kx + n);
-    float* kzt = reinterpret_cast<float*>(ix + n);
+    float2* kxi = tw + n;                     // slot e: (k_x, frequency index as int bits)
+    float* kzt = reinterpret_cast<float*>(kxi + n);
     fill_stage_twiddles(tw, a.pl);
     for (int e = threadIdx.x; e < n; e += T) {
         const int f = freq_of_slot(a.pl, e);
-        ix[e] = f;
-        kx[e] = kaxis(f, n, a.kfac, true);
+        kxi[e] = make_float2(kaxis(f, n, a.kfac, true), __int_as_float(f));
     }
     for (int z = threadIdx.x; z < a.nzh; z += T) kzt[z] = kaxis(z, a.nz, a.kfac, false);
     __syncthreads();
@@ -887,12 +885,48 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
             constexpr bool BOTH = decltype(both_c)::value, FAST = decltype(fast_c)::value;
             constexpr int WCC = BOTH ? W / 2 : W, NPC = WCC / 2;
             constexpr int PKM = FAST ? SMK_PK_ANALYTIC : -1, COMP = FAST ? SMK_ETA_ZZ : -1;
+            if constexpr (FAST && BOTH && !decltype(chk)::value) {
+                // the same arithmetic as draw_pair + eta_from_inv_k2, with the column pair fixed per
+                // thread (T is a multiple of NPC): its k_z and k_z^2 and the tile's k_y^2 stay in
+                // registers across the rows
+                static_assert(T % NPC == 0, "a thread keeps one column pair");
+                const int pr = threadIdx.x % NPC, c0 = 2 * pr, kz0 = cb * WCC + c0;
+                const float kzz[2] = {__fmul_rn(kzt[kz0], kzt[kz0]), __fmul_rn(kzt[kz0 + 1], kzt[kz0 + 1])};
+                const float kyy = __fmul_rn(ky, ky);
+                const float inv_k0sq = a.inv_k0 * a.inv_k0;
+#pragma unroll 2
+                for (int e = threadIdx.x / NPC; e < n; e += T / NPC) {
+                    const float2 kq = kxi[e];
+                    float g[4];
+                    u32x4 ctr;
+                    ctr.v[0] = (uint32_t)(kz0 >> 1);
+                    ctr.v[1] = (uint32_t)__float_as_int(kq.y);
+                    ctr.v[2] = (uint32_t)iy;
+                    ctr.v[3] = STREAM_KMODE;
+                    gauss4(philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32)), g);
+                    const float kxy = __fadd_rn(__fmul_rn(kq.x, kq.x), kyy);
+                    float2 v[2][2];
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const float kk = __fadd_rn(kxy, kzz[h]);
+                        const float r = hw_rsqrt(kk);
+                        const float den = fmaf(kk, inv_k0sq, 1.0f);
+                        const float2 d = cscale(make_float2(g[2 * h], g[2 * h + 1]), scale_c * hw_rsqrt(den * den * r));
+                        v[0][h] = d;
+                        v[1][h] = cscale(d, kzz[h] * (kk > 0.0f ? r * r : 1.0f));
+                    }
+                    *reinterpret_cast<float4*>(s + e * W + c0) = make_float4(v[0][0].x, v[0][0].y, v[0][1].x, v[0][1].y);
+                    *reinterpret_cast<float4*>(s + e * W + WCC + c0) = make_float4(v[1][0].x, v[1][0].y, v[1][1].x, v[1][1].y);
+                }
+                return;
+            }
 #pragma unroll 2
             for (int idx = threadIdx.x; idx < n * NPC; idx += T) {
                 const int e = idx / NPC, pr = idx % NPC;
                 const int c0 = 2 * pr, kz0 = cb * WCC + c0;
-                const float kxv = kx[e];
-                const ModePair mp = draw_pair<decltype(chk)::value, PKM>(a, seed, ix[e], iy, iym, kxv, ky, kz0, kzt, scale_c);
+                const float2 kq = kxi[e];
+                const float kxv = kq.x;
+                const ModePair mp = draw_pair<decltype(chk)::value, PKM>(a, seed, __float_as_int(kq.y), iy, iym, kxv, ky, kz0, kzt, scale_c);
                 // the two modes of a field as one 16-byte store (rows are 64 B apart, so 8-byte stores
                 // of lanes on rows e and e + 2 met on the same banks)
                 float2 v[2][2];
