@@ -604,10 +604,12 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
         __syncthreads();
         float2* d0 = a.I[0] + row0 * WC;
         float2* d1 = both ? a.I[1] + row0 * WC : nullptr;
+        // I holds whole column blocks, so every column of the tile is stored (those past nzh
+        // were loaded as zeros and stay zero)
         ifft_tile_out<W, W, T, C::RMAX, C::NF>(s, tw, a.pl, [&](int e, int w, float2 v) {
             const int f = both && w >= WC;
             const int c = w - f * WC;
-            if (c < cols) (f ? d1 : d0)[e * es + c] = v;
+            (f ? d1 : d0)[e * es + c] = v;
         });
         __syncthreads();
     }
@@ -992,8 +994,13 @@ struct ZInvArgs {
 // 1536, (16, 10, 16) for 2560), makes every stage's accesses conflict-free and spreads the
 // digit-reversed scatter of the half spectrum over the banks.  SWZ = 0: p + (p >> 5), one pad
 // per 32 slots (power-of-two lengths >= 2048, whose scatter the swizzle does not spread).
+// SWZ = 2: p + (p >> 4), one pad per 16 slots (compile-time plans (16, x, 16) whose strides m are 1
+// or multiples of 16: the R elements of a butterfly then lie a constant stride apart, and every
+// stage and the scatter are conflict-free).
 template <int SWZ>
-__host__ __device__ __forceinline__ int zslot(int p) { return SWZ ? (p ^ ((p >> 4) & 15)) : p + (p >> 5); }
+__host__ __device__ __forceinline__ int zslot(int p) {
+    return SWZ == 2 ? p + (p >> 4) : SWZ ? (p ^ ((p >> 4) & 15)) : p + (p >> 5);
+}
 __host__ __device__ __forceinline__ int zpad(int p) { return zslot<0>(p); }
 
 // One stage of a warp's line (slots padded by zpad) with the plan's per-stage twiddles.
@@ -1037,13 +1044,63 @@ __device__ __forceinline__ void warp_fft_stage(float2* __restrict__ s, const flo
     __syncwarp();
 }
 
+// Stage ST of the compile-time mid-ordered plan of length NF on a warp's line in the SWZ = 2
+// layout: element r of butterfly (blk, q) sits at slot(blk R m + q) + r ES, ES = m + m/16 (m a
+// multiple of 16) or 1 (m = 1, R = 16), so the loads and stores are immediate offsets from one
+// base.  Same butterflies and twiddles as warp_fft_stage (bit-identical results).
+template <int NF, int ST, bool LAST, class Out>
+__device__ __forceinline__ void warp_fft_stage_fixed(float2* __restrict__ s, const float2* __restrict__ stw,
+                                                     const int lane, Out&& out) {
+    using FP = FixedPlan<NF, 16, true>;
+    constexpr int R = FP::P.r[ST], m = FP::P.m[ST];
+    static_assert(m == 1 ? R == 16 : m % 16 == 0, "one-pad-per-16 layout needs strides 1 (R = 16) or 16k");
+    constexpr int ES = m == 1 ? 1 : m + m / 16;
+    constexpr int nb = NF / R;
+    const float2* tws = stw + FP::P.twoff[ST];
+    for (int j = lane; j < nb; j += 32) {
+        const int blk = j / m;
+        const int q = j - blk * m;
+        const int p0 = blk * R * m + q;
+        float2* b = s + zslot<2>(p0);
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = b[r * ES];
+        if constexpr (m > 1) {
+            const float2* t = tws + q * (R - 1) - 1;
+            if (q != 0) {
+#pragma unroll
+                for (int r = 1; r < R; ++r) v[r] = cmulc(v[r], t[r]);
+            }
+        }
+        Dft<R, true>::run(v);
+        if constexpr (LAST) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) out(p0 + r * m, v[r]);
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) b[r * ES] = v[r];
+        }
+    }
+    __syncwarp();
+}
+
 // Inverse transform of a warp's line (digit-reversed slots in, natural order out): every stage
-// but the last in place, the last one's outputs handed to out(e, value).  (A compile-time plan
-// for the z pass at 1536 measured slower: 39.2 against 38.8 ms.)
-template <int RMAX, int SWZ, class Out>
+// but the last in place, the last one's outputs handed to out(e, value).  NF > 0: the compile-time
+// mid-ordered plan of that length on the SWZ = 2 layout (the run-time plan on the XOR swizzle
+// measured 38.8 ms at 1536 and its compile-time form 39.2 ms).
+template <int RMAX, int SWZ, class Out, int NF = 0>
 __device__ __forceinline__ void warp_ifft_out(float2* s, const float2* stw, const FftPlan& pl, const int lane,
                                               Out&& out) {
     auto none = [](int, float2) {};
+    if constexpr (NF > 0) {
+        static_assert(SWZ == 2, "compile-time warp plans use the one-pad-per-16 layout");
+        constexpr int NST = FixedPlan<NF, 16, true>::P.nst;
+        static_for<0, NST - 1>([&](auto c) {
+            warp_fft_stage_fixed<NF, NST - 1 - decltype(c)::value, false>(s, stw, lane, none);
+        });
+        warp_fft_stage_fixed<NF, 0, true>(s, stw, lane, out);
+        return;
+    }
     for (int st = pl.nst - 1; st >= 0; --st) {
         const bool last = st == 0;
 #define SMK_WSTAGE(RR)                                                              \
@@ -1126,7 +1183,7 @@ __device__ __forceinline__ void warp_fft_fwd(float2* s, const float2* stw, const
 
 // Shared memory of zinvw_kernel for `warps` warps: stw[twn] | sof[n] | per-warp lines.
 __host__ __device__ inline size_t zinvw_line_slots(int n, int swz) {
-    return swz ? (size_t)(n + 15) / 16 * 16 : (size_t)zpad(n - 1) + 1;
+    return swz == 2 ? (size_t)zslot<2>(n - 1) + 1 : swz ? (size_t)(n + 15) / 16 * 16 : (size_t)zpad(n - 1) + 1;
 }
 inline size_t zinvw_smem(const FftPlan& pl, int warps, int swz) {
     return (size_t)pl.twn * sizeof(float2) + (size_t)(pl.n + (pl.n & 1)) * sizeof(int) +
@@ -1211,7 +1268,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) zinvw_kernel(const ZInvArgs a) 
         float* o2 = o1 + a.pitch;
         float p1 = 0.f, p2 = 0.f;
         const float sc = a.scale;
-        warp_ifft_out<C::RMAX, SWZ>(sw, stw, a.pl, lane, [&](int e, float2 z) {
+        auto out_fn = [&](int e, float2 z) {
             const float v0 = z.x * sc;
             __stcs(o1 + e, v0);
             p1 += v0;
@@ -1222,7 +1279,8 @@ __global__ void __launch_bounds__(C::T, C::MINB) zinvw_kernel(const ZInvArgs a) 
                 p1 += v1;
                 p2 = fmaf(v1, v1, p2);
             }
-        });
+        };
+        warp_ifft_out<C::RMAX, SWZ, decltype(out_fn)&, SWZ == 2 ? C::NF : 0>(sw, stw, a.pl, lane, out_fn);
         if (!(fabsf(p2) < INFINITY)) {
             // a non-finite value in this lane's share: recount it exactly (finite values only)
             // from the outputs this lane wrote (rows of this pair, read back from global)
@@ -1393,10 +1451,15 @@ static int launch_zinvw(ZInvArgs a, int64_t rows_per_box, cudaStream_t st) {
     if (!fixed_plan_ok<C>(a.pl)) return fail(SMK_EINVAL, "%s: length %d is not the variant's fixed length", "zinvw_kernel", a.pl.n);
     a.zt.rows_per_box = rows_per_box;
     a.zt.tiles_per_box = 0;
-    // layout: XOR swizzle with the odd radix mid-plan, except power-of-two lengths >= 2048
+    // layout: a compile-time plan on one pad per 16 slots; else the XOR swizzle with the odd radix
+    // mid-plan, except power-of-two lengths >= 2048
     const int n = a.pl.n;
-    const int swz = ((n & (n - 1)) != 0 || n < 2048) ? 1 : 0;
+    const int swz = C::NF > 0 ? 2 : ((n & (n - 1)) != 0 || n < 2048) ? 1 : 0;
     if (swz && !make_plan(n, &a.pl, C::RMAX, true)) return fail(SMK_ENOTSUPP, "zinvw_kernel: no plan for %d", n);
+    if constexpr (C::NF > 0) {
+        if (!same_plan(a.pl, FixedPlan<C::NF, 16, true>::P))
+            return fail(SMK_EINVAL, "zinvw_kernel: length %d is not the variant's fixed length", n);
+    }
     int dev = 0, smem_max = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
@@ -1404,7 +1467,9 @@ static int launch_zinvw(ZInvArgs a, int64_t rows_per_box, cudaStream_t st) {
     while (warps > 1 && zinvw_smem(a.pl, warps, swz) > (size_t)smem_max) --warps;
     const size_t smem = zinvw_smem(a.pl, warps, swz);
     if (smem > (size_t)smem_max) return fail(SMK_ENOTSUPP, "zinvw_kernel: line of %d does not fit", n);
-    auto kern = swz ? zinvw_kernel<C, 1> : zinvw_kernel<C, 0>;
+    void (*kern)(const ZInvArgs) = nullptr;
+    if constexpr (C::NF > 0) kern = zinvw_kernel<C, 2>;
+    else kern = swz ? zinvw_kernel<C, 1> : zinvw_kernel<C, 0>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return check_launch("cudaFuncSetAttribute(zinvw)");
     int per_sm = 0;
@@ -1514,12 +1579,13 @@ inline bool variant_fits(const TileVariant& v, int n) { return v.nmax < 0 ? n ==
     X(2, 128, 2560, 16, 4) X(4, 512, 4096, 16, 1) X(0, 512, 2560, 16, 1) X(0, 512, 4096, 16, 1)
 // z inverse: one warp per row pair (W = 0; as many warps per block as fit, up to T / 32)
 #define SMK_ZINV_VARIANTS(X) X(0, 512, 2560, 16, 1) X(0, 512, 1024, 16, 1) X(0, 256, 1024, 16, 2) \
-    X(0, 512, 4096, 16, 1) X(0, 256, 2560, 32, 1)
+    X(0, 512, 4096, 16, 1) X(0, 256, 2560, 32, 1) X(0, 512, -1536, 16, 1)
 // y pass (line): W = columns per tile
 #define SMK_LINE_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) \
     X(4, 512, 4096, 16, 1) X(8, 256, 2560, 16, 1) X(8, 512, -2560, 16, 1)
 // x pass of host noise: W = columns per tile
-#define SMK_X_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(4, 512, 4096, 16, 1)
+#define SMK_X_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(4, 512, 4096, 16, 1) \
+    X(8, 512, -2560, 16, 1)
 // x pass of GPU noise: W = lines per tile (one field per launch: W columns; both fields: W/2 + W/2)
 #define SMK_XGEN_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) \
     X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1) X(8, 512, -2560, 16, 1)
