@@ -187,6 +187,30 @@ __device__ __forceinline__ void hw_sincos(float x, float* s, float* c) {
     asm("cos.approx.ftz.f32 %0, %1;" : "=f"(*c) : "f"(x));
 }
 
+// The same block with the round keys precomputed (rk0[r] = k0 + r W0, rk1[r] = k1 + r W1, mod 2^32):
+// keys held in kernel parameters enter the XORs as constant operands, no key additions per round.
+__host__ __device__ __forceinline__ u32x4 philox4x32_10_rk(u32x4 ctr, const uint32_t* rk0, const uint32_t* rk1) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = (uint64_t)M0 * ctr.v[0];
+        const uint64_t p1 = (uint64_t)M1 * ctr.v[2];
+        u32x4 o;
+        o.v[0] = (uint32_t)(p1 >> 32) ^ ctr.v[1] ^ rk0[r];
+        o.v[1] = (uint32_t)p1;
+        o.v[2] = (uint32_t)(p0 >> 32) ^ ctr.v[3] ^ rk1[r];
+        o.v[3] = (uint32_t)p0;
+        ctr = o;
+    }
+    return ctr;
+}
+inline void philox_round_keys(uint64_t seed, uint32_t rk0[10], uint32_t rk1[10]) {
+    for (int r = 0; r < 10; ++r) {
+        rk0[r] = (uint32_t)seed + (uint32_t)r * 0x9E3779B9u;
+        rk1[r] = (uint32_t)(seed >> 32) + (uint32_t)r * 0xBB67AE85u;
+    }
+}
+
 // Stream tags keep the Fourier-mode noise of the boxes and the skewer noise in disjoint
 // counter spaces.
 enum : uint32_t { STREAM_KMODE = 0x4Bu, STREAM_SKEWER = 0x53u };

@@ -376,10 +376,17 @@ struct CtStage {
     __device__ __forceinline__ static int div(int x) { return M == 1 ? x : x / M; }
 };
 
+// Row swizzle of a tile (SWR > 0, an even radix: the plan's stage with m = 1 has radix SWR and
+// every other stage's m is a multiple of SWR): row e of the tile is stored at row
+// e ^ ((e / SWR) & 1), so the m = 1 stage's butterflies of one warp (rows blk SWR + r of one
+// parity before the swizzle) meet no bank twice.  Producers of such a tile write row e there.
+template <int SWR>
+__host__ __device__ __forceinline__ int tile_row(int e) { return SWR > 0 ? e ^ ((e / SWR) & 1) : e; }
+
 // Butterflies [bf0, bf1) of the stage (bf1 < 0: all); SYNC: a block barrier at the end (in-place
-// stages only).
+// stages only); SWR > 0: rows in the tile_row<SWR> order (compile-time stages only).
 template <int R, bool INV, int W, int SN, int T, bool OUT, bool PRE, class SP, class Out, class Pre,
-          bool SYNC = true>
+          bool SYNC = true, int SWR = 0>
 __device__ __forceinline__ void fft_stage_body(float2* __restrict__ s, const float2* __restrict__ tw, const SP& sp,
                                                Out&& out, Pre&& pre, const int bf0 = 0, const int bf1 = -1) {
     const int m = sp.m;
@@ -392,12 +399,34 @@ __device__ __forceinline__ void fft_stage_body(float2* __restrict__ s, const flo
         const int q = j - blk * m;
         float2* p = s + (blk * R * m + q) * SN + w;
         float2 v[R];
-        // 64-byte rows (W = 8), m = 1, even R: the 4 butterflies of a warp (rows blk R + r, all of
-        // one parity) met on the same banks; lanes of odd blk take their rows in the order r ^ 1
-        const bool m1 = W == 8 && SN == 8 && R % 2 == 0 && m == 1;
-        const bool fl = m1 && (blk & 1);
-        float2* pe = fl ? p + SN : p;
-        float2* po = fl ? p - SN : p;
+        // element r at (r & 1 ? po : pe)[r m SN]
+        bool m1 = false, fl = false;
+        float2 *pe, *po;
+        if constexpr (SWR > 0) {
+            // e = blk R m + q + r m: its row parity is q's (m even), and (e / SWR) & 1 is blk's for
+            // m = 1, else (blk R K + q / SWR + r K) & 1 with K = m / SWR
+            constexpr int M = SP::m;
+            static_assert(SWR % 2 == 0 && (M == 1 ? R == SWR : M % SWR == 0), "row swizzle of another plan");
+            if constexpr (M == 1) {
+                const int f = (blk & 1) * SN;
+                pe = p + f;
+                po = p - f;
+            } else {
+                constexpr int K = M / SWR;
+                const int A = (blk * R * K + q / SWR) & 1;
+                const int d = (q & 1) ? -SN : SN;
+                pe = p + (A ? d : 0);
+                po = (K & 1) ? p + (A ? 0 : d) : pe;
+            }
+        } else {
+            // 64-byte rows (W = 8), m = 1, even R: the 4 butterflies of a warp (rows blk R + r, all
+            // of one parity) met on the same banks; lanes of odd blk take their rows in the order
+            // r ^ 1 and swap them back in registers
+            m1 = W == 8 && SN == 8 && R % 2 == 0 && m == 1;
+            fl = m1 && (blk & 1);
+            pe = fl ? p + SN : p;
+            po = fl ? p - SN : p;
+        }
 #pragma unroll
         for (int r = 0; r < R; ++r) v[r] = (r & 1 ? po : pe)[r * m * SN];
         auto swap_pairs = [&]() {
@@ -451,13 +480,14 @@ __device__ __forceinline__ void fft_stage(float2* __restrict__ s, const float2* 
 
 // Stage st of the compile-time plan of length NF.
 template <int NF, int RMAX, int ST, bool INV, int W, int SN, int T, bool OUT = false, bool PRE = false,
-          class Out = NoOut, class Pre = NoPre>
+          class Out = NoOut, class Pre = NoPre, int SWR = 0>
 __device__ __forceinline__ void fft_stage_fixed(float2* __restrict__ s, const float2* __restrict__ tw,
                                                 Out&& out = Out{}, Pre&& pre = Pre{}) {
     using FP = FixedPlan<NF, RMAX>;
     constexpr int R = FP::P.r[ST];
     static_assert(R <= RMAX, "fixed plan radix above the kernel's");
-    fft_stage_body<R, INV, W, SN, T, OUT, PRE>(s, tw, CtStage<FP::P.m[ST], NF, FP::P.twoff[ST]>{}, out, pre);
+    using SP = CtStage<FP::P.m[ST], NF, FP::P.twoff[ST]>;
+    fft_stage_body<R, INV, W, SN, T, OUT, PRE, SP, Out&, Pre&, true, SWR>(s, tw, SP{}, out, pre);
 }
 
 template <bool INV, int W, int SN, int T, int RMAX, bool OUT = false, bool PRE = false, class Out = NoOut,
@@ -563,15 +593,18 @@ __device__ __forceinline__ void ifft_tile_out_parts(float2* __restrict__ s, cons
 // Inverse of the W lines with the last stage's natural-order results handed to out(e, w, v)
 // (element e of line w) instead of written back: every stage but the last ends with a block
 // barrier; the caller synchronises before it reuses s.
-template <int W, int SN, int T, int RMAX, int NF = 0, class Out>
+// SWR > 0 (compile-time plans): the tile's rows in the tile_row<SWR> order.
+template <int W, int SN, int T, int RMAX, int NF = 0, int SWR = 0, class Out>
 __device__ __forceinline__ void ifft_tile_out(float2* __restrict__ s, const float2* __restrict__ tw,
                                               const FftPlan& pl, Out&& out) {
+    static_assert(SWR == 0 || NF > 0, "row swizzle with compile-time plans only");
     if constexpr (NF > 0) {
         constexpr int NST = FixedPlan<NF, RMAX>::P.nst;
         static_for<0, NST - 1>([&](auto c) {
-            fft_stage_fixed<NF, RMAX, NST - 1 - decltype(c)::value, true, W, SN, T>(s, tw);
+            fft_stage_fixed<NF, RMAX, NST - 1 - decltype(c)::value, true, W, SN, T, false, false, NoOut, NoPre, SWR>(
+                s, tw);
         });
-        fft_stage_fixed<NF, RMAX, 0, true, W, SN, T, true>(s, tw, out);
+        fft_stage_fixed<NF, RMAX, 0, true, W, SN, T, true, false, Out&, NoPre, SWR>(s, tw, out);
     } else {
         for (int st = pl.nst - 1; st >= 1; --st) fft_stage_any<true, W, SN, T, RMAX>(s, tw, pl, st);
         fft_stage_any<true, W, SN, T, RMAX, true>(s, tw, pl, 0, out);

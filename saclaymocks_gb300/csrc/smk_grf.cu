@@ -316,6 +316,7 @@ int smk_grf_boxes(const SmkGrfParams* p, float* delta, float* eta, double* stats
         ga.sig_c = (float)sqrt(0.5 * ncell);
         ga.sig_r = (float)sqrt(ncell);
         ga.seed = p->seed;
+        philox_round_keys(p->seed, ga.rk0, ga.rk1);
         ga.eta_comp = p->eta_comp;
         ga.vfac = (float)p->vel_factor;
         const int nf = p->want_eta ? 2 : 1;

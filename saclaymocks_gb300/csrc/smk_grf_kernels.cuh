@@ -636,6 +636,7 @@ struct XGenArgs {
     float inv_k0, inv_vcell;
     float sig_c, sig_r;    // sqrt(N/2), sqrt(N)
     uint64_t seed;
+    uint32_t rk0[10], rk1[10];  // Philox round keys of seed (box 0; batch 1 uses them directly)
     int eta_comp;
     float vfac;
     int fields;            // XGEN_BOTH: W/2 delta + W/2 eta lines per tile; XGEN_DELTA / XGEN_ETA:
@@ -842,6 +843,21 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
     }
 }
 
+// Row swizzle of the x pass's tile (tile_row): the compile-time plan's last radix when it is even
+// and the tile has 64-byte rows (W = 8), else none.
+template <class C>
+constexpr int xgi_row_swizzle() {
+    if constexpr (C::NF > 0 && C::W == 8) {
+        constexpr FftPlan P = FixedPlan<C::NF, C::RMAX>::P;
+        constexpr int RL = P.r[P.nst - 1];
+        bool ok = RL % 2 == 0;
+        for (int st = 0; st + 1 < P.nst; ++st) ok = ok && P.m[st] % RL == 0;
+        return ok ? RL : 0;
+    } else {
+        return 0;
+    }
+}
+
 // ------------------------------------------------------------------ GPU-noise x pass into the
 // blocked intermediate
 // Tiles (box b, column block kb, y slot), y slot fastest: a tile draws the modes of its WC k_z
@@ -853,6 +869,8 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
 template <class C>
 __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
     constexpr int W = C::W, T = C::T;
+    // compile-time plan with an even last radix on 64-byte rows: rows in the tile_row order
+    constexpr int SWR = xgi_row_swizzle<C>();
     extern __shared__ __align__(128) float2 smem[];
     const bool both = a.fields == XGEN_BOTH;
     const int WC = both ? W / 2 : W;          // k_z columns per tile (= KB)
@@ -883,8 +901,9 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
         const uint64_t seed = a.seed + (uint64_t)b;
         // the column count per tile as a constant (BOTH: W/2 columns of each field, else W of one);
         // FAST: analytic P(k) and eta_zz fixed at compile time (no per-mode switches)
-        auto draw = [&](auto chk, auto both_c, auto fast_c) {
+        auto draw = [&](auto chk, auto both_c, auto fast_c, auto rk_c) {
             constexpr bool BOTH = decltype(both_c)::value, FAST = decltype(fast_c)::value;
+            constexpr bool RK = decltype(rk_c)::value;   // one box: the round keys from the parameters
             constexpr int WCC = BOTH ? W / 2 : W, NPC = WCC / 2;
             constexpr int PKM = FAST ? SMK_PK_ANALYTIC : -1, COMP = FAST ? SMK_ETA_ZZ : -1;
             if constexpr (FAST && BOTH && !decltype(chk)::value) {
@@ -905,7 +924,10 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
                     ctr.v[1] = (uint32_t)__float_as_int(kq.y);
                     ctr.v[2] = (uint32_t)iy;
                     ctr.v[3] = STREAM_KMODE;
-                    gauss4(philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32)), g);
+                    if constexpr (RK)
+                        gauss4(philox4x32_10_rk(ctr, a.rk0, a.rk1), g);
+                    else
+                        gauss4(philox4x32_10(ctr, (uint32_t)seed, (uint32_t)(seed >> 32)), g);
                     const float kxy = __fadd_rn(__fmul_rn(kq.x, kq.x), kyy);
                     float2 v[2][2];
 #pragma unroll
@@ -917,8 +939,9 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
                         v[0][h] = d;
                         v[1][h] = cscale(d, kzz[h] * (kk > 0.0f ? r * r : 1.0f));
                     }
-                    *reinterpret_cast<float4*>(s + e * W + c0) = make_float4(v[0][0].x, v[0][0].y, v[0][1].x, v[0][1].y);
-                    *reinterpret_cast<float4*>(s + e * W + WCC + c0) = make_float4(v[1][0].x, v[1][0].y, v[1][1].x, v[1][1].y);
+                    float2* row = s + tile_row<SWR>(e) * W;
+                    *reinterpret_cast<float4*>(row + c0) = make_float4(v[0][0].x, v[0][0].y, v[0][1].x, v[0][1].y);
+                    *reinterpret_cast<float4*>(row + WCC + c0) = make_float4(v[1][0].x, v[1][0].y, v[1][1].x, v[1][1].y);
                 }
                 return;
             }
@@ -942,19 +965,23 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
                         v[0][h] = a.fields == XGEN_DELTA ? mp.d[h] : et;
                     }
                 }
-                *reinterpret_cast<float4*>(s + e * W + c0) = make_float4(v[0][0].x, v[0][0].y, v[0][1].x, v[0][1].y);
+                float2* row = s + tile_row<SWR>(e) * W;
+                *reinterpret_cast<float4*>(row + c0) = make_float4(v[0][0].x, v[0][0].y, v[0][1].x, v[0][1].y);
                 if constexpr (BOTH)
-                    *reinterpret_cast<float4*>(s + e * W + WCC + c0) = make_float4(v[1][0].x, v[1][0].y, v[1][1].x, v[1][1].y);
+                    *reinterpret_cast<float4*>(row + WCC + c0) = make_float4(v[1][0].x, v[1][0].y, v[1][1].x, v[1][1].y);
             }
         };
         const bool fast = a.pk_mode == SMK_PK_ANALYTIC && a.eta_comp == SMK_ETA_ZZ;
+        using F_ = std::false_type;
+        using T_ = std::true_type;
         if (tile_needs_check(a, cb * WC, WC)) {
-            if (both) draw(std::true_type{}, std::true_type{}, std::false_type{});
-            else draw(std::true_type{}, std::false_type{}, std::false_type{});
+            if (both) draw(T_{}, T_{}, F_{}, F_{});
+            else draw(T_{}, F_{}, F_{}, F_{});
         } else {
-            if (both && fast) draw(std::false_type{}, std::true_type{}, std::true_type{});
-            else if (both) draw(std::false_type{}, std::true_type{}, std::false_type{});
-            else draw(std::false_type{}, std::false_type{}, std::false_type{});
+            if (both && fast && a.batch == 1) draw(F_{}, T_{}, T_{}, T_{});
+            else if (both && fast) draw(F_{}, T_{}, T_{}, F_{});
+            else if (both) draw(F_{}, T_{}, F_{}, F_{});
+            else draw(F_{}, F_{}, F_{}, F_{});
         }
         __syncthreads();
         const int64_t row0 = ((int64_t)kbl * nouter + b * a.nx) * a.ny + yslot;
@@ -963,7 +990,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
         const int64_t es = (int64_t)a.ny * WC;
         // I holds whole column blocks (a chunk is a multiple of 16 columns), so every column of the
         // tile is stored: those past nzh carry the zero modes the draw gives there
-        ifft_tile_out<W, W, T, C::RMAX, C::NF>(s, tw, a.pl, [&](int e, int w, float2 v) {
+        ifft_tile_out<W, W, T, C::RMAX, C::NF, SWR>(s, tw, a.pl, [&](int e, int w, float2 v) {
             const int f = both && w >= WC;
             const int c = w - f * WC;
             (f ? d1 : d0)[e * es + c] = v;
