@@ -520,14 +520,15 @@ __device__ __forceinline__ void fft_stage_any(float2* s, const float2* tw, const
 // (fill_stage_twiddles).  The caller synchronises after filling s; on
 // return the block is synchronised.  The plan's radices must be <= RMAX (plan_fits; the
 // launchers check it), larger radices are not compiled into the kernel.
-template <bool INV, int W, int SN, int T, int RMAX = fft_max_radix(T), int NF = 0>
+template <bool INV, int W, int SN, int T, int RMAX = fft_max_radix(T), int NF = 0, int SWR = 0>
 __device__ __forceinline__ void fft_tile(float2* __restrict__ s, const float2* __restrict__ tw,
                                          const FftPlan& pl) {
+    static_assert(SWR == 0 || NF > 0, "row swizzle with compile-time plans only");
     if constexpr (NF > 0) {
         constexpr int NST = FixedPlan<NF, RMAX>::P.nst;
         static_for<0, NST>([&](auto c) {
             constexpr int st = INV ? NST - 1 - decltype(c)::value : decltype(c)::value;
-            fft_stage_fixed<NF, RMAX, st, INV, W, SN, T>(s, tw);
+            fft_stage_fixed<NF, RMAX, st, INV, W, SN, T, false, false, NoOut, NoPre, SWR>(s, tw);
         });
     } else if (!INV) {
         for (int st = 0; st < pl.nst; ++st) fft_stage_any<false, W, SN, T, RMAX>(s, tw, pl, st);

@@ -359,6 +359,21 @@ __global__ void __launch_bounds__(C::T, C::MINB) line_kernel(const __grid_consta
     if (a.tma == 2 && threadIdx.x == 0) bulk_wait_all();
 }
 
+// Row swizzle of an x-pass tile (tile_row): the compile-time plan's last radix when it is even,
+// the other stages' strides are multiples of it and the tile has 64-byte rows (W = 8), else none.
+template <class C>
+constexpr int xpass_row_swizzle() {
+    if constexpr (C::NF > 0 && C::W == 8) {
+        constexpr FftPlan P = FixedPlan<C::NF, C::RMAX>::P;
+        constexpr int RL = P.r[P.nst - 1];
+        bool ok = RL % 2 == 0;
+        for (int st = 0; st + 1 < P.nst; ++st) ok = ok && P.m[st] % RL == 0;
+        return ok ? RL : 0;
+    } else {
+        return 0;
+    }
+}
+
 // ------------------------------------------------------------------ fused x pass
 struct XArgs {
     FftPlan pl;            // x axis
@@ -511,6 +526,7 @@ template <class C, bool BOTH>
 __global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
     constexpr int W = C::W, T = C::T;
     constexpr int KB = W / 2;
+    constexpr int SWR = xpass_row_swizzle<C>();   // rows of the tile in the tile_row order
     extern __shared__ __align__(128) float2 smem[];
     const int n = a.pl.n;  // == nx
     float2* s = smem;
@@ -547,7 +563,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
         for (int idx = threadIdx.x; idx < n * (WC / 2); idx += T) {
             const int e = idx / (WC / 2), w = 2 * (idx % (WC / 2));
             const int bytes = w < cols ? (w + 1 < cols ? 16 : 8) : 0;
-            cp_async<16>(s + e * W + w, bytes ? pa + e * rs + w : pa, bytes);
+            cp_async<16>(s + tile_row<SWR>(e) * W + w, bytes ? pa + e * rs + w : pa, bytes);
         }
         const int iy = freq_of_slot(a.ply, yslot);
         if (threadIdx.x == 0) kt[0] = kaxis(iy, a.ny, a.kfac, true);
@@ -565,16 +581,17 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
             for (int e = threadIdx.x; e < n; e += T) prefetch_l2(pn + e * rs);
         }
         if (both)
-            fft_tile<false, KB, W, T, C::RMAX, C::NF>(s, tw, a.pl);
+            fft_tile<false, KB, W, T, C::RMAX, C::NF, SWR>(s, tw, a.pl);
         else
-            fft_tile<false, W, W, T, C::RMAX, C::NF>(s, tw, a.pl);
+            fft_tile<false, W, W, T, C::RMAX, C::NF, SWR>(s, tw, a.pl);
         const float ky = kt[0];
         // two adjacent columns per thread, read and written as 16-byte pieces (rows are 64 B
         // apart, so 8-byte accesses of lanes on rows e and e + 2 met on the same banks)
         for (int idx = threadIdx.x; idx < n * (WC / 2); idx += T) {
             const int e = idx / (WC / 2), w0 = 2 * (idx % (WC / 2));
             const float kxv = kx[e];
-            const float4 in = *reinterpret_cast<const float4*>(s + e * W + w0);
+            float2* row = s + tile_row<SWR>(e) * W;
+            const float4 in = *reinterpret_cast<const float4*>(row + w0);
             float2 d[2] = {make_float2(in.x, in.y), make_float2(in.z, in.w)}, et[2];
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
@@ -597,16 +614,16 @@ __global__ void __launch_bounds__(C::T, C::MINB) xpi_kernel(const XArgs a) {
                     et[h] = eta_apply<true>(a.eta_comp, d[h], kxv, ky, kz, kk1, a.vfac);
                 }
             }
-            *reinterpret_cast<float4*>(s + e * W + w0) = make_float4(d[0].x, d[0].y, d[1].x, d[1].y);
+            *reinterpret_cast<float4*>(row + w0) = make_float4(d[0].x, d[0].y, d[1].x, d[1].y);
             if (both)
-                *reinterpret_cast<float4*>(s + e * W + KB + w0) = make_float4(et[0].x, et[0].y, et[1].x, et[1].y);
+                *reinterpret_cast<float4*>(row + KB + w0) = make_float4(et[0].x, et[0].y, et[1].x, et[1].y);
         }
         __syncthreads();
         float2* d0 = a.I[0] + row0 * WC;
         float2* d1 = both ? a.I[1] + row0 * WC : nullptr;
         // I holds whole column blocks, so every column of the tile is stored (those past nzh
         // were loaded as zeros and stay zero)
-        ifft_tile_out<W, W, T, C::RMAX, C::NF>(s, tw, a.pl, [&](int e, int w, float2 v) {
+        ifft_tile_out<W, W, T, C::RMAX, C::NF, SWR>(s, tw, a.pl, [&](int e, int w, float2 v) {
             const int f = both && w >= WC;
             const int c = w - f * WC;
             (f ? d1 : d0)[e * es + c] = v;
@@ -843,21 +860,6 @@ __global__ void __launch_bounds__(C::T, C::MINB) xgen_kernel(const XGenArgs a) {
     }
 }
 
-// Row swizzle of the x pass's tile (tile_row): the compile-time plan's last radix when it is even
-// and the tile has 64-byte rows (W = 8), else none.
-template <class C>
-constexpr int xgi_row_swizzle() {
-    if constexpr (C::NF > 0 && C::W == 8) {
-        constexpr FftPlan P = FixedPlan<C::NF, C::RMAX>::P;
-        constexpr int RL = P.r[P.nst - 1];
-        bool ok = RL % 2 == 0;
-        for (int st = 0; st + 1 < P.nst; ++st) ok = ok && P.m[st] % RL == 0;
-        return ok ? RL : 0;
-    } else {
-        return 0;
-    }
-}
-
 // ------------------------------------------------------------------ GPU-noise x pass into the
 // blocked intermediate
 // Tiles (box b, column block kb, y slot), y slot fastest: a tile draws the modes of its WC k_z
@@ -870,7 +872,7 @@ template <class C>
 __global__ void __launch_bounds__(C::T, C::MINB) xgi_kernel(const XGenArgs a) {
     constexpr int W = C::W, T = C::T;
     // compile-time plan with an even last radix on 64-byte rows: rows in the tile_row order
-    constexpr int SWR = xgi_row_swizzle<C>();
+    constexpr int SWR = xpass_row_swizzle<C>();
     extern __shared__ __align__(128) float2 smem[];
     const bool both = a.fields == XGEN_BOTH;
     const int WC = both ? W / 2 : W;          // k_z columns per tile (= KB)
@@ -1075,7 +1077,7 @@ __device__ __forceinline__ void warp_fft_stage(float2* __restrict__ s, const flo
 // layout: element r of butterfly (blk, q) sits at slot(blk R m + q) + r ES, ES = m + m/16 (m a
 // multiple of 16) or 1 (m = 1, R = 16), so the loads and stores are immediate offsets from one
 // base.  Same butterflies and twiddles as warp_fft_stage (bit-identical results).
-template <int NF, int ST, bool LAST, class Out>
+template <int NF, int ST, bool LAST, class Out, bool INV = true>
 __device__ __forceinline__ void warp_fft_stage_fixed(float2* __restrict__ s, const float2* __restrict__ stw,
                                                      const int lane, Out&& out) {
     using FP = FixedPlan<NF, 16, true>;
@@ -1092,14 +1094,24 @@ __device__ __forceinline__ void warp_fft_stage_fixed(float2* __restrict__ s, con
         float2 v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) v[r] = b[r * ES];
-        if constexpr (m > 1) {
-            const float2* t = tws + q * (R - 1) - 1;
-            if (q != 0) {
+        const float2* t = tws + q * (R - 1) - 1;
+        if constexpr (INV) {
+            if constexpr (m > 1) {
+                if (q != 0) {
 #pragma unroll
-                for (int r = 1; r < R; ++r) v[r] = cmulc(v[r], t[r]);
+                    for (int r = 1; r < R; ++r) v[r] = cmulc(v[r], t[r]);
+                }
+            }
+            Dft<R, true>::run(v);
+        } else {
+            Dft<R, false>::run(v);
+            if constexpr (m > 1) {
+                if (q != 0) {
+#pragma unroll
+                    for (int r = 1; r < R; ++r) v[r] = cmul(v[r], t[r]);
+                }
             }
         }
-        Dft<R, true>::run(v);
         if constexpr (LAST) {
 #pragma unroll
             for (int r = 0; r < R; ++r) out(p0 + r * m, v[r]);
@@ -1182,9 +1194,18 @@ __device__ __forceinline__ void warp_flush_stats(double s1, double s2, double ba
 }
 
 // Forward transform of a warp's line (natural-order slots in, digit-reversed out), in place.
-template <int RMAX, int SWZ>
+template <int RMAX, int SWZ, int NF = 0>
 __device__ __forceinline__ void warp_fft_fwd(float2* s, const float2* stw, const FftPlan& pl, const int lane) {
     auto none = [](int, float2) {};
+    if constexpr (NF > 0) {
+        // the compile-time mid-ordered plan on the SWZ = 2 layout (same butterflies and twiddles)
+        static_assert(SWZ == 2, "compile-time warp plans use the one-pad-per-16 layout");
+        constexpr int NST = FixedPlan<NF, 16, true>::P.nst;
+        static_for<0, NST>([&](auto c) {
+            warp_fft_stage_fixed<NF, decltype(c)::value, false, decltype(none)&, false>(s, stw, lane, none);
+        });
+        return;
+    }
     for (int st = 0; st < pl.nst; ++st) {
         switch (pl.r[st]) {
             case 32:
@@ -1404,7 +1425,7 @@ __global__ void __launch_bounds__(C::T, C::MINB) zfwdw_kernel(const ZFwdArgs a) 
             }
         }
         __syncwarp();
-        warp_fft_fwd<C::RMAX, SWZ>(sw, stw, a.pl, lane);
+        warp_fft_fwd<C::RMAX, SWZ, SWZ == 2 ? C::NF : 0>(sw, stw, a.pl, lane);
         // X1_k = (Z_k + Z*_{n-k})/2, X2_k = (Z_k - Z*_{n-k})/(2i)
         float2* o1 = out2 + row0 * cp;
         float2* o2 = o1 + cp;
@@ -1431,8 +1452,12 @@ static int launch_zfwdw(ZFwdArgs a, int64_t rows_per_box, cudaStream_t st) {
     a.zt.rows_per_box = rows_per_box;
     a.zt.tiles_per_box = 0;
     const int n = a.pl.n;
-    const int swz = ((n & (n - 1)) != 0 || n < 2048) ? 1 : 0;
+    const int swz = C::NF > 0 ? 2 : ((n & (n - 1)) != 0 || n < 2048) ? 1 : 0;
     if (swz && !make_plan(n, &a.pl, C::RMAX, true)) return fail(SMK_ENOTSUPP, "zfwdw_kernel: no plan for %d", n);
+    if constexpr (C::NF > 0) {
+        if (!same_plan(a.pl, FixedPlan<C::NF, 16, true>::P))
+            return fail(SMK_EINVAL, "zfwdw_kernel: length %d is not the variant's fixed length", n);
+    }
     int dev = 0, smem_max = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
@@ -1440,7 +1465,9 @@ static int launch_zfwdw(ZFwdArgs a, int64_t rows_per_box, cudaStream_t st) {
     while (warps > 1 && zinvw_smem(a.pl, warps, swz) > (size_t)smem_max) --warps;
     const size_t smem = zinvw_smem(a.pl, warps, swz);
     if (smem > (size_t)smem_max) return fail(SMK_ENOTSUPP, "zfwdw_kernel: line of %d does not fit", n);
-    auto kern = swz ? zfwdw_kernel<C, 1> : zfwdw_kernel<C, 0>;
+    void (*kern)(const ZFwdArgs) = nullptr;
+    if constexpr (C::NF > 0) kern = zfwdw_kernel<C, 2>;
+    else kern = swz ? zfwdw_kernel<C, 1> : zfwdw_kernel<C, 0>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return check_launch("cudaFuncSetAttribute(zfwdw)");
     int per_sm = 0;
@@ -1603,7 +1630,8 @@ struct TileVariant {
 inline bool variant_fits(const TileVariant& v, int n) { return v.nmax < 0 ? n == -v.nmax : v.nmax >= n; }
 // r2c along z of host noise (zfwd): W = row pairs per tile; W = 0: one warp per row pair (built-in)
 #define SMK_Z_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(4, 512, 2560, 16, 1) \
-    X(2, 128, 2560, 16, 4) X(4, 512, 4096, 16, 1) X(0, 512, 2560, 16, 1) X(0, 512, 4096, 16, 1)
+    X(2, 128, 2560, 16, 4) X(4, 512, 4096, 16, 1) X(0, 512, 2560, 16, 1) X(0, 512, 4096, 16, 1) \
+    X(0, 512, -1536, 16, 1)
 // z inverse: one warp per row pair (W = 0; as many warps per block as fit, up to T / 32)
 #define SMK_ZINV_VARIANTS(X) X(0, 512, 2560, 16, 1) X(0, 512, 1024, 16, 1) X(0, 256, 1024, 16, 2) \
     X(0, 512, 4096, 16, 1) X(0, 256, 2560, 32, 1) X(0, 512, -1536, 16, 1)
