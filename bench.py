@@ -422,18 +422,18 @@ def run_ours(args, cfg):
     # DRAM bytes per unit from ncu captures of the same kernels on boxes with the production
     # line lengths (2560 x 128 x 1536 for the x pass, 128 x 2560 x 1536 for y and z), scaled by
     # the units of this launch: x (xgi_kernel, both fields) 15.84 B per mode, y (compile-time
-    # plan variant) 16.92 and z 16.14 B per mode and field
-    traffic = [15.84 * modes, 16.92 * modes * 2, 16.14 * modes * 2][dom] / 1e9
+    # plan variant) 16.92 and z (compile-time plan variant) 16.42 B per mode and field
+    traffic = [15.84 * modes, 16.92 * modes * 2, 16.42 * modes * 2][dom] / 1e9
     grf_ms = float(np.sum(pass_ms))
     step_ms = ms / args.steps
     # The x pass is instruction-bound, so its issue-slot roofline is reported beside the HBM one:
-    # warp instructions per mode from the same ncu capture (1.5185e9 for 2560x128x769 modes, both
+    # warp instructions per mode from the same ncu capture (1.4248e9 for 2560x128x769 modes, both
     # fields), scaled by the modes of this launch; peak = SMs x 4 schedulers x the median SM clock
     # sampled during the timed region
     clk_sum = clk.summary()
     sm_hz = float(clk_sum.get("sm_mhz") or 2070.0) * 1e6
     nsm = torch.cuda.get_device_properties(dev).multi_processor_count
-    x_winst = 1.5185e9 / (2560 * 128 * 769) * modes
+    x_winst = 1.4248e9 / (2560 * 128 * 769) * modes
     issue = {"kernel": "x_gen", "warp_instructions": x_winst,
              "achieved_per_s": x_winst / (pass_ms[0] * 1e-3), "peak_per_s": nsm * 4 * sm_hz,
              "frac": x_winst / (pass_ms[0] * 1e-3) / (nsm * 4 * sm_hz),
@@ -448,9 +448,9 @@ def run_ours(args, cfg):
                "box_sector_bytes": sec / 1e9, "naive_upper_bytes": 68.0 * pixels / 1e9,
                "basis": "4 B/pixel flux + distinct 32-B sectors of delta and eta touched by the 8 corners"}
     # the stage is bound by instruction issue, not HBM: its issue-slot roofline from the warp
-    # instructions per pixel of an ncu capture of the same kernel (3.174e9 for the 2e5-skewer
+    # instructions per pixel of an ncu capture of the same kernel (3.1197e9 for the 2e5-skewer
     # production set of 1.5995e8 pixels)
-    sk_winst = 3.174e9 / 1.5995e8 * pixels
+    sk_winst = 3.1197e9 / 1.5995e8 * pixels
     sk_roof["issue"] = {"warp_instructions": sk_winst, "achieved_per_s": sk_winst / (sk_ms * 1e-3),
                         "peak_per_s": nsm * 4 * sm_hz, "frac": sk_winst / (sk_ms * 1e-3) / (nsm * 4 * sm_hz),
                         "basis": "ncu smsp__inst_executed.sum per pixel, scaled; peak SMs x 4 x SM clock"}

@@ -400,8 +400,7 @@ __device__ __forceinline__ void fft_stage_body(float2* __restrict__ s, const flo
         float2* p = s + (blk * R * m + q) * SN + w;
         float2 v[R];
         // element r at (r & 1 ? po : pe)[r m SN]
-        bool m1 = false, fl = false;
-        float2 *pe, *po;
+        float2 *pe = p, *po = p;
         if constexpr (SWR > 0) {
             // e = blk R m + q + r m: its row parity is q's (m even), and (e / SWR) & 1 is blk's for
             // m = 1, else (blk R K + q / SWR + r K) & 1 with K = m / SWR
@@ -418,28 +417,9 @@ __device__ __forceinline__ void fft_stage_body(float2* __restrict__ s, const flo
                 pe = p + (A ? d : 0);
                 po = (K & 1) ? p + (A ? 0 : d) : pe;
             }
-        } else {
-            // 64-byte rows (W = 8), m = 1, even R: the 4 butterflies of a warp (rows blk R + r, all
-            // of one parity) met on the same banks; lanes of odd blk take their rows in the order
-            // r ^ 1 and swap them back in registers
-            m1 = W == 8 && SN == 8 && R % 2 == 0 && m == 1;
-            fl = m1 && (blk & 1);
-            pe = fl ? p + SN : p;
-            po = fl ? p - SN : p;
         }
 #pragma unroll
         for (int r = 0; r < R; ++r) v[r] = (r & 1 ? po : pe)[r * m * SN];
-        auto swap_pairs = [&]() {
-            if constexpr (R % 2 == 0) {
-#pragma unroll
-                for (int r = 0; r < R; r += 2) {
-                    const float2 a0 = v[r], a1 = v[r + 1];
-                    v[r] = fl ? a1 : a0;
-                    v[r + 1] = fl ? a0 : a1;
-                }
-            }
-        };
-        if (m1) swap_pairs();
         if constexpr (PRE) {
             const int e0 = blk * R * m + q;
 #pragma unroll
@@ -463,7 +443,6 @@ __device__ __forceinline__ void fft_stage_body(float2* __restrict__ s, const flo
 #pragma unroll
             for (int r = 0; r < R; ++r) out(q + r * m, w, v[r]);
         } else {
-            if (m1) swap_pairs();
 #pragma unroll
             for (int r = 0; r < R; ++r) (r & 1 ? po : pe)[r * m * SN] = v[r];
         }
