@@ -1285,8 +1285,10 @@ __global__ void __launch_bounds__(C::T, C::MINB) zinvw_kernel(const ZInvArgs a) 
         }
         // Z_k = X1_k + i X2_k (k <= n/2), Z_{n-k} = X1_k* + i X2_k*; DC and Nyquist real parts.
         // Lanes take consecutive k (the scatter to slot_of_freq(k) then spreads over the banks),
-        // U loads per row in flight.
-        constexpr int U = 12;
+        // U loads per row in flight; a compile-time length takes the U that covers the n/2 + 1
+        // modes in two rounds (13 at 1536: 36.6 -> 34.3 ms against 12, whose third round loads
+        // the Nyquist mode alone).
+        constexpr int U = (C::NF > 0 && (C::NF / 2 + 64) / 64 <= 16) ? (C::NF / 2 + 64) / 64 : 12;
         for (int k0 = lane; k0 < nh; k0 += 32 * U) {
             float2 x1[U], x2[U];
 #pragma unroll
