@@ -1104,12 +1104,13 @@ __device__ __forceinline__ void warp_fft_stage_fixed(float2* __restrict__ s, con
             }
             Dft<R, true>::run(v);
         } else {
+            // forward: every butterfly of a stage with m > 1 multiplies (the q = 0 entries are 1,
+            // exact), with no divergent branch around the twiddles (z forward 19.1 -> 18.6 ms; the
+            // same in the inverse measured 0.3 ms slower)
             Dft<R, false>::run(v);
             if constexpr (m > 1) {
-                if (q != 0) {
 #pragma unroll
-                    for (int r = 1; r < R; ++r) v[r] = cmul(v[r], t[r]);
-                }
+                for (int r = 1; r < R; ++r) v[r] = cmul(v[r], t[r]);
             }
         }
         if constexpr (LAST) {
