@@ -422,8 +422,8 @@ def run_ours(args, cfg):
     # DRAM bytes per unit from ncu captures of the same kernels on boxes with the production
     # line lengths (2560 x 128 x 1536 for the x pass, 128 x 2560 x 1536 for y and z), scaled by
     # the units of this launch: x (xgi_kernel, both fields) 15.84 B per mode, y (compile-time
-    # plan variant) 16.92 and z (compile-time plan variant) 16.42 B per mode and field
-    traffic = [15.84 * modes, 16.92 * modes * 2, 16.42 * modes * 2][dom] / 1e9
+    # plan variant) 16.92 and z (compile-time plan variant) 16.37 B per mode and field
+    traffic = [15.84 * modes, 16.92 * modes * 2, 16.37 * modes * 2][dom] / 1e9
     grf_ms = float(np.sum(pass_ms))
     step_ms = ms / args.steps
     # The x pass is instruction-bound, so its issue-slot roofline is reported beside the HBM one:
