@@ -1634,19 +1634,19 @@ inline bool variant_fits(const TileVariant& v, int n) { return v.nmax < 0 ? n ==
 // r2c along z of host noise (zfwd): W = row pairs per tile; W = 0: one warp per row pair (built-in)
 #define SMK_Z_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(4, 512, 2560, 16, 1) \
     X(2, 128, 2560, 16, 4) X(4, 512, 4096, 16, 1) X(0, 512, 2560, 16, 1) X(0, 512, 4096, 16, 1) \
-    X(0, 512, -1536, 16, 1)
+    X(0, 512, -1536, 16, 1) X(0, 512, -1024, 16, 1)
 // z inverse: one warp per row pair (W = 0; as many warps per block as fit, up to T / 32)
 #define SMK_ZINV_VARIANTS(X) X(0, 512, 2560, 16, 1) X(0, 512, 1024, 16, 1) X(0, 256, 1024, 16, 2) \
-    X(0, 512, 4096, 16, 1) X(0, 256, 2560, 32, 1) X(0, 512, -1536, 16, 1)
+    X(0, 512, 4096, 16, 1) X(0, 256, 2560, 32, 1) X(0, 512, -1536, 16, 1) X(0, 512, -1024, 16, 1)
 // y pass (line): W = columns per tile
 #define SMK_LINE_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) \
-    X(4, 512, 4096, 16, 1) X(8, 256, 2560, 16, 1) X(8, 512, -2560, 16, 1)
+    X(4, 512, 4096, 16, 1) X(8, 256, 2560, 16, 1) X(8, 512, -2560, 16, 1) X(16, 512, -1024, 16, 1)
 // x pass of host noise: W = columns per tile
 #define SMK_X_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(4, 512, 4096, 16, 1) \
-    X(8, 512, -2560, 16, 1)
+    X(8, 512, -2560, 16, 1) X(16, 512, -1024, 16, 1)
 // x pass of GPU noise: W = lines per tile (one field per launch: W columns; both fields: W/2 + W/2)
 #define SMK_XGEN_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) \
-    X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1) X(8, 512, -2560, 16, 1)
+    X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1) X(8, 512, -2560, 16, 1) X(16, 512, -1024, 16, 1)
 
 enum { PASS_ZFWD = 0, PASS_LINE = 1, PASS_XPASS = 2, PASS_XGEN = 3, PASS_ZINV = 4, NPASS = 5 };
 
