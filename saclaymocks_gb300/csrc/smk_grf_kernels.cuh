@@ -1640,13 +1640,15 @@ inline bool variant_fits(const TileVariant& v, int n) { return v.nmax < 0 ? n ==
     X(0, 512, 4096, 16, 1) X(0, 256, 2560, 32, 1) X(0, 512, -1536, 16, 1) X(0, 512, -1024, 16, 1)
 // y pass (line): W = columns per tile
 #define SMK_LINE_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(8, 1024, 2560, 8, 1) \
-    X(4, 512, 4096, 16, 1) X(8, 256, 2560, 16, 1) X(8, 512, -2560, 16, 1) X(16, 512, -1024, 16, 1)
+    X(4, 512, 4096, 16, 1) X(8, 256, 2560, 16, 1) X(8, 512, -2560, 16, 1) X(16, 512, -1024, 16, 1) \
+    X(16, 256, -128, 16, 2)
 // x pass of host noise: W = columns per tile
 #define SMK_X_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) X(4, 512, 4096, 16, 1) \
     X(8, 512, -2560, 16, 1) X(16, 512, -1024, 16, 1)
 // x pass of GPU noise: W = lines per tile (one field per launch: W columns; both fields: W/2 + W/2)
 #define SMK_XGEN_VARIANTS(X) X(16, 256, 512, 32, 1) X(16, 512, 1024, 16, 1) X(8, 512, 2560, 16, 1) \
-    X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1) X(8, 512, -2560, 16, 1) X(16, 512, -1024, 16, 1)
+    X(8, 1024, 2560, 8, 1) X(4, 512, 4096, 16, 1) X(8, 512, -2560, 16, 1) X(16, 512, -1024, 16, 1) \
+    X(16, 256, -128, 16, 2)
 
 enum { PASS_ZFWD = 0, PASS_LINE = 1, PASS_XPASS = 2, PASS_XGEN = 3, PASS_ZINV = 4, NPASS = 5 };
 
