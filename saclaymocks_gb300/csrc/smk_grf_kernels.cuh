@@ -32,9 +32,10 @@ namespace cg = cooperative_groups;
 // W lines (or row pairs) per tile, T threads, largest FFT radix R in registers, at least B
 // resident blocks per SM requested from the register allocator; F > 0: the line length is F and
 // the FFT plan is a compile-time constant (FixedPlan<F, R>), else the plan is read at run time.
-template <int W_, int T_, int R_ = fft_max_radix(T_), int B_ = 1, int F_ = 0>
+template <int W_, int T_, int R_ = fft_max_radix(T_), int B_ = 1, int F_ = 0, int D_ = -1>
 struct TileCfg {
-    static constexpr int W = W_, T = T_, RMAX = R_, MINB = B_, NF = F_;
+    // D: y-pass direction compiled in (1 inverse, 0 forward, -1 both)
+    static constexpr int W = W_, T = T_, RMAX = R_, MINB = B_, NF = F_, DIR = D_;
 };
 
 // The launch's plan is the one a fixed-length variant was compiled for (always true otherwise).
@@ -1551,12 +1552,20 @@ static int launch_line(const LineArgs& a, bool inv, cudaStream_t st) {
     const size_t smem = (size_t)(a.pl.n * C::W + a.pl.n) * sizeof(float2);
     const int64_t ntiles = a.n_outer * ceil_div(a.ncol, C::W) * a.nbuf;
     int grid = 0, rc;
+    // one direction per instantiation (the two are compiled in separate translation units)
+    if constexpr (C::DIR >= 0) {
+        if (inv != (C::DIR == 1)) return fail(SMK_EINVAL, "line: direction of another unit");
+    }
     if (inv) {
-        if ((rc = persistent_grid(line_kernel<C, true>, C::T, smem, ntiles, &grid))) return rc;
-        line_kernel<C, true><<<grid, C::T, smem, st>>>(a);
+        if constexpr (C::DIR != 0) {
+            if ((rc = persistent_grid(line_kernel<C, true>, C::T, smem, ntiles, &grid))) return rc;
+            line_kernel<C, true><<<grid, C::T, smem, st>>>(a);
+        }
     } else {
-        if ((rc = persistent_grid(line_kernel<C, false>, C::T, smem, ntiles, &grid))) return rc;
-        line_kernel<C, false><<<grid, C::T, smem, st>>>(a);
+        if constexpr (C::DIR != 1) {
+            if ((rc = persistent_grid(line_kernel<C, false>, C::T, smem, ntiles, &grid))) return rc;
+            line_kernel<C, false><<<grid, C::T, smem, st>>>(a);
+        }
     }
     return check_launch("line_kernel");
 }
@@ -1662,6 +1671,8 @@ int variant_for(int pass, int n);
 int run_zfwd(int v, const ZFwdArgs& a, int64_t rows_per_box, cudaStream_t st);
 int run_zinv(int v, const ZInvArgs& a, int64_t rows_per_box, cudaStream_t st);
 int run_line(int v, const LineArgs& a, bool inv, cudaStream_t st);
+int run_line_inv(int v, const LineArgs& a, cudaStream_t st);
+int run_line_fwd(int v, const LineArgs& a, cudaStream_t st);
 int run_xpass(int v, const XArgs& a, cudaStream_t st);
 int run_xgen(int v, const XGenArgs& a, cudaStream_t st);
 int run_xgi(int v, const XGenArgs& a, cudaStream_t st);

@@ -1,4 +1,5 @@
-// Tile variants of the GPU-noise x passes (xgen: into the boxes, xgi: into the blocked intermediate).
+// Tile variants of the GPU-noise x pass in place in the boxes (xgen; xgi, into the blocked
+// intermediate, is in smk_grf_xi.cu).
 #include "smk_grf_kernels.cuh"
 
 namespace smk {
@@ -10,15 +11,6 @@ int run_xgen(int v, const XGenArgs& a, cudaStream_t st) {
     SMK_XGEN_VARIANTS(X)
 #undef X
     return fail(SMK_EINVAL, "xgen: no tile variant %d", v);
-}
-
-int run_xgi(int v, const XGenArgs& a, cudaStream_t st) {
-    int i = 0;
-#define X(W, T, N, R, B) \
-    if (v == i++) return launch_xgi<TileCfg<W, T, R, B, SMK_NFIX(N)>>(a, st);
-    SMK_XGEN_VARIANTS(X)
-#undef X
-    return fail(SMK_EINVAL, "xgi: no tile variant %d", v);
 }
 
 }  // namespace smk
